@@ -1,0 +1,427 @@
+#!/usr/bin/env python
+"""Step-rate benchmark of the GB300 global step.
+
+Workload: the Neo-Hookean beam (64x16x16 hex cells, 6 tets each: 98,304 tets,
+18,785 vertices), 8 local/global iterations per implicit-Euler step, plain
+float32 block-Jacobi PCG to 1e-6 relative residual.  A "step" is one solver
+step; the timed run is the workload's 50 steps from its initial state.
+
+  value  steps/s with the state resident on the GPU (CUDA-graph replays),
+         L2 flushed between steps outside the timed events.
+  e2e    the same steps through the public solver API with the state in
+         pinned host memory: H2D copy of (q, qd), step, D2H copy of (q, qd).
+  roofline  the persistent PCG kernel (the dominant kernel), from an eager
+         stage-by-stage pass timed with CUDA events on the launch stream.
+
+--impl reference times the CPU oracle (the restatement of the reference's
+step, float32) on the host instead.  With --gpus N under torchrun every rank
+runs an independent replica (the step does not shard across GPUs).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "warp-mfem_gb300"), ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "steps/s to 1e-6 rel. residual: learned+mixed PCG vs plain FP32 PCG, same GB300"
+FALLBACK_HBM_GBS = 6800.0
+L2_FLUSH_BYTES = 512 << 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", default="nh_beam")
+    ap.add_argument("--profile-steps", type=int, default=10, help="steps of the eager stage profile")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget-s", type=float, default=30.0, help="CPU time budget of the oracle leg")
+    return ap.parse_args()
+
+
+def workload_config(mesh, extra=None):
+    spec = mesh.spec
+    cfg = {
+        "workload": (f"{spec.name}: {spec.cells[0]}x{spec.cells[1]}x{spec.cells[2]} hex cells x 6 tets "
+                     f"({mesh.T} tets, {mesh.n} vertices, {3 * mesh.n} DoF), {spec.energy}, "
+                     f"E log-uniform [{spec.E[0]:.0e}, {spec.E[1]:.0e}] Pa (seed {spec.seed}), nu {spec.nu}, "
+                     f"rho {spec.density:g}, dt 1/{round(1 / spec.dt)}, {spec.iterations} local/global iterations, "
+                     f"block-Jacobi fp32 PCG to {spec.cg_tolerance:g}"),
+        "tets": mesh.T,
+        "vertices": mesh.n,
+        "steps_per_run": spec.steps,
+        "pcg": "plain fp32 block-Jacobi (the learned + mixed-precision variant is not built)",
+        "parallelism": "replicas",
+        "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write, outside the timed events)",
+    }
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            import tempfile
+            fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        power = [float(r[3]) for r in rows if re.match(r"^[0-9.]+$", r[3])]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(power) if power else None}
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+def hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback 6.8 TB/s"
+
+
+def ncu_traffic_per_launch():
+    """Per-launch DRAM bytes of the PCG kernel from the committed ncu summary,
+    scaled to this workload's PCG iterations by the summary's bytes/iteration."""
+    path = os.path.join(ROOT, "profiles", "pcg_kernel_nh_beam.md")
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_pcg_iteration:\s*([0-9.eE+]+)", text)
+    return float(m.group(1)) if m else None
+
+
+def pcg_bytes_per_iteration(nnzb: int, n: int) -> int:
+    """Algorithmic bytes of one plain fp32 PCG iteration: 36 B values + 4 B
+    column index per block; per row 4 B row pointer + 24 B (read p, write Ap)
+    + 48 B (read x, p, r, Ap) + 36 B block-Jacobi block + 36 B (write x, r, z)
+    + 36 B (read z, p, write p) = 40 nnzb + 172 n."""
+    return 40 * nnzb + 172 * n
+
+
+def cpu_oracle_rate(mesh, budget_s: float):
+    """Steps/s of the float32 oracle on this host (at least one full step,
+    more while within budget)."""
+    import numpy as np
+    from oracle import mfem_oracle
+
+    ref = mfem_oracle.OracleSolver(mesh, dtype=np.float32)
+    q, qd = mesh.q0, mesh.qd0
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        q, qd = ref.step(q, qd, mesh.spec.dt)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el * (steps + 1) / steps > budget_s or steps >= mesh.spec.steps:
+            break
+    return steps / el, steps, el
+
+
+# ---------------------------------------------------------------------------
+# reference arm
+# ---------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    from mfem_gb300 import beams
+    if rank != 0:
+        return 0
+    mesh = beams.build_beam(args.workload)
+    budget = max(10.0, min(150.0, args.cpu_budget_s * max(1, args.steps) / 10.0))
+    rate, steps, el = cpu_oracle_rate(mesh, budget)
+    sample = (f"{steps} step(s) of {args.workload} ({mesh.T} tets, {mesh.spec.iterations} local/global iterations "
+              f"each, scipy/numpy float32 oracle restating the reference step) in {el:.1f} s")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": args.gpus,
+        "steps": steps, "warmup": 0, "ms_per_step": 1000.0 / rate, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(mesh, {"reference": "CPU oracle port (the reference's Warp path cannot run: "
+                                                      "warp-lang / newton absent, Python >= 3.13 required)"}),
+        "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+def run_gb300(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    from mfem_gb300 import Model, MixedFEMSolver, beams, _lib
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    mesh = beams.build_beam(args.workload)
+    spec = mesh.spec
+    model = Model.from_beam(mesh, device=dev)
+    solver = MixedFEMSolver(model, iterations=spec.iterations, energy=spec.energy,
+                            cg_tolerance=spec.cg_tolerance, cg_max_iterations=spec.cg_max_iterations)
+    s_init = solver.tet_stretch.clone().reshape(-1)
+    lam0 = torch.zeros_like(s_init)
+    q0 = torch.as_tensor(mesh.q0, device=dev)
+    A, B = model.state(), model.state()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def reset():
+        A.particle_q.copy_(q0)
+        A.particle_qd.zero_()
+        solver.write_buffer("tet_stretch", s_init)
+        solver.write_buffer("tet_lambda", lam0)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    # ---- warm-up (captures the step graphs)
+    reset()
+    for _ in range(args.warmup):
+        solver.step(A, B, None, None, spec.dt)
+        A, B = B, A
+    torch.cuda.synchronize(dev)
+
+    # ---- value: resident state, graph replays
+    reset()
+    sampler = ClockSampler(local_rank)
+    barrier()
+    sampler.start()
+    launches0 = _lib.kernel_launch_count()
+    total_ms = 0.0
+    pcg_iters = []
+    statuses = set()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        solver.step(A, B, None, None, spec.dt)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        st = solver.solve_stats()
+        pcg_iters.append(sum(s["iterations"] for s in st))
+        statuses.update(s["status"] for s in st)
+        A, B = B, A
+    launches = _lib.kernel_launch_count() - launches0
+    barrier()
+    clocks = sampler.stop()
+    t_local = total_ms / 1000.0
+    if world > 1:
+        t = torch.tensor([t_local], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    else:
+        t_max = t_local
+    value = world * args.steps / t_max
+    q_final = A.particle_q.cpu().numpy()
+
+    # ---- e2e: host-resident state through the public API
+    reset()
+    hq = torch.empty((mesh.n, 3), dtype=torch.float32, pin_memory=True)
+    hqd = torch.empty_like(hq, pin_memory=True)
+    hq.copy_(q0.cpu())
+    hqd.zero_()
+    oq = torch.empty_like(hq, pin_memory=True)
+    oqd = torch.empty_like(hq, pin_memory=True)
+    e2e_ms = 0.0
+    barrier()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        A.particle_q.copy_(hq, non_blocking=True)
+        A.particle_qd.copy_(hqd, non_blocking=True)
+        solver.step(A, B, None, None, spec.dt)
+        oq.copy_(B.particle_q, non_blocking=True)
+        oqd.copy_(B.particle_qd, non_blocking=True)
+        e1.record(stream)
+        e1.synchronize()
+        e2e_ms += e0.elapsed_time(e1)
+        hq, oq = oq, hq
+        hqd, oqd = oqd, hqd
+    barrier()
+    if world > 1:
+        t = torch.tensor([e2e_ms / 1000.0], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    else:
+        e2e_s = e2e_ms / 1000.0
+    e2e_value = world * args.steps / e2e_s
+    e2e_match = bool(np.array_equal(hq.numpy(), q_final))
+    state_bytes = 2 * mesh.n * 3 * 4
+
+    # ---- stage profile: eager stages, CUDA events on the launch stream
+    reset()
+    stage_ms = {"element": 0.0, "assemble": 0.0, "pcg": 0.0, "local_solve": 0.0, "predict": 0.0}
+    stage_launches = {k: 0 for k in stage_ms}
+    prof_iters = 0
+    prof_solves = 0
+    prof_steps = max(1, min(args.profile_steps, args.steps))
+    x = B.particle_q
+    for _ in range(prof_steps):
+        flush.zero_()
+        evs = []
+
+        def mark(name):
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record(stream)
+            evs.append((name, ev))
+
+        mark("start")
+        solver.predict(A.particle_q, A.particle_qd, spec.dt)
+        mark("predict")
+        x.copy_(A.particle_q)
+        mark("copy")
+        for it in range(spec.iterations):
+            solver.update_system(x)
+            mark("element")
+            solver.assemble(x, spec.dt)
+            mark("assemble")
+            solver.global_solve(it)
+            mark("pcg")
+            solver.local_solve(x)
+            mark("local_solve")
+        torch.cuda.synchronize(dev)
+        for (_, a), (name, b) in zip(evs[:-1], evs[1:]):
+            if name in stage_ms:
+                stage_ms[name] += a.elapsed_time(b)
+                stage_launches[name] += 1
+        st = solver.solve_stats()
+        prof_iters += sum(s["iterations"] for s in st)
+        prof_solves += len(st)
+        B.particle_qd.copy_((x - A.particle_q) / spec.dt)
+        A, B = B, A
+        x = B.particle_q
+    nnzb = solver.nnzb
+    b_it = pcg_bytes_per_iteration(nnzb, mesh.n)
+    pcg_bytes = b_it * (prof_iters + prof_solves)  # +1 pass per solve: the initial residual
+    achieved = pcg_bytes / (stage_ms["pcg"] / 1000.0) / 1e9
+    peak, peak_src = hbm_peak()
+    per_launch_iters = (prof_iters + prof_solves) / prof_solves
+    traffic_it = ncu_traffic_per_launch()
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+        "traffic": (traffic_it * per_launch_iters) if traffic_it else None,
+        "kernel": "pcg_kernel (persistent cooperative block-Jacobi PCG)",
+        "algorithmic_bytes_per_launch": b_it * per_launch_iters,
+        "bytes_per_pcg_iteration": b_it, "pcg_iterations_per_launch": per_launch_iters - 1,
+        "avg_launch_ms": stage_ms["pcg"] / stage_launches["pcg"], "peak_source": peak_src,
+    }
+    total_stage = sum(stage_ms.values())
+    shares = {k: v / total_stage for k, v in stage_ms.items()}
+
+    if rank != 0:
+        return 0
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        rate, steps, el = cpu_oracle_rate(mesh, args.cpu_budget_s)
+        cpu = {"value": rate, "unit": "steps/s", "cores": 1, "kind": "port",
+               "sample": f"{steps} step(s) of {args.workload} ({mesh.T} tets, {spec.iterations} local/global "
+                         f"iterations each) by the float32 numpy/scipy oracle in {el:.1f} s"}
+    avg_iters = statistics.mean(pcg_iters)
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(mesh),
+        "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
+                "d2h_bytes_per_step": state_bytes, "matches_resident_run": e2e_match},
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "pcg_iterations_per_step": avg_iters,
+        "dof_iterations_per_s": world * 3 * mesh.n * sum(pcg_iters) / t_max,
+        "pcg_status_codes": sorted(statuses),
+        "stage_share": shares,
+        "stage_ms_per_step": {k: v / prof_steps for k, v in stage_ms.items()},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world != args.gpus and not (world == 1 and args.gpus == 1):
+        if world == 1:
+            print(json.dumps({"error": f"--gpus {args.gpus} needs torchrun with {args.gpus} processes"}))
+            return 2
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    try:
+        return run_gb300(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

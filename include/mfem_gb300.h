@@ -1,0 +1,209 @@
+/*
+ * mfem_gb300.h -- C ABI of the GB300 (sm_103a) global step of warp-mfem's
+ * mixed variational FEM solver.
+ *
+ * The reference (gjohns57/warp-mfem) is Python over NVIDIA Warp; it has no
+ * FFI.  Each entry point below replaces one stage of its
+ * RefinementSolver.step (src/mfem/refinement/solver.py:429-579), cited at the
+ * declaration, so a host in any language can drive the same step through
+ * plain pointers.  No torch (or other framework) type crosses this boundary.
+ *
+ * Conventions
+ *  - float32 everywhere, like the reference (src/mfem/types.py:4); indices int32.
+ *  - vec3 arrays are [n][3], matrices row-major.
+ *  - Pointers named d_* are CUDA device pointers, h_* host pointers.
+ *  - Every call returns an mfem_status.  Codes >= MFEM_NONFINITE are errors;
+ *    mfem_plan_last_error() gives the message.  Solver outcomes of the PCG
+ *    (converged / iteration cap / breakdown) are reported per Newton
+ *    iteration by mfem_step_stats() and never fail a step, matching the
+ *    reference, which uses the CG result whether or not it converged.
+ *  - Calls are asynchronous on the given stream unless documented otherwise.
+ *    A plan is not thread-safe: one host thread per plan.
+ */
+#ifndef MFEM_GB300_H
+#define MFEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mfem_plan mfem_plan;   /* opaque */
+typedef struct CUstream_st *mfem_stream; /* a cudaStream_t; NULL = legacy default stream */
+
+typedef enum mfem_status {
+    MFEM_OK = 0,
+    MFEM_MAXITER = 1,        /* PCG hit cg_max_iterations before the tolerance   */
+    MFEM_STAGNATION = 2,     /* PCG broke down (p.Ap <= 0)                       */
+    MFEM_NONFINITE = 3,      /* NaN/Inf met in the PCG reductions               */
+    MFEM_BAD_ARG = 4,        /* invalid argument or mesh                          */
+    MFEM_CUDA_ERROR = 5,     /* a CUDA runtime call failed                        */
+    MFEM_TIMEOUT = 6         /* a bounded device-side wait gave up                */
+} mfem_status;
+
+typedef enum mfem_energy {
+    MFEM_ENERGY_ARAP = 0,        /* src/mfem/refinement/elastic_energy.py:127-253 */
+    MFEM_ENERGY_NEOHOOKEAN = 1   /* src/mfem/refinement/elastic_energy.py:255-407 */
+} mfem_energy;
+
+/* Solver settings; the fields mirror RefinementSolver's kwargs
+ * (src/mfem/refinement/solver.py:56-128). */
+typedef struct mfem_config {
+    int32_t iterations;                   /* local/global iterations per step (solver.py:304)   */
+    int32_t energy;                       /* mfem_energy ("energy", solver.py:108-122)           */
+    int32_t cg_max_iterations;            /* solver.py:90, default 1000                          */
+    float cg_tolerance;                   /* relative, ||r|| <= tol ||b|| (solver.py:91)         */
+    float attachment_stiffness;           /* penalty on inv_mass==0 vertices (solver.py:106)     */
+    float preconditioner_singular_threshold; /* |det| below -> identity block (solver.py:93)     */
+    int32_t preconditioner;               /* 1 block-Jacobi, 0 none (solver.py:128)              */
+    int32_t use_cuda_graph;               /* capture mfem_step once per argument set and replay  */
+    int32_t pcg_ctas;                     /* persistent PCG CTAs; 0 = one per SM                 */
+    int32_t reserved[7];
+} mfem_config;
+
+/* Buffers owned by a plan that mfem_plan_copy_out / _copy_in expose.
+ * Layout per tet t (T tets) / vertex v (n vertices) / slot k (nnzb blocks). */
+typedef enum mfem_buffer {
+    MFEM_BUF_TET_STRETCH = 0,   /* f32 [T][6]  s       (additional_state.tet_stretch)     */
+    MFEM_BUF_TET_LAMBDA = 1,    /* f32 [T][6]  lambda  (additional_state.tet_lambda)      */
+    MFEM_BUF_CONSTRAINT = 2,    /* f32 [6][T]  c = SYM (sym6(S(F)) - s), component-major  */
+    MFEM_BUF_GRAD_CONSTRAINT = 3, /* f32 [72][T] G, entry (i, 3k+a) at (i*12 + 3k+a)*T+t  */
+    MFEM_BUF_GRAD_S = 4,        /* f32 [6][T]  g_s                                         */
+    MFEM_BUF_H_LAMBDA = 5,      /* f32 [21][T] H_lambda, packed upper triangle row-major  */
+    MFEM_BUF_HESS_S_INV = 6,    /* f32 [21][T] H_s^-1, packed upper triangle row-major    */
+    MFEM_BUF_G_LAMBDA = 7,      /* f32 [6][T]  g_lambda                                    */
+    MFEM_BUF_ELEMENT_HESSIAN = 8, /* f32 [T][10][3][3] upper blocks (k<=l) of G^T H_l G   */
+    MFEM_BUF_ELEMENT_RHS = 9,   /* f32 [T][12] (H_l G)^T g_lambda                          */
+    MFEM_BUF_ROW_PTR = 10,      /* i32 [n+1]   BSR row offsets                             */
+    MFEM_BUF_COL_IDX = 11,      /* i32 [nnzb]  BSR block columns, ascending per row        */
+    MFEM_BUF_TET_SLOTS = 12,    /* i32 [T][16] slot of block (tets[t][k], tets[t][l]) at k*4+l */
+    MFEM_BUF_H_VALUES = 13,     /* f32 [nnzb][3][3] global Hessian H                        */
+    MFEM_BUF_RHS = 14,          /* f32 [n][3]  g = sum G^T H_l g_l - g_x                    */
+    MFEM_BUF_PRECOND = 15,      /* f32 [n][3][3] block-Jacobi inverse diagonal             */
+    MFEM_BUF_X_TILDE = 16,      /* f32 [n][3]  predictor x~                                 */
+    MFEM_BUF_DX = 17,           /* f32 [n][3]  PCG solution dx (warm start x~ - x)          */
+    MFEM_BUF_COUNT = 18
+} mfem_buffer;
+
+/* Per Newton iteration outcome of the global solve. */
+typedef struct mfem_solve_stats {
+    int32_t iterations;     /* PCG iterations taken                       */
+    int32_t status;         /* MFEM_OK, MFEM_MAXITER, MFEM_STAGNATION, ... */
+    float rel_residual;     /* ||r|| / ||b|| of the recurrence residual    */
+    float reserved;
+} mfem_solve_stats;
+
+/* ---- configuration / diagnostics ------------------------------------ */
+
+/* Fills the reference's defaults: iterations 8, ARAP, cg_max_iterations 1000,
+ * cg_tolerance 1e-6, attachment_stiffness 10, singular threshold 1e-20,
+ * block-Jacobi on (src/mfem/refinement/solver.py:90-128). */
+void mfem_config_default(mfem_config *cfg);
+
+const char *mfem_status_string(int status);
+
+/* Total kernels this library has launched in this process (graph replays
+ * count every kernel node). */
+uint64_t mfem_kernel_launch_count(void);
+
+/* ---- host-side symbolic analysis (no GPU needed) --------------------- */
+
+/* Exact vertex-adjacency sparsity of the global Hessian, diagonal included,
+ * columns ascending.  Replaces the padded bsr_set_from_triplets / bsr_mm
+ * topology of src/mfem/refinement/solver.py:201-203, 685-724.
+ * Call with row_ptr/col_idx NULL to get *nnzb first. */
+int mfem_bsr_sparsity(int32_t n_particles, int32_t n_tets, const int32_t *h_tet_indices,
+                      int32_t *h_row_ptr, int32_t *h_col_idx, int64_t *nnzb);
+
+/* Element -> BSR-slot scatter map [T][16] for the sparsity above (the
+ * triplets of src/mfem/refinement/kernels.py:105-128 resolved to slots). */
+int mfem_tet_slot_map(int32_t n_particles, int32_t n_tets, const int32_t *h_tet_indices,
+                      const int32_t *h_row_ptr, const int32_t *h_col_idx, int32_t *h_slots);
+
+/* ---- plan ----------------------------------------------------------- */
+
+/* Builds a plan for one body on device `device`: uploads the model, runs the
+ * symbolic analysis, allocates the workspace and sets s = S(F_rest),
+ * lambda = 0.  Replaces RefinementSolver.__init__ with refinement, contact
+ * and shell off (src/mfem/refinement/solver.py:41-304;
+ * additional_state.py:139-202; the mass/attachment setup of
+ * solver.py:320-393).  Host arrays:
+ *   tet_indices [T][4], tet_poses [T][3][3] (DmInv, edges as columns),
+ *   tet_materials [T][3] (mu, lambda, damping), particle_q_rest [n][3]
+ *   (initial stretch and attachment targets), particle_mass [n],
+ *   particle_inv_mass [n] (0 = attached), gravity [3].
+ * This call synchronises the device. */
+int mfem_plan_create(const mfem_config *cfg, int32_t n_particles, int32_t n_tets,
+                     const int32_t *h_tet_indices, const float *h_tet_poses,
+                     const float *h_tet_materials, const float *h_particle_q_rest,
+                     const float *h_particle_mass, const float *h_particle_inv_mass,
+                     const float *h_gravity, int32_t device, mfem_plan **out);
+
+void mfem_plan_destroy(mfem_plan *plan);
+
+/* Message of the last error raised on this plan ("" if none). */
+const char *mfem_plan_last_error(const mfem_plan *plan);
+
+int mfem_plan_sizes(const mfem_plan *plan, int32_t *n_particles, int32_t *n_tets, int64_t *nnzb);
+
+/* Bytes of an exposed buffer. */
+int mfem_plan_buffer_bytes(const mfem_plan *plan, int32_t which, size_t *bytes);
+
+/* cudaMemcpyAsync between an exposed buffer and caller memory (host or
+ * device, any kind).  `bytes` must equal mfem_plan_buffer_bytes. */
+int mfem_plan_copy_out(const mfem_plan *plan, int32_t which, void *dst, size_t bytes, mfem_stream stream);
+int mfem_plan_copy_in(mfem_plan *plan, int32_t which, const void *src, size_t bytes, mfem_stream stream);
+
+/* ---- the step and its stages ---------------------------------------- */
+
+/* One implicit-Euler step: RefinementSolver.step
+ * (src/mfem/refinement/solver.py:429-579) with refinement off and no line
+ * search (the plain update of :555-557).  d_q_out/d_qd_out receive the new
+ * positions and velocities; d_q_in/d_qd_in are only read, and may alias the
+ * outputs.  s and lambda persist in the plan.  Asynchronous; allocates
+ * nothing. */
+int mfem_step(mfem_plan *plan, const float *d_q_in, const float *d_qd_in,
+              float *d_q_out, float *d_qd_out, float dt, mfem_stream stream);
+
+/* Outcome of the global solves of the last step (synchronises the stream).
+ * Writes min(max_entries, iterations) entries; *count = entries written. */
+int mfem_step_stats(mfem_plan *plan, mfem_solve_stats *h_stats, int32_t max_entries,
+                    int32_t *count, mfem_stream stream);
+
+/* Predictor x~ = x + v dt + g dt^2/2 into the plan
+ * (integrate_particles, src/mfem/refinement/kernels.py:77-91). */
+int mfem_predict(mfem_plan *plan, const float *d_q, const float *d_qd, float dt, mfem_stream stream);
+
+/* Element stage at (x, s): c, G, g_s, H_s (psd-fixed for Neo-Hookean),
+ * H_lambda, g_lambda and the element Hessian/rhs; replaces _update_system
+ * plus the per-tet half of _assemble_system
+ * (src/mfem/refinement/solver.py:633-679, 695-706, 930-980). */
+int mfem_update_system(mfem_plan *plan, const float *d_x, mfem_stream stream);
+
+/* Assembly: H = sum_e G^T H_l G + (M+Q)/dt^2, g = sum_e G^T H_l g_l - g_x,
+ * the block-Jacobi inverse and the warm start dx = x~ - x
+ * (src/mfem/refinement/solver.py:682-743, 530-531, 591-602). */
+int mfem_assemble(mfem_plan *plan, const float *d_x, float dt, mfem_stream stream);
+
+/* Block-Jacobi PCG on H dx = g (src/mfem/refinement/solver.py:581-609 and
+ * warp.optim.linear.cg).  Result in MFEM_BUF_DX; outcome recorded as entry
+ * `slot` of the stats that mfem_step_stats reads. */
+int mfem_global_solve(mfem_plan *plan, int32_t slot, mfem_stream stream);
+
+/* Local solve and update: lambda = -H_l (g_l - G dx), ds = -H_s^-1 (SYM
+ * lambda + g_s), s += ds, x += dx (src/mfem/refinement/kernels.py:252-283;
+ * solver.py:555-557). */
+int mfem_local_solve(mfem_plan *plan, float *d_x, mfem_stream stream);
+
+/* ||g - H dx|| / ||g|| accumulated in float64 for the current H, g, dx
+ * (synchronises the stream).  The reference has no counterpart: it is the
+ * true-residual check of the float32 recurrence. */
+int mfem_true_residual(mfem_plan *plan, double *h_rel_residual, mfem_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MFEM_GB300_H */

@@ -1,0 +1,270 @@
+"""GPU parity of the CUDA global step against the CPU oracle.
+
+Tolerances (float32 kernels against the float64 oracle on the same float32
+inputs): per-tet terms 2e-5 of each quantity's largest magnitude; assembled
+blocks and rhs 1e-5; positions after a step or a trajectory 1e-5 relative to
+the largest position (the bar of the benchmark spec: per-step positions within
+1e-5 relative in float32).  Sparsity and scatter maps are compared bit for bit.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from mfem_gb300 import Model, MixedFEMSolver, beams
+from oracle import mfem_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+DEV = "cuda:0"
+GOLD_DIR = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def close(a, b, rtol, atol=0.0):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    scale = max(np.abs(b).max(), 1e-30)
+    err = np.abs(a - b).max()
+    assert err <= rtol * scale + atol, f"max err {err:.3e} vs scale {scale:.3e} (rtol {rtol})"
+
+
+def unpack21(p):
+    """[21][T] packed upper triangles -> [T, 6, 6]."""
+    T = p.shape[-1]
+    M = np.zeros((T, 6, 6))
+    k = 0
+    for i in range(6):
+        for j in range(i, 6):
+            M[:, i, j] = M[:, j, i] = p[k]
+            k += 1
+    return M
+
+
+def ke_dense(Ke, T):
+    """[T][10][3][3] upper blocks -> [T, 12, 12]."""
+    Ke = Ke.reshape(T, 10, 3, 3)
+    K = np.zeros((T, 12, 12))
+    b = 0
+    for k in range(4):
+        for l in range(k, 4):
+            K[:, 3 * k:3 * k + 3, 3 * l:3 * l + 3] = Ke[:, b]
+            K[:, 3 * l:3 * l + 3, 3 * k:3 * k + 3] = np.swapaxes(Ke[:, b], 1, 2)
+            b += 1
+    return K
+
+
+def make(name, cells=None, **kw):
+    mesh = beams.build_beam(name, cells=cells)
+    model = Model.from_beam(mesh, device=DEV)
+    kw.setdefault("energy", mesh.spec.energy)
+    solver = MixedFEMSolver(model, iterations=kw.pop("iterations", mesh.spec.iterations), **kw)
+    return mesh, model, solver
+
+
+def deformed_inputs(mesh, seed=11, amp=0.01, s_amp=0.02):
+    rng = np.random.default_rng(seed)
+    x = (mesh.q0 + rng.normal(0, amp, mesh.q0.shape)).astype(np.float32)
+    s0 = O.precompute_tet_stretch(mesh.rest_q.astype(np.float64), mesh.tet_indices,
+                                  mesh.tet_poses.astype(np.float64))
+    s = (s0 + rng.normal(0, s_amp, s0.shape)).astype(np.float32)
+    return x, s
+
+
+def t(a):
+    return torch.as_tensor(np.ascontiguousarray(a), device=DEV)
+
+
+# ---------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("name,cells", [("cantilever", None), ("nh_beam", (16, 4, 4))])
+def test_sparsity_and_slot_map_bit_exact(name, cells):
+    mesh, _, solver = make(name, cells)
+    rp, ci = O.bsr_sparsity(mesh.tet_indices, mesh.n)
+    np.testing.assert_array_equal(solver.read_buffer("row_ptr").cpu().numpy(), rp)
+    np.testing.assert_array_equal(solver.read_buffer("col_idx").cpu().numpy(), ci)
+    np.testing.assert_array_equal(solver.read_buffer("tet_slots").cpu().numpy().reshape(mesh.T, 16),
+                                  O.tet_slot_map(mesh.tet_indices, rp, ci))
+
+
+def test_initial_stretch_matches_oracle():
+    mesh, _, solver = make("cantilever")
+    s = solver.tet_stretch.cpu().numpy()
+    s_ref = O.precompute_tet_stretch(mesh.rest_q.astype(np.float64), mesh.tet_indices,
+                                     mesh.tet_poses.astype(np.float64))
+    np.testing.assert_allclose(s, s_ref, atol=2e-6)
+    assert np.all(solver.tet_lambda.cpu().numpy() == 0)
+
+
+@pytest.mark.parametrize("energy", ["arap", "neohookean"])
+def test_element_stage_matches_oracle(energy):
+    mesh, _, solver = make("cantilever", energy=energy)
+    x, s = deformed_inputs(mesh)
+    solver.write_buffer("tet_stretch", torch.as_tensor(s).reshape(-1))
+    solver.update_system(t(x))
+    torch.cuda.synchronize()
+    T = mesh.T
+    rd = lambda k, shape: solver.read_buffer(k).cpu().numpy().reshape(shape)
+    ref = O.OracleSolver(mesh, energy=energy, dtype=np.float64)
+    ref.s = s.astype(np.float64)
+    el = ref.element_terms(x.astype(np.float64))
+    close(rd("constraint", (6, T)).T, el["c"], 2e-5)
+    close(np.transpose(rd("grad_constraint", (6, 12, T)), (2, 0, 1)), el["G"], 2e-5)
+    close(rd("grad_s", (6, T)).T, el["g_s"], 2e-5)
+    close(unpack21(rd("h_lambda", (21, T))), el["H_l"], 2e-5)
+    close(unpack21(rd("hess_s_inv", (21, T))), el["H_si"], 2e-5)
+    close(rd("g_lambda", (6, T)).T, el["g_l"], 2e-5)
+    K_ref = np.swapaxes(el["G"], 1, 2) @ el["H_l"] @ el["G"]
+    close(ke_dense(rd("element_hessian", (T, 90)), T), K_ref, 2e-5)
+    f_ref = np.einsum("tji,tj->ti", el["H_l"] @ el["G"], el["g_l"])
+    close(rd("element_rhs", (T, 12)), f_ref, 2e-5)
+
+
+@pytest.mark.parametrize("energy", ["arap", "neohookean"])
+def test_assembly_pcg_and_local_solve_match_oracle(energy):
+    mesh, _, solver = make("cantilever", energy=energy)
+    x, s = deformed_inputs(mesh, seed=5)
+    dt = mesh.spec.dt
+    q = t(mesh.q0)
+    qd = t(np.random.default_rng(2).normal(0, 0.05, mesh.q0.shape).astype(np.float32))
+    solver.write_buffer("tet_stretch", torch.as_tensor(s).reshape(-1))
+    solver.predict(q, qd, dt)
+    solver.update_system(t(x))
+    solver.assemble(t(x), dt)
+    torch.cuda.synchronize()
+    xt = solver.read_buffer("x_tilde").cpu().numpy().reshape(-1, 3)
+    xt_ref = mesh.q0.astype(np.float64) + qd.cpu().numpy() * dt + mesh.gravity * dt * dt / 2
+    close(xt, xt_ref, 1e-6)
+
+    ref = O.OracleSolver(mesh, energy=energy, dtype=np.float64)
+    ref.s = s.astype(np.float64)
+    x64 = x.astype(np.float64)
+    el = ref.element_terms(x64)
+    blocks, g, Hs = ref.assemble(x64, xt.astype(np.float64), dt, el)
+    H = solver.read_buffer("h_values").cpu().numpy().reshape(-1, 3, 3)
+    close(H, blocks, 1e-5)
+    close(solver.read_buffer("rhs").cpu().numpy().reshape(-1, 3), g, 1e-5)
+    Minv_ref = O.block_jacobi_inverse(ref.diag_blocks(blocks), 1e-20)
+    close(solver.read_buffer("precond").cpu().numpy().reshape(-1, 3, 3), Minv_ref, 1e-5)
+    close(solver.read_buffer("dx").cpu().numpy().reshape(-1, 3), xt - x, 1e-6)
+
+    solver.global_solve(0)
+    stats = solver.solve_stats()
+    assert stats[0]["status"] == 0
+    assert stats[0]["rel_residual"] <= 1e-6
+    rel = solver.true_residual()
+    assert rel <= 1e-5, rel
+    dx = solver.read_buffer("dx").cpu().numpy().reshape(-1, 3)
+    dx_direct = np.linalg.solve(Hs.toarray(), g.ravel()).reshape(-1, 3)
+    close(dx, dx_direct, 1e-4)
+
+    # local solve on the GPU's dx, compared with the oracle's on the same dx
+    xg = t(x)
+    solver.local_solve(xg)
+    torch.cuda.synchronize()
+    lam_ref, ds_ref = ref.local_solve(el, dx.astype(np.float64))
+    close(solver.tet_lambda.cpu().numpy(), lam_ref, 1e-4)
+    close(solver.tet_stretch.cpu().numpy() - s, ds_ref, 1e-4, atol=1e-7)
+    close(xg.cpu().numpy(), x64 + dx, 1e-6)
+
+
+def test_cantilever_trajectory_matches_golden():
+    """100 ARAP steps of the 10x2x2 cantilever against the float64 oracle's
+    committed trajectory: positions within 1e-5 relative at every step."""
+    gold = np.load(os.path.join(GOLD_DIR, "cantilever_fp64.npz"))
+    mesh, model, solver = make("cantilever")
+    s0, s1 = model.state(), model.state()
+    s0.particle_q.copy_(t(mesh.q0))
+    worst = 0.0
+    for k in range(mesh.spec.steps):
+        solver.step(s0, s1, None, None, mesh.spec.dt)
+        stats = solver.solve_stats()
+        assert all(st["status"] == 0 for st in stats), (k, stats)
+        q = s1.particle_q.cpu().numpy()
+        err = np.abs(q - gold["q"][k]).max() / np.abs(gold["q"][k]).max()
+        worst = max(worst, err)
+        assert err <= 1e-5, (k, err)
+        s0, s1 = s1, s0
+    close(solver.tet_stretch.cpu().numpy(), gold["s_final"], 1e-4)
+    print(f"worst relative position error over 100 steps: {worst:.2e}")
+
+
+def test_nh_beam_reduced_steps_match_oracle():
+    """The Neo-Hookean beam workload at 16x4x4 cells: 3 steps against the
+    float64 oracle."""
+    mesh, model, solver = make("nh_beam", cells=(16, 4, 4))
+    ref = O.OracleSolver(mesh, dtype=np.float64)
+    s0, s1 = model.state(), model.state()
+    s0.particle_q.copy_(t(mesh.q0))
+    q, qd = mesh.q0, mesh.qd0
+    for k in range(3):
+        solver.step(s0, s1, None, None, mesh.spec.dt)
+        q, qd = ref.step(q, qd, mesh.spec.dt)
+        stats = solver.solve_stats()
+        assert all(st["status"] == 0 for st in stats), stats
+        close(s1.particle_q.cpu().numpy(), q, 1e-5)
+        close(s1.particle_qd.cpu().numpy(), qd, 2e-3, atol=1e-6)
+        s0, s1 = s1, s0
+    close(solver.tet_stretch.cpu().numpy(), ref.s, 1e-4)
+
+
+def test_nh_beam_full_size_first_step():
+    """The full 64x16x16 Neo-Hookean beam (98,304 tets): one step against the
+    float64 oracle, every PCG converged, and the float64 true residual of the
+    last solve within 10x the tolerance."""
+    mesh, model, solver = make("nh_beam")
+    s0, s1 = model.state(), model.state()
+    s0.particle_q.copy_(t(mesh.q0))
+    solver.step(s0, s1, None, None, mesh.spec.dt)
+    stats = solver.solve_stats()
+    assert all(st["status"] == 0 and st["rel_residual"] <= 1e-6 for st in stats), stats
+    assert solver.true_residual() <= 1e-5
+    ref = O.OracleSolver(mesh, dtype=np.float64)
+    q, _ = ref.step(mesh.q0, mesh.qd0, mesh.spec.dt)
+    close(s1.particle_q.cpu().numpy(), q, 1e-5)
+
+
+def test_graph_and_eager_paths_agree_bitwise():
+    mesh = beams.build_beam("cantilever")
+    outs = []
+    for graph in (True, False):
+        model = Model.from_beam(mesh, device=DEV)
+        solver = MixedFEMSolver(model, iterations=8, use_cuda_graph=graph)
+        s0, s1 = model.state(), model.state()
+        for _ in range(5):
+            solver.step(s0, s1, None, None, mesh.spec.dt)
+            s0, s1 = s1, s0
+        outs.append((s0.particle_q.cpu().numpy(), s0.particle_qd.cpu().numpy(), solver.tet_stretch.cpu().numpy()))
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_step_is_deterministic_and_leaves_state_in_alone():
+    mesh = beams.build_beam("nh_beam", cells=(16, 4, 4))
+    results = []
+    for _ in range(2):
+        model = Model.from_beam(mesh, device=DEV)
+        solver = MixedFEMSolver(model, iterations=8, energy="neohookean")
+        s0, s1 = model.state(), model.state()
+        s0.particle_q.copy_(t(mesh.q0))
+        before = s0.particle_q.clone()
+        solver.step(s0, s1, None, None, mesh.spec.dt)
+        torch.cuda.synchronize()
+        assert torch.equal(s0.particle_q, before)
+        results.append(s1.particle_q.cpu().numpy())
+    np.testing.assert_array_equal(results[0], results[1])
+
+
+def test_aliased_in_out_state():
+    mesh = beams.build_beam("cantilever")
+    model = Model.from_beam(mesh, device=DEV)
+    a = MixedFEMSolver(model, iterations=8)
+    b = MixedFEMSolver(model, iterations=8)
+    s0, s1 = model.state(), model.state()
+    a.step(s0, s1, None, None, mesh.spec.dt)
+    s2 = model.state()
+    b.step(s2, s2, None, None, mesh.spec.dt)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(s1.particle_q.cpu().numpy(), s2.particle_q.cpu().numpy())
+    np.testing.assert_array_equal(s1.particle_qd.cpu().numpy(), s2.particle_qd.cpu().numpy())

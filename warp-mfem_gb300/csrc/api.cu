@@ -1,0 +1,597 @@
+// C ABI of libmfem_gb300: plan lifecycle, the step, its stages and the
+// buffer/diagnostic accessors declared in include/mfem_gb300.h.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace mfem {
+
+static std::atomic<uint64_t> g_launches{0};
+static thread_local bool t_capturing = false;
+static thread_local std::string t_create_error;
+
+void count_launches(uint64_t k) {
+    if (!t_capturing) g_launches += k;
+}
+
+}  // namespace mfem
+
+using namespace mfem;
+
+struct mfem_plan {
+    mfem_config cfg{};
+    int device = 0;
+    int n = 0;
+    int T = 0;
+    int64_t nnzb = 0;
+    int pcg_ctas = 1;
+    int max_stats = 1;
+    float gravity[3] = {0.0f, 0.0f, 0.0f};
+    std::string last_error;
+    std::vector<void *> allocs;
+    TetViews tv{};
+    VertexViews vv{};
+    BsrViews bv{};
+    PcgWork pw{};
+    int32_t *tet_slots = nullptr;
+    double *resid = nullptr;
+    cudaStream_t capture_stream = nullptr;
+    // captured steps, keyed by (q_in, qd_in, q_out, qd_out, dt); a simulation
+    // loop that swaps two states alternates between two entries
+    static constexpr int kGraphSlots = 4;
+    struct GraphEntry {
+        cudaGraphExec_t exec = nullptr;
+        const void *key[4] = {nullptr, nullptr, nullptr, nullptr};
+        float dt = 0.0f;
+        uint64_t kernels = 0;
+        uint64_t last_use = 0;
+    } graphs[kGraphSlots];
+    uint64_t graph_clock = 0;
+};
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) {
+            int cur = -1;
+            if (cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+        }
+    }
+};
+
+int fail(mfem_plan *p, int code, const std::string &msg) {
+    if (p) p->last_error = msg;
+    else t_create_error = msg;
+    return code;
+}
+
+int cuda_fail(mfem_plan *p, cudaError_t err, const char *what) {
+    return fail(p, MFEM_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(err));
+}
+
+template <class T>
+cudaError_t dev_alloc(mfem_plan *p, T **ptr, size_t count) {
+    void *raw = nullptr;
+    cudaError_t err = cudaMalloc(&raw, count == 0 ? 16 : count * sizeof(T));
+    if (err != cudaSuccess) return err;
+    p->allocs.push_back(raw);
+    *ptr = static_cast<T *>(raw);
+    return cudaSuccess;
+}
+
+template <class T>
+cudaError_t upload(T *dst, const T *src, size_t count) {
+    if (count == 0) return cudaSuccess;
+    return cudaMemcpy(dst, src, count * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+struct BufferRef {
+    void *ptr;
+    size_t bytes;
+};
+
+bool buffer_ref(const mfem_plan *p, int which, BufferRef &ref) {
+    const size_t T = p->T, n = p->n, nnzb = (size_t)p->nnzb;
+    switch (which) {
+        case MFEM_BUF_TET_STRETCH: ref = {p->tv.stretch, T * 6 * 4}; return true;
+        case MFEM_BUF_TET_LAMBDA: ref = {p->tv.lambda, T * 6 * 4}; return true;
+        case MFEM_BUF_CONSTRAINT: ref = {p->tv.c, T * 6 * 4}; return true;
+        case MFEM_BUF_GRAD_CONSTRAINT: ref = {p->tv.G, T * 72 * 4}; return true;
+        case MFEM_BUF_GRAD_S: ref = {p->tv.g_s, T * 6 * 4}; return true;
+        case MFEM_BUF_H_LAMBDA: ref = {p->tv.H_l, T * 21 * 4}; return true;
+        case MFEM_BUF_HESS_S_INV: ref = {p->tv.H_si, T * 21 * 4}; return true;
+        case MFEM_BUF_G_LAMBDA: ref = {p->tv.g_l, T * 6 * 4}; return true;
+        case MFEM_BUF_ELEMENT_HESSIAN: ref = {p->tv.Ke, T * kKeFloats * 4}; return true;
+        case MFEM_BUF_ELEMENT_RHS: ref = {p->tv.fe, T * kFeFloats * 4}; return true;
+        case MFEM_BUF_ROW_PTR: ref = {(void *)p->bv.row_ptr, (n + 1) * 4}; return true;
+        case MFEM_BUF_COL_IDX: ref = {(void *)p->bv.col_idx, nnzb * 4}; return true;
+        case MFEM_BUF_TET_SLOTS: ref = {p->tet_slots, T * 16 * 4}; return true;
+        case MFEM_BUF_H_VALUES: ref = {p->bv.values, nnzb * 9 * 4}; return true;
+        case MFEM_BUF_RHS: ref = {p->vv.rhs, n * 3 * 4}; return true;
+        case MFEM_BUF_PRECOND: ref = {p->vv.Minv, n * 9 * 4}; return true;
+        case MFEM_BUF_X_TILDE: ref = {p->vv.x_tilde, n * 3 * 4}; return true;
+        case MFEM_BUF_DX: ref = {p->vv.dx, n * 3 * 4}; return true;
+        default: return false;
+    }
+}
+
+bool valid_config(const mfem_config *cfg, std::string &err) {
+    if (cfg->iterations < 0 || cfg->iterations > 4096) err = "iterations must be in [0, 4096]";
+    else if (cfg->energy != MFEM_ENERGY_ARAP && cfg->energy != MFEM_ENERGY_NEOHOOKEAN) err = "unknown energy";
+    else if (cfg->cg_max_iterations < 0) err = "cg_max_iterations must be >= 0";
+    else if (!(cfg->cg_tolerance >= 0.0f) || !std::isfinite(cfg->cg_tolerance)) err = "cg_tolerance must be finite and >= 0";
+    else if (!std::isfinite(cfg->attachment_stiffness) || cfg->attachment_stiffness < 0.0f)
+        err = "attachment_stiffness must be finite and >= 0";
+    else if (!(cfg->preconditioner_singular_threshold >= 0.0f)) err = "preconditioner_singular_threshold must be >= 0";
+    else if (cfg->pcg_ctas < 0) err = "pcg_ctas must be >= 0";
+    else return true;
+    return false;
+}
+
+// The whole step as a launch sequence on one stream.
+cudaError_t run_step(mfem_plan *p, const float *q_in, const float *qd_in, float *q_out, float *qd_out, float dt,
+                     cudaStream_t s) {
+    cudaError_t err = launch_predict(q_in, qd_in, q_out, p->gravity, dt, p->vv, s);
+    for (int it = 0; err == cudaSuccess && it < p->cfg.iterations; ++it) {
+        err = launch_element(q_out, p->cfg.energy, p->tv, s);
+        if (err == cudaSuccess)
+            err = launch_assemble(q_out, dt, p->cfg.preconditioner_singular_threshold, p->cfg.preconditioner, p->tv,
+                                  p->vv, p->bv, s);
+        if (err == cudaSuccess)
+            err = launch_pcg(p->bv, p->vv, p->pw, p->pcg_ctas, it, p->cfg.cg_tolerance, p->cfg.cg_max_iterations,
+                             p->cfg.preconditioner, s);
+        if (err == cudaSuccess) err = launch_local_solve(q_out, p->tv, p->vv, s);
+    }
+    if (err == cudaSuccess) err = launch_velocity(q_out, qd_out, dt, p->vv, s);
+    return err;
+}
+
+uint64_t count_kernel_nodes(cudaGraph_t g) {
+    size_t num = 0;
+    if (cudaGraphGetNodes(g, nullptr, &num) != cudaSuccess || num == 0) return 0;
+    std::vector<cudaGraphNode_t> nodes(num);
+    if (cudaGraphGetNodes(g, nodes.data(), &num) != cudaSuccess) return 0;
+    uint64_t k = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType ty;
+        if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
+}
+
+}  // namespace
+
+extern "C" {
+
+void mfem_config_default(mfem_config *cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->iterations = 8;
+    cfg->energy = MFEM_ENERGY_ARAP;
+    cfg->cg_max_iterations = 1000;
+    cfg->cg_tolerance = 1.0e-6f;
+    cfg->attachment_stiffness = 10.0f;
+    cfg->preconditioner_singular_threshold = 1.0e-20f;
+    cfg->preconditioner = 1;
+    cfg->use_cuda_graph = 1;
+    cfg->pcg_ctas = 0;
+}
+
+const char *mfem_status_string(int status) {
+    switch (status) {
+        case MFEM_OK: return "ok";
+        case MFEM_MAXITER: return "PCG reached cg_max_iterations";
+        case MFEM_STAGNATION: return "PCG broke down (p.Ap <= 0)";
+        case MFEM_NONFINITE: return "non-finite value in the PCG";
+        case MFEM_BAD_ARG: return "invalid argument";
+        case MFEM_CUDA_ERROR: return "CUDA error";
+        case MFEM_TIMEOUT: return "device-side wait timed out";
+        default: return "unknown status";
+    }
+}
+
+uint64_t mfem_kernel_launch_count(void) { return g_launches.load(); }
+
+int mfem_bsr_sparsity(int32_t n_particles, int32_t n_tets, const int32_t *h_tet_indices, int32_t *h_row_ptr,
+                      int32_t *h_col_idx, int64_t *nnzb) {
+    std::vector<int32_t> rp, ci;
+    std::string err;
+    if (!build_sparsity(n_particles, n_tets, h_tet_indices, rp, ci, err)) return fail(nullptr, MFEM_BAD_ARG, err);
+    if (nnzb) *nnzb = (int64_t)ci.size();
+    if (h_row_ptr) std::memcpy(h_row_ptr, rp.data(), rp.size() * sizeof(int32_t));
+    if (h_col_idx && !ci.empty()) std::memcpy(h_col_idx, ci.data(), ci.size() * sizeof(int32_t));
+    return MFEM_OK;
+}
+
+int mfem_tet_slot_map(int32_t n_particles, int32_t n_tets, const int32_t *h_tet_indices, const int32_t *h_row_ptr,
+                      const int32_t *h_col_idx, int32_t *h_slots) {
+    if (n_tets > 0 && (!h_row_ptr || !h_col_idx || !h_slots)) return fail(nullptr, MFEM_BAD_ARG, "NULL argument");
+    std::string err;
+    if (!build_slot_map(n_particles, n_tets, h_tet_indices, h_row_ptr, h_col_idx, h_slots, err))
+        return fail(nullptr, MFEM_BAD_ARG, err);
+    return MFEM_OK;
+}
+
+void mfem_plan_destroy(mfem_plan *p) {
+    if (!p) return;
+    {
+        DeviceGuard g(p->device);
+        for (auto &ge : p->graphs)
+            if (ge.exec) cudaGraphExecDestroy(ge.exec);
+        if (p->capture_stream) cudaStreamDestroy(p->capture_stream);
+        for (void *a : p->allocs) cudaFree(a);
+    }
+    delete p;
+}
+
+int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int32_t *h_tets, const float *h_poses,
+                     const float *h_materials, const float *h_rest_q, const float *h_mass, const float *h_inv_mass,
+                     const float *h_gravity, int32_t device, mfem_plan **out) {
+    t_create_error.clear();
+    if (!out) return fail(nullptr, MFEM_BAD_ARG, "out is NULL");
+    *out = nullptr;
+    mfem_config cfg;
+    if (cfg_in) cfg = *cfg_in;
+    else mfem_config_default(&cfg);
+    std::string err;
+    if (!valid_config(&cfg, err)) return fail(nullptr, MFEM_BAD_ARG, err);
+    if (n <= 0) return fail(nullptr, MFEM_BAD_ARG, "n_particles must be > 0");
+    if (T < 0) return fail(nullptr, MFEM_BAD_ARG, "n_tets must be >= 0");
+    if ((T > 0 && (!h_tets || !h_poses || !h_materials)) || !h_rest_q || !h_mass || !h_inv_mass || !h_gravity)
+        return fail(nullptr, MFEM_BAD_ARG, "NULL model array");
+    for (int v = 0; v < n; ++v)
+        if (!(h_inv_mass[v] >= 0.0f) || !std::isfinite(h_inv_mass[v]))
+            return fail(nullptr, MFEM_BAD_ARG, "particle_inv_mass must be finite and >= 0");
+
+    Symbolic sym;
+    if (!build_sparsity(n, T, h_tets, sym.row_ptr, sym.col_idx, err)) return fail(nullptr, MFEM_BAD_ARG, err);
+    sym.tet_slots.resize((size_t)T * 16);
+    if (!build_slot_map(n, T, h_tets, sym.row_ptr.data(), sym.col_idx.data(), sym.tet_slots.data(), err))
+        return fail(nullptr, MFEM_BAD_ARG, err);
+    if (!build_contributions(n, T, h_tets, sym.row_ptr.data(), sym.tet_slots.data(), sym, err))
+        return fail(nullptr, MFEM_BAD_ARG, err);
+
+    // (M + Q) diagonal: Hessian mass is identity on attached vertices and
+    // I / inv_mass elsewhere (kernels.py:21-27); Q = k I on attached ones
+    // (boundary_condition.py:18-42); summed in float32 like bsr_axpy.
+    std::vector<float> hess_diag(n), pin_k(n);
+    for (int v = 0; v < n; ++v) {
+        const bool att = h_inv_mass[v] == 0.0f;
+        const float m_h = att ? 1.0f : 1.0f / h_inv_mass[v];
+        pin_k[v] = att ? cfg.attachment_stiffness : 0.0f;
+        hess_diag[v] = att ? (m_h + cfg.attachment_stiffness) : m_h;
+    }
+
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || device < 0 || device >= dev_count)
+        return fail(nullptr, MFEM_BAD_ARG, "no such CUDA device");
+    DeviceGuard guard(device);
+    if (!guard.ok) return fail(nullptr, MFEM_CUDA_ERROR, "cudaSetDevice failed");
+
+    mfem_plan *p = new mfem_plan();
+    p->cfg = cfg;
+    p->device = device;
+    p->n = n;
+    p->T = T;
+    p->nnzb = (int64_t)sym.col_idx.size();
+    p->max_stats = cfg.iterations > 0 ? cfg.iterations : 1;
+    for (int a = 0; a < 3; ++a) p->gravity[a] = h_gravity[a];
+
+    const size_t nT = T, nn = n, nz = (size_t)p->nnzb;
+    const int n_chunks = (int)sym.chunk_ptr.size() - 1;
+    cudaError_t e = cudaSuccess;
+    int4 *tets = nullptr;
+    float *dminv = nullptr, *materials = nullptr, *mass = nullptr, *hd = nullptr, *pk = nullptr, *pt = nullptr;
+    int32_t *row_ptr = nullptr, *col_idx = nullptr, *chunk_ptr = nullptr, *ccode = nullptr, *cslot = nullptr;
+    float *rest = nullptr;
+#define ALLOC(ptr, count)                                  \
+    if (e == cudaSuccess) e = dev_alloc(p, &(ptr), (count));
+    ALLOC(tets, nT);
+    ALLOC(dminv, nT * 9);
+    ALLOC(materials, nT * 3);
+    ALLOC(p->tv.stretch, nT * 6);
+    ALLOC(p->tv.lambda, nT * 6);
+    ALLOC(p->tv.c, nT * 6);
+    ALLOC(p->tv.G, nT * 72);
+    ALLOC(p->tv.g_s, nT * 6);
+    ALLOC(p->tv.H_l, nT * 21);
+    ALLOC(p->tv.H_si, nT * 21);
+    ALLOC(p->tv.g_l, nT * 6);
+    ALLOC(p->tv.Ke, nT * kKeFloats);
+    ALLOC(p->tv.fe, nT * kFeFloats);
+    ALLOC(p->tet_slots, nT * 16);
+    ALLOC(mass, nn);
+    ALLOC(hd, nn);
+    ALLOC(pk, nn);
+    ALLOC(pt, nn * 3);
+    ALLOC(rest, nn * 3);
+    ALLOC(p->vv.x_tilde, nn * 3);
+    ALLOC(p->vv.x_start, nn * 3);
+    ALLOC(p->vv.rhs, nn * 3);
+    ALLOC(p->vv.dx, nn * 3);
+    ALLOC(p->vv.Minv, nn * 9);
+    ALLOC(row_ptr, nn + 1);
+    ALLOC(col_idx, nz);
+    ALLOC(p->bv.values, nz * 9);
+    ALLOC(chunk_ptr, (size_t)n_chunks + 1);
+    ALLOC(ccode, sym.contrib_code.size());
+    ALLOC(cslot, sym.contrib_slot.size());
+    ALLOC(p->pw.r, nn * 3);
+    ALLOC(p->pw.z, nn * 3);
+    ALLOC(p->pw.p, nn * 3);
+    ALLOC(p->pw.Ap, nn * 3);
+    ALLOC(p->pw.barrier, 1);
+    ALLOC(p->pw.error, 1);
+    ALLOC(p->pw.stats, (size_t)p->max_stats);
+    ALLOC(p->resid, 2);
+#undef ALLOC
+    if (e != cudaSuccess) {
+        int rc = cuda_fail(nullptr, e, "cudaMalloc");
+        mfem_plan_destroy(p);
+        return rc;
+    }
+    int max_ctas = 1;
+    e = pcg_max_ctas(device, &max_ctas);
+    if (e == cudaSuccess) {
+        int want = cfg.pcg_ctas > 0 ? cfg.pcg_ctas : std::max(1, std::min(max_ctas, (n + 63) / 64));
+        p->pcg_ctas = std::max(1, std::min(want, max_ctas));
+        e = dev_alloc(p, &p->pw.partials, (size_t)2 * p->pcg_ctas * 4);
+    }
+    if (e == cudaSuccess) e = upload(tets, reinterpret_cast<const int4 *>(h_tets), nT);
+    if (e == cudaSuccess) e = upload(dminv, h_poses, nT * 9);
+    if (e == cudaSuccess) e = upload(materials, h_materials, nT * 3);
+    if (e == cudaSuccess) e = upload(p->tet_slots, sym.tet_slots.data(), nT * 16);
+    if (e == cudaSuccess) e = upload(mass, h_mass, nn);
+    if (e == cudaSuccess) e = upload(hd, hess_diag.data(), nn);
+    if (e == cudaSuccess) e = upload(pk, pin_k.data(), nn);
+    if (e == cudaSuccess) e = upload(pt, h_rest_q, nn * 3);
+    if (e == cudaSuccess) e = upload(rest, h_rest_q, nn * 3);
+    if (e == cudaSuccess) e = upload(row_ptr, sym.row_ptr.data(), nn + 1);
+    if (e == cudaSuccess) e = upload(col_idx, sym.col_idx.data(), nz);
+    if (e == cudaSuccess) e = upload(chunk_ptr, sym.chunk_ptr.data(), (size_t)n_chunks + 1);
+    if (e == cudaSuccess) e = upload(ccode, sym.contrib_code.data(), sym.contrib_code.size());
+    if (e == cudaSuccess) e = upload(cslot, sym.contrib_slot.data(), sym.contrib_slot.size());
+    if (e == cudaSuccess) e = cudaMemset(p->pw.barrier, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(p->pw.error, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(p->pw.stats, 0, sizeof(SolveStats) * p->max_stats);
+    if (e == cudaSuccess) e = cudaMemset(p->vv.dx, 0, nn * 3 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(p->bv.values, 0, nz * 9 * sizeof(float));
+    if (e != cudaSuccess) {
+        int rc = cuda_fail(nullptr, e, "plan upload");
+        mfem_plan_destroy(p);
+        return rc;
+    }
+    p->tv.n_tets = T;
+    p->tv.tets = tets;
+    p->tv.dminv = dminv;
+    p->tv.materials = materials;
+    p->vv.n = n;
+    p->vv.mass = mass;
+    p->vv.hess_diag = hd;
+    p->vv.pin_k = pk;
+    p->vv.pin_target = pt;
+    p->bv.n = n;
+    p->bv.nnzb = p->nnzb;
+    p->bv.row_ptr = row_ptr;
+    p->bv.col_idx = col_idx;
+    p->bv.n_chunks = n_chunks;
+    p->bv.chunk_ptr = chunk_ptr;
+    p->bv.contrib_code = ccode;
+    p->bv.contrib_slot = cslot;
+
+    // s = S(F) at rest, lambda = 0 (additional_state.py:146-189)
+    e = launch_initial_stretch(rest, p->tv, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        int rc = cuda_fail(nullptr, e, "plan initialisation");
+        mfem_plan_destroy(p);
+        return rc;
+    }
+    *out = p;
+    return MFEM_OK;
+}
+
+const char *mfem_plan_last_error(const mfem_plan *p) { return p ? p->last_error.c_str() : t_create_error.c_str(); }
+
+int mfem_plan_sizes(const mfem_plan *p, int32_t *n, int32_t *T, int64_t *nnzb) {
+    if (!p) return MFEM_BAD_ARG;
+    if (n) *n = p->n;
+    if (T) *T = p->T;
+    if (nnzb) *nnzb = p->nnzb;
+    return MFEM_OK;
+}
+
+int mfem_plan_buffer_bytes(const mfem_plan *p, int32_t which, size_t *bytes) {
+    if (!p || !bytes) return MFEM_BAD_ARG;
+    BufferRef ref;
+    if (!buffer_ref(p, which, ref)) return fail(const_cast<mfem_plan *>(p), MFEM_BAD_ARG, "unknown buffer");
+    *bytes = ref.bytes;
+    return MFEM_OK;
+}
+
+int mfem_plan_copy_out(const mfem_plan *pc, int32_t which, void *dst, size_t bytes, mfem_stream stream) {
+    mfem_plan *p = const_cast<mfem_plan *>(pc);
+    if (!p) return MFEM_BAD_ARG;
+    BufferRef ref;
+    if (!buffer_ref(p, which, ref)) return fail(p, MFEM_BAD_ARG, "unknown buffer");
+    if (bytes != ref.bytes) return fail(p, MFEM_BAD_ARG, "byte count does not match the buffer");
+    if (bytes == 0) return MFEM_OK;
+    if (!dst) return fail(p, MFEM_BAD_ARG, "dst is NULL");
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaMemcpyAsync(dst, ref.ptr, bytes, cudaMemcpyDefault, (cudaStream_t)stream);
+    return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "copy_out");
+}
+
+int mfem_plan_copy_in(mfem_plan *p, int32_t which, const void *src, size_t bytes, mfem_stream stream) {
+    if (!p) return MFEM_BAD_ARG;
+    BufferRef ref;
+    if (!buffer_ref(p, which, ref)) return fail(p, MFEM_BAD_ARG, "unknown buffer");
+    if (which == MFEM_BUF_ROW_PTR || which == MFEM_BUF_COL_IDX || which == MFEM_BUF_TET_SLOTS)
+        return fail(p, MFEM_BAD_ARG, "the sparsity and slot map are read-only");
+    if (bytes != ref.bytes) return fail(p, MFEM_BAD_ARG, "byte count does not match the buffer");
+    if (bytes == 0) return MFEM_OK;
+    if (!src) return fail(p, MFEM_BAD_ARG, "src is NULL");
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaMemcpyAsync(ref.ptr, src, bytes, cudaMemcpyDefault, (cudaStream_t)stream);
+    return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "copy_in");
+}
+
+int mfem_step(mfem_plan *p, const float *q_in, const float *qd_in, float *q_out, float *qd_out, float dt,
+              mfem_stream stream_) {
+    if (!p) return MFEM_BAD_ARG;
+    if (!q_in || !qd_in || !q_out || !qd_out) return fail(p, MFEM_BAD_ARG, "NULL state pointer");
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(p, MFEM_BAD_ARG, "dt must be finite and > 0");
+    if ((const void *)qd_in == (const void *)q_out || (const void *)q_in == (const void *)qd_out)
+        return fail(p, MFEM_BAD_ARG, "positions and velocities must not alias");
+    cudaStream_t stream = (cudaStream_t)stream_;
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaSuccess;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (stream) e = cudaStreamIsCapturing(stream, &cap);
+    if (e != cudaSuccess) return cuda_fail(p, e, "cudaStreamIsCapturing");
+    if (p->cfg.use_cuda_graph && cap == cudaStreamCaptureStatusNone) {
+        const void *key[4] = {q_in, qd_in, q_out, qd_out};
+        mfem_plan::GraphEntry *ge = nullptr;
+        for (auto &cand : p->graphs) {
+            bool hit = cand.exec && cand.dt == dt;
+            for (int i = 0; i < 4 && hit; ++i) hit = cand.key[i] == key[i];
+            if (hit) {
+                ge = &cand;
+                break;
+            }
+        }
+        if (!ge) {
+            ge = &p->graphs[0];
+            for (auto &cand : p->graphs)
+                if (!cand.exec || cand.last_use < ge->last_use) ge = &cand;
+            if (ge->exec) {
+                cudaGraphExecDestroy(ge->exec);
+                ge->exec = nullptr;
+            }
+            cudaGraph_t graph = nullptr;
+            t_capturing = true;
+            e = cudaStreamBeginCapture(p->capture_stream, cudaStreamCaptureModeThreadLocal);
+            cudaError_t run_err = cudaSuccess;
+            if (e == cudaSuccess) {
+                run_err = run_step(p, q_in, qd_in, q_out, qd_out, dt, p->capture_stream);
+                e = cudaStreamEndCapture(p->capture_stream, &graph);
+            }
+            t_capturing = false;
+            if (e == cudaSuccess && run_err != cudaSuccess) e = run_err;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&ge->exec, graph, 0);
+            if (graph) {
+                ge->kernels = count_kernel_nodes(graph);
+                cudaGraphDestroy(graph);
+            }
+            if (e != cudaSuccess) {
+                ge->exec = nullptr;
+                cudaGetLastError();
+                return cuda_fail(p, e, "step graph capture");
+            }
+            for (int i = 0; i < 4; ++i) ge->key[i] = key[i];
+            ge->dt = dt;
+        }
+        ge->last_use = ++p->graph_clock;
+        e = cudaGraphLaunch(ge->exec, stream);
+        if (e != cudaSuccess) return cuda_fail(p, e, "cudaGraphLaunch");
+        count_launches(ge->kernels);
+        return MFEM_OK;
+    }
+    e = run_step(p, q_in, qd_in, q_out, qd_out, dt, stream);
+    return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "step launch");
+}
+
+int mfem_step_stats(mfem_plan *p, mfem_solve_stats *h_stats, int32_t max_entries, int32_t *count,
+                    mfem_stream stream) {
+    if (!p || (max_entries > 0 && !h_stats)) return MFEM_BAD_ARG;
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(p, e, "cudaStreamSynchronize");
+    const int k = std::max(0, std::min<int>(max_entries, p->cfg.iterations));
+    std::vector<SolveStats> tmp(p->max_stats);
+    e = cudaMemcpy(tmp.data(), p->pw.stats, sizeof(SolveStats) * p->max_stats, cudaMemcpyDeviceToHost);
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&flag, p->pw.error, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(p, e, "stats readback");
+    for (int i = 0; i < k; ++i) std::memcpy(&h_stats[i], &tmp[i], sizeof(mfem_solve_stats));
+    if (count) *count = k;
+    if (flag) {
+        // a bounded wait gave up: re-arm the barrier for the next solve
+        cudaMemset(p->pw.barrier, 0, sizeof(unsigned long long));
+        cudaMemset(p->pw.error, 0, sizeof(int));
+        return fail(p, MFEM_TIMEOUT, "a PCG grid barrier timed out");
+    }
+    return MFEM_OK;
+}
+
+int mfem_predict(mfem_plan *p, const float *q, const float *qd, float dt, mfem_stream stream) {
+    if (!p) return MFEM_BAD_ARG;
+    if (!q || !qd) return fail(p, MFEM_BAD_ARG, "NULL state pointer");
+    DeviceGuard g(p->device);
+    // the predictor also snapshots x and copies it to q_out; pass x_start as
+    // the output so the caller's q is left untouched
+    cudaError_t e = launch_predict(q, qd, p->vv.x_start, p->gravity, dt, p->vv, (cudaStream_t)stream);
+    return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "predict");
+}
+
+int mfem_update_system(mfem_plan *p, const float *x, mfem_stream stream) {
+    if (!p) return MFEM_BAD_ARG;
+    if (!x) return fail(p, MFEM_BAD_ARG, "x is NULL");
+    DeviceGuard g(p->device);
+    cudaError_t e = launch_element(x, p->cfg.energy, p->tv, (cudaStream_t)stream);
+    return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "update_system");
+}
+
+int mfem_assemble(mfem_plan *p, const float *x, float dt, mfem_stream stream) {
+    if (!p) return MFEM_BAD_ARG;
+    if (!x) return fail(p, MFEM_BAD_ARG, "x is NULL");
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(p, MFEM_BAD_ARG, "dt must be finite and > 0");
+    DeviceGuard g(p->device);
+    cudaError_t e = launch_assemble(x, dt, p->cfg.preconditioner_singular_threshold, p->cfg.preconditioner, p->tv,
+                                   p->vv, p->bv, (cudaStream_t)stream);
+    return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "assemble");
+}
+
+int mfem_global_solve(mfem_plan *p, int32_t slot, mfem_stream stream) {
+    if (!p) return MFEM_BAD_ARG;
+    if (slot < 0 || slot >= p->max_stats) return fail(p, MFEM_BAD_ARG, "stats slot out of range");
+    DeviceGuard g(p->device);
+    cudaError_t e = launch_pcg(p->bv, p->vv, p->pw, p->pcg_ctas, slot, p->cfg.cg_tolerance,
+                               p->cfg.cg_max_iterations, p->cfg.preconditioner, (cudaStream_t)stream);
+    return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "global_solve");
+}
+
+int mfem_local_solve(mfem_plan *p, float *x, mfem_stream stream) {
+    if (!p) return MFEM_BAD_ARG;
+    if (!x) return fail(p, MFEM_BAD_ARG, "x is NULL");
+    DeviceGuard g(p->device);
+    cudaError_t e = launch_local_solve(x, p->tv, p->vv, (cudaStream_t)stream);
+    return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "local_solve");
+}
+
+int mfem_true_residual(mfem_plan *p, double *h_rel, mfem_stream stream) {
+    if (!p || !h_rel) return MFEM_BAD_ARG;
+    DeviceGuard g(p->device);
+    cudaError_t e = launch_true_residual(p->bv, p->vv, p->resid, (cudaStream_t)stream);
+    double out[2] = {0.0, 0.0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, p->resid, sizeof(out), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(p, e, "true_residual");
+    *h_rel = out[1] > 0.0 ? std::sqrt(out[0] / out[1]) : std::sqrt(out[0]);
+    return MFEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,266 @@
+// Per-tet and per-vertex kernels of the global step.
+//
+//  element_kernel      one thread per tet: the reference's compute_constraints,
+//                      energy gradient/Hessian in s, compute_H_lmbda_blocks,
+//                      compute_g_lmbda and compute_H_lmbda_G_x_blocks fused,
+//                      plus the element blocks G^T H_l G and rhs (H_l G)^T g_l
+//                      that the assembly gathers.
+//  local_solve_kernel  tets: local_solve_lambda + local_solve_stretch + s += ds;
+//                      vertices: x += dx  (one launch, two index ranges).
+//  predict_kernel      integrate_particles + state_out.assign(state_in).
+//  velocity_kernel     get_particle_velocity.
+#include "element_math.cuh"
+#include "internal.h"
+
+namespace mfem {
+namespace {
+
+constexpr int kElementThreads = 128;
+constexpr int kVertexThreads = 256;
+
+__device__ __forceinline__ void load_vec3(const float *__restrict__ p, int i, float v[3]) {
+    v[0] = p[3 * i + 0];
+    v[1] = p[3 * i + 1];
+    v[2] = p[3 * i + 2];
+}
+
+__global__ void __launch_bounds__(kElementThreads)
+    element_kernel(const float *__restrict__ x, int energy, TetViews tv) {
+    const int T = tv.n_tets;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    const int4 tt = tv.tets[t];
+    float xv[4][3];
+    load_vec3(x, tt.x, xv[0]);
+    load_vec3(x, tt.y, xv[1]);
+    load_vec3(x, tt.z, xv[2]);
+    load_vec3(x, tt.w, xv[3]);
+    float Dm[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) Dm[i][j] = tv.dminv[(size_t)t * 9 + i * 3 + j];
+    float s[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) s[i] = tv.stretch[(size_t)t * 6 + i];
+    const float mu = tv.materials[(size_t)t * 3 + 0];
+    const float lam = tv.materials[(size_t)t * 3 + 1];
+    // rest volume 1/(6 det DmInv) (elastic_energy.py:143-145)
+    const float vol = 1.0f / (6.0f * em::det3(Dm));
+
+    float g_s[6], H_l[21], H_si[21];
+    em::energy_terms(energy, s, mu, lam, vol, g_s, H_l, H_si);
+    float hsg[6];  // H_s^-1 g_s
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) acc += H_si[em::p21(i, j)] * g_s[j];
+        hsg[i] = acc;
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) tv.g_s[(size_t)i * T + t] = g_s[i];
+#pragma unroll
+    for (int k = 0; k < 21; ++k) {
+        tv.H_l[(size_t)k * T + t] = H_l[k];
+        tv.H_si[(size_t)k * T + t] = H_si[k];
+    }
+
+    float c[6], G[6][12];
+    em::element_geometry(xv, Dm, s, c, G);
+    float g_l[6];  // c + SYM H_s^-1 g_s (kernels.py:189-205)
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        g_l[i] = c[i] + em::sym_w(i) * hsg[i];
+        tv.c[(size_t)i * T + t] = c[i];
+        tv.g_l[(size_t)i * T + t] = g_l[i];
+    }
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int col = 0; col < 12; ++col) tv.G[(size_t)(r * 12 + col) * T + t] = G[r][col];
+
+    float *Ke = tv.Ke + (size_t)t * kKeFloats;
+    float *fe = tv.fe + (size_t)t * kFeFloats;
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        float P[6][3];  // H_l G_l
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                float acc = 0.0f;
+#pragma unroll
+                for (int j = 0; j < 6; ++j) acc += H_l[em::p21(i, j)] * G[j][3 * l + b];
+                P[i][b] = acc;
+            }
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) acc += P[i][b] * g_l[i];
+            fe[3 * l + b] = acc;
+        }
+#pragma unroll
+        for (int k = 0; k <= l; ++k) {
+            float *blk = Ke + ke_block(k, l) * 9;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) {
+                    float acc = 0.0f;
+#pragma unroll
+                    for (int i = 0; i < 6; ++i) acc += G[i][3 * k + a] * P[i][b];
+                    blk[a * 3 + b] = acc;
+                }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kElementThreads)
+    initial_stretch_kernel(const float *__restrict__ rest_q, TetViews tv) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= tv.n_tets) return;
+    const int4 tt = tv.tets[t];
+    float xv[4][3];
+    load_vec3(rest_q, tt.x, xv[0]);
+    load_vec3(rest_q, tt.y, xv[1]);
+    load_vec3(rest_q, tt.z, xv[2]);
+    load_vec3(rest_q, tt.w, xv[3]);
+    float Dm[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) Dm[i][j] = tv.dminv[(size_t)t * 9 + i * 3 + j];
+    float F[3][3], U[3][3], sig[3], V[3][3], sF[6];
+    em::deformation_gradient(xv, Dm, F);
+    em::polar_svd(F, U, sig, V);
+    em::stretch_sym6(sig, V, sF);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        tv.stretch[(size_t)t * 6 + i] = sF[i];
+        tv.lambda[(size_t)t * 6 + i] = 0.0f;
+    }
+}
+
+__global__ void __launch_bounds__(kVertexThreads)
+    predict_kernel(const float *__restrict__ q_in, const float *__restrict__ qd_in, float *q_out, float gx,
+                   float gy, float gz, float dt, VertexViews vv) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= vv.n) return;
+    const float g[3] = {gx, gy, gz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float q = q_in[3 * v + a];
+        const float qd = qd_in[3 * v + a];
+        vv.x_tilde[3 * v + a] = q + qd * dt + g[a] * dt * dt / 2.0f;
+        vv.x_start[3 * v + a] = q;
+        q_out[3 * v + a] = q;
+    }
+}
+
+__global__ void __launch_bounds__(kVertexThreads)
+    local_solve_kernel(float *x, TetViews tv, VertexViews vv, int tet_blocks) {
+    if ((int)blockIdx.x >= tet_blocks) {
+        const int v = (blockIdx.x - tet_blocks) * blockDim.x + threadIdx.x;
+        if (v >= vv.n) return;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) x[3 * v + a] += vv.dx[3 * v + a];
+        return;
+    }
+    const int T = tv.n_tets;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    const int4 tt = tv.tets[t];
+    const int vid[4] = {tt.x, tt.y, tt.z, tt.w};
+    float lam[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) lam[i] = tv.g_l[(size_t)i * T + t];
+    // lambda -= G_k dx[v_k], block by block (kernels.py:266-268)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float d[3];
+        load_vec3(vv.dx, vid[k], d);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            const float *g = tv.G + (size_t)(i * 12 + 3 * k) * T + t;
+            lam[i] -= g[0] * d[0] + g[(size_t)T] * d[1] + g[(size_t)2 * T] * d[2];
+        }
+    }
+    float Hl[21];
+#pragma unroll
+    for (int k = 0; k < 21; ++k) Hl[k] = tv.H_l[(size_t)k * T + t];
+    float nl[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) acc += Hl[em::p21(i, j)] * lam[j];
+        nl[i] = -acc;
+    }
+    // ds = -H_s^-1 (SYM lambda + g_s) (kernels.py:271-283)
+    float rhs[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) rhs[i] = em::sym_w(i) * nl[i] + tv.g_s[(size_t)i * T + t];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) acc += tv.H_si[(size_t)em::p21(i, j) * T + t] * rhs[j];
+        tv.stretch[(size_t)t * 6 + i] += -acc;
+        tv.lambda[(size_t)t * 6 + i] = nl[i];
+    }
+}
+
+__global__ void __launch_bounds__(kVertexThreads)
+    velocity_kernel(const float *__restrict__ q_out, float *qd_out, float dt, VertexViews vv) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= vv.n) return;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) qd_out[3 * v + a] = (q_out[3 * v + a] - vv.x_start[3 * v + a]) / dt;
+}
+
+inline int blocks_for(int n, int threads) { return (n + threads - 1) / threads; }
+
+}  // namespace
+
+cudaError_t launch_initial_stretch(const float *rest_q, const TetViews &tv, cudaStream_t s) {
+    if (tv.n_tets == 0) return cudaSuccess;
+    initial_stretch_kernel<<<blocks_for(tv.n_tets, kElementThreads), kElementThreads, 0, s>>>(rest_q, tv);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_predict(const float *q_in, const float *qd_in, float *q_out, const float *gravity, float dt,
+                           const VertexViews &vv, cudaStream_t s) {
+    if (vv.n == 0) return cudaSuccess;
+    predict_kernel<<<blocks_for(vv.n, kVertexThreads), kVertexThreads, 0, s>>>(q_in, qd_in, q_out, gravity[0],
+                                                                               gravity[1], gravity[2], dt, vv);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_element(const float *x, int energy, const TetViews &tv, cudaStream_t s) {
+    if (tv.n_tets == 0) return cudaSuccess;
+    element_kernel<<<blocks_for(tv.n_tets, kElementThreads), kElementThreads, 0, s>>>(x, energy, tv);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_local_solve(float *x, const TetViews &tv, const VertexViews &vv, cudaStream_t s) {
+    const int tb = blocks_for(tv.n_tets, kVertexThreads);
+    const int vb = blocks_for(vv.n, kVertexThreads);
+    if (tb + vb == 0) return cudaSuccess;
+    local_solve_kernel<<<tb + vb, kVertexThreads, 0, s>>>(x, tv, vv, tb);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_velocity(const float *q_out, float *qd_out, float dt, const VertexViews &vv, cudaStream_t s) {
+    if (vv.n == 0) return cudaSuccess;
+    velocity_kernel<<<blocks_for(vv.n, kVertexThreads), kVertexThreads, 0, s>>>(q_out, qd_out, dt, vv);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+}  // namespace mfem

@@ -1,0 +1,122 @@
+// Internal definitions shared by the translation units of libmfem_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "mfem_gb300.h"
+
+namespace mfem {
+
+// Element Hessian blocks kept per tet: the upper (k <= l) 3x3 blocks of the
+// symmetric 12x12 G^T H_lambda G, numbered row by row:
+//   0:(0,0) 1:(0,1) 2:(0,2) 3:(0,3) 4:(1,1) 5:(1,2) 6:(1,3) 7:(2,2) 8:(2,3) 9:(3,3)
+constexpr int kKeBlocks = 10;
+constexpr int kKeFloats = kKeBlocks * 9;
+constexpr int kFeFloats = 12;
+
+__host__ __device__ __forceinline__ int ke_block(int k, int l) {
+    // k <= l
+    return k * 4 - (k * (k - 1)) / 2 + (l - k);
+}
+
+// Packed upper triangle of a symmetric 6x6, row-major: (0,0)..(0,5),(1,1)..(5,5).
+__host__ __device__ __forceinline__ constexpr int sym6_index(int i, int j) {
+    return (i <= j) ? (i * 6 - (i * (i - 1)) / 2 + (j - i)) : (j * 6 - (j * (j - 1)) / 2 + (i - j));
+}
+
+// Per-solve outcome written by the PCG kernel (same layout as mfem_solve_stats).
+struct SolveStats {
+    int32_t iterations;
+    int32_t status;
+    float rel_residual;
+    float reserved;
+};
+
+// Device views used by the kernels.  All arrays are owned by the plan.
+struct TetViews {
+    int n_tets;
+    const int4 *tets;          // [T]
+    const float *dminv;        // [T][9] row-major DmInv
+    const float *materials;    // [T][3] (mu, lambda, damping)
+    float *stretch;            // [T][6] s
+    float *lambda;             // [T][6]
+    // per-tet Newton terms, component-major [k][T]
+    float *c;                  // [6][T]
+    float *G;                  // [72][T]
+    float *g_s;                // [6][T]
+    float *H_l;                // [21][T]
+    float *H_si;               // [21][T]
+    float *g_l;                // [6][T]
+    // element contributions gathered by the assembly, tet-major
+    float *Ke;                 // [T][90]
+    float *fe;                 // [T][12]
+};
+
+struct VertexViews {
+    int n;
+    const float *mass;         // [n] particle_mass (kinetic gradient)
+    const float *hess_diag;    // [n] Hessian mass + attachment stiffness, (M+Q) diagonal
+    const float *pin_k;        // [n] attachment stiffness (0 if free)
+    const float *pin_target;   // [n][3]
+    float *x_tilde;            // [n][3]
+    float *x_start;            // [n][3]
+    float *rhs;                // [n][3]
+    float *dx;                 // [n][3]
+    float *Minv;               // [n][9]
+};
+
+struct BsrViews {
+    int n;
+    int64_t nnzb;
+    const int *row_ptr;        // [n+1]
+    const int *col_idx;        // [nnzb]
+    float *values;             // [nnzb][9]
+    // contribution lists sorted by slot, packed into warp-sized chunks
+    int n_chunks;
+    const int *chunk_ptr;      // [n_chunks+1]
+    const int *contrib_code;   // e*16 + k*4 + l, or -(row+1) for an empty diagonal
+    const int *contrib_slot;   // slot of each contribution
+};
+
+struct PcgWork {
+    float *r, *z, *p, *Ap;     // [n][3]
+    double *partials;          // [2][ctas][4]
+    unsigned long long *barrier;
+    int *error;                // sticky device error flag (timeouts)
+    SolveStats *stats;         // [max solves per step]
+};
+
+// Host-side symbolic analysis (symbolic.cpp).
+struct Symbolic {
+    std::vector<int32_t> row_ptr, col_idx, tet_slots;
+    std::vector<int32_t> chunk_ptr, contrib_code, contrib_slot;
+};
+bool build_sparsity(int n, int T, const int32_t *tets, std::vector<int32_t> &row_ptr,
+                    std::vector<int32_t> &col_idx, std::string &err);
+bool build_slot_map(int n, int T, const int32_t *tets, const int32_t *row_ptr, const int32_t *col_idx,
+                    int32_t *slots, std::string &err);
+bool build_contributions(int n, int T, const int32_t *tets, const int32_t *row_ptr,
+                         const int32_t *slots, Symbolic &sym, std::string &err);
+
+// Kernel launchers (each returns cudaGetLastError()).
+cudaError_t launch_initial_stretch(const float *rest_q, const TetViews &tv, cudaStream_t s);
+cudaError_t launch_predict(const float *q_in, const float *qd_in, float *q_out, const float *gravity_dev,
+                           float dt, const VertexViews &vv, cudaStream_t s);
+cudaError_t launch_element(const float *x, int energy, const TetViews &tv, cudaStream_t s);
+cudaError_t launch_assemble(const float *x, float dt, float singular_threshold, int use_precond,
+                            const TetViews &tv, const VertexViews &vv, const BsrViews &bv, cudaStream_t s);
+cudaError_t launch_local_solve(float *x, const TetViews &tv, const VertexViews &vv, cudaStream_t s);
+cudaError_t launch_velocity(const float *q_out, float *qd_out, float dt, const VertexViews &vv, cudaStream_t s);
+cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, int ctas, int slot,
+                       float tol, int maxiter, int use_precond, cudaStream_t s);
+cudaError_t pcg_max_ctas(int device, int *ctas);
+cudaError_t launch_true_residual(const BsrViews &bv, const VertexViews &vv, double *out3, cudaStream_t s);
+
+// Number of kernels launched by the launchers above (process-wide).
+void count_launches(uint64_t k);
+
+}  // namespace mfem

@@ -1,0 +1,176 @@
+// Host-side symbolic analysis of the global system (run once per mesh).
+//
+// The reference rebuilds padded BSR topologies every Newton iteration with
+// bsr_set_from_triplets and bsr_mm (src/mfem/refinement/solver.py:685-724),
+// sized by a row capacity of 1 + 3 * max incident tets (solver.py:203).  The
+// topology only changes with the mesh, so here it is computed once, exactly:
+//
+//  * the vertex-adjacency sparsity of H, diagonal included, ascending columns;
+//  * the element -> slot map: the slot of block (tets[e][k], tets[e][l]);
+//  * the same map inverted and sorted by slot (then by tet), which the
+//    numeric assembly reduces with warp shuffles; whole slots are packed into
+//    warp-sized chunks so no slot is split between warps.
+#include <algorithm>
+#include <cstring>
+
+#include "internal.h"
+
+namespace mfem {
+
+static bool check_tets(int n, int T, const int32_t *tets, std::string &err) {
+    if (n < 0 || T < 0) {
+        err = "negative particle or tet count";
+        return false;
+    }
+    if (T > 0 && tets == nullptr) {
+        err = "tet_indices is NULL";
+        return false;
+    }
+    if ((int64_t)T * 16 > (int64_t)INT32_MAX) {
+        err = "too many tets for 32-bit contribution codes";
+        return false;
+    }
+    for (int64_t i = 0; i < (int64_t)T * 4; ++i) {
+        if (tets[i] < 0 || tets[i] >= n) {
+            err = "tet_indices[" + std::to_string(i / 4) + "] references vertex " + std::to_string(tets[i]) +
+                  " outside [0, " + std::to_string(n) + ")";
+            return false;
+        }
+    }
+    for (int e = 0; e < T; ++e) {
+        const int32_t *t = tets + 4 * (int64_t)e;
+        for (int a = 0; a < 4; ++a)
+            for (int b = a + 1; b < 4; ++b)
+                if (t[a] == t[b]) {
+                    err = "tet " + std::to_string(e) + " repeats vertex " + std::to_string(t[a]);
+                    return false;
+                }
+    }
+    return true;
+}
+
+bool build_sparsity(int n, int T, const int32_t *tets, std::vector<int32_t> &row_ptr, std::vector<int32_t> &col_idx,
+                    std::string &err) {
+    if (!check_tets(n, T, tets, err)) return false;
+    // candidate columns per row: the diagonal plus 4 per incident tet
+    std::vector<int64_t> cap(n + 1, 0);
+    for (int v = 0; v < n; ++v) cap[v + 1] = 1;
+    for (int64_t i = 0; i < (int64_t)T * 4; ++i) cap[tets[i] + 1] += 4;
+    for (int v = 0; v < n; ++v) cap[v + 1] += cap[v];
+    std::vector<int32_t> cand(cap[n]);
+    std::vector<int64_t> fill(cap.begin(), cap.end() - 1);
+    for (int v = 0; v < n; ++v) cand[fill[v]++] = v;
+    for (int e = 0; e < T; ++e) {
+        const int32_t *t = tets + 4 * (int64_t)e;
+        for (int k = 0; k < 4; ++k)
+            for (int l = 0; l < 4; ++l) cand[fill[t[k]]++] = t[l];
+    }
+    row_ptr.assign(n + 1, 0);
+    col_idx.clear();
+    col_idx.reserve(cap[n] / 2);
+    for (int v = 0; v < n; ++v) {
+        auto b = cand.begin() + cap[v], e = cand.begin() + cap[v + 1];
+        std::sort(b, e);
+        auto u = std::unique(b, e);
+        col_idx.insert(col_idx.end(), b, u);
+        if (col_idx.size() > (size_t)INT32_MAX) {
+            err = "sparsity exceeds 2^31 blocks";
+            return false;
+        }
+        row_ptr[v + 1] = (int32_t)col_idx.size();
+    }
+    return true;
+}
+
+bool build_slot_map(int n, int T, const int32_t *tets, const int32_t *row_ptr, const int32_t *col_idx, int32_t *slots,
+                    std::string &err) {
+    if (!check_tets(n, T, tets, err)) return false;
+    for (int e = 0; e < T; ++e) {
+        const int32_t *t = tets + 4 * (int64_t)e;
+        for (int k = 0; k < 4; ++k) {
+            const int32_t *b = col_idx + row_ptr[t[k]];
+            const int32_t *en = col_idx + row_ptr[t[k] + 1];
+            for (int l = 0; l < 4; ++l) {
+                const int32_t *p = std::lower_bound(b, en, t[l]);
+                if (p == en || *p != t[l]) {
+                    err = "sparsity lacks block (" + std::to_string(t[k]) + ", " + std::to_string(t[l]) + ")";
+                    return false;
+                }
+                slots[(int64_t)e * 16 + k * 4 + l] = (int32_t)(p - col_idx);
+            }
+        }
+    }
+    return true;
+}
+
+bool build_contributions(int n, int T, const int32_t *tets, const int32_t *row_ptr, const int32_t *slots,
+                         Symbolic &sym, std::string &err) {
+    (void)tets;
+    const int64_t nnzb = row_ptr[n];
+    std::vector<int32_t> count(nnzb + 1, 0);
+    for (int64_t i = 0; i < (int64_t)T * 16; ++i) count[slots[i] + 1]++;
+    // a vertex without tets still owns its diagonal block (mass + attachment):
+    // give it one empty contribution so the assembly visits it
+    std::vector<int32_t> isolated;  // vertices in no tet
+    std::vector<int32_t> isolated_slot;
+    for (int v = 0; v < n; ++v) {
+        const int32_t *b = sym.col_idx.data() + row_ptr[v];
+        const int32_t *e = sym.col_idx.data() + row_ptr[v + 1];
+        const int32_t *p = std::lower_bound(b, e, v);
+        if (p == e || *p != v) {
+            err = "sparsity lacks diagonal block of vertex " + std::to_string(v);
+            return false;
+        }
+        const int32_t ds = (int32_t)(p - sym.col_idx.data());
+        if (count[ds + 1] == 0) {
+            count[ds + 1] = 1;
+            isolated.push_back(v);
+            isolated_slot.push_back(ds);
+        }
+    }
+    std::vector<int64_t> start(nnzb + 1, 0);
+    for (int64_t s = 0; s < nnzb; ++s) start[s + 1] = start[s] + count[s + 1];
+    const int64_t total = start[nnzb];
+    if (total > (int64_t)INT32_MAX) {
+        err = "too many contributions";
+        return false;
+    }
+    sym.contrib_code.assign(total, 0);
+    sym.contrib_slot.assign(total, 0);
+    std::vector<int64_t> fill(start.begin(), start.end() - 1);
+    for (size_t i = 0; i < isolated.size(); ++i) {
+        const int32_t s = isolated_slot[i];
+        sym.contrib_code[fill[s]] = -(isolated[i] + 1);
+        sym.contrib_slot[fill[s]] = s;
+        fill[s]++;
+    }
+    for (int e = 0; e < T; ++e)
+        for (int kl = 0; kl < 16; ++kl) {
+            const int32_t s = slots[(int64_t)e * 16 + kl];
+            const int64_t pos = fill[s]++;
+            sym.contrib_code[pos] = e * 16 + kl;
+            sym.contrib_slot[pos] = s;
+        }
+    // pack whole slots into chunks of <= 32 contributions (a longer slot gets
+    // a chunk of its own)
+    sym.chunk_ptr.clear();
+    sym.chunk_ptr.push_back(0);
+    int64_t chunk_len = 0;
+    for (int64_t s = 0; s < nnzb; ++s) {
+        const int64_t len = start[s + 1] - start[s];
+        if (len == 0) continue;
+        if (chunk_len > 0 && chunk_len + len > 32) {
+            sym.chunk_ptr.push_back((int32_t)start[s]);
+            chunk_len = 0;
+        }
+        chunk_len += len;
+        if (chunk_len >= 32) {
+            sym.chunk_ptr.push_back((int32_t)start[s + 1]);
+            chunk_len = 0;
+        }
+    }
+    if (chunk_len > 0) sym.chunk_ptr.push_back((int32_t)total);
+    return true;
+}
+
+}  // namespace mfem

@@ -1,0 +1,210 @@
+"""The reference-facing solver: ``RefinementSolver``'s constructor and
+``step(state_in, state_out, control, contacts, dt)`` over the CUDA library.
+
+Reference: src/mfem/refinement/solver.py:40-579.  Every step runs on the GPU
+through libmfem_gb300 (element kernel, assembly, persistent PCG, local solve,
+replayed as one CUDA graph); there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from .model import Model, State
+
+_OUT_OF_SCOPE_TRUE = {
+    "enable_refinement": "adaptive refinement",
+    "line_search": "the backtracking line search",
+}
+
+
+def _stream_handle(device: torch.device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+class MixedFEMSolver:
+    """Mixed variational FEM global step on one GPU.
+
+    Accepts ``RefinementSolver``'s arguments (src/mfem/refinement/solver.py:41-128).
+    Refinement, line search, contact against rigid shapes and the membrane
+    shell are outside this solver: ``enable_refinement`` / ``line_search``
+    default to False here and raise if set True; ``shell_mu`` must be 0.
+    """
+
+    def __init__(self, model: Model, iterations: int, max_tets: Optional[int] = None,
+                 max_particles: Optional[int] = None, max_tris: Optional[int] = None,
+                 refine_every_n_steps: int = 10, min_refine_score: float = 10.1, **kwargs):
+        for key, what in _OUT_OF_SCOPE_TRUE.items():
+            if kwargs.get(key, False):
+                raise NotImplementedError(f"{key}=True: {what} is not part of this solver")
+        if kwargs.get("shell_mu", 0.0) != 0.0:
+            raise NotImplementedError("shell_mu > 0: the membrane shell is not part of this solver")
+        if max_particles is not None and max_particles != model.particle_count:
+            raise ValueError(
+                f"max_particles={max_particles} does not match model.particle_count={model.particle_count}")
+        if max_tets is not None and max_tets < model.tet_count:
+            raise ValueError(f"max_tets={max_tets} is below model.tet_count={model.tet_count}")
+        energy = kwargs.get("energy", "arap")
+        if energy not in _lib.ENERGY:
+            raise ValueError(f"Unknown energy type: {energy}")
+        if model.device.type != "cuda":
+            raise ValueError("the model must live on a CUDA device")
+
+        self.model = model
+        self.iterations = int(iterations)
+        self.device = model.device
+        self._lib = _lib.load()
+        cfg = _lib.default_config()
+        cfg.iterations = self.iterations
+        cfg.energy = _lib.ENERGY[energy]
+        cfg.cg_max_iterations = int(kwargs.get("cg_max_iterations", 1000))
+        cfg.cg_tolerance = float(kwargs.get("cg_tolerance", 1.0e-6))
+        cfg.attachment_stiffness = float(kwargs.get("attachment_stiffness", 10.0))
+        cfg.preconditioner_singular_threshold = float(kwargs.get("preconditioner_singular_threshold", 1.0e-20))
+        cfg.preconditioner = 1 if kwargs.get("preconditioner", True) else 0
+        cfg.use_cuda_graph = 1 if kwargs.get("use_cuda_graph", True) else 0
+        cfg.pcg_ctas = int(kwargs.get("pcg_ctas", 0))
+        self.config = cfg
+
+        host = lambda t, dt: np.ascontiguousarray(t.detach().to("cpu").numpy(), dtype=dt)
+        self._host = dict(
+            tets=host(model.tet_indices, np.int32), poses=host(model.tet_poses, np.float32),
+            materials=host(model.tet_materials, np.float32), rest=host(model.particle_q, np.float32),
+            mass=host(model.particle_mass, np.float32), inv_mass=host(model.particle_inv_mass, np.float32),
+            gravity=host(model.gravity.reshape(-1)[:3], np.float32))
+        h = self._host
+        plan = ctypes.c_void_p()
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        rc = self._lib.mfem_plan_create(
+            ctypes.byref(cfg), model.particle_count, model.tet_count, P(h["tets"]), P(h["poses"]),
+            P(h["materials"]), P(h["rest"]), P(h["mass"]), P(h["inv_mass"]), P(h["gravity"]),
+            self.device.index if self.device.index is not None else torch.cuda.current_device(), ctypes.byref(plan))
+        if rc != _lib.MFEM_OK:
+            msg = self._lib.mfem_plan_last_error(None).decode()
+            raise _lib.MfemError(rc, f"mfem_plan_create: {msg}")
+        self._plan = plan
+        n = ctypes.c_int32()
+        T = ctypes.c_int32()
+        nnzb = ctypes.c_int64()
+        self._lib.mfem_plan_sizes(plan, ctypes.byref(n), ctypes.byref(T), ctypes.byref(nnzb))
+        self.n, self.T, self.nnzb = n.value, T.value, nnzb.value
+
+    # ------------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_plan", None):
+            self._lib.mfem_plan_destroy(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check_state(self, t: torch.Tensor, name: str) -> int:
+        if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and tuple(t.shape) == (self.n, 3)):
+            raise ValueError(f"{name} must be a contiguous float32 CUDA tensor of shape ({self.n}, 3)")
+        if t.device != self.device:
+            raise ValueError(f"{name} lives on {t.device}, the solver on {self.device}")
+        return t.data_ptr()
+
+    # ------------------------------------------------------------------
+    def step(self, state_in: State, state_out: State, control, contacts, dt: float) -> None:
+        """One implicit-Euler step (src/mfem/refinement/solver.py:429-579): writes
+        state_out.particle_q / particle_qd; state_in is not modified."""
+        q_in = self._check_state(state_in.particle_q, "state_in.particle_q")
+        qd_in = self._check_state(state_in.particle_qd, "state_in.particle_qd")
+        q_out = self._check_state(state_out.particle_q, "state_out.particle_q")
+        qd_out = self._check_state(state_out.particle_qd, "state_out.particle_qd")
+        rc = self._lib.mfem_step(self._plan, q_in, qd_in, q_out, qd_out, float(dt), _stream_handle(self.device))
+        _lib.check(rc, self._plan)
+
+    def solve_stats(self) -> list[dict]:
+        """PCG outcome of each Newton iteration of the last step (synchronises)."""
+        buf = (_lib.MfemSolveStats * max(1, self.iterations))()
+        count = ctypes.c_int32()
+        rc = self._lib.mfem_step_stats(self._plan, buf, max(1, self.iterations), ctypes.byref(count),
+                                       _stream_handle(self.device))
+        _lib.check(rc, self._plan)
+        return [dict(iterations=buf[i].iterations, status=buf[i].status, rel_residual=buf[i].rel_residual)
+                for i in range(count.value)]
+
+    # -- stages (the reference's operators) ----------------------------------
+    def predict(self, q: torch.Tensor, qd: torch.Tensor, dt: float) -> None:
+        _lib.check(self._lib.mfem_predict(self._plan, self._check_state(q, "q"), self._check_state(qd, "qd"),
+                                          float(dt), _stream_handle(self.device)), self._plan)
+
+    def update_system(self, x: torch.Tensor) -> None:
+        _lib.check(self._lib.mfem_update_system(self._plan, self._check_state(x, "x"), _stream_handle(self.device)),
+                   self._plan)
+
+    def assemble(self, x: torch.Tensor, dt: float) -> None:
+        _lib.check(self._lib.mfem_assemble(self._plan, self._check_state(x, "x"), float(dt),
+                                           _stream_handle(self.device)), self._plan)
+
+    def global_solve(self, slot: int = 0) -> None:
+        _lib.check(self._lib.mfem_global_solve(self._plan, int(slot), _stream_handle(self.device)), self._plan)
+
+    def local_solve(self, x: torch.Tensor) -> None:
+        _lib.check(self._lib.mfem_local_solve(self._plan, self._check_state(x, "x"), _stream_handle(self.device)),
+                   self._plan)
+
+    def true_residual(self) -> float:
+        out = ctypes.c_double()
+        _lib.check(self._lib.mfem_true_residual(self._plan, ctypes.byref(out), _stream_handle(self.device)),
+                   self._plan)
+        return out.value
+
+    # -- buffers ---------------------------------------------------------------
+    _BUF_DTYPE = {"row_ptr": torch.int32, "col_idx": torch.int32, "tet_slots": torch.int32}
+
+    def read_buffer(self, name: str) -> torch.Tensor:
+        """Device copy of an internal buffer (flat; layouts in include/mfem_gb300.h)."""
+        which = _lib.BUF[name]
+        nbytes = ctypes.c_size_t()
+        _lib.check(self._lib.mfem_plan_buffer_bytes(self._plan, which, ctypes.byref(nbytes)), self._plan)
+        dt = self._BUF_DTYPE.get(name, torch.float32)
+        out = torch.empty(nbytes.value // 4, dtype=dt, device=self.device)
+        _lib.check(self._lib.mfem_plan_copy_out(self._plan, which, ctypes.c_void_p(out.data_ptr()), nbytes.value,
+                                                _stream_handle(self.device)), self._plan)
+        return out
+
+    def write_buffer(self, name: str, values: torch.Tensor) -> None:
+        which = _lib.BUF[name]
+        nbytes = ctypes.c_size_t()
+        _lib.check(self._lib.mfem_plan_buffer_bytes(self._plan, which, ctypes.byref(nbytes)), self._plan)
+        src = values.to(self.device).contiguous()
+        if src.numel() * src.element_size() != nbytes.value:
+            raise ValueError(f"{name}: expected {nbytes.value} bytes")
+        _lib.check(self._lib.mfem_plan_copy_in(self._plan, which, ctypes.c_void_p(src.data_ptr()), nbytes.value,
+                                               _stream_handle(self.device)), self._plan)
+        torch.cuda.current_stream(self.device).synchronize()
+
+    @property
+    def tet_stretch(self) -> torch.Tensor:
+        return self.read_buffer("tet_stretch").reshape(self.T, 6)
+
+    @property
+    def tet_lambda(self) -> torch.Tensor:
+        return self.read_buffer("tet_lambda").reshape(self.T, 6)
+
+    # -- checkpoint / resume ---------------------------------------------------
+    def save_state(self, path: str, state: State) -> None:
+        """Writes x, v, s and lambda to an npz file."""
+        np.savez(path, particle_q=state.particle_q.cpu().numpy(), particle_qd=state.particle_qd.cpu().numpy(),
+                 tet_stretch=self.tet_stretch.cpu().numpy(), tet_lambda=self.tet_lambda.cpu().numpy())
+
+    def load_state(self, path: str, state: State) -> None:
+        d = np.load(path)
+        state.particle_q.copy_(torch.as_tensor(d["particle_q"], device=self.device))
+        state.particle_qd.copy_(torch.as_tensor(d["particle_qd"], device=self.device))
+        self.write_buffer("tet_stretch", torch.as_tensor(d["tet_stretch"]).reshape(-1))
+        self.write_buffer("tet_lambda", torch.as_tensor(d["tet_lambda"]).reshape(-1))
+
+
+# The reference's class name, for drop-in use.
+RefinementSolver = MixedFEMSolver
