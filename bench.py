@@ -47,6 +47,8 @@ def parse_args():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", default="nh_beam")
     ap.add_argument("--profile-steps", type=int, default=10, help="steps of the eager stage profile")
+    ap.add_argument("--pcg-ctas", type=int, default=0, help="persistent PCG CTAs (0: one per SM)")
+    ap.add_argument("--pcg-variant", default="auto", choices=["auto", "standard", "single_reduction"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget-s", type=float, default=30.0, help="CPU time budget of the oracle leg")
     return ap.parse_args()
@@ -214,7 +216,8 @@ def run_gb300(args, rank, world, local_rank):
     spec = mesh.spec
     model = Model.from_beam(mesh, device=dev)
     solver = MixedFEMSolver(model, iterations=spec.iterations, energy=spec.energy,
-                            cg_tolerance=spec.cg_tolerance, cg_max_iterations=spec.cg_max_iterations)
+                            cg_tolerance=spec.cg_tolerance, cg_max_iterations=spec.cg_max_iterations,
+                            pcg_ctas=args.pcg_ctas, pcg_variant=args.pcg_variant)
     s_init = solver.tet_stretch.clone().reshape(-1)
     lam0 = torch.zeros_like(s_init)
     q0 = torch.as_tensor(mesh.q0, device=dev)

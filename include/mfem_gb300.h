@@ -60,7 +60,9 @@ typedef struct mfem_config {
     int32_t preconditioner;               /* 1 block-Jacobi, 0 none (solver.py:128)              */
     int32_t use_cuda_graph;               /* capture mfem_step once per argument set and replay  */
     int32_t pcg_ctas;                     /* persistent PCG CTAs; 0 = one per SM                 */
-    int32_t reserved[7];
+    int32_t pcg_variant;                  /* 0 auto, 1 standard (two reductions per iteration),
+                                             2 single-reduction (Chronopoulos-Gear)             */
+    int32_t reserved[6];
 } mfem_config;
 
 /* Buffers owned by a plan that mfem_plan_copy_out / _copy_in expose.

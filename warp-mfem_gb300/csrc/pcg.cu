@@ -3,22 +3,50 @@
 //
 // The reference runs warp.optim.linear.cg (check_every=0, graph-captured,
 // M = block-Jacobi inverse) (src/mfem/refinement/solver.py:220-235, 581-609).
-// Here every CTA owns a contiguous range of block rows and the solve loops on
-// the device with no host round trip.  One iteration is two phases, each
-// ended by a grid barrier that also completes a deterministic reduction:
+// Here the whole solve loops on the device, with no host round trip.
 //
-//   A: w = H z (z gathered from every CTA), Ap = w + beta Ap, p = z + beta p
-//      (so H p needs no extra pass), partial p.Ap
-//   B: alpha = rz / p.Ap; x += alpha p; r -= alpha Ap; z = M r; partial r.z, r.r
+// Data placement.  Each CTA owns a contiguous range of block rows, keeps that
+// range's vectors in shared memory and -- when it fits -- its slice of H
+// (values and window-local column indices), so H is read once per solve.
+// Before each sparse product the CTA stages the contiguous "window" of rows
+// that its columns reach (the mesh ordering keeps it narrow) from global into
+// shared memory with bulk asynchronous copies (cp.async.bulk, completion on
+// an mbarrier), issued as soon as the data is published.
 //
-// Every CTA sums the per-CTA partials in the same fixed order, so all CTAs
-// take the same convergence decision.  Stopping test: ||r|| <= tol ||g||,
-// checked before the first iteration and after every phase B.  Scalars
-// (dot products, alpha, beta) are accumulated in float64.
+// Two formulations of the same PCG iteration (equal iterates in exact
+// arithmetic):
 //
-// The grid barrier counts arrivals on a 64-bit counter that is never reset:
-// the k-th barrier of a launch releases at base + k * CTAs.  Each wait is
-// bounded (globaltimer); a timeout sets the sticky error flag and every CTA
+//  * single-reduction (Chronopoulos & Gear 1989, "s-step iterative methods
+//    for symmetric linear systems"; the "CG-CG" of Ghysels & Vanroose 2014):
+//        p = u + beta p;  s = w + beta s;  x += alpha p;  r -= alpha s;
+//        u = M r;  w = H u;  gamma = (r, u), delta = (w, u), (r, r)
+//        beta' = gamma' / gamma;  alpha' = gamma' / (delta' - beta' gamma' / alpha)
+//    One grid barrier per iteration: the neighbours' u = M (r - alpha (w +
+//    beta s)) is rebuilt by each CTA over its window from the (r, w, s) that
+//    the owners published at the end of the previous iteration (double
+//    buffered by iteration parity).  Every CTA computes its window rows with
+//    the same instructions from the same published values, so owners and
+//    neighbours agree bit for bit.
+//  * standard (Hestenes-Stiefel, the reference's form), two barriers per
+//    iteration: A: p = z + beta p over the window, Ap = H p, (p, Ap);
+//    B: x += alpha p, r -= alpha Ap, z = M r, (r, z), (r, r).  Used when the
+//    single-reduction windows do not fit in shared memory.
+//
+// Grid synchronisation is a reduction: each CTA stores its partial sums
+// (double buffered by barrier parity), then arrives on a 64-bit counter that
+// is never reset -- the k-th barrier of a launch releases at base + k * CTAs
+// -- with one thread per CTA polling it.  (Measured on GB300 with 152 CTAs:
+// 1.3 us per barrier, against 4.6 us for per-CTA flag words that every CTA
+// polls.)  After the release every CTA reads all partials in one round trip
+// while its thread 0 issues the next window copies, and sums them in the same
+// fixed order, so all CTAs take the same decisions and the result is
+// deterministic.  Dot products and the scalar recurrence are float32 like
+// the reference's CG (GB300's float64 rate is low); the scalars are computed
+// by one thread per CTA and broadcast.  Stopping test ||r|| <= tol ||g|| on
+// the recurrence residual, before the first iteration and after each one.
+//
+// Every wait (barrier, mbarrier) is bounded; after a timeout the kernel sets
+// the sticky error flag, waits (bounded) for its own copies in flight and
 // leaves, reporting MFEM_TIMEOUT.
 #include "internal.h"
 
@@ -26,52 +54,52 @@ namespace mfem {
 namespace {
 
 constexpr int kPcgThreads = 512;
-constexpr int kGroup = 16;                       // lanes per block row in the SpMV
-constexpr unsigned long long kWaitLimitNs = 5000000000ull;  // 5 s per barrier wait
+constexpr int kGroup = 4;                         // lanes per block row in the product
+constexpr int kMaxCtas = 256;
+constexpr long long kWaitCycles = 8000000000ll;   // ~4 s at 2 GHz per wait
+constexpr size_t kStaticSmem = 12 * 1024;         // static shared memory reserve
 
-__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
+struct PcgArgs {
+    int n;
+    const int *row_ptr;
+    const int *col_idx;
+    const float *values;
+    const float *Minv;   // [n_pad][9]
+    const float *b;
+    float *x;            // [n_pad][3] warm start in, solution out
+    float *pub;          // published vectors, 6 x [n_pad][3]
+    int n_pad;
+    const int4 *cta;     // [ctas] (row_lo, row_hi, win_lo, win_hi)
+    int rows_max, blk_max, win_max;
+    float *partials;            // [2][kMaxCtas][4] per-CTA partial sums
+    unsigned long long *counter;  // grid barrier arrivals (never reset)
+    int *error;
+    SolveStats *stats;
+    int slot;
+    float tol;
+    int maxiter;
+    int use_precond;
+};
+
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *p) {
     unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
-}
-
-__device__ __forceinline__ unsigned long long globaltimer() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
 }
 
 __device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
 
-// Grid barrier; false if the wait gave up (or another CTA did).
-__device__ bool grid_barrier(unsigned long long *bar, unsigned long long &target, int *error, int *s_ok) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        target += gridDim.x;
-        __threadfence();
-        atomicAdd(bar, 1ull);
-        int ok = 1;
-        if (ld_acquire(bar) < target) {
-            const unsigned long long t0 = globaltimer();
-            while (ld_acquire(bar) < target) {
-                if (ld_volatile(error) != 0 || globaltimer() - t0 > kWaitLimitNs) {
-                    atomicExch(error, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        __threadfence();
-        *s_ok = ok;
-    }
-    __syncthreads();
-    return *s_ok != 0;
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-// Deterministic block reduction of up to 3 doubles; result valid in thread 0.
+// ---- reduction barrier --------------------------------------------------------
+// Block-reduces NV per-thread float partials, stores the CTA's sums for
+// barrier `k` (parity buffer) and waits at the grid barrier.  Returns false
+// if the wait gave up.  CTA-uniform.
 template <int NV>
-__device__ void block_reduce(double (&v)[NV], double (*s_red)[32]) {
+__device__ bool reduce_arrive(float (&v)[NV], float *partials, unsigned k, unsigned long long *counter,
+                              unsigned long long &target, int *error, float (*s_redf)[32], int *s_ok) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
@@ -80,301 +108,764 @@ __device__ void block_reduce(double (&v)[NV], double (*s_red)[32]) {
     }
     if (lane == 0) {
 #pragma unroll
-        for (int i = 0; i < NV; ++i) s_red[i][wid] = v[i];
+        for (int i = 0; i < NV; ++i) s_redf[i][wid] = v[i];
     }
     __syncthreads();
     if (wid == 0) {
         const int nw = blockDim.x >> 5;
+        float part[NV];
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
-            v[i] = lane < nw ? s_red[i][lane] : 0.0;
+            part[i] = lane < nw ? s_redf[i][lane] : 0.0f;
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) v[i] += __shfl_down_sync(0xffffffffu, v[i], off);
+            for (int off = 16; off > 0; off >>= 1) part[i] += __shfl_down_sync(0xffffffffu, part[i], off);
+        }
+        if (lane == 0) {
+            float *buf = partials + (size_t)(k & 1u) * kMaxCtas * 4 + (size_t)blockIdx.x * 4;
+#pragma unroll
+            for (int i = 0; i < NV; ++i) buf[i] = part[i];
+            // arrive: every earlier store of this CTA (published vectors,
+            // partials) is released before the counter moves
+            target += gridDim.x;
+            __threadfence();
+            atomicAdd(counter, 1ull);
+            int ok = 1;
+            const long long t0 = clock64();
+            unsigned spins = 0;
+            while (ld_relaxed(counter) < target) {
+                if ((++spins & 1023u) == 0 && (ld_volatile(error) != 0 || clock64() - t0 > kWaitCycles)) {
+                    atomicExch(error, 1);
+                    ok = 0;
+                    break;
+                }
+            }
+            __threadfence();
+            *s_ok = ok;
         }
     }
     __syncthreads();
+    return *s_ok != 0;
 }
 
-// Sum of the per-CTA partials (stride 4 doubles) in a fixed order; every
-// thread of the CTA gets the totals.
+// Sums the partials of barrier `k` over all CTAs (after reduce_arrive):
+// threads 0..nb*NV-1 fetch one each (one round trip), warp 0 adds them in a
+// fixed order.  tot[] is valid for every thread on return.
 template <int NV>
-__device__ void grid_totals(const double *part, double (&tot)[NV], double *s_tot) {
+__device__ void reduce_totals(const float *partials, unsigned k, float *s_val, float *tot) {
+    const int nb = gridDim.x;
+    const float *buf = partials + (size_t)(k & 1u) * kMaxCtas * 4;
+    for (int t = threadIdx.x; t < nb * NV; t += blockDim.x) {
+        const int b = t / NV, i = t - b * NV;
+        s_val[b * 4 + i] = __ldcg(buf + (size_t)b * 4 + i);
+    }
+    __syncthreads();
     if (threadIdx.x < 32) {
-        double acc[NV];
+        const int lane = threadIdx.x;
+        float acc[NV];
 #pragma unroll
-        for (int i = 0; i < NV; ++i) acc[i] = 0.0;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {
+        for (int i = 0; i < NV; ++i) acc[i] = 0.0f;
+        for (int b = lane; b < nb; b += 32) {
 #pragma unroll
-            for (int i = 0; i < NV; ++i) acc[i] += __ldcg(part + (size_t)b * 4 + i);
+            for (int i = 0; i < NV; ++i) acc[i] += s_val[b * 4 + i];
         }
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) acc[i] += __shfl_down_sync(0xffffffffu, acc[i], off);
         }
-        if (threadIdx.x == 0) {
+        if (lane == 0) {
 #pragma unroll
-            for (int i = 0; i < NV; ++i) s_tot[i] = acc[i];
+            for (int i = 0; i < NV; ++i) tot[i] = acc[i];
         }
     }
     __syncthreads();
-#pragma unroll
-    for (int i = 0; i < NV; ++i) tot[i] = s_tot[i];
-    __syncthreads();
 }
 
-// y_row = sum_k H[k] v[col[k]] over one block row, by a group of kGroup
-// lanes; every lane of the group returns the row's sum.
-__device__ __forceinline__ void row_product(const BsrViews &bv, const float *__restrict__ vec, int row, int g_lane,
-                                            unsigned gmask, float y[3]) {
-    const int rb = __ldg(bv.row_ptr + row);
-    const int re = __ldg(bv.row_ptr + row + 1);
-    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-    for (int k = rb + g_lane; k < re; k += kGroup) {
-        const int col = __ldg(bv.col_idx + k);
-        const float *h = bv.values + (size_t)k * 9;
-        const float v0 = __ldcg(vec + 3 * col + 0);
-        const float v1 = __ldcg(vec + 3 * col + 1);
-        const float v2 = __ldcg(vec + 3 * col + 2);
-        a0 += __ldg(h + 0) * v0 + __ldg(h + 1) * v1 + __ldg(h + 2) * v2;
-        a1 += __ldg(h + 3) * v0 + __ldg(h + 4) * v1 + __ldg(h + 5) * v2;
-        a2 += __ldg(h + 6) * v0 + __ldg(h + 7) * v1 + __ldg(h + 8) * v2;
-    }
-#pragma unroll
-    for (int off = kGroup / 2; off > 0; off >>= 1) {
-        a0 += __shfl_xor_sync(gmask, a0, off);
-        a1 += __shfl_xor_sync(gmask, a1, off);
-        a2 += __shfl_xor_sync(gmask, a2, off);
-    }
-    y[0] = a0;
-    y[1] = a1;
-    y[2] = a2;
+// Scalars of the iteration, decided by thread 0 and broadcast.
+struct Scalars {
+    float alpha, beta, gamma, rr, bb, thr2;
+    int status, done;
+};
+
+// ---- bulk copies -----------------------------------------------------------
+// Issued by thread 0 after a __syncthreads that ended every read of the
+// destinations and after the reduction that published the sources.
+__device__ __forceinline__ void tma_expect(uint64_t *mbar, uint32_t bytes) {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(bytes)
+                 : "memory");
 }
 
-__device__ __forceinline__ void apply_precond(const float *__restrict__ Minv, int row, const float r[3], float z[3],
-                                              int use_precond) {
-    if (!use_precond) {
+__device__ __forceinline__ void tma_copy(void *dst, const void *src, uint32_t bytes, uint64_t *mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(mbar))
+                 : "memory");
+}
+
+// Waits for the mbarrier phase `parity` (bounded; a second bounded wait after
+// a timeout so no copy is still writing when the CTA leaves).  CTA-uniform.
+__device__ bool tma_wait(uint64_t *mbar, uint32_t &parity, int *error) {
+    const uint32_t mb = smem_addr(mbar);
+    bool ok = true;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        uint32_t done = 0;
+        const long long t0 = clock64();
+        unsigned spins = 0;
+        while (!done) {
+            asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(done)
+                : "r"(mb), "r"(parity)
+                : "memory");
+            if (!done && (++spins & 255u) == 0 && clock64() - t0 > kWaitCycles / 2) break;
+        }
+        if (done) break;
+        ok = false;
+    }
+    ok = __syncthreads_and(ok) != 0;
+    if (!ok && threadIdx.x == 0) atomicExch(error, 1);
+    parity ^= 1u;
+    return ok;
+}
+
+// out[i] = sum_k H[k] win[col_k] over the CTA's rows, kGroup lanes per row.
+template <bool CACHE>
+__device__ __forceinline__ void window_product(const PcgArgs &a, const int *rowoff, const float *sH, const int *sCol,
+                                               int blk_lo, int win_lo, int nrows, const float *win, float *out) {
+    const int g_lane = threadIdx.x & (kGroup - 1);
+    const int group = threadIdx.x / kGroup;
+    const int ngroups = blockDim.x / kGroup;
+    const unsigned gmask = ((1u << kGroup) - 1u) << (threadIdx.x & (32 - kGroup));
+    for (int i = group; i < nrows; i += ngroups) {
+        const int kb = rowoff[i], ke = rowoff[i + 1];
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+#pragma unroll 4
+        for (int k = kb + g_lane; k < ke; k += kGroup) {
+            const float *h;
+            int c;
+            if (CACHE) {
+                h = sH + (size_t)k * 9;
+                c = sCol[k];
+            } else {
+                h = a.values + (size_t)(blk_lo + k) * 9;
+                c = __ldg(a.col_idx + blk_lo + k) - win_lo;
+            }
+            const float v0 = win[3 * c + 0], v1 = win[3 * c + 1], v2 = win[3 * c + 2];
+            a0 += h[0] * v0 + h[1] * v1 + h[2] * v2;
+            a1 += h[3] * v0 + h[4] * v1 + h[5] * v2;
+            a2 += h[6] * v0 + h[7] * v1 + h[8] * v2;
+        }
+#pragma unroll
+        for (int off = kGroup / 2; off > 0; off >>= 1) {
+            a0 += __shfl_xor_sync(gmask, a0, off);
+            a1 += __shfl_xor_sync(gmask, a1, off);
+            a2 += __shfl_xor_sync(gmask, a2, off);
+        }
+        if (g_lane == 0) {
+            out[3 * i + 0] = a0;
+            out[3 * i + 1] = a1;
+            out[3 * i + 2] = a2;
+        }
+    }
+}
+
+__device__ __forceinline__ void precond(const float *m, const float r[3], float z[3], int use) {
+    if (!use) {
         z[0] = r[0];
         z[1] = r[1];
         z[2] = r[2];
         return;
     }
-    const float *m = Minv + (size_t)row * 9;
     z[0] = m[0] * r[0] + m[1] * r[1] + m[2] * r[2];
     z[1] = m[3] * r[0] + m[4] * r[1] + m[5] * r[2];
     z[2] = m[6] * r[0] + m[7] * r[1] + m[8] * r[2];
 }
 
-__global__ void __launch_bounds__(kPcgThreads, 1)
-    pcg_kernel(BsrViews bv, const float *__restrict__ Minv, const float *__restrict__ b, float *x, PcgWork w,
-               int slot, float tol, int maxiter, int use_precond) {
-    __shared__ double s_red[3][32];
-    __shared__ double s_tot[4];
-    __shared__ int s_ok;
-    __shared__ unsigned long long s_base;
+struct Common {
+    int row_lo, nrows, win_lo, nwin, blk_lo, nblk;
+};
 
-    const int n = bv.n;
-    const int cta = blockIdx.x;
-    const int nb = gridDim.x;
-    const int row_lo = (int)(((long long)n * cta) / nb);
-    const int row_hi = (int)(((long long)n * (cta + 1)) / nb);
-    const int g_lane = threadIdx.x & (kGroup - 1);
-    const int group = threadIdx.x / kGroup;
-    const int ngroups = blockDim.x / kGroup;
-    const unsigned gmask = 0xffffu << (threadIdx.x & 16);
-    double *partA = w.partials;
-    double *partB = w.partials + (size_t)nb * 4;
+__device__ __forceinline__ Common setup_common(const PcgArgs &a) {
+    const int4 info = a.cta[blockIdx.x];
+    Common c;
+    c.row_lo = info.x;
+    c.nrows = info.y - info.x;
+    c.win_lo = info.z;
+    c.nwin = info.w - info.z;
+    c.blk_lo = a.row_ptr[c.row_lo];
+    c.nblk = a.row_ptr[info.y] - c.blk_lo;
+    return c;
+}
 
-    if (threadIdx.x == 0) {
-        s_base = (ld_acquire(w.barrier) / (unsigned long long)nb) * (unsigned long long)nb;
-        s_ok = ld_volatile(w.error) == 0;
+__device__ __forceinline__ void load_matrix_slice(const PcgArgs &a, const Common &c, int *rowoff, float *sH,
+                                                  int *sCol, bool cache) {
+    for (int i = threadIdx.x; i <= c.nrows; i += blockDim.x) rowoff[i] = a.row_ptr[c.row_lo + i] - c.blk_lo;
+    if (cache) {
+        for (int k = threadIdx.x; k < 9 * c.nblk; k += blockDim.x) sH[k] = a.values[(size_t)9 * c.blk_lo + k];
+        for (int k = threadIdx.x; k < c.nblk; k += blockDim.x) sCol[k] = a.col_idx[c.blk_lo + k] - c.win_lo;
     }
-    __syncthreads();
-    unsigned long long target = s_base;
-    if (!s_ok) {
-        if (cta == 0 && threadIdx.x == 0) {
-            w.stats[slot].iterations = 0;
-            w.stats[slot].status = MFEM_TIMEOUT;
-            w.stats[slot].rel_residual = 0.0f;
+}
+
+// Final bookkeeping: solution rows and stats.
+__device__ __forceinline__ void finish(const PcgArgs &a, const Common &cm, const float *sX, const Scalars &sc,
+                                       int it) {
+    for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) a.x[(size_t)3 * cm.row_lo + i] = sX[i];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const float rel = sc.bb > 0.0f ? sqrtf(sc.rr / sc.bb) : sqrtf(sc.rr);
+        a.stats[a.slot] = SolveStats{it, sc.status, rel, 0.0f};
+    }
+}
+
+#define PCG_PROLOGUE                                                                        \
+    __shared__ float s_redf[4][32];                                                         \
+    __shared__ float s_val[4 * kMaxCtas];                                                   \
+    __shared__ float s_tot[4];                                                              \
+    __shared__ Scalars sc;                                                                  \
+    __shared__ int s_ok;                                                                    \
+    __shared__ unsigned long long s_base;                                                   \
+    __shared__ __align__(8) uint64_t s_mbar;                                                \
+    const Common cm = setup_common(a);                                                      \
+    if (threadIdx.x == 0) {                                                                 \
+        s_base = (ld_relaxed(a.counter) / gridDim.x) * (unsigned long long)gridDim.x;     \
+        s_ok = ld_volatile(a.error) == 0;                                                   \
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&s_mbar)) : "memory"); \
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");                  \
+    }                                                                                       \
+    __syncthreads();                                                                        \
+    unsigned long long target = s_base;                                                     \
+    unsigned bar = 0;                                                                       \
+    uint32_t parity = 0;                                                                    \
+    if (!s_ok) {                                                                            \
+        if (blockIdx.x == 0 && threadIdx.x == 0) a.stats[a.slot] = SolveStats{0, MFEM_TIMEOUT, 0.0f, 0.0f}; \
+        return;                                                                             \
+    }
+
+// ===========================================================================
+// single-reduction (Chronopoulos-Gear) PCG
+// ===========================================================================
+template <bool CACHE>
+__global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    PCG_PROLOGUE
+    const int rows_max = a.rows_max, win_max = a.win_max;
+    // own rows
+    float *sX = reinterpret_cast<float *>(smem);
+    float *sU = sX + 3 * rows_max;
+    float *sP = sU + 3 * rows_max;
+    float *sW = sP + 3 * rows_max;
+    // window rows
+    float *wR = sW + 3 * rows_max;
+    float *wW = wR + 3 * win_max;
+    float *wS = wW + 3 * win_max;
+    float *wM = wS + 3 * win_max;
+    int *rowoff = reinterpret_cast<int *>(wM + 9 * win_max);
+    float *sH = reinterpret_cast<float *>(rowoff + rows_max + 4);
+    int *sCol = reinterpret_cast<int *>(sH + (CACHE ? 9 * a.blk_max : 0));
+
+    const size_t vec = (size_t)3 * a.n_pad;
+    float *pubR[2] = {a.pub, a.pub + vec};
+    float *pubW[2] = {a.pub + 2 * vec, a.pub + 3 * vec};
+    float *pubS[2] = {a.pub + 4 * vec, a.pub + 5 * vec};
+    const int own = cm.row_lo - cm.win_lo;  // offset of the own rows inside the window
+    const uint32_t wbytes = (uint32_t)cm.nwin * 12u;
+
+    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE);
+    // window of M^-1 blocks (kept for the whole solve) and of the warm start
+    bool ok = true;
+    if (threadIdx.x == 0 && cm.nwin > 0) {
+        tma_expect(&s_mbar, wbytes * 4u);
+        tma_copy(wM, a.Minv + (size_t)9 * cm.win_lo, wbytes * 3u, &s_mbar);
+        tma_copy(wR, a.x + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+    }
+    if (cm.nwin > 0) ok = tma_wait(&s_mbar, parity, a.error);
+
+    int it = 0;
+    // ---- r0 = g - H x0, published
+    if (ok) {
+        for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = wR[3 * own + i];
+        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wR, sW);
+        __syncthreads();
+        float acc[1] = {0.0f};
+        for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) {
+            const float bg = a.b[(size_t)3 * cm.row_lo + i];
+            pubR[0][(size_t)3 * cm.row_lo + i] = bg - sW[i];
+            acc[0] = __fmaf_rn(bg, bg, acc[0]);
         }
-        return;
+        ok = reduce_arrive<1>(acc, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok);
+        if (ok) {
+            reduce_totals<1>(a.partials, bar, s_val, s_tot);
+            if (threadIdx.x == 0) {
+                sc.bb = s_tot[0];
+                sc.thr2 = a.tol * a.tol * s_tot[0];
+            }
+        }
+        ++bar;
     }
-
-    // ---- phase I: r = g - H x0, z = M r; partials r.z, r.r, g.g
-    for (int row = row_lo + group; row < row_hi; row += ngroups) {
-        float y[3];
-        row_product(bv, x, row, g_lane, gmask, y);
-        if (g_lane == 0) {
+    // ---- u0 = M r0 over the window, w0 = H u0, gamma0, delta0, (r0, r0)
+    if (ok) {
+        if (threadIdx.x == 0 && cm.nwin > 0) {
+            tma_expect(&s_mbar, wbytes);
+            tma_copy(wR, pubR[0] + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+        }
+        if (cm.nwin > 0) ok = tma_wait(&s_mbar, parity, a.error);
+    }
+    if (ok) {
+        for (int j = threadIdx.x; j < cm.nwin; j += blockDim.x) {
+            float u[3];
+            precond(wM + 9 * j, wR + 3 * j, u, a.use_precond);
+            wW[3 * j + 0] = u[0];
+            wW[3 * j + 1] = u[1];
+            wW[3 * j + 2] = u[2];
+        }
+        __syncthreads();
+        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wW, sW);
+        __syncthreads();
+        float acc[3] = {0.0f, 0.0f, 0.0f};
+        for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) {
+            const float r = wR[3 * own + i], u = wW[3 * own + i], w = sW[i];
+            sU[i] = u;
+            pubW[0][(size_t)3 * cm.row_lo + i] = w;
+            acc[0] = __fmaf_rn(r, u, acc[0]);
+            acc[1] = __fmaf_rn(w, u, acc[1]);
+            acc[2] = __fmaf_rn(r, r, acc[2]);
+        }
+        ok = reduce_arrive<3>(acc, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok);
+    }
+    bool pending = false;  // a staging copy is in flight
+    if (ok) {
+        if (threadIdx.x == 0 && cm.nwin > 0) {
+            tma_expect(&s_mbar, 2u * wbytes);
+            tma_copy(wR, pubR[0] + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+            tma_copy(wW, pubW[0] + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+        }
+        pending = cm.nwin > 0;
+        reduce_totals<3>(a.partials, bar, s_val, s_tot);
+        if (threadIdx.x == 0) {
+            const float gamma = s_tot[0], delta = s_tot[1], rr = s_tot[2];
+            sc.gamma = gamma;
+            sc.rr = rr;
+            sc.beta = 0.0f;
+            sc.status = MFEM_OK;
+            if (!isfinite(gamma) || !isfinite(delta) || !isfinite(rr) || !isfinite(sc.bb))
+                sc.status = MFEM_NONFINITE;
+            else if (!(delta > 0.0f) && rr > 0.0f)
+                sc.status = MFEM_STAGNATION;
+            sc.alpha = delta > 0.0f ? gamma / delta : 0.0f;
+            sc.done = sc.status != MFEM_OK || rr <= sc.thr2;
+        }
+    } else if (threadIdx.x == 0) {
+        sc.status = MFEM_TIMEOUT;
+        sc.done = 1;
+        sc.rr = 0.0f;
+        sc.bb = 1.0f;
+    }
+    ++bar;
+    __syncthreads();
+    while (!sc.done) {
+        if (it >= a.maxiter) {
+            if (threadIdx.x == 0) sc.status = MFEM_MAXITER;
+            break;
+        }
+        // state `it` of the window: r, w (and s of the previous iteration)
+        if (pending && !tma_wait(&s_mbar, parity, a.error)) {
+            pending = false;
+            if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+            break;
+        }
+        pending = false;
+        const float fa = sc.alpha, fb = sc.beta;
+        // s = w + beta s; r' = r - alpha s; u' = M r'   (every window row)
+        for (int j = threadIdx.x; j < cm.nwin; j += blockDim.x) {
+            float r[3], u[3];
 #pragma unroll
-            for (int a = 0; a < 3; ++a) w.r[3 * row + a] = b[3 * row + a] - y[a];
+            for (int c = 0; c < 3; ++c) {
+                const float sv = it == 0 ? wW[3 * j + c] : __fmaf_rn(fb, wS[3 * j + c], wW[3 * j + c]);
+                wS[3 * j + c] = sv;
+                r[c] = __fmaf_rn(-fa, sv, wR[3 * j + c]);
+                wR[3 * j + c] = r[c];
+            }
+            precond(wM + 9 * j, r, u, a.use_precond);
+            wW[3 * j + 0] = u[0];
+            wW[3 * j + 1] = u[1];
+            wW[3 * j + 2] = u[2];
         }
+        __syncthreads();
+        // own rows: p = u + beta p, x += alpha p; publish r', s
+        float *pr = pubR[(it + 1) & 1];
+        float *ps = pubS[(it + 1) & 1];
+        for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) {
+            const float pv = it == 0 ? sU[i] : __fmaf_rn(fb, sP[i], sU[i]);
+            sP[i] = pv;
+            sX[i] = __fmaf_rn(fa, pv, sX[i]);
+            sU[i] = wW[3 * own + i];
+            pr[(size_t)3 * cm.row_lo + i] = wR[3 * own + i];
+            ps[(size_t)3 * cm.row_lo + i] = wS[3 * own + i];
+        }
+        // w' = H u'
+        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wW, sW);
+        __syncthreads();
+        float *pw = pubW[(it + 1) & 1];
+        float acc[3] = {0.0f, 0.0f, 0.0f};
+        for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) {
+            const float r = wR[3 * own + i], u = sU[i], w = sW[i];
+            pw[(size_t)3 * cm.row_lo + i] = w;
+            acc[0] = __fmaf_rn(r, u, acc[0]);
+            acc[1] = __fmaf_rn(w, u, acc[1]);
+            acc[2] = __fmaf_rn(r, r, acc[2]);
+        }
+        if (!reduce_arrive<3>(acc, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok)) {
+            if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+            break;
+        }
+        ++it;
+        // stage the next state while the totals are fetched
+        if (threadIdx.x == 0 && cm.nwin > 0) {
+            tma_expect(&s_mbar, 3u * wbytes);
+            tma_copy(wR, pr + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+            tma_copy(wW, pw + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+            tma_copy(wS, ps + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+        }
+        pending = cm.nwin > 0;
+        reduce_totals<3>(a.partials, bar, s_val, s_tot);
+        ++bar;
+        if (threadIdx.x == 0) {
+            const float gamma_new = s_tot[0], delta = s_tot[1], rr = s_tot[2];
+            sc.rr = rr;
+            if (!isfinite(gamma_new) || !isfinite(delta) || !isfinite(rr)) {
+                sc.status = MFEM_NONFINITE;
+                sc.done = 1;
+            } else if (rr <= sc.thr2) {
+                sc.done = 1;
+            } else {
+                const float beta = gamma_new / sc.gamma;
+                const float denom = delta - beta * gamma_new / sc.alpha;
+                if (!(denom > 0.0f)) {
+                    sc.status = MFEM_STAGNATION;
+                    sc.done = 1;
+                } else {
+                    sc.beta = beta;
+                    sc.alpha = gamma_new / denom;
+                    sc.gamma = gamma_new;
+                }
+            }
+        }
+        __syncthreads();
     }
+    if (pending) tma_wait(&s_mbar, parity, a.error);
     __syncthreads();
-    {
-        double acc[3] = {0.0, 0.0, 0.0};
-        for (int row = row_lo + threadIdx.x; row < row_hi; row += blockDim.x) {
+    finish(a, cm, sX, sc, it);
+}
+
+// ===========================================================================
+// standard (two-barrier) PCG
+// ===========================================================================
+template <bool CACHE>
+__global__ void __launch_bounds__(kPcgThreads, 1) pcg_standard_kernel(PcgArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    PCG_PROLOGUE
+    const int rows_max = a.rows_max, win_max = a.win_max;
+    float *sX = reinterpret_cast<float *>(smem);
+    float *sR = sX + 3 * rows_max;
+    float *sAp = sR + 3 * rows_max;
+    float *sM = sAp + 3 * rows_max;
+    float *winA = sM + 9 * rows_max;
+    float *winB = winA + 3 * win_max;
+    int *rowoff = reinterpret_cast<int *>(winB + 3 * win_max);
+    float *sH = reinterpret_cast<float *>(rowoff + rows_max + 4);
+    int *sCol = reinterpret_cast<int *>(sH + (CACHE ? 9 * a.blk_max : 0));
+
+    const size_t vec = (size_t)3 * a.n_pad;
+    float *pubZ = a.pub;
+    float *pubP[2] = {a.pub + vec, a.pub + 2 * vec};
+    const int own = cm.row_lo - cm.win_lo;
+    const uint32_t wbytes = (uint32_t)cm.nwin * 12u;
+
+    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE);
+    for (int i = threadIdx.x; i < 9 * cm.nrows; i += blockDim.x) sM[i] = a.Minv[(size_t)9 * cm.row_lo + i];
+    bool ok = true;
+    if (threadIdx.x == 0 && cm.nwin > 0) {
+        tma_expect(&s_mbar, wbytes);
+        tma_copy(winA, a.x + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+    }
+    if (cm.nwin > 0) ok = tma_wait(&s_mbar, parity, a.error);
+
+    int it = 0;
+    if (ok) {
+        for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = winA[3 * own + i];
+        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp);
+        __syncthreads();
+        float acc[3] = {0.0f, 0.0f, 0.0f};
+        for (int i = threadIdx.x; i < cm.nrows; i += blockDim.x) {
+            const int row = cm.row_lo + i;
             float r[3], z[3];
 #pragma unroll
-            for (int a = 0; a < 3; ++a) r[a] = w.r[3 * row + a];
-            apply_precond(Minv, row, r, z, use_precond);
+            for (int c = 0; c < 3; ++c) {
+                const float bc = a.b[3 * row + c];
+                r[c] = bc - sAp[3 * i + c];
+                sR[3 * i + c] = r[c];
+                acc[2] = __fmaf_rn(bc, bc, acc[2]);
+            }
+            precond(sM + 9 * i, r, z, a.use_precond);
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                w.z[3 * row + a] = z[a];
-                const double bg = b[3 * row + a];
-                acc[0] += (double)r[a] * (double)z[a];
-                acc[1] += (double)r[a] * (double)r[a];
-                acc[2] += bg * bg;
+            for (int c = 0; c < 3; ++c) {
+                pubZ[3 * row + c] = z[c];
+                acc[0] = __fmaf_rn(r[c], z[c], acc[0]);
+                acc[1] = __fmaf_rn(r[c], r[c], acc[1]);
             }
         }
-        block_reduce<3>(acc, s_red);
+        ok = reduce_arrive<3>(acc, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok);
+    }
+    bool pending = false;
+    if (ok) {
+        if (threadIdx.x == 0 && cm.nwin > 0) {
+            tma_expect(&s_mbar, wbytes);
+            tma_copy(winA, pubZ + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+        }
+        reduce_totals<3>(a.partials, bar, s_val, s_tot);
         if (threadIdx.x == 0) {
-            partB[(size_t)cta * 4 + 0] = acc[0];
-            partB[(size_t)cta * 4 + 1] = acc[1];
-            partB[(size_t)cta * 4 + 2] = acc[2];
+            sc.gamma = s_tot[0];  // r.z
+            sc.rr = s_tot[1];
+            sc.bb = s_tot[2];
+            sc.thr2 = a.tol * a.tol * s_tot[2];
+            sc.beta = 0.0f;
+            sc.status = (!isfinite(s_tot[0]) || !isfinite(s_tot[1]) || !isfinite(s_tot[2])) ? MFEM_NONFINITE : MFEM_OK;
+            sc.done = sc.status != MFEM_OK || s_tot[1] <= sc.thr2;
         }
+        pending = cm.nwin > 0;
+    } else if (threadIdx.x == 0) {
+        sc.status = MFEM_TIMEOUT;
+        sc.done = 1;
+        sc.rr = 0.0f;
+        sc.bb = 1.0f;
     }
-    int status = MFEM_OK;
-    int it = 0;
-    double rz, rr, bb;
-    if (!grid_barrier(w.barrier, target, w.error, &s_ok)) {
-        status = MFEM_TIMEOUT;
-        rr = 0.0;
-        bb = 1.0;
-    } else {
-        double tot[3];
-        grid_totals<3>(partB, tot, s_tot);
-        rz = tot[0];
-        rr = tot[1];
-        bb = tot[2];
-        const double thr2 = (double)tol * (double)tol * bb;
-        if (!isfinite(rr) || !isfinite(bb) || !isfinite(rz)) status = MFEM_NONFINITE;
-        double beta = 0.0;
-        bool done = (status != MFEM_OK) || rr <= thr2;
-        while (!done) {
-            if (it >= maxiter) {
-                status = MFEM_MAXITER;
-                break;
-            }
-            // ---- phase A: Ap = H z + beta Ap, p = z + beta p, partial p.Ap
-            const float fbeta = (float)beta;
-            double pap = 0.0;
-            for (int row = row_lo + group; row < row_hi; row += ngroups) {
-                float y[3];
-                row_product(bv, w.z, row, g_lane, gmask, y);
-                if (g_lane == 0) {
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) {
-                        const float zr = __ldcg(w.z + 3 * row + a);
-                        float ap, pp;
-                        if (it == 0) {
-                            ap = y[a];
-                            pp = zr;
-                        } else {
-                            ap = y[a] + fbeta * w.Ap[3 * row + a];
-                            pp = zr + fbeta * w.p[3 * row + a];
-                        }
-                        w.Ap[3 * row + a] = ap;
-                        w.p[3 * row + a] = pp;
-                        pap += (double)pp * (double)ap;
-                    }
-                }
-            }
-            {
-                double acc[1] = {pap};
-                block_reduce<1>(acc, s_red);
-                if (threadIdx.x == 0) partA[(size_t)cta * 4] = acc[0];
-            }
-            if (!grid_barrier(w.barrier, target, w.error, &s_ok)) {
-                status = MFEM_TIMEOUT;
-                break;
-            }
-            double totA[1];
-            grid_totals<1>(partA, totA, s_tot);
-            const double pAp = totA[0];
+    ++bar;
+    __syncthreads();
+    while (!sc.done) {
+        if (it >= a.maxiter) {
+            if (threadIdx.x == 0) sc.status = MFEM_MAXITER;
+            break;
+        }
+        // ---- phase A: p = z + beta p over the window, Ap = H p, partial p.Ap
+        float *p_new = pubP[it & 1];
+        if (pending && !tma_wait(&s_mbar, parity, a.error)) {
+            pending = false;
+            if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+            break;
+        }
+        pending = false;
+        const float fbeta = sc.beta;
+        if (it > 0) {
+            for (int j = threadIdx.x; j < 3 * cm.nwin; j += blockDim.x) winA[j] = __fmaf_rn(fbeta, winB[j], winA[j]);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x)
+            p_new[(size_t)3 * cm.row_lo + i] = winA[3 * own + i];
+        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp);
+        __syncthreads();
+        float pap[1] = {0.0f};
+        for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x)
+            pap[0] = __fmaf_rn(winA[3 * own + i], sAp[i], pap[0]);
+        if (!reduce_arrive<1>(pap, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok)) {
+            if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+            break;
+        }
+        reduce_totals<1>(a.partials, bar, s_val, s_tot);
+        ++bar;
+        if (threadIdx.x == 0) {
+            const float pAp = s_tot[0];
             if (!isfinite(pAp)) {
-                status = MFEM_NONFINITE;
-                break;
+                sc.status = MFEM_NONFINITE;
+                sc.done = 1;
+            } else if (!(pAp > 0.0f)) {
+                sc.status = MFEM_STAGNATION;
+                sc.done = 1;
+            } else {
+                sc.alpha = sc.gamma / pAp;
             }
-            if (!(pAp > 0.0)) {
-                status = MFEM_STAGNATION;
-                break;
-            }
-            const float alpha = (float)(rz / pAp);
-            // ---- phase B: x += alpha p, r -= alpha Ap, z = M r
-            double acc[2] = {0.0, 0.0};
-            for (int row = row_lo + threadIdx.x; row < row_hi; row += blockDim.x) {
-                float r[3], z[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    x[3 * row + a] += alpha * w.p[3 * row + a];
-                    r[a] = w.r[3 * row + a] - alpha * w.Ap[3 * row + a];
-                    w.r[3 * row + a] = r[a];
-                }
-                apply_precond(Minv, row, r, z, use_precond);
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    w.z[3 * row + a] = z[a];
-                    acc[0] += (double)r[a] * (double)z[a];
-                    acc[1] += (double)r[a] * (double)r[a];
-                }
-            }
-            block_reduce<2>(acc, s_red);
-            if (threadIdx.x == 0) {
-                partB[(size_t)cta * 4 + 0] = acc[0];
-                partB[(size_t)cta * 4 + 1] = acc[1];
-            }
-            if (!grid_barrier(w.barrier, target, w.error, &s_ok)) {
-                status = MFEM_TIMEOUT;
-                break;
-            }
-            double totB[2];
-            grid_totals<2>(partB, totB, s_tot);
-            ++it;
-            const double rz_new = totB[0];
-            rr = totB[1];
-            if (!isfinite(rr) || !isfinite(rz_new)) {
-                status = MFEM_NONFINITE;
-                break;
-            }
-            beta = rz_new / rz;
-            rz = rz_new;
-            done = rr <= thr2;
         }
+        __syncthreads();
+        if (sc.done) break;
+        const float alpha = sc.alpha;
+        // ---- phase B: x += alpha p, r -= alpha Ap, z = M r
+        float acc[2] = {0.0f, 0.0f};
+        for (int i = threadIdx.x; i < cm.nrows; i += blockDim.x) {
+            const int row = cm.row_lo + i;
+            const float *pp = winA + 3 * (own + i);
+            float r[3], z[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                sX[3 * i + c] = __fmaf_rn(alpha, pp[c], sX[3 * i + c]);
+                r[c] = __fmaf_rn(-alpha, sAp[3 * i + c], sR[3 * i + c]);
+                sR[3 * i + c] = r[c];
+            }
+            precond(sM + 9 * i, r, z, a.use_precond);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                pubZ[3 * row + c] = z[c];
+                acc[0] = __fmaf_rn(r[c], z[c], acc[0]);
+                acc[1] = __fmaf_rn(r[c], r[c], acc[1]);
+            }
+        }
+        if (!reduce_arrive<2>(acc, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok)) {
+            if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+            break;
+        }
+        ++it;
+        if (threadIdx.x == 0 && cm.nwin > 0) {
+            tma_expect(&s_mbar, 2u * wbytes);
+            tma_copy(winA, pubZ + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+            tma_copy(winB, p_new + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+        }
+        pending = cm.nwin > 0;
+        reduce_totals<2>(a.partials, bar, s_val, s_tot);
+        ++bar;
+        if (threadIdx.x == 0) {
+            sc.rr = s_tot[1];
+            if (!isfinite(s_tot[0]) || !isfinite(s_tot[1])) {
+                sc.status = MFEM_NONFINITE;
+                sc.done = 1;
+            } else {
+                sc.beta = s_tot[0] / sc.gamma;
+                sc.gamma = s_tot[0];
+                sc.done = s_tot[1] <= sc.thr2;
+            }
+        }
+        __syncthreads();
     }
-    if (cta == 0 && threadIdx.x == 0) {
-        w.stats[slot].iterations = it;
-        w.stats[slot].status = status;
-        w.stats[slot].rel_residual = (float)(bb > 0.0 ? sqrt(rr / bb) : sqrt(rr));
-        w.stats[slot].reserved = 0.0f;
-    }
+    if (pending) tma_wait(&s_mbar, parity, a.error);
+    __syncthreads();
+    finish(a, cm, sX, sc, it);
+}
+
+size_t smem_single(int rows_max, int win_max, int blk_max, bool cache) {
+    size_t floats = (size_t)rows_max * 12 + (size_t)win_max * 18;
+    size_t bytes = floats * 4 + (size_t)(rows_max + 4) * 4;
+    if (cache) bytes += (size_t)blk_max * 40;
+    return (bytes + 15) & ~(size_t)15;
+}
+
+size_t smem_standard(int rows_max, int win_max, int blk_max, bool cache) {
+    size_t floats = (size_t)rows_max * 18 + (size_t)win_max * 6;
+    size_t bytes = floats * 4 + (size_t)(rows_max + 4) * 4;
+    if (cache) bytes += (size_t)blk_max * 40;
+    return (bytes + 15) & ~(size_t)15;
+}
+
+typedef void (*PcgKernel)(PcgArgs);
+
+PcgKernel pick_kernel(const PcgLayout &L) {
+    if (L.variant == PcgLayout::kSingleReduction)
+        return L.cache_matrix ? pcg_single_kernel<true> : pcg_single_kernel<false>;
+    return L.cache_matrix ? pcg_standard_kernel<true> : pcg_standard_kernel<false>;
 }
 
 }  // namespace
 
 cudaError_t pcg_max_ctas(int device, int *ctas) {
-    int sms = 0, per_sm = 0;
+    int sms = 0;
     cudaError_t err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    if (err != cudaSuccess) return err;
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_kernel, kPcgThreads, 0);
-    if (err != cudaSuccess) return err;
-    *ctas = sms * per_sm;
-    return cudaSuccess;
+    *ctas = std::min(sms, kMaxCtas);
+    return err;
 }
 
-cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, int ctas, int slot, float tol,
-                       int maxiter, int use_precond, cudaStream_t s) {
+cudaError_t pcg_plan_layout(int device, PcgLayout &L, const int32_t *row_ptr, const int32_t *col_idx, int n,
+                            int ctas, int variant, std::vector<int4> &cta_info, std::string &err) {
+    int optin = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (e != cudaSuccess) return e;
+    const size_t budget = (size_t)optin > kStaticSmem ? (size_t)optin - kStaticSmem : 0;
+    if (ctas > kMaxCtas) {
+        err = "pcg_ctas above " + std::to_string(kMaxCtas);
+        return cudaErrorInvalidValue;
+    }
+    cta_info.assign(ctas, make_int4(0, 0, 0, 0));
+    int rows_max = 0, win_max = 0, blk_max = 0;
+    for (int c = 0; c < ctas; ++c) {
+        const int lo = (int)(((long long)n * c) / ctas);
+        const int hi = (int)(((long long)n * (c + 1)) / ctas);
+        int wlo = lo, whi = hi;
+        for (int64_t k = row_ptr[lo]; k < row_ptr[hi]; ++k) {
+            wlo = std::min(wlo, (int)col_idx[k]);
+            whi = std::max(whi, (int)col_idx[k] + 1);
+        }
+        wlo &= ~3;             // 48-byte (3 x 16 B) aligned start
+        whi = (whi + 3) & ~3;  // length a multiple of 4 rows
+        if (hi == lo) wlo = whi = lo & ~3;
+        cta_info[c] = make_int4(lo, hi, wlo, whi);
+        rows_max = std::max(rows_max, hi - lo);
+        win_max = std::max(win_max, whi - wlo);
+        blk_max = std::max(blk_max, (int)(row_ptr[hi] - row_ptr[lo]));
+    }
+    L.rows_max = (rows_max + 3) & ~3;
+    L.win_max = (win_max + 3) & ~3;
+    L.blk_max = (blk_max + 3) & ~3;
+    struct Option {
+        int variant;
+        bool cache;
+        size_t bytes;
+    } opts[4] = {
+        {PcgLayout::kSingleReduction, true, smem_single(L.rows_max, L.win_max, L.blk_max, true)},
+        {PcgLayout::kStandard, true, smem_standard(L.rows_max, L.win_max, L.blk_max, true)},
+        {PcgLayout::kSingleReduction, false, smem_single(L.rows_max, L.win_max, L.blk_max, false)},
+        {PcgLayout::kStandard, false, smem_standard(L.rows_max, L.win_max, L.blk_max, false)},
+    };
+    bool found = false;
+    for (const auto &o : opts) {
+        if (variant != PcgLayout::kAuto && o.variant != variant) continue;
+        if (o.bytes <= budget) {
+            L.variant = o.variant;
+            L.cache_matrix = o.cache ? 1 : 0;
+            L.smem = o.bytes;
+            found = true;
+            break;
+        }
+    }
+    if (!found) {
+        err = "mesh too large for the persistent PCG (shared memory per CTA exceeded)";
+        return cudaErrorInvalidValue;
+    }
+    PcgKernel k = pick_kernel(L);
+    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
+}
+
+cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const PcgLayout &L, int ctas,
+                       int slot, float tol, int maxiter, int use_precond, cudaStream_t s) {
+    PcgArgs a;
+    a.n = bv.n;
+    a.row_ptr = bv.row_ptr;
+    a.col_idx = bv.col_idx;
+    a.values = bv.values;
+    a.Minv = vv.Minv;
+    a.b = vv.rhs;
+    a.x = vv.dx;
+    a.pub = w.pub;
+    a.n_pad = w.n_pad;
+    a.cta = L.cta_info;
+    a.rows_max = L.rows_max;
+    a.blk_max = L.blk_max;
+    a.win_max = L.win_max;
+    a.partials = w.partials;
+    a.counter = w.counter;
+    a.error = w.error;
+    a.stats = w.stats;
+    a.slot = slot;
+    a.tol = tol;
+    a.maxiter = maxiter;
+    a.use_precond = use_precond;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(ctas);
     cfg.blockDim = dim3(kPcgThreads);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = L.smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t err = cudaLaunchKernelEx(&cfg, pcg_kernel, bv, (const float *)vv.Minv, (const float *)vv.rhs, vv.dx, w,
-                                         slot, tol, maxiter, use_precond);
+    cudaError_t err = cudaLaunchKernelEx(&cfg, pick_kernel(L), a);
     count_launches(1);
     return err;
 }

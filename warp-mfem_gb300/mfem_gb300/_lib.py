@@ -43,7 +43,8 @@ class MfemConfig(ctypes.Structure):
         ("preconditioner", ctypes.c_int32),
         ("use_cuda_graph", ctypes.c_int32),
         ("pcg_ctas", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 7),
+        ("pcg_variant", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 6),
     ]
 
 

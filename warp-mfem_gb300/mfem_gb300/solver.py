@@ -68,6 +68,7 @@ class MixedFEMSolver:
         cfg.preconditioner = 1 if kwargs.get("preconditioner", True) else 0
         cfg.use_cuda_graph = 1 if kwargs.get("use_cuda_graph", True) else 0
         cfg.pcg_ctas = int(kwargs.get("pcg_ctas", 0))
+        cfg.pcg_variant = {"auto": 0, "standard": 1, "single_reduction": 2}[kwargs.get("pcg_variant", "auto")]
         self.config = cfg
 
         host = lambda t, dt: np.ascontiguousarray(t.detach().to("cpu").numpy(), dtype=dt)
