@@ -204,6 +204,28 @@ int mfem_local_solve(mfem_plan *plan, float *d_x, mfem_stream stream);
  * true-residual check of the float32 recurrence. */
 int mfem_true_residual(mfem_plan *plan, double *h_rel_residual, mfem_stream stream);
 
+/* ---- allocation-free solve ---------------------------------------------- */
+
+/* Block-Jacobi PCG on a caller-provided 3x3-block BSR system that allocates
+ * nothing, for callers that cannot call cudaMalloc when they solve (a
+ * framework's caching allocator owns the heap, or the host forbids
+ * allocation after start-up).  It has no counterpart in the reference.
+ * Device arrays, all caller-owned: row_ptr [n+1], col_idx [nnzb], values
+ * [nnzb][3][3], precond [n][3][3] block inverse (NULL: unpreconditioned),
+ * b [n][3]; x [n][3] holds the warm start and receives the solution;
+ * stats (device pointer, may be NULL) receives the outcome.  Stops when
+ * ||r|| <= tol ||b|| or after maxiter iterations.
+ * Its scratch is a fixed array of about 2 MB inside the library (every GPU
+ * that loads the library holds it until exit) serving at most 32768 block
+ * rows; larger systems return MFEM_BAD_ARG.  All calls share that array:
+ * calls whose kernels overlap on the GPU race and must be serialised.  The
+ * first call on a device looks up the array's address with that device
+ * current; make it before any stream capture.  Asynchronous on `stream`;
+ * errors are reported by mfem_plan_last_error(NULL). */
+int mfem_pcg_solve_noalloc(int32_t n, const int32_t *d_row_ptr, const int32_t *d_col_idx,
+                           const float *d_values, const float *d_precond, const float *d_b, float *d_x,
+                           float tol, int32_t maxiter, mfem_solve_stats *d_stats, mfem_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,6 +19,11 @@ void count_launches(uint64_t k) {
     if (!t_capturing) g_launches += k;
 }
 
+int set_create_error(int code, const std::string &msg) {
+    t_create_error = msg;
+    return code;
+}
+
 }  // namespace mfem
 
 using namespace mfem;

@@ -132,4 +132,8 @@ cudaError_t launch_true_residual(const BsrViews &bv, const VertexViews &vv, doub
 // Number of kernels launched by the launchers above (process-wide).
 void count_launches(uint64_t k);
 
+// Records the message returned by mfem_plan_last_error(NULL) for a call
+// that has no plan; returns `code`.
+int set_create_error(int code, const std::string &msg);
+
 }  // namespace mfem

@@ -90,6 +90,7 @@ _SIGNATURES = {
     "mfem_global_solve": (ctypes.c_int, [_P, _I32, _P]),
     "mfem_local_solve": (ctypes.c_int, [_P, _P, _P]),
     "mfem_true_residual": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _P]),
+    "mfem_pcg_solve_noalloc": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _P, _F32, _I32, _P, _P]),
 }
 
 _lib = None
