@@ -138,14 +138,14 @@ def hbm_peak():
 
 
 def ncu_traffic_per_launch():
-    """Per-launch DRAM bytes of the PCG kernel from the committed ncu summary,
-    scaled to this workload's PCG iterations by the summary's bytes/iteration."""
+    """DRAM bytes (read + write) of one PCG launch from the committed ncu
+    summary of this workload (profiles/pcg_kernel_nh_beam.md)."""
     path = os.path.join(ROOT, "profiles", "pcg_kernel_nh_beam.md")
     try:
         text = open(path).read()
     except OSError:
         return None
-    m = re.search(r"dram_bytes_per_pcg_iteration:\s*([0-9.eE+]+)", text)
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", text)
     return float(m.group(1)) if m else None
 
 
@@ -362,10 +362,11 @@ def run_gb300(args, rank, world, local_rank):
     achieved = pcg_bytes / (stage_ms["pcg"] / 1000.0) / 1e9
     peak, peak_src = hbm_peak()
     per_launch_iters = (prof_iters + prof_solves) / prof_solves
-    traffic_it = ncu_traffic_per_launch()
+    traffic = ncu_traffic_per_launch()
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-        "traffic": (traffic_it * per_launch_iters) if traffic_it else None,
+        "traffic": traffic,
+        "traffic_note": "DRAM bytes of one captured launch (about 378 iterations), profiles/pcg_kernel_nh_beam.md",
         "kernel": "pcg_kernel (persistent cooperative block-Jacobi PCG)",
         "algorithmic_bytes_per_launch": b_it * per_launch_iters,
         "bytes_per_pcg_iteration": b_it, "pcg_iterations_per_launch": per_launch_iters - 1,
