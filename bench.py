@@ -149,6 +149,22 @@ def ncu_traffic_per_launch():
     return float(m.group(1)) if m else None
 
 
+def max_over_ranks(seconds: float, world: int, device=None) -> float:
+    """Largest per-rank time of the job (a no-op on one rank)."""
+    if world <= 1:
+        return seconds
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(steps_per_rank: int, world: int, t_max: float) -> float:
+    """Whole-job steps/s of `world` independent replicas."""
+    return world * steps_per_rank / t_max
+
+
 def pcg_bytes_per_iteration(nnzb: int, n: int) -> int:
     """Algorithmic bytes of one plain fp32 PCG iteration: 36 B values + 4 B
     column index per block; per row 4 B row pointer + 24 B (read p, write Ap)
@@ -268,14 +284,8 @@ def run_gb300(args, rank, world, local_rank):
     launches = _lib.kernel_launch_count() - launches0
     barrier()
     clocks = sampler.stop()
-    t_local = total_ms / 1000.0
-    if world > 1:
-        t = torch.tensor([t_local], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    else:
-        t_max = t_local
-    value = world * args.steps / t_max
+    t_max = max_over_ranks(total_ms / 1000.0, world, dev)
+    value = job_rate(args.steps, world, t_max)
     q_final = A.particle_q.cpu().numpy()
 
     # ---- e2e: host-resident state through the public API
@@ -304,13 +314,8 @@ def run_gb300(args, rank, world, local_rank):
         hq, oq = oq, hq
         hqd, oqd = oqd, hqd
     barrier()
-    if world > 1:
-        t = torch.tensor([e2e_ms / 1000.0], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    else:
-        e2e_s = e2e_ms / 1000.0
-    e2e_value = world * args.steps / e2e_s
+    e2e_s = max_over_ranks(e2e_ms / 1000.0, world, dev)
+    e2e_value = job_rate(args.steps, world, e2e_s)
     e2e_match = bool(np.array_equal(hq.numpy(), q_final))
     state_bytes = 2 * mesh.n * 3 * 4
 

@@ -61,7 +61,8 @@ typedef struct mfem_config {
     int32_t use_cuda_graph;               /* capture mfem_step once per argument set and replay  */
     int32_t pcg_ctas;                     /* persistent PCG CTAs; 0 = one per SM                 */
     int32_t pcg_variant;                  /* 0 auto, 1 standard (two reductions per iteration),
-                                             2 single-reduction (Chronopoulos-Gear)             */
+                                             2 single-reduction (Chronopoulos-Gear), 3 gather
+                                             (standard, no column windows: any vertex order)    */
     int32_t reserved[6];
 } mfem_config;
 
@@ -149,6 +150,13 @@ void mfem_plan_destroy(mfem_plan *plan);
 const char *mfem_plan_last_error(const mfem_plan *plan);
 
 int mfem_plan_sizes(const mfem_plan *plan, int32_t *n_particles, int32_t *n_tets, int64_t *nnzb);
+
+/* The persistent PCG the plan chose: variant (1 standard, 2 single-reduction,
+ * 3 gather), CTAs, whether each CTA keeps its slice of H in shared memory,
+ * and the dynamic shared memory per CTA.  Diagnostics; no reference
+ * counterpart. */
+int mfem_plan_pcg_layout(const mfem_plan *plan, int32_t *variant, int32_t *ctas, int32_t *cache_matrix,
+                         int64_t *smem_bytes);
 
 /* Bytes of an exposed buffer. */
 int mfem_plan_buffer_bytes(const mfem_plan *plan, int32_t which, size_t *bytes);

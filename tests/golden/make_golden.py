@@ -8,6 +8,9 @@ known_answers.npz -- the inputs of the reference's own known-answer tests for
 cantilever_fp64.npz -- the float64 oracle's 100-step trajectory of the
     10x2x2 ARAP cantilever (positions after every step, final s and lambda,
     PCG iterations per Newton iteration).
+reference_fixture_digests.json -- sha256 digests and shapes of the arrays of
+    the reference's fem_beam.npz (written only where the reference tree is
+    present), so the 5-tet grid generator is pinned to it without copying it.
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -112,7 +115,30 @@ def cantilever_trajectory():
                 pcg_iterations=np.array(iters, dtype=np.int32))
 
 
+REFERENCE_TREE = "/root/reference"
+
+
+def array_digest(a: np.ndarray) -> dict:
+    import hashlib
+    a = np.ascontiguousarray(a)
+    return {"dtype": str(a.dtype), "shape": list(a.shape), "sha256": hashlib.sha256(a.tobytes()).hexdigest()}
+
+
+def reference_fixture_digests():
+    path = os.path.join(REFERENCE_TREE, "fem_beam.npz")
+    if not os.path.exists(path):
+        return None
+    d = np.load(path)
+    return {"fem_beam.npz": {k: array_digest(d[k]) for k in ("particles", "tet_indices", "tet_materials")}
+            | {"parameters": d["parameters"].tolist()}}
+
+
 def main():
+    import json
+    digests = reference_fixture_digests()
+    if digests is not None:
+        with open(os.path.join(HERE, "reference_fixture_digests.json"), "w") as f:
+            json.dump(digests, f, indent=1)
     np.savez_compressed(os.path.join(HERE, "known_answers.npz"), **known_answers())
     np.savez_compressed(os.path.join(HERE, "cantilever_fp64.npz"), **cantilever_trajectory())
     print("wrote", os.listdir(HERE))

@@ -142,7 +142,7 @@ bool valid_config(const mfem_config *cfg, std::string &err) {
         err = "attachment_stiffness must be finite and >= 0";
     else if (!(cfg->preconditioner_singular_threshold >= 0.0f)) err = "preconditioner_singular_threshold must be >= 0";
     else if (cfg->pcg_ctas < 0) err = "pcg_ctas must be >= 0";
-    else if (cfg->pcg_variant < 0 || cfg->pcg_variant > 2) err = "pcg_variant must be 0 (auto), 1 or 2";
+    else if (cfg->pcg_variant < 0 || cfg->pcg_variant > 3) err = "pcg_variant must be 0 (auto), 1, 2 or 3";
     else return true;
     return false;
 }
@@ -435,6 +435,16 @@ int mfem_plan_sizes(const mfem_plan *p, int32_t *n, int32_t *T, int64_t *nnzb) {
     if (n) *n = p->n;
     if (T) *T = p->T;
     if (nnzb) *nnzb = p->nnzb;
+    return MFEM_OK;
+}
+
+int mfem_plan_pcg_layout(const mfem_plan *p, int32_t *variant, int32_t *ctas, int32_t *cache_matrix,
+                         int64_t *smem_bytes) {
+    if (!p) return MFEM_BAD_ARG;
+    if (variant) *variant = p->pl.variant;
+    if (ctas) *ctas = p->pcg_ctas;
+    if (cache_matrix) *cache_matrix = p->pl.cache_matrix;
+    if (smem_bytes) *smem_bytes = (int64_t)p->pl.smem;
     return MFEM_OK;
 }
 

@@ -93,7 +93,7 @@ struct PcgWork {
 
 // Row partition and shared-memory plan of the persistent PCG.
 struct PcgLayout {
-    enum { kAuto = 0, kStandard = 1, kSingleReduction = 2 };
+    enum { kAuto = 0, kStandard = 1, kSingleReduction = 2, kGather = 3 };
     const int4 *cta_info;      // device [ctas]: (row_lo, row_hi, win_lo, win_hi)
     int variant = kSingleReduction;
     int rows_max = 0, blk_max = 0, win_max = 0;

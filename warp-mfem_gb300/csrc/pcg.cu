@@ -31,6 +31,8 @@
 //    iteration: A: p = z + beta p over the window, Ap = H p, (p, Ap);
 //    B: x += alpha p, r -= alpha Ap, z = M r, (r, z), (r, r).  Used when the
 //    single-reduction windows do not fit in shared memory.
+//  * gather: the standard form without windows, other rows gathered from L2;
+//    for meshes whose vertex order is not banded.
 //
 // Grid synchronisation is a reduction: each CTA stores its partial sums
 // (double buffered by barrier parity), then arrives on a 64-bit counter that
@@ -740,6 +742,221 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_standard_kernel(PcgArgs a)
     finish(a, cm, sX, sc, it);
 }
 
+// ===========================================================================
+// gather variant: standard two-barrier PCG for any vertex order
+// ===========================================================================
+// When the column windows do not fit in shared memory (a mesh whose vertex
+// order is not banded), each CTA keeps only its own rows in shared memory and
+// gathers the other rows' published z and previous p straight from L2 in the
+// product; p_j = z_j + beta p_j is formed on the fly, with the same
+// instructions the owner uses, so every CTA sees the same p.
+template <bool CACHE>
+__device__ __forceinline__ void gather_product(const PcgArgs &a, const int *rowoff, const float *sH, const int *sCol,
+                                               int blk_lo, int nrows, const float *z, const float *p_old, float beta,
+                                               float *out) {
+    const int g_lane = threadIdx.x & (kGroup - 1);
+    const int group = threadIdx.x / kGroup;
+    const int ngroups = blockDim.x / kGroup;
+    const unsigned gmask = ((1u << kGroup) - 1u) << (threadIdx.x & (32 - kGroup));
+    for (int i = group; i < nrows; i += ngroups) {
+        const int kb = rowoff[i], ke = rowoff[i + 1];
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+        for (int k = kb + g_lane; k < ke; k += kGroup) {
+            const float *h;
+            int c;
+            if (CACHE) {
+                h = sH + (size_t)k * 9;
+                c = sCol[k];
+            } else {
+                h = a.values + (size_t)(blk_lo + k) * 9;
+                c = __ldg(a.col_idx + blk_lo + k);
+            }
+            float v[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const float zc = __ldcg(z + 3 * c + q);
+                v[q] = p_old ? __fmaf_rn(beta, __ldcg(p_old + 3 * c + q), zc) : zc;
+            }
+            a0 += h[0] * v[0] + h[1] * v[1] + h[2] * v[2];
+            a1 += h[3] * v[0] + h[4] * v[1] + h[5] * v[2];
+            a2 += h[6] * v[0] + h[7] * v[1] + h[8] * v[2];
+        }
+#pragma unroll
+        for (int off = kGroup / 2; off > 0; off >>= 1) {
+            a0 += __shfl_xor_sync(gmask, a0, off);
+            a1 += __shfl_xor_sync(gmask, a1, off);
+            a2 += __shfl_xor_sync(gmask, a2, off);
+        }
+        if (g_lane == 0) {
+            out[3 * i + 0] = a0;
+            out[3 * i + 1] = a1;
+            out[3 * i + 2] = a2;
+        }
+    }
+}
+
+template <bool CACHE>
+__global__ void __launch_bounds__(kPcgThreads, 1) pcg_gather_kernel(PcgArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    PCG_PROLOGUE
+    const int rows_max = a.rows_max;
+    float *sX = reinterpret_cast<float *>(smem);
+    float *sR = sX + 3 * rows_max;
+    float *sAp = sR + 3 * rows_max;
+    float *sP = sAp + 3 * rows_max;
+    float *sM = sP + 3 * rows_max;
+    int *rowoff = reinterpret_cast<int *>(sM + 9 * rows_max);
+    float *sH = reinterpret_cast<float *>(rowoff + rows_max + 4);
+    int *sCol = reinterpret_cast<int *>(sH + (CACHE ? 9 * a.blk_max : 0));
+    (void)parity;
+
+    const size_t vec = (size_t)3 * a.n_pad;
+    float *pubZ = a.pub;
+    float *pubP[2] = {a.pub + vec, a.pub + 2 * vec};
+    const size_t own3 = (size_t)3 * cm.row_lo;
+
+    for (int i = threadIdx.x; i <= cm.nrows; i += blockDim.x) rowoff[i] = a.row_ptr[cm.row_lo + i] - cm.blk_lo;
+    if (CACHE) {
+        for (int k = threadIdx.x; k < 9 * cm.nblk; k += blockDim.x) sH[k] = a.values[(size_t)9 * cm.blk_lo + k];
+        for (int k = threadIdx.x; k < cm.nblk; k += blockDim.x) sCol[k] = a.col_idx[cm.blk_lo + k];
+    }
+    for (int i = threadIdx.x; i < 9 * cm.nrows; i += blockDim.x) sM[i] = a.Minv[(size_t)9 * cm.row_lo + i];
+    for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = a.x[own3 + i];
+    __syncthreads();
+
+    int it = 0;
+    bool ok;
+    {
+        // r = g - H x0 (x0 was written before the launch), z = M r
+        gather_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.nrows, a.x, nullptr, 0.0f, sAp);
+        __syncthreads();
+        float acc[3] = {0.0f, 0.0f, 0.0f};
+        for (int i = threadIdx.x; i < cm.nrows; i += blockDim.x) {
+            float r[3], z[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float bc = a.b[own3 + 3 * i + c];
+                r[c] = bc - sAp[3 * i + c];
+                sR[3 * i + c] = r[c];
+                acc[2] = __fmaf_rn(bc, bc, acc[2]);
+            }
+            precond(sM + 9 * i, r, z, a.use_precond);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                pubZ[own3 + 3 * i + c] = z[c];
+                acc[0] = __fmaf_rn(r[c], z[c], acc[0]);
+                acc[1] = __fmaf_rn(r[c], r[c], acc[1]);
+            }
+        }
+        ok = reduce_arrive<3>(acc, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok);
+    }
+    if (ok) {
+        reduce_totals<3>(a.partials, bar, s_val, s_tot);
+        if (threadIdx.x == 0) {
+            sc.gamma = s_tot[0];
+            sc.rr = s_tot[1];
+            sc.bb = s_tot[2];
+            sc.thr2 = a.tol * a.tol * s_tot[2];
+            sc.beta = 0.0f;
+            sc.status = (!isfinite(s_tot[0]) || !isfinite(s_tot[1]) || !isfinite(s_tot[2])) ? MFEM_NONFINITE : MFEM_OK;
+            sc.done = sc.status != MFEM_OK || s_tot[1] <= sc.thr2;
+        }
+    } else if (threadIdx.x == 0) {
+        sc.status = MFEM_TIMEOUT;
+        sc.done = 1;
+        sc.rr = 0.0f;
+        sc.bb = 1.0f;
+    }
+    ++bar;
+    __syncthreads();
+    while (!sc.done) {
+        if (it >= a.maxiter) {
+            if (threadIdx.x == 0) sc.status = MFEM_MAXITER;
+            break;
+        }
+        // ---- phase A: p = z + beta p (formed on the fly), Ap = H p, p.Ap
+        float *p_new = pubP[it & 1];
+        const float *p_old = it == 0 ? nullptr : pubP[(it + 1) & 1];
+        const float fbeta = sc.beta;
+        for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) {
+            const float zc = __ldcg(pubZ + own3 + i);
+            const float pv = p_old ? __fmaf_rn(fbeta, __ldcg(p_old + own3 + i), zc) : zc;
+            sP[i] = pv;
+            p_new[own3 + i] = pv;
+        }
+        gather_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.nrows, pubZ, p_old, fbeta, sAp);
+        __syncthreads();
+        float pap[1] = {0.0f};
+        for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) pap[0] = __fmaf_rn(sP[i], sAp[i], pap[0]);
+        if (!reduce_arrive<1>(pap, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok)) {
+            if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+            break;
+        }
+        reduce_totals<1>(a.partials, bar, s_val, s_tot);
+        ++bar;
+        if (threadIdx.x == 0) {
+            const float pAp = s_tot[0];
+            if (!isfinite(pAp)) {
+                sc.status = MFEM_NONFINITE;
+                sc.done = 1;
+            } else if (!(pAp > 0.0f)) {
+                sc.status = MFEM_STAGNATION;
+                sc.done = 1;
+            } else {
+                sc.alpha = sc.gamma / pAp;
+            }
+        }
+        __syncthreads();
+        if (sc.done) break;
+        const float alpha = sc.alpha;
+        // ---- phase B: x += alpha p, r -= alpha Ap, z = M r
+        float acc[2] = {0.0f, 0.0f};
+        for (int i = threadIdx.x; i < cm.nrows; i += blockDim.x) {
+            float r[3], z[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                sX[3 * i + c] = __fmaf_rn(alpha, sP[3 * i + c], sX[3 * i + c]);
+                r[c] = __fmaf_rn(-alpha, sAp[3 * i + c], sR[3 * i + c]);
+                sR[3 * i + c] = r[c];
+            }
+            precond(sM + 9 * i, r, z, a.use_precond);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                pubZ[own3 + 3 * i + c] = z[c];
+                acc[0] = __fmaf_rn(r[c], z[c], acc[0]);
+                acc[1] = __fmaf_rn(r[c], r[c], acc[1]);
+            }
+        }
+        if (!reduce_arrive<2>(acc, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok)) {
+            if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+            break;
+        }
+        ++it;
+        reduce_totals<2>(a.partials, bar, s_val, s_tot);
+        ++bar;
+        if (threadIdx.x == 0) {
+            sc.rr = s_tot[1];
+            if (!isfinite(s_tot[0]) || !isfinite(s_tot[1])) {
+                sc.status = MFEM_NONFINITE;
+                sc.done = 1;
+            } else {
+                sc.beta = s_tot[0] / sc.gamma;
+                sc.gamma = s_tot[0];
+                sc.done = s_tot[1] <= sc.thr2;
+            }
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    finish(a, cm, sX, sc, it);
+}
+
+size_t smem_gather(int rows_max, int blk_max, bool cache) {
+    size_t bytes = (size_t)rows_max * 21 * 4 + (size_t)(rows_max + 4) * 4;
+    if (cache) bytes += (size_t)blk_max * 40;
+    return (bytes + 15) & ~(size_t)15;
+}
+
 size_t smem_single(int rows_max, int win_max, int blk_max, bool cache) {
     size_t floats = (size_t)rows_max * 12 + (size_t)win_max * 18;
     size_t bytes = floats * 4 + (size_t)(rows_max + 4) * 4;
@@ -759,6 +976,8 @@ typedef void (*PcgKernel)(PcgArgs);
 PcgKernel pick_kernel(const PcgLayout &L) {
     if (L.variant == PcgLayout::kSingleReduction)
         return L.cache_matrix ? pcg_single_kernel<true> : pcg_single_kernel<false>;
+    if (L.variant == PcgLayout::kGather)
+        return L.cache_matrix ? pcg_gather_kernel<true> : pcg_gather_kernel<false>;
     return L.cache_matrix ? pcg_standard_kernel<true> : pcg_standard_kernel<false>;
 }
 
@@ -806,11 +1025,13 @@ cudaError_t pcg_plan_layout(int device, PcgLayout &L, const int32_t *row_ptr, co
         int variant;
         bool cache;
         size_t bytes;
-    } opts[4] = {
+    } opts[6] = {
         {PcgLayout::kSingleReduction, true, smem_single(L.rows_max, L.win_max, L.blk_max, true)},
         {PcgLayout::kStandard, true, smem_standard(L.rows_max, L.win_max, L.blk_max, true)},
         {PcgLayout::kSingleReduction, false, smem_single(L.rows_max, L.win_max, L.blk_max, false)},
         {PcgLayout::kStandard, false, smem_standard(L.rows_max, L.win_max, L.blk_max, false)},
+        {PcgLayout::kGather, true, smem_gather(L.rows_max, L.blk_max, true)},
+        {PcgLayout::kGather, false, smem_gather(L.rows_max, L.blk_max, false)},
     };
     bool found = false;
     for (const auto &o : opts) {

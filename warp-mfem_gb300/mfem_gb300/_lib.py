@@ -80,6 +80,8 @@ _SIGNATURES = {
     "mfem_plan_last_error": (ctypes.c_char_p, [_P]),
     "mfem_plan_sizes": (ctypes.c_int, [_P, ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(_I64)]),
     "mfem_plan_buffer_bytes": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_size_t)]),
+    "mfem_plan_pcg_layout": (ctypes.c_int, [_P, ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(_I32),
+                                            ctypes.POINTER(_I64)]),
     "mfem_plan_copy_out": (ctypes.c_int, [_P, _I32, _P, ctypes.c_size_t, _P]),
     "mfem_plan_copy_in": (ctypes.c_int, [_P, _I32, _P, ctypes.c_size_t, _P]),
     "mfem_step": (ctypes.c_int, [_P, _P, _P, _P, _P, _F32, _P]),

@@ -68,7 +68,8 @@ class MixedFEMSolver:
         cfg.preconditioner = 1 if kwargs.get("preconditioner", True) else 0
         cfg.use_cuda_graph = 1 if kwargs.get("use_cuda_graph", True) else 0
         cfg.pcg_ctas = int(kwargs.get("pcg_ctas", 0))
-        cfg.pcg_variant = {"auto": 0, "standard": 1, "single_reduction": 2}[kwargs.get("pcg_variant", "auto")]
+        cfg.pcg_variant = {"auto": 0, "standard": 1, "single_reduction": 2,
+                           "gather": 3}[kwargs.get("pcg_variant", "auto")]
         self.config = cfg
 
         host = lambda t, dt: np.ascontiguousarray(t.detach().to("cpu").numpy(), dtype=dt)
@@ -93,6 +94,16 @@ class MixedFEMSolver:
         nnzb = ctypes.c_int64()
         self._lib.mfem_plan_sizes(plan, ctypes.byref(n), ctypes.byref(T), ctypes.byref(nnzb))
         self.n, self.T, self.nnzb = n.value, T.value, nnzb.value
+
+    def pcg_layout(self) -> dict:
+        """The persistent PCG this plan uses (variant, CTAs, matrix cached in
+        shared memory, dynamic shared memory per CTA)."""
+        v, c, m = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        smem = ctypes.c_int64()
+        _lib.check(self._lib.mfem_plan_pcg_layout(self._plan, ctypes.byref(v), ctypes.byref(c), ctypes.byref(m),
+                                                  ctypes.byref(smem)), self._plan)
+        name = {1: "standard", 2: "single_reduction", 3: "gather"}[v.value]
+        return dict(variant=name, ctas=c.value, cache_matrix=bool(m.value), smem_bytes=smem.value)
 
     # ------------------------------------------------------------------
     def close(self) -> None:
