@@ -233,7 +233,8 @@ def run_gb300(args, rank, world, local_rank):
     model = Model.from_beam(mesh, device=dev)
     solver = MixedFEMSolver(model, iterations=spec.iterations, energy=spec.energy,
                             cg_tolerance=spec.cg_tolerance, cg_max_iterations=spec.cg_max_iterations,
-                            pcg_ctas=args.pcg_ctas, pcg_variant=args.pcg_variant)
+                            pcg_ctas=args.pcg_ctas, pcg_variant=args.pcg_variant,
+                            line_search=False)  # the workload is the plain local/global step
     s_init = solver.tet_stretch.clone().reshape(-1)
     lam0 = torch.zeros_like(s_init)
     q0 = torch.as_tensor(mesh.q0, device=dev)

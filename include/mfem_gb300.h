@@ -63,7 +63,14 @@ typedef struct mfem_config {
     int32_t pcg_variant;                  /* 0 auto, 1 standard (two reductions per iteration),
                                              2 single-reduction (Chronopoulos-Gear), 3 gather
                                              (standard, no column windows: any vertex order)    */
-    int32_t reserved[6];
+    /* backtracking line search on the merit function in place of x += dx,
+     * s += ds (solver.py:99-103, 185, 539-557; src/mfem/line_search.py:76-163) */
+    int32_t line_search;                  /* 1 on (the reference's default), 0 plain update      */
+    int32_t line_search_max_iterations;   /* default 20                                          */
+    float line_search_alpha0;             /* first step, default 1                               */
+    float line_search_tau;                /* step shrink factor, default 0.5                     */
+    float line_search_c;                  /* Armijo constant, default 0.01                       */
+    float line_search_threshold;          /* slack added to the decrease, default 1e-8           */
 } mfem_config;
 
 /* Buffers owned by a plan that mfem_plan_copy_out / _copy_in expose.
@@ -87,7 +94,8 @@ typedef enum mfem_buffer {
     MFEM_BUF_PRECOND = 15,      /* f32 [n][3][3] block-Jacobi inverse diagonal             */
     MFEM_BUF_X_TILDE = 16,      /* f32 [n][3]  predictor x~                                 */
     MFEM_BUF_DX = 17,           /* f32 [n][3]  PCG solution dx (warm start x~ - x)          */
-    MFEM_BUF_COUNT = 18
+    MFEM_BUF_STRETCH_DIRECTION = 18, /* f32 [6][T] ds of the last local solve (line search on) */
+    MFEM_BUF_COUNT = 19
 } mfem_buffer;
 
 /* Per Newton iteration outcome of the global solve. */
@@ -98,11 +106,23 @@ typedef struct mfem_solve_stats {
     float reserved;
 } mfem_solve_stats;
 
+/* Per Newton iteration outcome of the line search. */
+typedef struct mfem_line_search_stats {
+    int32_t evaluations;    /* trial evaluations: the reference's iteration counter     */
+    int32_t accepted;       /* 1 if x, s moved to the last trial, 0 if left unchanged   */
+    float alpha;            /* step of the last trial                                   */
+    int32_t status;         /* MFEM_OK, or MFEM_TIMEOUT if a grid wait gave up          */
+    double f0;              /* merit function at (x, s)                                 */
+    double f1;              /* merit function at the last trial                         */
+    double t;               /* -c (gradient . direction)                                */
+} mfem_line_search_stats;
+
 /* ---- configuration / diagnostics ------------------------------------ */
 
 /* Fills the reference's defaults: iterations 8, ARAP, cg_max_iterations 1000,
  * cg_tolerance 1e-6, attachment_stiffness 10, singular threshold 1e-20,
- * block-Jacobi on (src/mfem/refinement/solver.py:90-128). */
+ * block-Jacobi on, line search on with 20 iterations, alpha0 1, tau 0.5,
+ * c 0.01, threshold 1e-8 (src/mfem/refinement/solver.py:90-128, 185). */
 void mfem_config_default(mfem_config *cfg);
 
 const char *mfem_status_string(int status);
@@ -182,6 +202,13 @@ int mfem_step(mfem_plan *plan, const float *d_q_in, const float *d_qd_in,
 int mfem_step_stats(mfem_plan *plan, mfem_solve_stats *h_stats, int32_t max_entries,
                     int32_t *count, mfem_stream stream);
 
+/* Outcome of the line searches of the last step, one entry per Newton
+ * iteration (synchronises the stream; entries are zero with the line search
+ * off).  The reference keeps these in device scalars it does not return
+ * (src/mfem/line_search.py:89-94). */
+int mfem_step_line_search_stats(mfem_plan *plan, mfem_line_search_stats *h_stats, int32_t max_entries,
+                                int32_t *count, mfem_stream stream);
+
 /* Predictor x~ = x + v dt + g dt^2/2 into the plan
  * (integrate_particles, src/mfem/refinement/kernels.py:77-91). */
 int mfem_predict(mfem_plan *plan, const float *d_q, const float *d_qd, float dt, mfem_stream stream);
@@ -203,8 +230,11 @@ int mfem_assemble(mfem_plan *plan, const float *d_x, float dt, mfem_stream strea
 int mfem_global_solve(mfem_plan *plan, int32_t slot, mfem_stream stream);
 
 /* Local solve and update: lambda = -H_l (g_l - G dx), ds = -H_s^-1 (SYM
- * lambda + g_s), s += ds, x += dx (src/mfem/refinement/kernels.py:252-283;
- * solver.py:555-557). */
+ * lambda + g_s) (src/mfem/refinement/kernels.py:252-283), then s += ds,
+ * x += dx (solver.py:555-557), or with the line search on, the backtracking
+ * search along (dx, ds) (solver.py:539-553, 871-928), recorded as the line
+ * search entry of the last mfem_global_solve slot.  Needs the g_x of the
+ * assembly at the same x (mfem_assemble). */
 int mfem_local_solve(mfem_plan *plan, float *d_x, mfem_stream stream);
 
 /* ||g - H dx|| / ||g|| accumulated in float64 for the current H, g, dx

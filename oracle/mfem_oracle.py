@@ -4,7 +4,8 @@ This module is the checker, never the product: only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may import it.
 
 It restates, in batched numpy (float64 or float32), the reference's
-``RefinementSolver.step`` with refinement, contact, shell and line search off:
+``RefinementSolver.step`` with refinement, contact and shell off, with the
+line search on or off:
 
 =========================================  =====================================================
 stage                                      reference (warp-mfem, paths within the project)
@@ -27,6 +28,9 @@ block-Jacobi preconditioner                src/mfem/refinement/kernels.py:32-53;
 PCG (warm start dx = x~ - x)               src/mfem/refinement/solver.py:220-235, 529-532
 local solve for lambda and ds              src/mfem/refinement/kernels.py:252-283
 update and velocity                        src/mfem/refinement/solver.py:555-577; kernels.py:351-363
+line search (merit function, Armijo)       src/mfem/line_search.py:76-163; refinement/solver.py:803-928;
+                                           kernels.py:285-348; elastic_energy.py:155-176, 287-311;
+                                           boundary_condition.py:62-71
 initial stretch s = S(F_rest), lambda = 0  src/mfem/refinement/additional_state.py:146-189
 =========================================  =====================================================
 
@@ -48,7 +52,11 @@ stretch, the PSD-fix matrices: tests/test_kernels.py, tests/test_functions.py,
 tests/numerical/test_psd_fix.py).  The reference ships no test of the
 assembly, the PCG or a whole step and cannot be run here (warp-lang / newton are
 absent), so at step level the oracle's parity with the reference is UNPINNED:
-it follows the reference's code line by line, nothing more.
+it follows the reference's code line by line, nothing more.  The same holds
+for the line search, which no reference test exercises.  It keeps the
+reference's slope sign: the x-gradient is g_x - G^T lambda with G = dC_dX =
+-dc/dx (kernels.py:159, solver.py:905), which is not the merit function's
+x-gradient g_x + G^T lambda.
 """
 from __future__ import annotations
 
@@ -456,13 +464,58 @@ def pcg(apply_A, b, x0, Minv_blocks, tol, maxiter):
     return x, PCGResult(it, r_norm, b_norm, r_norm <= target)
 
 
+def elastic_energy_only(energy, s, materials, DmInv):
+    """Per-tet elastic energy in s (the *_energy_only kernels,
+    src/mfem/refinement/elastic_energy.py:155-176, 287-311)."""
+    if energy == "arap":
+        return arap_energy(s, materials, DmInv)[0]
+    mu = materials[:, 0]
+    lam = materials[:, 1]
+    vol = rest_volume(DmInv)
+    I2 = s[:, 0] ** 2 + s[:, 1] ** 2 + s[:, 2] ** 2 + 2.0 * (s[:, 3] ** 2 + s[:, 4] ** 2 + s[:, 5] ** 2)
+    J = det_sym6(s)
+    return vol * (mu * (I2 - 3.0) / 2.0 - mu * (J - 1.0) + lam / 2.0 * (J - 1.0) * (J - 1.0))
+
+
+@dataclass
+class LineSearchResult:
+    accepted: bool
+    alpha: float
+    evaluations: int
+    f0: float
+    f1: float
+    t: float
+
+
+def backtracking(f, f0, t, alpha0, tau, threshold, max_iterations) -> LineSearchResult:
+    """The device loop of src/mfem/line_search.py:76-163 on the host.
+    f(alpha) is the merit at the trial alpha.  Trial j uses alpha0 tau^j; the
+    loop goes on while (f0 - f1) + threshold < alpha t and the counter (j
+    before the trial) is below max_iterations (_condition_kernel, :44-63),
+    so it runs at most max_iterations + 1 trials.  The last trial is written
+    only if the counter after it is below max_iterations
+    (_iteration_condition and capture_if, :66-72, 148-161)."""
+    alpha = alpha0
+    j = 0
+    while True:
+        f1 = f(alpha)
+        more = ((f0 - f1) + threshold < alpha * t) and j < max_iterations
+        j += 1
+        if not more:
+            break
+        alpha = alpha * tau
+    return LineSearchResult(j < max_iterations, float(alpha), j, float(f0), float(f1), float(t))
+
+
 class OracleSolver:
     """The reference's step on the CPU.  ``dtype`` float64 is the accuracy
     judge; float32 mirrors the reference's own precision."""
 
     def __init__(self, mesh, iterations=None, energy=None, cg_tolerance=None,
                  cg_max_iterations=None, attachment_stiffness=10.0,
-                 preconditioner_singular_threshold=1.0e-20, dtype=np.float64):
+                 preconditioner_singular_threshold=1.0e-20, dtype=np.float64,
+                 line_search=False, line_search_max_iterations=20, line_search_alpha0=1.0,
+                 line_search_tau=0.5, line_search_c=0.01, line_search_threshold=1.0e-8):
         spec = mesh.spec
         self.dtype = np.dtype(dtype)
         f = lambda a: np.asarray(a).astype(self.dtype)
@@ -495,6 +548,13 @@ class OracleSolver:
         self.lmbda = np.zeros((self.T, 6), dtype=self.dtype)
         self.row_ptr, self.col_idx = bsr_sparsity(self.tets, self.n)
         self.last_pcg: list[PCGResult] = []
+        self.line_search = line_search
+        self.ls_max_iterations = line_search_max_iterations
+        self.ls_alpha0 = line_search_alpha0
+        self.ls_tau = line_search_tau
+        self.ls_c = line_search_c
+        self.ls_threshold = line_search_threshold
+        self.last_line_search: list[LineSearchResult] = []
 
     # -- stages ------------------------------------------------------------
     def element_terms(self, x):
@@ -578,17 +638,76 @@ class OracleSolver:
         ds = -np.einsum("tij,tj->ti", el["H_si"], SYM * lam + el["g_s"])
         return lam, ds
 
+    def objective(self, x, s, x_tilde, dt):
+        """Merit function with lambda fixed: kinetic + attachment terms over
+        dt^2 plus, per tet, elastic energy minus lambda . c(x, s)
+        (src/mfem/refinement/solver.py:803-869).  The attachment energy
+        0.5 k |x - p|^2 is the reference's x.(0.5 Q x + b) + c
+        (src/mfem/boundary_condition.py:62-71) in a cancellation-free form."""
+        dtp = self.dtype
+        d = x - x_tilde
+        kin = np.sum(dtp.type(0.5) * self.mass * np.sum(d * d, axis=1), dtype=dtp)
+        e = x - self.pin_target
+        att = np.sum(dtp.type(0.5) * self.hess_attach * np.sum(e * e, axis=1), dtype=dtp)
+        inv_dt2 = dtp.type(1.0 / (dt * dt))
+        c, _ = compute_constraints(x, self.tets, self.DmInv, s)
+        tet = elastic_energy_only(self.energy, s, self.materials, self.DmInv) - np.sum(c * self.lmbda, axis=1)
+        return inv_dt2 * kin + inv_dt2 * att + np.sum(tet, dtype=dtp)
+
+    def line_search_update(self, x, x_tilde, dt, el, dx, ds):
+        """Backtracking Armijo search along (dx, ds) (src/mfem/line_search.py:
+        76-163): alpha = alpha0 tau^j until (f0 - f1) + threshold >= alpha t,
+        t = -c (g_x . dx + g_s,lambda . ds) with g_x = kinetic/attachment
+        gradient - G^T lambda and g_s,lambda = g_s + SYM lambda
+        (src/mfem/refinement/solver.py:897-915).  The update is written only
+        if the accepting trial index j has j + 1 < max_iterations; a search
+        that never passes stops after trial max_iterations and writes nothing
+        (the counter test of src/mfem/line_search.py:44-63, 148-161).  The
+        x-gradient keeps the reference's sign: G is its dC_dX, which is
+        -dc/dx (kernels.py:159), so g_x - G^T lambda is not the gradient of
+        the merit function, whose x-part is g_x + G^T lambda."""
+        dtp = self.dtype
+        SYM = SYM_DIAG.astype(dtp)
+        gx = self.kinetic_gradient(x, x_tilde, dt)
+        GtL = np.zeros_like(x)
+        contrib = np.einsum("tik,ti->tk", el["G"], self.lmbda).reshape(self.T, 4, 3)
+        np.add.at(GtL, self.tets.ravel(), contrib.reshape(-1, 3))
+        grad_x = gx - GtL
+        grad_s = el["g_s"] + SYM * self.lmbda
+        m = np.sum(grad_x * dx, dtype=dtp) + np.sum(grad_s * ds, dtype=dtp)
+        t = -dtp.type(self.ls_c) * m
+        f0 = self.objective(x, self.s, x_tilde, dt)
+        trial = {}
+
+        def f(alpha):
+            trial["x"], trial["s"] = x + alpha * dx, self.s + alpha * ds
+            return self.objective(trial["x"], trial["s"], x_tilde, dt)
+
+        res = backtracking(f, f0, t, dtp.type(self.ls_alpha0), dtp.type(self.ls_tau),
+                           dtp.type(self.ls_threshold), self.ls_max_iterations)
+        self.last_line_search.append(res)
+        if res.accepted:
+            return trial["x"], trial["s"]
+        return x, self.s
+
     # -- the step ------------------------------------------------------------
+    def predictor(self, q, qd, dt):
+        """x~ = x + v dt + g dt^2 / 2 (src/mfem/refinement/kernels.py:77-91)."""
+        dtp = self.dtype
+        dtc = dtp.type(dt)
+        return (np.asarray(q).astype(dtp) + np.asarray(qd).astype(dtp) * dtc
+                + self.gravity[None, :] * dtc * dtc / dtp.type(2.0))
+
     def step(self, q, qd, dt):
         """One implicit-Euler step: returns (q_out, qd_out); s and lambda
         persist in the solver (src/mfem/refinement/solver.py:429-579)."""
         dtp = self.dtype
         x_in = np.asarray(q).astype(dtp)
-        v_in = np.asarray(qd).astype(dtp)
         dtc = dtp.type(dt)
-        x_tilde = x_in + v_in * dtc + self.gravity[None, :] * dtc * dtc / dtp.type(2.0)
+        x_tilde = self.predictor(q, qd, dt)
         x = x_in.copy()
         self.last_pcg = []
+        self.last_line_search = []
         for _ in range(self.iterations):
             el = self.element_terms(x)
             blocks, g, _ = self.assemble(x, x_tilde, dt, el)
@@ -597,7 +716,10 @@ class OracleSolver:
             self.last_pcg.append(res)
             lam, ds = self.local_solve(el, dx)
             self.lmbda = lam
-            x = x + dx
-            self.s = self.s + ds
+            if self.line_search:
+                x, self.s = self.line_search_update(x, x_tilde, dt, el, dx, ds)
+            else:
+                x = x + dx
+                self.s = self.s + ds
         v = (x - x_in) / dtc
         return x, v

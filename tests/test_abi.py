@@ -28,8 +28,15 @@ def test_default_config_matches_reference_defaults(built_lib):
     assert cfg.attachment_stiffness == pytest.approx(10.0)
     assert cfg.preconditioner_singular_threshold == pytest.approx(1e-20)
     assert cfg.preconditioner == 1
+    # line search on by default (solver.py:99-103, 185)
+    assert cfg.line_search == 1
+    assert cfg.line_search_max_iterations == 20
+    assert cfg.line_search_alpha0 == 1.0 and cfg.line_search_tau == 0.5
+    assert cfg.line_search_c == pytest.approx(0.01)
+    assert cfg.line_search_threshold == pytest.approx(1e-8)
     assert ctypes.sizeof(_lib.MfemConfig) == 64
     assert ctypes.sizeof(_lib.MfemSolveStats) == 16
+    assert ctypes.sizeof(_lib.MfemLineSearchStats) == 40
 
 
 def test_status_strings(built_lib):

@@ -18,7 +18,8 @@ DEV = "cuda:0"
 def _solver(mesh, **kw):
     model = Model.from_beam(mesh, device=DEV)
     kw.setdefault("energy", mesh.spec.energy)
-    return model, MixedFEMSolver(model, iterations=kw.pop("iterations", 2), **kw)
+    return model, MixedFEMSolver(model, iterations=kw.pop("iterations", 2),
+                                  line_search=kw.pop("line_search", False), **kw)
 
 
 def test_iteration_cap_reports_maxiter_and_continues():
@@ -62,7 +63,7 @@ def test_isolated_vertex_falls_freely():
     model = Model(np.concatenate([mesh.rest_q, extra]), np.zeros((n + 1, 3), np.float32),
                   np.concatenate([mesh.particle_mass, [2.0]]), np.concatenate([mesh.particle_inv_mass, [0.5]]),
                   mesh.tet_indices, mesh.tet_poses, mesh.tet_materials, mesh.gravity, device=DEV)
-    solver = MixedFEMSolver(model, iterations=3)
+    solver = MixedFEMSolver(model, iterations=3, line_search=False)
     s0, s1 = model.state(), model.state()
     solver.step(s0, s1, None, None, mesh.spec.dt)
     assert all(s["status"] == 0 for s in solver.solve_stats())
@@ -76,7 +77,7 @@ def test_mesh_without_tets():
     model = Model(q, np.zeros_like(q), np.ones(2, np.float32), np.array([0.0, 1.0], np.float32),
                   np.zeros((0, 4), np.int32), np.zeros((0, 3, 3), np.float32), np.zeros((0, 3), np.float32),
                   np.array([0.0, -9.81, 0.0], np.float32), device=DEV)
-    solver = MixedFEMSolver(model, iterations=2)
+    solver = MixedFEMSolver(model, iterations=2, line_search=False)
     s0, s1 = model.state(), model.state()
     solver.step(s0, s1, None, None, 0.01)
     assert all(s["status"] == 0 for s in solver.solve_stats())
@@ -107,7 +108,9 @@ def test_bad_arguments_raise():
     with pytest.raises(_lib.MfemError):
         solver.step(s0, model.state(), None, None, -1.0)
     with pytest.raises(NotImplementedError):
-        MixedFEMSolver(model, iterations=2, line_search=True)
+        MixedFEMSolver(model, iterations=2, enable_refinement=True)
+    with pytest.raises(_lib.MfemError):
+        MixedFEMSolver(model, iterations=2, line_search_max_iterations=-1)
     with pytest.raises(ValueError):
         MixedFEMSolver(model, iterations=2, energy="stvk")
 

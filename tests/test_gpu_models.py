@@ -35,7 +35,7 @@ def _fem_beam_mesh(tmp_path, mu, energy):
 def test_fem_beam_npz_model_steps_match_oracle(tmp_path, energy):
     mesh = _fem_beam_mesh(tmp_path, mu=100.0, energy=energy)
     model = Model.from_beam(mesh, device=DEV)
-    solver = MixedFEMSolver(model, iterations=8, energy=energy)
+    solver = MixedFEMSolver(model, iterations=8, energy=energy, line_search=False)
     ref = O.OracleSolver(mesh, dtype=np.float64)
     s0, s1 = model.state(), model.state()
     q, qd = mesh.q0, mesh.qd0

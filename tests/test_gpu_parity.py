@@ -58,7 +58,8 @@ def make(name, cells=None, **kw):
     mesh = beams.build_beam(name, cells=cells)
     model = Model.from_beam(mesh, device=DEV)
     kw.setdefault("energy", mesh.spec.energy)
-    solver = MixedFEMSolver(model, iterations=kw.pop("iterations", mesh.spec.iterations), **kw)
+    solver = MixedFEMSolver(model, iterations=kw.pop("iterations", mesh.spec.iterations),
+                            line_search=kw.pop("line_search", False), **kw)
     return mesh, model, solver
 
 
@@ -249,7 +250,7 @@ def test_graph_and_eager_paths_agree_bitwise():
     outs = []
     for graph in (True, False):
         model = Model.from_beam(mesh, device=DEV)
-        solver = MixedFEMSolver(model, iterations=8, use_cuda_graph=graph)
+        solver = MixedFEMSolver(model, iterations=8, use_cuda_graph=graph, line_search=False)
         s0, s1 = model.state(), model.state()
         for _ in range(5):
             solver.step(s0, s1, None, None, mesh.spec.dt)
@@ -264,7 +265,7 @@ def test_step_is_deterministic_and_leaves_state_in_alone():
     results = []
     for _ in range(2):
         model = Model.from_beam(mesh, device=DEV)
-        solver = MixedFEMSolver(model, iterations=8, energy="neohookean")
+        solver = MixedFEMSolver(model, iterations=8, energy="neohookean", line_search=False)
         s0, s1 = model.state(), model.state()
         s0.particle_q.copy_(t(mesh.q0))
         before = s0.particle_q.clone()
@@ -278,8 +279,8 @@ def test_step_is_deterministic_and_leaves_state_in_alone():
 def test_aliased_in_out_state():
     mesh = beams.build_beam("cantilever")
     model = Model.from_beam(mesh, device=DEV)
-    a = MixedFEMSolver(model, iterations=8)
-    b = MixedFEMSolver(model, iterations=8)
+    a = MixedFEMSolver(model, iterations=8, line_search=False)
+    b = MixedFEMSolver(model, iterations=8, line_search=False)
     s0, s1 = model.state(), model.state()
     a.step(s0, s1, None, None, mesh.spec.dt)
     s2 = model.state()
@@ -297,7 +298,8 @@ def test_pcg_variants_agree(name, cells, steps):
     outs = {}
     for variant in ("standard", "single_reduction"):
         model = Model.from_beam(mesh, device=DEV)
-        solver = MixedFEMSolver(model, iterations=8, energy=mesh.spec.energy, pcg_variant=variant)
+        solver = MixedFEMSolver(model, iterations=8, energy=mesh.spec.energy, pcg_variant=variant,
+                                line_search=False)
         s0, s1 = model.state(), model.state()
         s0.particle_q.copy_(t(mesh.q0))
         for _ in range(steps):

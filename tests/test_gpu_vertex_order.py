@@ -26,7 +26,7 @@ def _model(mesh, order=None):
 
 def _one_step(mesh, order=None, **kw):
     model, q0 = _model(mesh, order)
-    solver = MixedFEMSolver(model, iterations=8, energy=mesh.spec.energy, **kw)
+    solver = MixedFEMSolver(model, iterations=8, energy=mesh.spec.energy, line_search=False, **kw)
     s0, s1 = model.state(), model.state()
     s0.particle_q.copy_(torch.as_tensor(q0, device=DEV))
     solver.step(s0, s1, None, None, mesh.spec.dt)

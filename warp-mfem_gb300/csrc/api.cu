@@ -44,6 +44,9 @@ struct mfem_plan {
     BsrViews bv{};
     PcgWork pw{};
     PcgLayout pl{};
+    LineSearchWork ls{};
+    float stage_dt = 0.0f;     // dt of the last mfem_assemble (the line search's 1/dt^2)
+    int stage_slot = 0;        // slot of the last mfem_global_solve
     int32_t *tet_slots = nullptr;
     double *resid = nullptr;
     cudaStream_t capture_stream = nullptr;
@@ -129,6 +132,7 @@ bool buffer_ref(const mfem_plan *p, int which, BufferRef &ref) {
         case MFEM_BUF_PRECOND: ref = {p->vv.Minv, n * 9 * 4}; return true;
         case MFEM_BUF_X_TILDE: ref = {p->vv.x_tilde, n * 3 * 4}; return true;
         case MFEM_BUF_DX: ref = {p->vv.dx, n * 3 * 4}; return true;
+        case MFEM_BUF_STRETCH_DIRECTION: ref = {p->ls.ds, T * 6 * 4}; return true;
         default: return false;
     }
 }
@@ -143,11 +147,26 @@ bool valid_config(const mfem_config *cfg, std::string &err) {
     else if (!(cfg->preconditioner_singular_threshold >= 0.0f)) err = "preconditioner_singular_threshold must be >= 0";
     else if (cfg->pcg_ctas < 0) err = "pcg_ctas must be >= 0";
     else if (cfg->pcg_variant < 0 || cfg->pcg_variant > 3) err = "pcg_variant must be 0 (auto), 1, 2 or 3";
+    else if (cfg->line_search != 0 && cfg->line_search != 1) err = "line_search must be 0 or 1";
+    else if (cfg->line_search_max_iterations < 0 || cfg->line_search_max_iterations > (1 << 20))
+        err = "line_search_max_iterations must be in [0, 2^20]";
+    else if (!std::isfinite(cfg->line_search_alpha0) || !std::isfinite(cfg->line_search_tau) ||
+             !std::isfinite(cfg->line_search_c) || !std::isfinite(cfg->line_search_threshold))
+        err = "line search parameters must be finite";
     else return true;
     return false;
 }
 
 // The whole step as a launch sequence on one stream.
+// Local solve then either the plain update x += dx, s += ds or the line
+// search (solver.py:539-557).
+cudaError_t local_update(mfem_plan *p, float *x, float dt, int slot, cudaStream_t s) {
+    if (!p->cfg.line_search) return launch_local_solve(x, p->tv, p->vv, s);
+    cudaError_t err = launch_local_solve_deferred(x, p->cfg.energy, dt, p->tv, p->vv, p->ls, s);
+    if (err == cudaSuccess) err = launch_line_search(x, p->cfg.energy, dt, p->tv, p->vv, p->ls, p->pw.error, slot, s);
+    return err;
+}
+
 cudaError_t run_step(mfem_plan *p, const float *q_in, const float *qd_in, float *q_out, float *qd_out, float dt,
                      cudaStream_t s) {
     cudaError_t err = launch_predict(q_in, qd_in, q_out, p->gravity, dt, p->vv, s);
@@ -159,7 +178,7 @@ cudaError_t run_step(mfem_plan *p, const float *q_in, const float *qd_in, float 
         if (err == cudaSuccess)
             err = launch_pcg(p->bv, p->vv, p->pw, p->pl, p->pcg_ctas, it, p->cfg.cg_tolerance,
                              p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
-        if (err == cudaSuccess) err = launch_local_solve(q_out, p->tv, p->vv, s);
+        if (err == cudaSuccess) err = local_update(p, q_out, dt, it, s);
     }
     if (err == cudaSuccess) err = launch_velocity(q_out, qd_out, dt, p->vv, s);
     return err;
@@ -195,6 +214,12 @@ void mfem_config_default(mfem_config *cfg) {
     cfg->use_cuda_graph = 1;
     cfg->pcg_ctas = 0;
     cfg->pcg_variant = 0;
+    cfg->line_search = 1;
+    cfg->line_search_max_iterations = 20;
+    cfg->line_search_alpha0 = 1.0f;
+    cfg->line_search_tau = 0.5f;
+    cfg->line_search_c = 0.01f;
+    cfg->line_search_threshold = 1.0e-8f;
 }
 
 const char *mfem_status_string(int status) {
@@ -343,6 +368,12 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
     ALLOC(p->pw.error, 1);
     ALLOC(p->pw.stats, (size_t)p->max_stats);
     ALLOC(p->resid, 2);
+    const int local_blocks = std::max(1, local_solve_blocks(T, n));
+    ALLOC(p->ls.ds, nT * 6);
+    ALLOC(p->ls.local_partials, (size_t)local_blocks * 2);
+    ALLOC(p->ls.partials, (size_t)2 * kLsMaxCtas * 3);
+    ALLOC(p->ls.counter, 1);
+    ALLOC(p->ls.stats, (size_t)p->max_stats);
 #undef ALLOC
     if (e != cudaSuccess) {
         int rc = cuda_fail(nullptr, e, "cudaMalloc");
@@ -356,6 +387,19 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
     if (e == cudaSuccess) {
         int want = cfg.pcg_ctas > 0 ? cfg.pcg_ctas : std::max(1, std::min(max_ctas, (n + 63) / 64));
         p->pcg_ctas = std::max(1, std::min(want, max_ctas));
+    }
+    if (e == cudaSuccess) {
+        int ls_max = 1;
+        e = line_search_max_ctas(device, &ls_max);
+        // one trial touches every tet and vertex once: about one per thread
+        const int want = std::max(1, (std::max(T, n) + 255) / 256);
+        p->ls.ctas = std::max(1, std::min(want, ls_max));
+        p->ls.local_blocks = local_blocks;
+        p->ls.max_iter = cfg.line_search_max_iterations;
+        p->ls.alpha0 = cfg.line_search_alpha0;
+        p->ls.tau = cfg.line_search_tau;
+        p->ls.c = cfg.line_search_c;
+        p->ls.threshold = cfg.line_search_threshold;
     }
     if (e == cudaSuccess) {
         std::string lerr;
@@ -387,6 +431,10 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
     if (e == cudaSuccess) e = cudaMemset(p->pw.partials, 0, 2 * 256 * 4 * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(p->pw.counter, 0, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(p->pw.error, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(p->ls.counter, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(p->ls.stats, 0, sizeof(LineSearchStats) * p->max_stats);
+    if (e == cudaSuccess) e = cudaMemset(p->ls.ds, 0, nT * 6 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(p->ls.local_partials, 0, (size_t)local_blocks * 2 * sizeof(double));
     if (e == cudaSuccess) e = cudaMemset(p->pw.stats, 0, sizeof(SolveStats) * p->max_stats);
     if (e == cudaSuccess) e = cudaMemset(p->vv.dx, 0, n_pad * 3 * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(p->pw.pub, 0, 6 * n_pad * 3 * sizeof(float));
@@ -565,9 +613,26 @@ int mfem_step_stats(mfem_plan *p, mfem_solve_stats *h_stats, int32_t max_entries
     if (flag) {
         // a bounded wait gave up: re-arm the grid barrier for the next solve
         cudaMemset(p->pw.counter, 0, sizeof(unsigned long long));
+        cudaMemset(p->ls.counter, 0, sizeof(unsigned long long));
         cudaMemset(p->pw.error, 0, sizeof(int));
-        return fail(p, MFEM_TIMEOUT, "a PCG grid barrier timed out");
+        return fail(p, MFEM_TIMEOUT, "a PCG or line-search grid barrier timed out");
     }
+    return MFEM_OK;
+}
+
+int mfem_step_line_search_stats(mfem_plan *p, mfem_line_search_stats *h_stats, int32_t max_entries, int32_t *count,
+                           mfem_stream stream) {
+    static_assert(sizeof(mfem_line_search_stats) == sizeof(LineSearchStats), "stats layout");
+    if (!p || (max_entries > 0 && !h_stats)) return MFEM_BAD_ARG;
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(p, e, "cudaStreamSynchronize");
+    const int k = std::max(0, std::min<int>(max_entries, p->cfg.iterations));
+    std::vector<LineSearchStats> tmp(p->max_stats);
+    e = cudaMemcpy(tmp.data(), p->ls.stats, sizeof(LineSearchStats) * p->max_stats, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(p, e, "stats readback");
+    for (int i = 0; i < k; ++i) std::memcpy(&h_stats[i], &tmp[i], sizeof(mfem_line_search_stats));
+    if (count) *count = k;
     return MFEM_OK;
 }
 
@@ -596,6 +661,7 @@ int mfem_assemble(mfem_plan *p, const float *x, float dt, mfem_stream stream) {
     DeviceGuard g(p->device);
     cudaError_t e = launch_assemble(x, dt, p->cfg.preconditioner_singular_threshold, p->cfg.preconditioner, p->tv,
                                    p->vv, p->bv, (cudaStream_t)stream);
+    p->stage_dt = dt;
     return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "assemble");
 }
 
@@ -605,14 +671,17 @@ int mfem_global_solve(mfem_plan *p, int32_t slot, mfem_stream stream) {
     DeviceGuard g(p->device);
     cudaError_t e = launch_pcg(p->bv, p->vv, p->pw, p->pl, p->pcg_ctas, slot, p->cfg.cg_tolerance,
                                p->cfg.cg_max_iterations, p->cfg.preconditioner, (cudaStream_t)stream);
+    p->stage_slot = slot;
     return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "global_solve");
 }
 
 int mfem_local_solve(mfem_plan *p, float *x, mfem_stream stream) {
     if (!p) return MFEM_BAD_ARG;
     if (!x) return fail(p, MFEM_BAD_ARG, "x is NULL");
+    if (p->cfg.line_search && !(p->stage_dt > 0.0f))
+        return fail(p, MFEM_BAD_ARG, "the line search needs mfem_assemble (its dt) first");
     DeviceGuard g(p->device);
-    cudaError_t e = launch_local_solve(x, p->tv, p->vv, (cudaStream_t)stream);
+    cudaError_t e = local_update(p, x, p->stage_dt, p->stage_slot, (cudaStream_t)stream);
     return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "local_solve");
 }
 

@@ -7,10 +7,11 @@
 //                      that the assembly gathers.
 //  local_solve_kernel  tets: local_solve_lambda + local_solve_stretch + s += ds;
 //                      vertices: x += dx  (one launch, two index ranges).
+//  local_solve_deferred_kernel  the same local solve ahead of the line search:
+//                      stores ds, leaves x and s, sums the merit and slope.
 //  predict_kernel      integrate_particles + state_out.assign(state_in).
 //  velocity_kernel     get_particle_velocity.
-#include "element_math.cuh"
-#include "internal.h"
+#include "merit.cuh"
 
 namespace mfem {
 namespace {
@@ -159,38 +160,36 @@ __global__ void __launch_bounds__(kVertexThreads)
     }
 }
 
-__global__ void __launch_bounds__(kVertexThreads)
-    local_solve_kernel(float *x, TetViews tv, VertexViews vv, int tet_blocks) {
-    if ((int)blockIdx.x >= tet_blocks) {
-        const int v = (blockIdx.x - tet_blocks) * blockDim.x + threadIdx.x;
-        if (v >= vv.n) return;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) x[3 * v + a] += vv.dx[3 * v + a];
-        return;
-    }
+// lambda and ds of tet t (local_solve_lambda, local_solve_stretch,
+// kernels.py:252-283):  lambda = -H_l (g_l - G dx), ds = -H_s^-1 (SYM lambda
+// + g_s); gdx = G dx, accumulated block by block as it is subtracted.
+__device__ __forceinline__ void local_tet(const TetViews &tv, const float *__restrict__ dx, int t, float nl[6],
+                                          float ds[6], float gdx[6]) {
     const int T = tv.n_tets;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= T) return;
     const int4 tt = tv.tets[t];
     const int vid[4] = {tt.x, tt.y, tt.z, tt.w};
     float lam[6];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) lam[i] = tv.g_l[(size_t)i * T + t];
+    for (int i = 0; i < 6; ++i) {
+        lam[i] = tv.g_l[(size_t)i * T + t];
+        gdx[i] = 0.0f;
+    }
     // lambda -= G_k dx[v_k], block by block (kernels.py:266-268)
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         float d[3];
-        load_vec3(vv.dx, vid[k], d);
+        load_vec3(dx, vid[k], d);
 #pragma unroll
         for (int i = 0; i < 6; ++i) {
             const float *g = tv.G + (size_t)(i * 12 + 3 * k) * T + t;
-            lam[i] -= g[0] * d[0] + g[(size_t)T] * d[1] + g[(size_t)2 * T] * d[2];
+            const float gd = g[0] * d[0] + g[(size_t)T] * d[1] + g[(size_t)2 * T] * d[2];
+            lam[i] -= gd;
+            gdx[i] += gd;
         }
     }
     float Hl[21];
 #pragma unroll
     for (int k = 0; k < 21; ++k) Hl[k] = tv.H_l[(size_t)k * T + t];
-    float nl[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
         float acc = 0.0f;
@@ -207,8 +206,102 @@ __global__ void __launch_bounds__(kVertexThreads)
         float acc = 0.0f;
 #pragma unroll
         for (int j = 0; j < 6; ++j) acc += tv.H_si[(size_t)em::p21(i, j) * T + t] * rhs[j];
-        tv.stretch[(size_t)t * 6 + i] += -acc;
+        ds[i] = -acc;
+    }
+}
+
+__global__ void __launch_bounds__(kVertexThreads)
+    local_solve_kernel(float *x, TetViews tv, VertexViews vv, int tet_blocks) {
+    if ((int)blockIdx.x >= tet_blocks) {
+        const int v = (blockIdx.x - tet_blocks) * blockDim.x + threadIdx.x;
+        if (v >= vv.n) return;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) x[3 * v + a] += vv.dx[3 * v + a];
+        return;
+    }
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= tv.n_tets) return;
+    float nl[6], ds[6], gdx[6];
+    local_tet(tv, vv.dx, t, nl, ds, gdx);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        tv.stretch[(size_t)t * 6 + i] += ds[i];
         tv.lambda[(size_t)t * 6 + i] = nl[i];
+    }
+}
+
+// The local solve ahead of the line search: x and s stay, lambda and ds are
+// stored, and each block writes its sums of the merit function at (x, s)
+// with the new lambda and of the slope (g_x - G^T lambda) . dx +
+// (g_s + SYM lambda) . ds (solver.py:803-869, 893-915).
+__global__ void __launch_bounds__(kVertexThreads)
+    local_solve_deferred_kernel(const float *__restrict__ x, int energy, float dt, double inv_dt2, TetViews tv,
+                                VertexViews vv, LineSearchWork w, int tet_blocks) {
+    __shared__ double s_red[2][kVertexThreads / 32];
+    double merit = 0.0, slope = 0.0;
+    if ((int)blockIdx.x >= tet_blocks) {
+        const int v = (blockIdx.x - tet_blocks) * blockDim.x + threadIdx.x;
+        if (v < vv.n) {
+            merit = vertex_merit(vv, x, v, 0.0f, inv_dt2);
+            // g_x as in the assembly: m (x - x~)/dt^2 + (k x - k p)/dt^2
+            const float dt2 = dt * dt;
+            const float m = vv.mass[v];
+            const float kp = vv.pin_k[v];
+            float sl = 0.0f;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const float xa = x[3 * v + a];
+                const float gx = m * (xa - vv.x_tilde[3 * v + a]) / dt2 + (kp * xa + (-(kp * vv.pin_target[3 * v + a]))) / dt2;
+                sl += gx * vv.dx[3 * v + a];
+            }
+            slope = sl;
+        }
+    } else {
+        const int T = tv.n_tets;
+        const int t = blockIdx.x * blockDim.x + threadIdx.x;
+        if (t < T) {
+            float nl[6], ds[6], gdx[6];
+            local_tet(tv, vv.dx, t, nl, ds, gdx);
+            float s[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                s[i] = tv.stretch[(size_t)t * 6 + i];
+                tv.lambda[(size_t)t * 6 + i] = nl[i];
+                w.ds[(size_t)i * T + t] = ds[i];
+            }
+            float Dm[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) Dm[i][j] = tv.dminv[(size_t)t * 9 + i * 3 + j];
+            const float vol = 1.0f / (6.0f * em::det3(Dm));
+            float lc = 0.0f, sl = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                lc += nl[i] * tv.c[(size_t)i * T + t];
+                sl += (tv.g_s[(size_t)i * T + t] + em::sym_w(i) * nl[i]) * ds[i] - nl[i] * gdx[i];
+            }
+            merit = (double)em::elastic_energy(energy, s, tv.materials[(size_t)t * 3 + 0],
+                                               tv.materials[(size_t)t * 3 + 1], vol) - (double)lc;
+            slope = sl;
+        }
+    }
+    merit = warp_sum(merit);
+    slope = warp_sum(slope);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        s_red[0][wid] = merit;
+        s_red[1][wid] = slope;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a0 = 0.0, a1 = 0.0;
+        for (int k = 0; k < kVertexThreads / 32; ++k) {
+            a0 += s_red[0][k];
+            a1 += s_red[1][k];
+        }
+        w.local_partials[2 * blockIdx.x + 0] = a0;
+        w.local_partials[2 * blockIdx.x + 1] = a1;
     }
 }
 
@@ -252,6 +345,19 @@ cudaError_t launch_local_solve(float *x, const TetViews &tv, const VertexViews &
     const int vb = blocks_for(vv.n, kVertexThreads);
     if (tb + vb == 0) return cudaSuccess;
     local_solve_kernel<<<tb + vb, kVertexThreads, 0, s>>>(x, tv, vv, tb);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+int local_solve_blocks(int n_tets, int n) { return blocks_for(n_tets, kVertexThreads) + blocks_for(n, kVertexThreads); }
+
+cudaError_t launch_local_solve_deferred(const float *x, int energy, float dt, const TetViews &tv,
+                                        const VertexViews &vv, const LineSearchWork &w, cudaStream_t s) {
+    const int tb = blocks_for(tv.n_tets, kVertexThreads);
+    const int vb = blocks_for(vv.n, kVertexThreads);
+    if (tb + vb == 0) return cudaSuccess;
+    const double inv_dt2 = 1.0 / ((double)dt * (double)dt);
+    local_solve_deferred_kernel<<<tb + vb, kVertexThreads, 0, s>>>(x, energy, dt, inv_dt2, tv, vv, w, tb);
     count_launches(1);
     return cudaGetLastError();
 }

@@ -385,6 +385,27 @@ MFEM_HD void energy_terms(int energy, const float s[6], float mu, float lam, flo
     }
 }
 
+// Elastic energy value in s (the *_energy_only kernels,
+// src/mfem/refinement/elastic_energy.py:155-176 ARAP, 287-311 Neo-Hookean),
+// written in E = s - I so that no O(1) terms cancel near rest:
+//   ARAP  vol mu (I2 + 3 - 2 I1) / 2 with the reference's
+//         I2 = s0 s1 + s1 s2 + s2 s0 + 2 (s3^2 + s4^2 + s5^2)
+//         = vol mu (e0 e1 + e1 e2 + e2 e0 + 2 (s3^2 + s4^2 + s5^2)) / 2;
+//   NH    vol (mu (|s|_F^2 - 3) / 2 - mu (J - 1) + lam (J - 1)^2 / 2)
+//         = vol (mu (|E|_F^2 / 2 - m2(E) - det E) + lam (J - 1)^2 / 2),
+//         J - 1 = tr E + m2(E) + det E, m2 = sum of the principal 2x2 minors.
+MFEM_HD float elastic_energy(int energy, const float s[6], float mu, float lam, float vol) {
+    const float e0 = s[0] - 1.0f, e1 = s[1] - 1.0f, e2 = s[2] - 1.0f;
+    const float oo = s[3] * s[3] + s[4] * s[4] + s[5] * s[5];
+    if (energy == 0) return vol * (mu * (e0 * e1 + e1 * e2 + e2 * e0 + 2.0f * oo) / 2.0f);
+    const float m2 = e0 * e1 + e1 * e2 + e2 * e0 - oo;
+    const float dE = e0 * e1 * e2 + 2.0f * s[3] * s[4] * s[5] - e0 * s[5] * s[5] - e1 * s[4] * s[4] -
+                     e2 * s[3] * s[3];
+    const float jm1 = (e0 + e1 + e2) + m2 + dE;
+    const float fro = e0 * e0 + e1 * e1 + e2 * e2 + 2.0f * oo;
+    return vol * (mu * (0.5f * fro - m2 - dE) + 0.5f * lam * jm1 * jm1);
+}
+
 // F = [x1-x0, x2-x0, x3-x0] DmInv (src/mfem/refinement/kernels.py:145-156).
 MFEM_HD void deformation_gradient(const float x[4][3], const float Dm[3][3], float F[3][3]) {
     float e[3][3];  // e[c] = x_{c+1} - x0

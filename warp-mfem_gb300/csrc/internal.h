@@ -91,6 +91,30 @@ struct PcgWork {
     SolveStats *stats;         // [max solves per step]
 };
 
+// Per-Newton-iteration outcome of the line search (same layout as
+// mfem_line_search_stats).
+struct LineSearchStats {
+    int32_t evaluations;
+    int32_t accepted;
+    float alpha;
+    int32_t status;
+    double f0, f1, t;
+};
+
+constexpr int kLsMaxCtas = 512;  // capacity of the line search's per-CTA partials
+
+struct LineSearchWork {
+    float *ds;                     // [6][T] stretch direction of the local solve
+    double *local_partials;        // [local_blocks][2] (merit, slope) per local-solve block
+    int local_blocks;
+    double *partials;              // [2][kLsMaxCtas][3] per-CTA sums, double buffered by round parity
+    unsigned long long *counter;   // grid barrier arrivals, never reset
+    LineSearchStats *stats;        // [max solves per step]
+    int ctas;                      // persistent CTAs, fixed for the plan
+    int max_iter;
+    float alpha0, tau, c, threshold;
+};
+
 // Row partition and shared-memory plan of the persistent PCG.
 struct PcgLayout {
     enum { kAuto = 0, kStandard = 1, kSingleReduction = 2, kGather = 3 };
@@ -121,6 +145,14 @@ cudaError_t launch_element(const float *x, int energy, const TetViews &tv, cudaS
 cudaError_t launch_assemble(const float *x, float dt, float singular_threshold, int use_precond,
                             const TetViews &tv, const VertexViews &vv, const BsrViews &bv, cudaStream_t s);
 cudaError_t launch_local_solve(float *x, const TetViews &tv, const VertexViews &vv, cudaStream_t s);
+// Local solve that leaves x and s for the line search: writes lambda, ds and
+// the per-block partial sums of the merit function and the slope.
+cudaError_t launch_local_solve_deferred(const float *x, int energy, float dt, const TetViews &tv,
+                                        const VertexViews &vv, const LineSearchWork &w, cudaStream_t s);
+int local_solve_blocks(int n_tets, int n);
+cudaError_t launch_line_search(float *x, int energy, float dt, const TetViews &tv, const VertexViews &vv,
+                               const LineSearchWork &w, int *error, int slot, cudaStream_t s);
+cudaError_t line_search_max_ctas(int device, int *ctas);
 cudaError_t launch_velocity(const float *q_out, float *qd_out, float dt, const VertexViews &vv, cudaStream_t s);
 cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const PcgLayout &L, int ctas,
                        int slot, float tol, int maxiter, int use_precond, cudaStream_t s);

@@ -28,7 +28,7 @@ BUF = {
     "tet_stretch": 0, "tet_lambda": 1, "constraint": 2, "grad_constraint": 3, "grad_s": 4,
     "h_lambda": 5, "hess_s_inv": 6, "g_lambda": 7, "element_hessian": 8, "element_rhs": 9,
     "row_ptr": 10, "col_idx": 11, "tet_slots": 12, "h_values": 13, "rhs": 14, "precond": 15,
-    "x_tilde": 16, "dx": 17,
+    "x_tilde": 16, "dx": 17, "stretch_direction": 18,
 }
 
 
@@ -44,7 +44,12 @@ class MfemConfig(ctypes.Structure):
         ("use_cuda_graph", ctypes.c_int32),
         ("pcg_ctas", ctypes.c_int32),
         ("pcg_variant", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 6),
+        ("line_search", ctypes.c_int32),
+        ("line_search_max_iterations", ctypes.c_int32),
+        ("line_search_alpha0", ctypes.c_float),
+        ("line_search_tau", ctypes.c_float),
+        ("line_search_c", ctypes.c_float),
+        ("line_search_threshold", ctypes.c_float),
     ]
 
 
@@ -54,6 +59,18 @@ class MfemSolveStats(ctypes.Structure):
         ("status", ctypes.c_int32),
         ("rel_residual", ctypes.c_float),
         ("reserved", ctypes.c_float),
+    ]
+
+
+class MfemLineSearchStats(ctypes.Structure):
+    _fields_ = [
+        ("evaluations", ctypes.c_int32),
+        ("accepted", ctypes.c_int32),
+        ("alpha", ctypes.c_float),
+        ("status", ctypes.c_int32),
+        ("f0", ctypes.c_double),
+        ("f1", ctypes.c_double),
+        ("t", ctypes.c_double),
     ]
 
 
@@ -86,6 +103,8 @@ _SIGNATURES = {
     "mfem_plan_copy_in": (ctypes.c_int, [_P, _I32, _P, ctypes.c_size_t, _P]),
     "mfem_step": (ctypes.c_int, [_P, _P, _P, _P, _P, _F32, _P]),
     "mfem_step_stats": (ctypes.c_int, [_P, ctypes.POINTER(MfemSolveStats), _I32, ctypes.POINTER(_I32), _P]),
+    "mfem_step_line_search_stats": (ctypes.c_int, [_P, ctypes.POINTER(MfemLineSearchStats), _I32,
+                                                   ctypes.POINTER(_I32), _P]),
     "mfem_predict": (ctypes.c_int, [_P, _P, _P, _F32, _P]),
     "mfem_update_system": (ctypes.c_int, [_P, _P, _P]),
     "mfem_assemble": (ctypes.c_int, [_P, _P, _F32, _P]),

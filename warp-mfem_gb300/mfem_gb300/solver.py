@@ -18,7 +18,6 @@ from .model import Model, State
 
 _OUT_OF_SCOPE_TRUE = {
     "enable_refinement": "adaptive refinement",
-    "line_search": "the backtracking line search",
 }
 
 
@@ -30,9 +29,12 @@ class MixedFEMSolver:
     """Mixed variational FEM global step on one GPU.
 
     Accepts ``RefinementSolver``'s arguments (src/mfem/refinement/solver.py:41-128).
-    Refinement, line search, contact against rigid shapes and the membrane
-    shell are outside this solver: ``enable_refinement`` / ``line_search``
-    default to False here and raise if set True; ``shell_mu`` must be 0.
+    ``line_search`` defaults to True like the reference's (solver.py:185),
+    with its ``line_search_max_iterations`` / ``_alpha0`` / ``_tau`` / ``_c`` /
+    ``_threshold`` (solver.py:99-103); ``line_search=False`` gives the plain
+    update x += dx, s += ds.  Refinement, contact against rigid shapes and
+    the membrane shell are outside this solver: ``enable_refinement``
+    defaults to False here and raises if set True; ``shell_mu`` must be 0.
     """
 
     def __init__(self, model: Model, iterations: int, max_tets: Optional[int] = None,
@@ -70,6 +72,13 @@ class MixedFEMSolver:
         cfg.pcg_ctas = int(kwargs.get("pcg_ctas", 0))
         cfg.pcg_variant = {"auto": 0, "standard": 1, "single_reduction": 2,
                            "gather": 3}[kwargs.get("pcg_variant", "auto")]
+        self.line_search = bool(kwargs.get("line_search", True))
+        cfg.line_search = 1 if self.line_search else 0
+        cfg.line_search_max_iterations = int(kwargs.get("line_search_max_iterations", 20))
+        cfg.line_search_alpha0 = float(kwargs.get("line_search_alpha0", 1.0))
+        cfg.line_search_tau = float(kwargs.get("line_search_tau", 0.5))
+        cfg.line_search_c = float(kwargs.get("line_search_c", 0.01))
+        cfg.line_search_threshold = float(kwargs.get("line_search_threshold", 1.0e-8))
         self.config = cfg
 
         host = lambda t, dt: np.ascontiguousarray(t.detach().to("cpu").numpy(), dtype=dt)
@@ -145,6 +154,17 @@ class MixedFEMSolver:
         return [dict(iterations=buf[i].iterations, status=buf[i].status, rel_residual=buf[i].rel_residual)
                 for i in range(count.value)]
 
+    def line_search_stats(self) -> list[dict]:
+        """Line-search outcome of each Newton iteration of the last step
+        (synchronises; all zero with the line search off)."""
+        buf = (_lib.MfemLineSearchStats * max(1, self.iterations))()
+        count = ctypes.c_int32()
+        rc = self._lib.mfem_step_line_search_stats(self._plan, buf, max(1, self.iterations), ctypes.byref(count),
+                                                   _stream_handle(self.device))
+        _lib.check(rc, self._plan)
+        return [dict(evaluations=buf[i].evaluations, accepted=bool(buf[i].accepted), alpha=buf[i].alpha,
+                     status=buf[i].status, f0=buf[i].f0, f1=buf[i].f1, t=buf[i].t) for i in range(count.value)]
+
     # -- stages (the reference's operators) ----------------------------------
     def predict(self, q: torch.Tensor, qd: torch.Tensor, dt: float) -> None:
         _lib.check(self._lib.mfem_predict(self._plan, self._check_state(q, "q"), self._check_state(qd, "qd"),
@@ -162,6 +182,9 @@ class MixedFEMSolver:
         _lib.check(self._lib.mfem_global_solve(self._plan, int(slot), _stream_handle(self.device)), self._plan)
 
     def local_solve(self, x: torch.Tensor) -> None:
+        """Local solve and update of x and s: the plain x += dx, s += ds, or
+        with the line search on, the search along (dx, ds) at the dt of the
+        last assemble(), recorded in the slot of the last global_solve()."""
         _lib.check(self._lib.mfem_local_solve(self._plan, self._check_state(x, "x"), _stream_handle(self.device)),
                    self._plan)
 
