@@ -95,8 +95,37 @@ typedef enum mfem_buffer {
     MFEM_BUF_X_TILDE = 16,      /* f32 [n][3]  predictor x~                                 */
     MFEM_BUF_DX = 17,           /* f32 [n][3]  PCG solution dx (warm start x~ - x)          */
     MFEM_BUF_STRETCH_DIRECTION = 18, /* f32 [6][T] ds of the last local solve (line search on) */
-    MFEM_BUF_COUNT = 19
+    /* contact (empty until mfem_plan_set_contact turns it on) */
+    MFEM_BUF_CONTACT_BLOCK = 19,   /* f32 [n][3][3] barrier + friction Hessian block of each vertex */
+    MFEM_BUF_CONTACT_GRADIENT = 20, /* f32 [n][3] barrier + friction + tri barrier gradient      */
+    MFEM_BUF_CONTACT_ENERGY = 21,  /* f32 [n]    barrier + friction energy of each vertex        */
+    MFEM_BUF_TRI_CONTACT = 22,     /* f32 [m][12] per contact tri: d, k b, k b', k max(b'',0),
+                                      n[3], w[3], shape, 0                                     */
+    MFEM_BUF_FRICTION_NORMAL = 23, /* f32 [n][3] lagged contact normal of the step               */
+    MFEM_BUF_FRICTION_FORCE = 24,  /* f32 [n]    lagged normal force of the step                 */
+    MFEM_BUF_COUNT = 25
 } mfem_buffer;
+
+/* Rigid shapes that contact takes into account (Newton's GeoType PLANE and
+ * CAPSULE; the reference ignores the other types, src/mfem/refinement/
+ * contact.py:134-141).  A plane passes through its pose's origin with normal
+ * local +Z; a capsule is centred on its origin along local +Z with
+ * scale = (radius, half height, -) (src/mfem/ipc/distance.py:5-57). */
+typedef enum mfem_shape_type {
+    MFEM_SHAPE_PLANE = 0,
+    MFEM_SHAPE_CAPSULE = 1
+} mfem_shape_type;
+
+/* Contact settings: RefinementSolver's contact kwargs
+ * (src/mfem/refinement/solver.py:241-265). */
+typedef struct mfem_contact_config {
+    float d0;               /* contact_d0, default 1e-2: quadratic barrier below   */
+    float d1;               /* contact_d1, default 1e-1: barrier support           */
+    float stiffness;        /* contact_stiffness, default 1e7                      */
+    float friction_eps_v;   /* friction_eps_v, default 1e-3 (static below eps_v dt) */
+    int32_t tri_contact;    /* 1 (default): per-tri barrier against capsules       */
+    int32_t reserved[3];
+} mfem_contact_config;
 
 /* Per Newton iteration outcome of the global solve. */
 typedef struct mfem_solve_stats {
@@ -149,8 +178,8 @@ int mfem_tet_slot_map(int32_t n_particles, int32_t n_tets, const int32_t *h_tet_
 
 /* Builds a plan for one body on device `device`: uploads the model, runs the
  * symbolic analysis, allocates the workspace and sets s = S(F_rest),
- * lambda = 0.  Replaces RefinementSolver.__init__ with refinement, contact
- * and shell off (src/mfem/refinement/solver.py:41-304;
+ * lambda = 0.  Replaces RefinementSolver.__init__ with refinement and
+ * shell off, contact off until mfem_plan_set_contact (src/mfem/refinement/solver.py:41-304;
  * additional_state.py:139-202; the mass/attachment setup of
  * solver.py:320-393).  Host arrays:
  *   tet_indices [T][4], tet_poses [T][3][3] (DmInv, edges as columns),
@@ -186,11 +215,42 @@ int mfem_plan_buffer_bytes(const mfem_plan *plan, int32_t which, size_t *bytes);
 int mfem_plan_copy_out(const mfem_plan *plan, int32_t which, void *dst, size_t bytes, mfem_stream stream);
 int mfem_plan_copy_in(mfem_plan *plan, int32_t which, const void *src, size_t bytes, mfem_stream stream);
 
+/* ---- contact against rigid shapes ------------------------------------ */
+
+void mfem_contact_config_default(mfem_contact_config *cfg);
+
+/* Turns contact on (n_shapes > 0) or off (n_shapes == 0): the per-vertex log
+ * barrier against the shapes and the lagged friction, and, with
+ * cfg->tri_contact, the per-tri barrier of the surface tris against the
+ * capsules (Contact of src/mfem/refinement/contact.py:778-1106, added into
+ * H and g at solver.py:734-779 and into the line search's merit at
+ * :856-862, 909).  Host arrays:
+ *   shape_type [S] (mfem_shape_type; others are ignored),
+ *   shape_pose [S][7] (px, py, pz, qx, qy, qz, qw) in the frame of its body,
+ *   shape_scale [S][3], shape_body [S] (< 0: static, else < n_bodies),
+ *   friction_mu [S] (Coulomb coefficient per shape),
+ *   tris [m][3] surface tris (each pair of their vertices must share a tet).
+ * Body poses start at the identity; set them with mfem_set_body_poses
+ * before each step.  S <= 64.  Synchronises the device and drops the
+ * plan's captured graphs. */
+int mfem_plan_set_contact(mfem_plan *plan, const mfem_contact_config *cfg, int32_t n_shapes,
+                          const int32_t *h_shape_type, const float *h_shape_pose,
+                          const float *h_shape_scale, const int32_t *h_shape_body,
+                          const float *h_friction_mu, int32_t n_bodies, int32_t n_tris,
+                          const int32_t *h_tris);
+
+/* Copies the body poses [n_bodies][7] the next steps read (the
+ * reference's state_out.body_q) into the plan, asynchronously on `stream`
+ * (host or device memory).  n_bodies must match mfem_plan_set_contact. */
+int mfem_set_body_poses(mfem_plan *plan, const float *body_q, int32_t n_bodies, mfem_stream stream);
+
 /* ---- the step and its stages ---------------------------------------- */
 
 /* One implicit-Euler step: RefinementSolver.step
- * (src/mfem/refinement/solver.py:429-579) with refinement off and no line
- * search (the plain update of :555-557).  d_q_out/d_qd_out receive the new
+ * (src/mfem/refinement/solver.py:429-579) with refinement off; the update is
+ * the plain x += dx, s += ds (:555-557) or, with the config's line_search,
+ * the backtracking line search (:539-553); contact terms as set by
+ * mfem_plan_set_contact.  d_q_out/d_qd_out receive the new
  * positions and velocities; d_q_in/d_qd_in are only read, and may alias the
  * outputs.  s and lambda persist in the plan.  Asynchronous; allocates
  * nothing. */
@@ -210,7 +270,9 @@ int mfem_step_line_search_stats(mfem_plan *plan, mfem_line_search_stats *h_stats
                                 int32_t *count, mfem_stream stream);
 
 /* Predictor x~ = x + v dt + g dt^2/2 into the plan
- * (integrate_particles, src/mfem/refinement/kernels.py:77-91). */
+ * (integrate_particles, src/mfem/refinement/kernels.py:77-91), and with
+ * contact the lagged friction snapshot at x = d_q (Contact.begin_step,
+ * src/mfem/refinement/contact.py:937-967). */
 int mfem_predict(mfem_plan *plan, const float *d_q, const float *d_qd, float dt, mfem_stream stream);
 
 /* Element stage at (x, s): c, G, g_s, H_s (psd-fixed for Neo-Hookean),
@@ -221,7 +283,9 @@ int mfem_update_system(mfem_plan *plan, const float *d_x, mfem_stream stream);
 
 /* Assembly: H = sum_e G^T H_l G + (M+Q)/dt^2, g = sum_e G^T H_l g_l - g_x,
  * the block-Jacobi inverse and the warm start dx = x~ - x
- * (src/mfem/refinement/solver.py:682-743, 530-531, 591-602). */
+ * (src/mfem/refinement/solver.py:682-743, 530-531, 591-602); with contact,
+ * first the contact terms at x (Contact.evaluate, solver.py:637), whose
+ * blocks and gradients go into H and g (:734-779). */
 int mfem_assemble(mfem_plan *plan, const float *d_x, float dt, mfem_stream stream);
 
 /* Block-Jacobi PCG on H dx = g (src/mfem/refinement/solver.py:581-609 and

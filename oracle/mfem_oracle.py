@@ -515,7 +515,7 @@ class OracleSolver:
                  cg_max_iterations=None, attachment_stiffness=10.0,
                  preconditioner_singular_threshold=1.0e-20, dtype=np.float64,
                  line_search=False, line_search_max_iterations=20, line_search_alpha0=1.0,
-                 line_search_tau=0.5, line_search_c=0.01, line_search_threshold=1.0e-8):
+                 line_search_tau=0.5, line_search_c=0.01, line_search_threshold=1.0e-8, contact=None):
         spec = mesh.spec
         self.dtype = np.dtype(dtype)
         f = lambda a: np.asarray(a).astype(self.dtype)
@@ -555,6 +555,10 @@ class OracleSolver:
         self.ls_c = line_search_c
         self.ls_threshold = line_search_threshold
         self.last_line_search: list[LineSearchResult] = []
+        # contact against rigid shapes (oracle/contact_oracle.ContactOracle)
+        # and the body poses the step reads (state_out.body_q)
+        self.contact = contact
+        self.body_q = np.zeros((0, 7))
 
     # -- stages ------------------------------------------------------------
     def element_terms(self, x):
@@ -599,6 +603,23 @@ class OracleSolver:
         g = np.zeros((n, 3), dtype=np.float64)
         np.add.at(g, self.tets.ravel(), f.reshape(-1, 3).astype(np.float64))
         g = g - self.kinetic_gradient(x, x_tilde, dt)
+        if self.contact is not None:
+            # barrier + friction blocks on the diagonal, tri blocks on tri
+            # vertex pairs; their gradients leave g (solver.py:734-779)
+            _, gv, Hv = self.contact.vertex_terms(x.astype(np.float64), self.body_q, dt)
+            _, gt, tri_blocks = self.contact.tri_terms(x.astype(np.float64), self.body_q)
+            rows = np.repeat(3 * np.arange(n), 9) + np.tile(np.repeat(np.arange(3), 3), n)
+            cols = np.repeat(3 * np.arange(n), 9) + np.tile(np.tile(np.arange(3), 3), n)
+            C = sp.coo_matrix((Hv.reshape(-1), (rows, cols)), shape=(3 * n, 3 * n))
+            if tri_blocks:
+                bi = np.array([b[0] for b in tri_blocks])
+                bj = np.array([b[1] for b in tri_blocks])
+                bv = np.stack([b[2] for b in tri_blocks])
+                r2 = (3 * bi[:, None, None] + np.arange(3)[None, :, None]).repeat(3, axis=2).reshape(-1)
+                c2 = (3 * bj[:, None, None] + np.arange(3)[None, None, :]).repeat(3, axis=1).reshape(-1)
+                C = C + sp.coo_matrix((bv.reshape(-1), (r2, c2)), shape=(3 * n, 3 * n))
+            Hs = (Hs + C).tocsr()
+            g = g - gv - gt
         # gather the BSR blocks in slot order
         rp, ci = self.row_ptr, self.col_idx
         br = np.repeat(np.arange(n), np.diff(rp))
@@ -652,7 +673,10 @@ class OracleSolver:
         inv_dt2 = dtp.type(1.0 / (dt * dt))
         c, _ = compute_constraints(x, self.tets, self.DmInv, s)
         tet = elastic_energy_only(self.energy, s, self.materials, self.DmInv) - np.sum(c * self.lmbda, axis=1)
-        return inv_dt2 * kin + inv_dt2 * att + np.sum(tet, dtype=dtp)
+        f = inv_dt2 * kin + inv_dt2 * att + np.sum(tet, dtype=dtp)
+        if self.contact is not None:
+            f = f + dtp.type(self.contact.energy(np.asarray(x, dtype=np.float64), self.body_q, dt))
+        return f
 
     def line_search_update(self, x, x_tilde, dt, el, dx, ds):
         """Backtracking Armijo search along (dx, ds) (src/mfem/line_search.py:
@@ -673,6 +697,11 @@ class OracleSolver:
         contrib = np.einsum("tik,ti->tk", el["G"], self.lmbda).reshape(self.T, 4, 3)
         np.add.at(GtL, self.tets.ravel(), contrib.reshape(-1, 3))
         grad_x = gx - GtL
+        if self.contact is not None:
+            # + barrier and friction gradients (solver.py:909)
+            _, gv, _ = self.contact.vertex_terms(np.asarray(x, dtype=np.float64), self.body_q, dt)
+            _, gt, _ = self.contact.tri_terms(np.asarray(x, dtype=np.float64), self.body_q)
+            grad_x = grad_x + (gv + gt).astype(dtp)
         grad_s = el["g_s"] + SYM * self.lmbda
         m = np.sum(grad_x * dx, dtype=dtp) + np.sum(grad_s * ds, dtype=dtp)
         t = -dtp.type(self.ls_c) * m
@@ -706,6 +735,8 @@ class OracleSolver:
         dtc = dtp.type(dt)
         x_tilde = self.predictor(q, qd, dt)
         x = x_in.copy()
+        if self.contact is not None:
+            self.contact.begin_step(x_in.astype(np.float64), self.body_q)
         self.last_pcg = []
         self.last_line_search = []
         for _ in range(self.iterations):

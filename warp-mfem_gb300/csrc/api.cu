@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "internal.h"
@@ -47,6 +48,15 @@ struct mfem_plan {
     LineSearchWork ls{};
     float stage_dt = 0.0f;     // dt of the last mfem_assemble (the line search's 1/dt^2)
     int stage_slot = 0;        // slot of the last mfem_global_solve
+    // contact against rigid shapes (mfem_plan_set_contact); off until set
+    ContactViews cv{};
+    int n_bodies = 0;
+    int n_tris = 0;
+    std::vector<void *> contact_allocs;
+    // host copies kept to rebuild the assembly's contribution lists
+    std::vector<int32_t> h_tets, h_row_ptr, h_col_idx, h_tet_slots;
+    const int32_t *base_chunk_ptr = nullptr, *base_code = nullptr, *base_slot = nullptr;
+    int base_chunks = 0;
     int32_t *tet_slots = nullptr;
     double *resid = nullptr;
     cudaStream_t capture_stream = nullptr;
@@ -133,6 +143,12 @@ bool buffer_ref(const mfem_plan *p, int which, BufferRef &ref) {
         case MFEM_BUF_X_TILDE: ref = {p->vv.x_tilde, n * 3 * 4}; return true;
         case MFEM_BUF_DX: ref = {p->vv.dx, n * 3 * 4}; return true;
         case MFEM_BUF_STRETCH_DIRECTION: ref = {p->ls.ds, T * 6 * 4}; return true;
+        case MFEM_BUF_CONTACT_BLOCK: ref = {p->cv.vblock, p->cv.on ? n * 9 * 4 : 0}; return true;
+        case MFEM_BUF_CONTACT_GRADIENT: ref = {p->cv.gtot, p->cv.on ? n * 3 * 4 : 0}; return true;
+        case MFEM_BUF_CONTACT_ENERGY: ref = {p->cv.venergy, p->cv.on ? n * 4 : 0}; return true;
+        case MFEM_BUF_TRI_CONTACT: ref = {p->cv.tri, p->cv.on ? (size_t)p->n_tris * kTriData * 4 : 0}; return true;
+        case MFEM_BUF_FRICTION_NORMAL: ref = {p->cv.normal_lagged, p->cv.on ? n * 3 * 4 : 0}; return true;
+        case MFEM_BUF_FRICTION_FORCE: ref = {p->cv.force_lagged, p->cv.on ? n * 4 : 0}; return true;
         default: return false;
     }
 }
@@ -162,19 +178,30 @@ bool valid_config(const mfem_config *cfg, std::string &err) {
 // search (solver.py:539-557).
 cudaError_t local_update(mfem_plan *p, float *x, float dt, int slot, cudaStream_t s) {
     if (!p->cfg.line_search) return launch_local_solve(x, p->tv, p->vv, s);
-    cudaError_t err = launch_local_solve_deferred(x, p->cfg.energy, dt, p->tv, p->vv, p->ls, s);
-    if (err == cudaSuccess) err = launch_line_search(x, p->cfg.energy, dt, p->tv, p->vv, p->ls, p->pw.error, slot, s);
+    cudaError_t err = launch_local_solve_deferred(x, p->cfg.energy, dt, p->tv, p->vv, p->cv, p->ls, s);
+    if (err == cudaSuccess)
+        err = launch_line_search(x, p->cfg.energy, dt, p->tv, p->vv, p->cv, p->ls, p->pw.error, slot, s);
+    return err;
+}
+
+// Contact terms at x, then the assembly (Contact.evaluate runs in
+// _update_system, solver.py:637; it needs dt for the friction threshold).
+cudaError_t contact_and_assemble(mfem_plan *p, const float *x, float dt, cudaStream_t s) {
+    cudaError_t err = launch_contact(x, dt, p->cv, p->vv, s);
+    if (err == cudaSuccess)
+        err = launch_assemble(x, dt, p->cfg.preconditioner_singular_threshold, p->cfg.preconditioner, p->tv, p->vv,
+                              p->bv, p->cv, s);
     return err;
 }
 
 cudaError_t run_step(mfem_plan *p, const float *q_in, const float *qd_in, float *q_out, float *qd_out, float dt,
                      cudaStream_t s) {
     cudaError_t err = launch_predict(q_in, qd_in, q_out, p->gravity, dt, p->vv, s);
+    // lagged friction anchor at the start-of-step positions (solver.py:515-520)
+    if (err == cudaSuccess) err = launch_contact_begin(p->cv, p->vv, s);
     for (int it = 0; err == cudaSuccess && it < p->cfg.iterations; ++it) {
         err = launch_element(q_out, p->cfg.energy, p->tv, s);
-        if (err == cudaSuccess)
-            err = launch_assemble(q_out, dt, p->cfg.preconditioner_singular_threshold, p->cfg.preconditioner, p->tv,
-                                  p->vv, p->bv, s);
+        if (err == cudaSuccess) err = contact_and_assemble(p, q_out, dt, s);
         if (err == cudaSuccess)
             err = launch_pcg(p->bv, p->vv, p->pw, p->pl, p->pcg_ctas, it, p->cfg.cg_tolerance,
                              p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
@@ -265,6 +292,7 @@ void mfem_plan_destroy(mfem_plan *p) {
             if (ge.exec) cudaGraphExecDestroy(ge.exec);
         if (p->capture_stream) cudaStreamDestroy(p->capture_stream);
         for (void *a : p->allocs) cudaFree(a);
+        for (void *a : p->contact_allocs) cudaFree(a);
     }
     delete p;
 }
@@ -368,7 +396,7 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
     ALLOC(p->pw.error, 1);
     ALLOC(p->pw.stats, (size_t)p->max_stats);
     ALLOC(p->resid, 2);
-    const int local_blocks = std::max(1, local_solve_blocks(T, n));
+    const int local_blocks = std::max(1, local_solve_blocks(T, n));  // grown by mfem_plan_set_contact
     ALLOC(p->ls.ds, nT * 6);
     ALLOC(p->ls.local_partials, (size_t)local_blocks * 2);
     ALLOC(p->ls.partials, (size_t)2 * kLsMaxCtas * 3);
@@ -462,6 +490,15 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
     p->bv.chunk_ptr = chunk_ptr;
     p->bv.contrib_code = ccode;
     p->bv.contrib_slot = cslot;
+    p->base_chunk_ptr = chunk_ptr;
+    p->base_code = ccode;
+    p->base_slot = cslot;
+    p->base_chunks = n_chunks;
+    p->h_tets.assign(h_tets, h_tets + (size_t)T * 4);
+    p->h_row_ptr = sym.row_ptr;
+    p->h_col_idx = sym.col_idx;
+    p->h_tet_slots = sym.tet_slots;
+    p->cv.tri_code_base = INT32_MAX;
 
     // s = S(F) at rest, lambda = 0 (additional_state.py:146-189)
     e = launch_initial_stretch(rest, p->tv, 0);
@@ -620,6 +657,202 @@ int mfem_step_stats(mfem_plan *p, mfem_solve_stats *h_stats, int32_t max_entries
     return MFEM_OK;
 }
 
+void mfem_contact_config_default(mfem_contact_config *cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->d0 = 1.0e-2f;
+    cfg->d1 = 1.0e-1f;
+    cfg->stiffness = 1.0e7f;
+    cfg->friction_eps_v = 1.0e-3f;
+    cfg->tri_contact = 1;
+}
+
+int mfem_plan_set_contact(mfem_plan *p, const mfem_contact_config *cfg_in, int32_t n_shapes,
+                          const int32_t *h_shape_type, const float *h_shape_pose, const float *h_shape_scale,
+                          const int32_t *h_shape_body, const float *h_friction_mu, int32_t n_bodies, int32_t n_tris,
+                          const int32_t *h_tris) {
+    if (!p) return MFEM_BAD_ARG;
+    mfem_contact_config cfg;
+    if (cfg_in) cfg = *cfg_in;
+    else mfem_contact_config_default(&cfg);
+    if (n_shapes < 0 || n_shapes > kMaxShapes) return fail(p, MFEM_BAD_ARG, "n_shapes must be in [0, 64]");
+    if (n_bodies < 0 || n_tris < 0) return fail(p, MFEM_BAD_ARG, "negative n_bodies or n_tris");
+    if (n_shapes > 0 && (!h_shape_type || !h_shape_pose || !h_shape_scale || !h_shape_body || !h_friction_mu))
+        return fail(p, MFEM_BAD_ARG, "NULL shape array");
+    if (n_tris > 0 && !h_tris) return fail(p, MFEM_BAD_ARG, "h_tris is NULL");
+    if (!(cfg.d1 > cfg.d0) || !(cfg.d0 > 0.0f) || !std::isfinite(cfg.d1))
+        return fail(p, MFEM_BAD_ARG, "contact distances need 0 < d0 < d1");
+    if (!(cfg.stiffness >= 0.0f) || !std::isfinite(cfg.stiffness) || !(cfg.friction_eps_v >= 0.0f) ||
+        !std::isfinite(cfg.friction_eps_v))
+        return fail(p, MFEM_BAD_ARG, "contact stiffness and friction_eps_v must be finite and >= 0");
+    bool friction = false;
+    for (int s = 0; s < n_shapes; ++s) {
+        if (h_shape_body[s] >= n_bodies) return fail(p, MFEM_BAD_ARG, "shape body index out of range");
+        if (!(h_friction_mu[s] >= 0.0f) || !std::isfinite(h_friction_mu[s]))
+            return fail(p, MFEM_BAD_ARG, "friction_mu must be finite and >= 0");
+        for (int i = 0; i < 7; ++i)
+            if (!std::isfinite(h_shape_pose[7 * s + i])) return fail(p, MFEM_BAD_ARG, "non-finite shape pose");
+        friction = friction || h_friction_mu[s] > 0.0f;
+    }
+    const int m = (cfg.tri_contact && n_shapes > 0) ? n_tris : 0;
+    std::vector<int32_t> tri_slots((size_t)m * 9), vt_ptr, vt_code;
+    std::string err;
+    if (m > 0 && !build_tri_slots(p->n, m, h_tris, p->h_row_ptr.data(), p->h_col_idx.data(), tri_slots.data(),
+                                  vt_ptr, vt_code, err))
+        return fail(p, MFEM_BAD_ARG, err);
+    Symbolic sym;
+    sym.col_idx = p->h_col_idx;
+    if (m > 0 && !build_contributions(p->n, p->T, p->h_tets.data(), p->h_row_ptr.data(), p->h_tet_slots.data(), sym,
+                                      err, m, tri_slots.data()))
+        return fail(p, MFEM_BAD_ARG, err);
+
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaDeviceSynchronize();  // no step of this plan may still read the old buffers
+    if (e != cudaSuccess) return cuda_fail(p, e, "cudaDeviceSynchronize");
+    for (auto &ge : p->graphs) {
+        if (ge.exec) cudaGraphExecDestroy(ge.exec);
+        ge = mfem_plan::GraphEntry{};
+    }
+    for (void *a : p->contact_allocs) cudaFree(a);
+    p->contact_allocs.clear();
+    p->cv = ContactViews{};
+    p->cv.tri_code_base = INT32_MAX;
+    p->bv.chunk_ptr = p->base_chunk_ptr;
+    p->bv.contrib_code = p->base_code;
+    p->bv.contrib_slot = p->base_slot;
+    p->bv.n_chunks = p->base_chunks;
+    p->n_bodies = 0;
+    p->n_tris = 0;
+    if (n_shapes == 0) return MFEM_OK;  // contact off
+
+    const size_t n = p->n;
+    auto alloc = [&](auto **ptr, size_t count) {
+        if (e != cudaSuccess) return;
+        void *raw = nullptr;
+        e = cudaMalloc(&raw, std::max<size_t>(count, 1) * sizeof(**ptr));
+        if (e == cudaSuccess) {
+            p->contact_allocs.push_back(raw);
+            *ptr = static_cast<std::remove_reference_t<decltype(*ptr)>>(raw);
+        }
+    };
+    int *type = nullptr, *body = nullptr, *tris = nullptr, *vtp = nullptr, *vtc = nullptr;
+    float *pose = nullptr, *scale = nullptr, *mu = nullptr, *body_q = nullptr;
+    int32_t *chunk_ptr = nullptr, *ccode = nullptr, *cslot = nullptr;
+    ContactViews &cv = p->cv;
+    alloc(&type, n_shapes);
+    alloc(&pose, (size_t)n_shapes * 7);
+    alloc(&scale, (size_t)n_shapes * 3);
+    alloc(&body, n_shapes);
+    alloc(&mu, n_shapes);
+    alloc(&body_q, (size_t)std::max(n_bodies, 1) * 7);
+    alloc(&cv.normal_lagged, n * 3);
+    alloc(&cv.force_lagged, n);
+    alloc(&cv.shape_lagged, n);
+    alloc(&cv.vblock, n * 9);
+    alloc(&cv.vgrad, n * 3);
+    alloc(&cv.venergy, n);
+    alloc(&cv.gtot, n * 3);
+    alloc(&cv.tri, (size_t)m * kTriData);
+    alloc(&tris, (size_t)m * 3);
+    alloc(&vtp, n + 1);
+    alloc(&vtc, (size_t)m * 3);
+    const int n_chunks = m > 0 ? (int)sym.chunk_ptr.size() - 1 : 0;
+    if (m > 0) {
+        alloc(&chunk_ptr, sym.chunk_ptr.size());
+        alloc(&ccode, sym.contrib_code.size());
+        alloc(&cslot, sym.contrib_slot.size());
+    }
+    // the deferred local solve's partials cover max(vertices, tris); they
+    // live as long as the plan
+    const int local_blocks = std::max(1, local_solve_blocks(p->T, std::max(p->n, m)));
+    double *local_partials = nullptr;
+    if (e == cudaSuccess && local_blocks > p->ls.local_blocks) e = dev_alloc(p, &local_partials, (size_t)local_blocks * 2);
+    std::vector<float> ident((size_t)std::max(n_bodies, 1) * 7, 0.0f);
+    for (size_t b = 0; b < ident.size() / 7; ++b) ident[7 * b + 6] = 1.0f;
+    if (e == cudaSuccess) e = upload(type, h_shape_type, n_shapes);
+    if (e == cudaSuccess) e = upload(pose, h_shape_pose, (size_t)n_shapes * 7);
+    if (e == cudaSuccess) e = upload(scale, h_shape_scale, (size_t)n_shapes * 3);
+    if (e == cudaSuccess) e = upload(body, h_shape_body, n_shapes);
+    if (e == cudaSuccess) e = upload(mu, h_friction_mu, n_shapes);
+    if (e == cudaSuccess) e = upload(body_q, ident.data(), ident.size());
+    if (e == cudaSuccess && m > 0) e = upload(tris, h_tris, (size_t)m * 3);
+    if (e == cudaSuccess && m > 0) e = upload(vtp, vt_ptr.data(), n + 1);
+    else if (e == cudaSuccess) e = cudaMemset(vtp, 0, (n + 1) * sizeof(int));
+    if (e == cudaSuccess && m > 0) e = upload(vtc, vt_code.data(), (size_t)m * 3);
+    if (e == cudaSuccess && m > 0) e = upload(chunk_ptr, sym.chunk_ptr.data(), sym.chunk_ptr.size());
+    if (e == cudaSuccess && m > 0) e = upload(ccode, sym.contrib_code.data(), sym.contrib_code.size());
+    if (e == cudaSuccess && m > 0) e = upload(cslot, sym.contrib_slot.data(), sym.contrib_slot.size());
+    if (e == cudaSuccess) e = cudaMemset(cv.normal_lagged, 0, n * 3 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(cv.force_lagged, 0, n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(cv.shape_lagged, 0xff, n * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(cv.vblock, 0, n * 9 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(cv.vgrad, 0, n * 3 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(cv.venergy, 0, n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(cv.gtot, 0, n * 3 * sizeof(float));
+    if (e == cudaSuccess && m > 0) e = cudaMemset(cv.tri, 0, (size_t)m * kTriData * sizeof(float));
+    if (e != cudaSuccess) {
+        for (void *a : p->contact_allocs) cudaFree(a);
+        p->contact_allocs.clear();
+        p->cv = ContactViews{};
+        p->cv.tri_code_base = INT32_MAX;
+        return cuda_fail(p, e, "contact buffers");
+    }
+    if (local_partials) {
+        p->ls.local_partials = local_partials;
+        p->ls.local_blocks = local_blocks;
+    }
+    float q0, q1, q2;
+    {
+        // (b, b', b'') of the log branch at d0 (contact.py:799)
+        const float d = cfg.d0, d1 = cfg.d1;
+        const float l = std::log(d / d1), a = d - d1;
+        q0 = -a * a * l;
+        q1 = -(2.0f * a * l + a * a / d);
+        q2 = -(2.0f * l + 4.0f * a / d - a * a / (d * d));
+    }
+    cv.on = 1;
+    cv.n_shapes = n_shapes;
+    cv.type = type;
+    cv.pose = pose;
+    cv.scale = scale;
+    cv.body = body;
+    cv.mu = mu;
+    cv.body_q = body_q;
+    cv.friction = friction ? 1 : 0;
+    cv.d0 = cfg.d0;
+    cv.d1 = cfg.d1;
+    cv.k = cfg.stiffness;
+    cv.eps_v = cfg.friction_eps_v;
+    cv.q[0] = q0;
+    cv.q[1] = q1;
+    cv.q[2] = q2;
+    cv.n_tris = m;
+    cv.tris = tris;
+    cv.vt_ptr = vtp;
+    cv.vt_code = vtc;
+    cv.tri_code_base = m > 0 ? 16 * p->T : INT32_MAX;
+    if (m > 0) {
+        p->bv.chunk_ptr = chunk_ptr;
+        p->bv.contrib_code = ccode;
+        p->bv.contrib_slot = cslot;
+        p->bv.n_chunks = n_chunks;
+    }
+    p->n_bodies = n_bodies;
+    p->n_tris = m;
+    return MFEM_OK;
+}
+
+int mfem_set_body_poses(mfem_plan *p, const float *body_q, int32_t n_bodies, mfem_stream stream) {
+    if (!p) return MFEM_BAD_ARG;
+    if (n_bodies != p->n_bodies) return fail(p, MFEM_BAD_ARG, "n_bodies does not match mfem_plan_set_contact");
+    if (n_bodies == 0) return MFEM_OK;
+    if (!body_q) return fail(p, MFEM_BAD_ARG, "body_q is NULL");
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaMemcpyAsync(const_cast<float *>(p->cv.body_q), body_q, (size_t)n_bodies * 7 * sizeof(float),
+                                    cudaMemcpyDefault, (cudaStream_t)stream);
+    return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "set_body_poses");
+}
+
 int mfem_step_line_search_stats(mfem_plan *p, mfem_line_search_stats *h_stats, int32_t max_entries, int32_t *count,
                            mfem_stream stream) {
     static_assert(sizeof(mfem_line_search_stats) == sizeof(LineSearchStats), "stats layout");
@@ -643,6 +876,7 @@ int mfem_predict(mfem_plan *p, const float *q, const float *qd, float dt, mfem_s
     // the predictor also snapshots x and copies it to q_out; pass x_start as
     // the output so the caller's q is left untouched
     cudaError_t e = launch_predict(q, qd, p->vv.x_start, p->gravity, dt, p->vv, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = launch_contact_begin(p->cv, p->vv, (cudaStream_t)stream);
     return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "predict");
 }
 
@@ -659,8 +893,7 @@ int mfem_assemble(mfem_plan *p, const float *x, float dt, mfem_stream stream) {
     if (!x) return fail(p, MFEM_BAD_ARG, "x is NULL");
     if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(p, MFEM_BAD_ARG, "dt must be finite and > 0");
     DeviceGuard g(p->device);
-    cudaError_t e = launch_assemble(x, dt, p->cfg.preconditioner_singular_threshold, p->cfg.preconditioner, p->tv,
-                                   p->vv, p->bv, (cudaStream_t)stream);
+    cudaError_t e = contact_and_assemble(p, x, dt, (cudaStream_t)stream);
     p->stage_dt = dt;
     return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "assemble");
 }

@@ -14,7 +14,9 @@
 // the result is deterministic.  A diagonal slot's first lane also adds the
 // mass/attachment term, inverts the block for the block-Jacobi
 // preconditioner, and writes the vertex's rhs g = sum fe - g_x and the warm
-// start dx = x~ - x.
+// start dx = x~ - x.  With contact, the contribution lists also carry the
+// surface tris' barrier blocks, and the diagonal lane adds the vertex's
+// barrier and friction block and takes the contact gradients off the rhs.
 #include "internal.h"
 
 namespace mfem {
@@ -33,7 +35,7 @@ __device__ __forceinline__ float seg_sum(float v, int lane, int last) {
 
 __global__ void __launch_bounds__(kAssembleThreads)
     assemble_kernel(const float *__restrict__ x, float dt, float alpha_mass, float singular_threshold,
-                    int use_precond, TetViews tv, VertexViews vv, BsrViews bv) {
+                    int use_precond, TetViews tv, VertexViews vv, BsrViews bv, ContactViews cv) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= bv.n_chunks) return;  // uniform per warp
@@ -49,7 +51,18 @@ __global__ void __launch_bounds__(kAssembleThreads)
     for (int c = beg + lane; c < end; c += 32) {
         code = __ldg(bv.contrib_code + c);
         slot = __ldg(bv.contrib_slot + c);
-        if (code >= 0) {
+        if (code >= cv.tri_code_base) {
+            // tri contact block w_i w_j k max(b'', 0) n n^T (contact.py:733-741)
+            const int tc = code - cv.tri_code_base;
+            const int tri = tc / 9;
+            const int i = (tc - 9 * tri) / 3, j = tc - 9 * tri - 3 * i;
+            const float *td = cv.tri + (size_t)tri * kTriData;
+            const float hw = (td[7 + i] * td[7 + j]) * td[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int bb = 0; bb < 3; ++bb) v[a * 3 + bb] += hw * (td[4 + a] * td[4 + bb]);
+        } else if (code >= 0) {
             const int e = code >> 4;
             const int k = (code >> 2) & 3;
             const int l = code & 3;
@@ -85,7 +98,13 @@ __global__ void __launch_bounds__(kAssembleThreads)
 
     bool diag;
     int row = 0;
-    if (code >= 0) {
+    if (code >= cv.tri_code_base) {
+        const int tc = code - cv.tri_code_base;
+        const int tri = tc / 9;
+        const int i = (tc - 9 * tri) / 3, j = tc - 9 * tri - 3 * i;
+        diag = (i == j);
+        if (diag) row = cv.tris[3 * tri + i];
+    } else if (code >= 0) {
         const int e = code >> 4;
         const int k = (code >> 2) & 3;
         const int l = code & 3;
@@ -104,6 +123,25 @@ __global__ void __launch_bounds__(kAssembleThreads)
         v[0] += hd;
         v[4] += hd;
         v[8] += hd;
+        // + the vertex's barrier and friction blocks (solver.py:745-779)
+        float gc[3] = {0.0f, 0.0f, 0.0f};
+        if (cv.on) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) v[i] += cv.vblock[9 * row + i];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) gc[a] = cv.vgrad[3 * row + a];
+            // tri barrier gradients scattered with the barycentric weights
+            for (int k = cv.vt_ptr[row]; k < cv.vt_ptr[row + 1]; ++k) {
+                const int code3 = cv.vt_code[k];
+                const int tri = code3 / 3, corner = code3 - 3 * tri;
+                const float *td = cv.tri + (size_t)tri * kTriData;
+                const float gw = td[7 + corner] * td[2];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) gc[a] += gw * td[4 + a];
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) cv.gtot[3 * row + a] = gc[a];
+        }
         // block-Jacobi inverse, identity for |det| < threshold (kernels.py:32-53)
         const float c00 = v[4] * v[8] - v[5] * v[7];
         const float c01 = v[5] * v[6] - v[3] * v[8];
@@ -136,7 +174,8 @@ __global__ void __launch_bounds__(kAssembleThreads)
             const float xt = vv.x_tilde[3 * row + a];
             const float pt = vv.pin_target[3 * row + a];
             const float gx = m * (xa - xt) / dt2 + (kp * xa + (-(kp * pt))) / dt2;
-            vv.rhs[3 * row + a] = f[a] - gx;
+            // - barrier and friction gradients (solver.py:734-735)
+            vv.rhs[3 * row + a] = (f[a] - gx) - gc[a];
             vv.dx[3 * row + a] = xt - xa;
         }
     }
@@ -181,7 +220,8 @@ __global__ void true_residual_kernel(BsrViews bv, const float *__restrict__ rhs,
 }  // namespace
 
 cudaError_t launch_assemble(const float *x, float dt, float singular_threshold, int use_precond,
-                            const TetViews &tv, const VertexViews &vv, const BsrViews &bv, cudaStream_t s) {
+                            const TetViews &tv, const VertexViews &vv, const BsrViews &bv, const ContactViews &cv,
+                            cudaStream_t s) {
     if (bv.n_chunks == 0) return cudaSuccess;
     const int warps_per_block = kAssembleThreads / 32;
     const int blocks = (bv.n_chunks + warps_per_block - 1) / warps_per_block;
@@ -189,7 +229,7 @@ cudaError_t launch_assemble(const float *x, float dt, float singular_threshold, 
     // bsr_axpy scale of the reference (solver.py:737-743)
     const float alpha_mass = (float)(1.0 / ((double)dt * (double)dt));
     assemble_kernel<<<blocks, kAssembleThreads, 0, s>>>(x, dt, alpha_mass, singular_threshold, use_precond, tv, vv,
-                                                        bv);
+                                                        bv, cv);
     count_launches(1);
     return cudaGetLastError();
 }

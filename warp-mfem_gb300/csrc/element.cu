@@ -11,6 +11,8 @@
 //                      stores ds, leaves x and s, sums the merit and slope.
 //  predict_kernel      integrate_particles + state_out.assign(state_in).
 //  velocity_kernel     get_particle_velocity.
+#include <algorithm>
+
 #include "merit.cuh"
 
 namespace mfem {
@@ -236,13 +238,21 @@ __global__ void __launch_bounds__(kVertexThreads)
 // (g_s + SYM lambda) . ds (solver.py:803-869, 893-915).
 __global__ void __launch_bounds__(kVertexThreads)
     local_solve_deferred_kernel(const float *__restrict__ x, int energy, float dt, double inv_dt2, TetViews tv,
-                                VertexViews vv, LineSearchWork w, int tet_blocks) {
+                                VertexViews vv, ContactViews cv, LineSearchWork w, int tet_blocks) {
     __shared__ double s_red[2][kVertexThreads / 32];
     double merit = 0.0, slope = 0.0;
     if ((int)blockIdx.x >= tet_blocks) {
         const int v = (blockIdx.x - tet_blocks) * blockDim.x + threadIdx.x;
+        // contact: the energies and gradients the contact kernel left at x
+        // (barrier_gradient + friction_gradient in the slope, solver.py:909)
+        if (cv.on && v < cv.n_tris) merit += (double)cv.tri[(size_t)v * kTriData + 1];
+        if (cv.on && v < vv.n) {
+            merit += (double)cv.venergy[v];
+            slope += (double)(cv.gtot[3 * v] * vv.dx[3 * v] + cv.gtot[3 * v + 1] * vv.dx[3 * v + 1] +
+                              cv.gtot[3 * v + 2] * vv.dx[3 * v + 2]);
+        }
         if (v < vv.n) {
-            merit = vertex_merit(vv, x, v, 0.0f, inv_dt2);
+            merit += vertex_merit(vv, x, v, 0.0f, inv_dt2);
             // g_x as in the assembly: m (x - x~)/dt^2 + (k x - k p)/dt^2
             const float dt2 = dt * dt;
             const float m = vv.mass[v];
@@ -254,7 +264,7 @@ __global__ void __launch_bounds__(kVertexThreads)
                 const float gx = m * (xa - vv.x_tilde[3 * v + a]) / dt2 + (kp * xa + (-(kp * vv.pin_target[3 * v + a]))) / dt2;
                 sl += gx * vv.dx[3 * v + a];
             }
-            slope = sl;
+            slope += sl;
         }
     } else {
         const int T = tv.n_tets;
@@ -349,15 +359,19 @@ cudaError_t launch_local_solve(float *x, const TetViews &tv, const VertexViews &
     return cudaGetLastError();
 }
 
-int local_solve_blocks(int n_tets, int n) { return blocks_for(n_tets, kVertexThreads) + blocks_for(n, kVertexThreads); }
+int local_solve_blocks(int n_tets, int n_vertex_range) {
+    return blocks_for(n_tets, kVertexThreads) + blocks_for(n_vertex_range, kVertexThreads);
+}
 
 cudaError_t launch_local_solve_deferred(const float *x, int energy, float dt, const TetViews &tv,
-                                        const VertexViews &vv, const LineSearchWork &w, cudaStream_t s) {
+                                        const VertexViews &vv, const ContactViews &cv, const LineSearchWork &w,
+                                        cudaStream_t s) {
     const int tb = blocks_for(tv.n_tets, kVertexThreads);
-    const int vb = blocks_for(vv.n, kVertexThreads);
+    const int vb = blocks_for(std::max(vv.n, cv.on ? cv.n_tris : 0), kVertexThreads);
     if (tb + vb == 0) return cudaSuccess;
+    if (tb + vb > w.local_blocks) return cudaErrorInvalidValue;  // partials sized for fewer blocks
     const double inv_dt2 = 1.0 / ((double)dt * (double)dt);
-    local_solve_deferred_kernel<<<tb + vb, kVertexThreads, 0, s>>>(x, energy, dt, inv_dt2, tv, vv, w, tb);
+    local_solve_deferred_kernel<<<tb + vb, kVertexThreads, 0, s>>>(x, energy, dt, inv_dt2, tv, vv, cv, w, tb);
     count_launches(1);
     return cudaGetLastError();
 }

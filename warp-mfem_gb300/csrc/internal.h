@@ -115,6 +115,40 @@ struct LineSearchWork {
     float alpha0, tau, c, threshold;
 };
 
+// Contact against rigid shapes: per-vertex barrier and lagged friction,
+// per-tri barrier against capsules.  on == 0: no contact term at all.
+constexpr int kTriData = 12;  // per tri: d, k b, k b', k max(b'', 0), n[3], w[3], shape, unused
+constexpr int kMaxShapes = 64;
+
+struct ContactViews {
+    int on;
+    int n_shapes;
+    const int *type;          // [S] shape type (contact.cuh kShape*)
+    const float *pose;        // [S][7] shape pose in its body's frame
+    const float *scale;       // [S][3] capsule (radius, half height, -)
+    const int *body;          // [S] body index, < 0: static
+    const float *mu;          // [S] Coulomb coefficient
+    const float *body_q;      // [B][7] body poses of the step
+    int friction;             // some shape has mu > 0
+    float d0, d1, k, eps_v;
+    float q[3];               // barrier extrapolation (b, b', b'') at d0
+    // lagged friction, frozen at the start of the step
+    float *normal_lagged;     // [n][3]
+    float *force_lagged;      // [n]
+    int *shape_lagged;        // [n]
+    // per Newton iteration
+    float *vblock;            // [n][9] barrier + friction Hessian block
+    float *vgrad;             // [n][3] barrier + friction gradient
+    float *venergy;           // [n]
+    float *gtot;              // [n][3] vertex + tri gradient
+    int n_tris;               // 0: no tri contact
+    const int *tris;          // [m][3]
+    float *tri;               // [m][kTriData]
+    const int *vt_ptr;        // [n+1] incident tri corners per vertex
+    const int *vt_code;       // tri * 3 + corner
+    int tri_code_base;        // assembly codes >= base are tri blocks
+};
+
 // Row partition and shared-memory plan of the persistent PCG.
 struct PcgLayout {
     enum { kAuto = 0, kStandard = 1, kSingleReduction = 2, kGather = 3 };
@@ -134,8 +168,14 @@ bool build_sparsity(int n, int T, const int32_t *tets, std::vector<int32_t> &row
                     std::vector<int32_t> &col_idx, std::string &err);
 bool build_slot_map(int n, int T, const int32_t *tets, const int32_t *row_ptr, const int32_t *col_idx,
                     int32_t *slots, std::string &err);
+// Slots of the 9 blocks (i, j) of each surface tri and the incident tri
+// corners (tri * 3 + corner) of each vertex.
+bool build_tri_slots(int n, int n_tris, const int32_t *tris, const int32_t *row_ptr, const int32_t *col_idx,
+                     int32_t *tri_slots, std::vector<int32_t> &vt_ptr, std::vector<int32_t> &vt_code,
+                     std::string &err);
 bool build_contributions(int n, int T, const int32_t *tets, const int32_t *row_ptr,
-                         const int32_t *slots, Symbolic &sym, std::string &err);
+                         const int32_t *slots, Symbolic &sym, std::string &err, int n_tris = 0,
+                         const int32_t *tri_slots = nullptr);
 
 // Kernel launchers (each returns cudaGetLastError()).
 cudaError_t launch_initial_stretch(const float *rest_q, const TetViews &tv, cudaStream_t s);
@@ -143,15 +183,21 @@ cudaError_t launch_predict(const float *q_in, const float *qd_in, float *q_out, 
                            float dt, const VertexViews &vv, cudaStream_t s);
 cudaError_t launch_element(const float *x, int energy, const TetViews &tv, cudaStream_t s);
 cudaError_t launch_assemble(const float *x, float dt, float singular_threshold, int use_precond,
-                            const TetViews &tv, const VertexViews &vv, const BsrViews &bv, cudaStream_t s);
+                            const TetViews &tv, const VertexViews &vv, const BsrViews &bv, const ContactViews &cv,
+                            cudaStream_t s);
+cudaError_t launch_contact(const float *x, float dt, const ContactViews &cv, const VertexViews &vv, cudaStream_t s);
+cudaError_t launch_contact_begin(const ContactViews &cv, const VertexViews &vv, cudaStream_t s);
 cudaError_t launch_local_solve(float *x, const TetViews &tv, const VertexViews &vv, cudaStream_t s);
 // Local solve that leaves x and s for the line search: writes lambda, ds and
 // the per-block partial sums of the merit function and the slope.
 cudaError_t launch_local_solve_deferred(const float *x, int energy, float dt, const TetViews &tv,
-                                        const VertexViews &vv, const LineSearchWork &w, cudaStream_t s);
-int local_solve_blocks(int n_tets, int n);
+                                        const VertexViews &vv, const ContactViews &cv, const LineSearchWork &w,
+                                        cudaStream_t s);
+// blocks of the deferred local solve: tets, then max(vertices, contact tris)
+int local_solve_blocks(int n_tets, int n_vertex_range);
 cudaError_t launch_line_search(float *x, int energy, float dt, const TetViews &tv, const VertexViews &vv,
-                               const LineSearchWork &w, int *error, int slot, cudaStream_t s);
+                               const ContactViews &cv, const LineSearchWork &w, int *error, int slot,
+                               cudaStream_t s);
 cudaError_t line_search_max_ctas(int device, int *ctas);
 cudaError_t launch_velocity(const float *q_out, float *qd_out, float dt, const VertexViews &vv, cudaStream_t s);
 cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const PcgLayout &L, int ctas,

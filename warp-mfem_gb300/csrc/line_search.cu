@@ -28,6 +28,10 @@
 // The first round also carries each CTA's slice of the local-solve partials,
 // so f0 and t come with the first trial at no extra barrier.
 //
+// With contact, the merit also carries the barrier and friction energies
+// of the vertices and the barrier energies of the surface tris, evaluated at
+// each trial point (solver.py:858-862), and the slope their gradients.
+//
 // Every wait is bounded; after a timeout the kernel sets the sticky error
 // flag and leaves x and s unchanged, reporting MFEM_TIMEOUT.
 #include <algorithm>
@@ -44,6 +48,8 @@ constexpr long long kWaitCycles = 8000000000ll;  // ~4 s at 2 GHz per wait
 struct LsArgs {
     TetViews tv;
     VertexViews vv;
+    ContactViews cv;
+    float ev;  // friction threshold eps_v dt
     float *x;
     LineSearchWork w;
     int *error;
@@ -103,6 +109,17 @@ __global__ void __launch_bounds__(kLsThreads, 4) line_search_kernel(LsArgs a) {
         double e = 0.0;
         for (int t = first; t < T; t += stride) e += tet_merit(a.tv, a.x, a.vv.dx, w.ds, a.energy, t, alpha);
         for (int v = first; v < n; v += stride) e += vertex_merit(a.vv, a.x, v, alpha, a.inv_dt2);
+        if (a.cv.on) {
+            // barrier and friction energies at the trial (Contact.evaluate_energy_only)
+            for (int v = first; v < n; v += stride) {
+                float xt[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) xt[c] = fmaf(alpha, a.vv.dx[3 * v + c], a.x[3 * v + c]);
+                e += (double)vertex_contact_energy(a.cv, a.vv, v, xt, a.ev);
+            }
+            for (int t = first; t < a.cv.n_tris; t += stride)
+                e += (double)tri_contact_energy(a.cv, a.x, a.vv.dx, t, alpha);
+        }
         double part[3] = {e, j == 0 ? lf : 0.0, j == 0 ? lsl : 0.0};
 #pragma unroll
         for (int i = 0; i < 3; ++i) part[i] = warp_sum(part[i]);
@@ -205,10 +222,13 @@ cudaError_t line_search_max_ctas(int device, int *ctas) {
 }
 
 cudaError_t launch_line_search(float *x, int energy, float dt, const TetViews &tv, const VertexViews &vv,
-                               const LineSearchWork &w, int *error, int slot, cudaStream_t s) {
+                               const ContactViews &cv, const LineSearchWork &w, int *error, int slot,
+                               cudaStream_t s) {
     LsArgs a;
     a.tv = tv;
     a.vv = vv;
+    a.cv = cv;
+    a.ev = (float)((double)cv.eps_v * (double)dt);
     a.x = x;
     a.w = w;
     a.error = error;

@@ -4,6 +4,7 @@
 // Reference: the objective of src/mfem/refinement/solver.py:803-869.
 #pragma once
 
+#include "contact_terms.cuh"
 #include "element_math.cuh"
 #include "internal.h"
 

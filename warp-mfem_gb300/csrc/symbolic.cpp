@@ -103,12 +103,55 @@ bool build_slot_map(int n, int T, const int32_t *tets, const int32_t *row_ptr, c
     return true;
 }
 
+bool build_tri_slots(int n, int n_tris, const int32_t *tris, const int32_t *row_ptr, const int32_t *col_idx,
+                     int32_t *tri_slots, std::vector<int32_t> &vt_ptr, std::vector<int32_t> &vt_code,
+                     std::string &err) {
+    for (int t = 0; t < n_tris; ++t) {
+        const int32_t *v = tris + 3 * (int64_t)t;
+        for (int k = 0; k < 3; ++k) {
+            if (v[k] < 0 || v[k] >= n) {
+                err = "tri " + std::to_string(t) + " has a vertex index out of range";
+                return false;
+            }
+        }
+        if (v[0] == v[1] || v[1] == v[2] || v[0] == v[2]) {
+            err = "tri " + std::to_string(t) + " repeats a vertex";
+            return false;
+        }
+        for (int i = 0; i < 3; ++i) {
+            const int32_t *b = col_idx + row_ptr[v[i]];
+            const int32_t *e = col_idx + row_ptr[v[i] + 1];
+            for (int j = 0; j < 3; ++j) {
+                const int32_t *p = std::lower_bound(b, e, v[j]);
+                if (p == e || *p != v[j]) {
+                    err = "tri " + std::to_string(t) + " joins vertices that share no tet";
+                    return false;
+                }
+                tri_slots[(int64_t)t * 9 + i * 3 + j] = (int32_t)(p - col_idx);
+            }
+        }
+    }
+    // incident tri corners of each vertex, in tri order
+    vt_ptr.assign(n + 1, 0);
+    for (int64_t i = 0; i < (int64_t)n_tris * 3; ++i) vt_ptr[tris[i] + 1]++;
+    for (int v = 0; v < n; ++v) vt_ptr[v + 1] += vt_ptr[v];
+    vt_code.assign((size_t)n_tris * 3, 0);
+    std::vector<int32_t> fill(vt_ptr.begin(), vt_ptr.end() - 1);
+    for (int64_t i = 0; i < (int64_t)n_tris * 3; ++i) vt_code[fill[tris[i]]++] = (int32_t)i;
+    return true;
+}
+
 bool build_contributions(int n, int T, const int32_t *tets, const int32_t *row_ptr, const int32_t *slots,
-                         Symbolic &sym, std::string &err) {
+                         Symbolic &sym, std::string &err, int n_tris, const int32_t *tri_slots) {
     (void)tets;
     const int64_t nnzb = row_ptr[n];
+    if ((int64_t)T * 16 + (int64_t)n_tris * 9 > (int64_t)INT32_MAX) {
+        err = "too many tets and tris for 32-bit contribution codes";
+        return false;
+    }
     std::vector<int32_t> count(nnzb + 1, 0);
     for (int64_t i = 0; i < (int64_t)T * 16; ++i) count[slots[i] + 1]++;
+    for (int64_t i = 0; i < (int64_t)n_tris * 9; ++i) count[tri_slots[i] + 1]++;
     // a vertex without tets still owns its diagonal block (mass + attachment):
     // give it one empty contribution so the assembly visits it
     std::vector<int32_t> isolated;  // vertices in no tet
@@ -149,6 +192,15 @@ bool build_contributions(int n, int T, const int32_t *tets, const int32_t *row_p
             const int32_t s = slots[(int64_t)e * 16 + kl];
             const int64_t pos = fill[s]++;
             sym.contrib_code[pos] = e * 16 + kl;
+            sym.contrib_slot[pos] = s;
+        }
+    // surface-tri contact blocks (i, j) after the tets of their slot, coded
+    // 16 T + 9 tri + 3 i + j
+    for (int t = 0; t < n_tris; ++t)
+        for (int ij = 0; ij < 9; ++ij) {
+            const int32_t s = tri_slots[(int64_t)t * 9 + ij];
+            const int64_t pos = fill[s]++;
+            sym.contrib_code[pos] = 16 * T + 9 * t + ij;
             sym.contrib_slot[pos] = s;
         }
     // pack whole slots into chunks of <= 32 contributions (a longer slot gets

@@ -28,8 +28,12 @@ BUF = {
     "tet_stretch": 0, "tet_lambda": 1, "constraint": 2, "grad_constraint": 3, "grad_s": 4,
     "h_lambda": 5, "hess_s_inv": 6, "g_lambda": 7, "element_hessian": 8, "element_rhs": 9,
     "row_ptr": 10, "col_idx": 11, "tet_slots": 12, "h_values": 13, "rhs": 14, "precond": 15,
-    "x_tilde": 16, "dx": 17, "stretch_direction": 18,
+    "x_tilde": 16, "dx": 17, "stretch_direction": 18, "contact_block": 19, "contact_gradient": 20,
+    "contact_energy": 21, "tri_contact": 22, "friction_normal": 23, "friction_force": 24,
 }
+
+SHAPE_PLANE = 0
+SHAPE_CAPSULE = 1
 
 
 class MfemConfig(ctypes.Structure):
@@ -74,6 +78,17 @@ class MfemLineSearchStats(ctypes.Structure):
     ]
 
 
+class MfemContactConfig(ctypes.Structure):
+    _fields_ = [
+        ("d0", ctypes.c_float),
+        ("d1", ctypes.c_float),
+        ("stiffness", ctypes.c_float),
+        ("friction_eps_v", ctypes.c_float),
+        ("tri_contact", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 3),
+    ]
+
+
 class MfemError(RuntimeError):
     def __init__(self, code: int, message: str):
         super().__init__(f"{message} (status {code})")
@@ -105,6 +120,10 @@ _SIGNATURES = {
     "mfem_step_stats": (ctypes.c_int, [_P, ctypes.POINTER(MfemSolveStats), _I32, ctypes.POINTER(_I32), _P]),
     "mfem_step_line_search_stats": (ctypes.c_int, [_P, ctypes.POINTER(MfemLineSearchStats), _I32,
                                                    ctypes.POINTER(_I32), _P]),
+    "mfem_contact_config_default": (None, [ctypes.POINTER(MfemContactConfig)]),
+    "mfem_plan_set_contact": (ctypes.c_int, [_P, ctypes.POINTER(MfemContactConfig), _I32, _P, _P, _P, _P, _P, _I32,
+                                             _I32, _P]),
+    "mfem_set_body_poses": (ctypes.c_int, [_P, _P, _I32, _P]),
     "mfem_predict": (ctypes.c_int, [_P, _P, _P, _F32, _P]),
     "mfem_update_system": (ctypes.c_int, [_P, _P, _P]),
     "mfem_assemble": (ctypes.c_int, [_P, _P, _F32, _P]),

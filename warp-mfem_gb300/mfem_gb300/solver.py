@@ -32,9 +32,13 @@ class MixedFEMSolver:
     ``line_search`` defaults to True like the reference's (solver.py:185),
     with its ``line_search_max_iterations`` / ``_alpha0`` / ``_tau`` / ``_c`` /
     ``_threshold`` (solver.py:99-103); ``line_search=False`` gives the plain
-    update x += dx, s += ds.  Refinement, contact against rigid shapes and
-    the membrane shell are outside this solver: ``enable_refinement``
-    defaults to False here and raises if set True; ``shell_mu`` must be 0.
+    update x += dx, s += ds.  Contact against the model's rigid shapes
+    (planes, capsules) takes the reference's ``contact_d0``, ``contact_d1``,
+    ``contact_stiffness``, ``friction_mu`` (one value or one per shape),
+    ``friction_eps_v`` and ``tri_contact`` (solver.py:241-265); it is on when
+    the model has shapes.  Refinement and the membrane shell are outside this
+    solver: ``enable_refinement`` defaults to False here and raises if set
+    True; ``shell_mu`` must be 0.
     """
 
     def __init__(self, model: Model, iterations: int, max_tets: Optional[int] = None,
@@ -103,6 +107,53 @@ class MixedFEMSolver:
         nnzb = ctypes.c_int64()
         self._lib.mfem_plan_sizes(plan, ctypes.byref(n), ctypes.byref(T), ctypes.byref(nnzb))
         self.n, self.T, self.nnzb = n.value, T.value, nnzb.value
+        self.n_bodies = 0
+        self.n_contact_tris = 0
+        if getattr(model, "shape_count", 0) > 0:
+            self._set_contact(model, kwargs)
+
+    def _set_contact(self, model, kwargs) -> None:
+        """Contact against the model's shapes (Contact.__init__,
+        src/mfem/refinement/contact.py:778-862)."""
+        ccfg = _lib.MfemContactConfig()
+        self._lib.mfem_contact_config_default(ctypes.byref(ccfg))
+        ccfg.d0 = float(kwargs.get("contact_d0", 1.0e-2))
+        ccfg.d1 = float(kwargs.get("contact_d1", 1.0e-1))
+        ccfg.stiffness = float(kwargs.get("contact_stiffness", 1.0e7))
+        ccfg.friction_eps_v = float(kwargs.get("friction_eps_v", 1.0e-3))
+        ccfg.tri_contact = 1 if kwargs.get("tri_contact", True) else 0
+        S = model.shape_count
+        mu = np.asarray(kwargs.get("friction_mu", 0.0), dtype=np.float32)
+        if mu.ndim == 0:
+            mu = np.full(S, float(mu), dtype=np.float32)
+        elif mu.shape[0] != S:
+            raise ValueError(f"friction_mu has {mu.shape[0]} entries but the model has {S} shapes")
+        host = lambda t, dt: np.ascontiguousarray(t.detach().to("cpu").numpy(), dtype=dt)
+        tris = getattr(model, "tri_indices", None)
+        tris = host(tris, np.int32).reshape(-1, 3) if tris is not None else np.zeros((0, 3), np.int32)
+        self._contact_host = dict(type=host(model.shape_type, np.int32), pose=host(model.shape_transform, np.float32),
+                                  scale=host(model.shape_scale, np.float32), body=host(model.shape_body, np.int32),
+                                  mu=np.ascontiguousarray(mu), tris=np.ascontiguousarray(tris))
+        h = self._contact_host
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        n_bodies = int(getattr(model, "body_count", 0))
+        rc = self._lib.mfem_plan_set_contact(self._plan, ctypes.byref(ccfg), S, P(h["type"]), P(h["pose"]),
+                                             P(h["scale"]), P(h["body"]), P(h["mu"]), n_bodies, tris.shape[0],
+                                             P(h["tris"]))
+        _lib.check(rc, self._plan)
+        self.contact_config = ccfg
+        self.n_bodies = n_bodies
+        self.n_contact_tris = tris.shape[0] if ccfg.tri_contact else 0
+        if n_bodies > 0:
+            self.set_body_poses(model.body_q)
+
+    def set_body_poses(self, body_q: torch.Tensor) -> None:
+        """Body poses [bodies, 7] the next steps read (asynchronous)."""
+        if not (body_q.is_cuda and body_q.dtype == torch.float32 and body_q.is_contiguous()
+                and tuple(body_q.shape) == (self.n_bodies, 7)):
+            raise ValueError(f"body_q must be a contiguous float32 CUDA tensor of shape ({self.n_bodies}, 7)")
+        _lib.check(self._lib.mfem_set_body_poses(self._plan, ctypes.c_void_p(body_q.data_ptr()), self.n_bodies,
+                                                 _stream_handle(self.device)), self._plan)
 
     def pcg_layout(self) -> dict:
         """The persistent PCG this plan uses (variant, CTAs, matrix cached in
@@ -141,6 +192,9 @@ class MixedFEMSolver:
         qd_in = self._check_state(state_in.particle_qd, "state_in.particle_qd")
         q_out = self._check_state(state_out.particle_q, "state_out.particle_q")
         qd_out = self._check_state(state_out.particle_qd, "state_out.particle_qd")
+        if self.n_bodies > 0 and getattr(state_out, "body_q", None) is not None:
+            # the reference reads the rigid bodies' poses from state_out
+            self.set_body_poses(state_out.body_q)
         rc = self._lib.mfem_step(self._plan, q_in, qd_in, q_out, qd_out, float(dt), _stream_handle(self.device))
         _lib.check(rc, self._plan)
 
@@ -196,6 +250,11 @@ class MixedFEMSolver:
 
     # -- buffers ---------------------------------------------------------------
     _BUF_DTYPE = {"row_ptr": torch.int32, "col_idx": torch.int32, "tet_slots": torch.int32}
+
+    def contact_tris(self) -> np.ndarray:
+        """The per-tri contact record [m, 12] (d, k b, k b', k max(b'', 0),
+        n[3], w[3], shape, 0) of the last assembly."""
+        return self.read_buffer("tri_contact").cpu().numpy().reshape(-1, 12)
 
     def read_buffer(self, name: str) -> torch.Tensor:
         """Device copy of an internal buffer (flat; layouts in include/mfem_gb300.h)."""
