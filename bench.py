@@ -49,13 +49,22 @@ def parse_args():
     ap.add_argument("--profile-steps", type=int, default=10, help="steps of the eager stage profile")
     ap.add_argument("--pcg-ctas", type=int, default=0, help="persistent PCG CTAs (0: one per SM)")
     ap.add_argument("--pcg-variant", default="auto", choices=["auto", "standard", "single_reduction"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16", "fp16"],
+                    help="global solve: fp32 PCG (the workload's) or mixed-precision iterative refinement")
+    ap.add_argument("--outer-tolerance", type=float, default=1.0e-6,
+                    help="fp64 relative residual of the mixed-precision solve")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget-s", type=float, default=30.0, help="CPU time budget of the oracle leg")
     return ap.parse_args()
 
 
-def workload_config(mesh, extra=None):
+def workload_config(mesh, extra=None, precision="fp32", outer_tolerance=1e-6):
     spec = mesh.spec
+    if precision == "fp32":
+        pcg = "plain fp32 block-Jacobi (the learned + mixed-precision variant is not built)"
+    else:
+        pcg = (f"{precision} blocks with per-row scales, fp32 block-Jacobi inner PCG to 1e-3, fp64 iterative "
+               f"refinement to {outer_tolerance:g}")
     cfg = {
         "workload": (f"{spec.name}: {spec.cells[0]}x{spec.cells[1]}x{spec.cells[2]} hex cells x 6 tets "
                      f"({mesh.T} tets, {mesh.n} vertices, {3 * mesh.n} DoF), {spec.energy}, "
@@ -65,7 +74,7 @@ def workload_config(mesh, extra=None):
         "tets": mesh.T,
         "vertices": mesh.n,
         "steps_per_run": spec.steps,
-        "pcg": "plain fp32 block-Jacobi (the learned + mixed-precision variant is not built)",
+        "pcg": pcg,
         "parallelism": "replicas",
         "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write, outside the timed events)",
     }
@@ -234,7 +243,8 @@ def run_gb300(args, rank, world, local_rank):
     solver = MixedFEMSolver(model, iterations=spec.iterations, energy=spec.energy,
                             cg_tolerance=spec.cg_tolerance, cg_max_iterations=spec.cg_max_iterations,
                             pcg_ctas=args.pcg_ctas, pcg_variant=args.pcg_variant,
-                            line_search=False)  # the workload is the plain local/global step
+                            line_search=False,  # the workload is the plain local/global step
+                            solver_precision=args.precision, outer_tolerance=args.outer_tolerance)
     s_init = solver.tet_stretch.clone().reshape(-1)
     lam0 = torch.zeros_like(s_init)
     q0 = torch.as_tensor(mesh.q0, device=dev)
@@ -378,6 +388,10 @@ def run_gb300(args, rank, world, local_rank):
         "bytes_per_pcg_iteration": b_it, "pcg_iterations_per_launch": per_launch_iters - 1,
         "avg_launch_ms": stage_ms["pcg"] / stage_launches["pcg"], "peak_source": peak_src,
     }
+    if args.precision != "fp32":
+        # the persistent fp32 PCG does not run: the mixed-precision solves are
+        # reported as a whole (stage_ms_per_step["pcg"])
+        roofline = None
     total_stage = sum(stage_ms.values())
     shares = {k: v / total_stage for k, v in stage_ms.items()}
 
@@ -394,7 +408,7 @@ def run_gb300(args, rank, world, local_rank):
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(mesh),
+        "config": workload_config(mesh, precision=args.precision, outer_tolerance=args.outer_tolerance),
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes, "matches_resident_run": e2e_match},
         "gpu_launches": int(launches),

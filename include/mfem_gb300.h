@@ -103,7 +103,9 @@ typedef enum mfem_buffer {
                                       n[3], w[3], shape, 0                                     */
     MFEM_BUF_FRICTION_NORMAL = 23, /* f32 [n][3] lagged contact normal of the step               */
     MFEM_BUF_FRICTION_FORCE = 24,  /* f32 [n]    lagged normal force of the step                 */
-    MFEM_BUF_COUNT = 25
+    MFEM_BUF_MIXED_DX = 25,        /* f64 [n][3] solution of the last mixed-precision solve
+                                      (empty with the FP32 solve)                              */
+    MFEM_BUF_COUNT = 26
 } mfem_buffer;
 
 /* Rigid shapes that contact takes into account (Newton's GeoType PLANE and
@@ -134,6 +136,34 @@ typedef struct mfem_solve_stats {
     float rel_residual;     /* ||r|| / ||b|| of the recurrence residual    */
     float reserved;
 } mfem_solve_stats;
+
+/* Precision of the global solve.  FP32 is the reference's float32 PCG;
+ * BF16 / FP16 store the BSR blocks in 16 bits (each block row scaled by its
+ * largest |entry|) for an inner PCG with fp32 vectors, inside an iterative
+ * refinement whose residual g - H dx is formed in fp64 from the fp32 H. */
+typedef enum mfem_precision {
+    MFEM_PRECISION_FP32 = 0,
+    MFEM_PRECISION_BF16 = 1,
+    MFEM_PRECISION_FP16 = 2
+} mfem_precision;
+
+typedef struct mfem_solver_config {
+    int32_t precision;              /* mfem_precision                                   */
+    float inner_tolerance;          /* inner PCG: ||r|| <= tol ||rhs||, default 1e-3     */
+    int32_t outer_max_iterations;   /* corrections per solve, default 10                */
+    int32_t reserved0;
+    double outer_tolerance;         /* fp64 ||g - H dx|| <= tol ||g||, default 1e-8     */
+    int32_t reserved[4];
+} mfem_solver_config;
+
+/* Per Newton iteration outcome of a mixed-precision solve. */
+typedef struct mfem_mixed_solve_stats {
+    int32_t outer_iterations;       /* corrections applied                              */
+    int32_t inner_iterations;       /* PCG iterations over all corrections              */
+    int32_t status;                 /* MFEM_OK, MFEM_MAXITER (outer cap), ...           */
+    int32_t reserved;
+    double rel_residual;            /* fp64 ||g - H dx|| / ||g|| of the returned dx     */
+} mfem_mixed_solve_stats;
 
 /* Per Newton iteration outcome of the line search. */
 typedef struct mfem_line_search_stats {
@@ -243,6 +273,27 @@ int mfem_plan_set_contact(mfem_plan *plan, const mfem_contact_config *cfg, int32
  * reference's state_out.body_q) into the plan, asynchronously on `stream`
  * (host or device memory).  n_bodies must match mfem_plan_set_contact. */
 int mfem_set_body_poses(mfem_plan *plan, const float *body_q, int32_t n_bodies, mfem_stream stream);
+
+/* ---- precision of the global solve ----------------------------------- */
+
+void mfem_solver_config_default(mfem_solver_config *cfg);
+
+/* Selects the global solve: the reference's float32 block-Jacobi PCG
+ * (precision FP32, the default) or the mixed-precision iterative refinement
+ * (BF16 / FP16 blocks, fp32 inner PCG to inner_tolerance with the fp32
+ * block-Jacobi inverse, fp64 residual; stops at outer_tolerance or after
+ * outer_max_iterations corrections, starting from the reference's warm
+ * start).  It has no reference counterpart: it is the mixed-precision variant
+ * of src/mfem/refinement/solver.py:581-609.  Synchronises the device and
+ * drops the plan's captured graphs. */
+int mfem_plan_set_solver(mfem_plan *plan, const mfem_solver_config *cfg);
+
+/* Outcomes of the mixed-precision solves of the last step (synchronises the
+ * stream; *count = 0 with the FP32 solve).  mfem_step_stats reports the same
+ * solves with iterations = inner iterations and rel_residual = the fp64
+ * residual. */
+int mfem_step_mixed_stats(mfem_plan *plan, mfem_mixed_solve_stats *h_stats, int32_t max_entries,
+                          int32_t *count, mfem_stream stream);
 
 /* ---- the step and its stages ---------------------------------------- */
 

@@ -1,0 +1,134 @@
+"""The mixed-precision global solve (16-bit blocks with per-row scales, fp32
+inner PCG, fp64 iterative refinement) on the GPU.
+
+It has no reference counterpart.  Its bar is the benchmark spec's:
+* the fp64 residual ||g - H dx|| / ||g|| of the returned fp64 solution,
+  recomputed here in numpy from the same fp32 H and g, is below the outer
+  tolerance, and agrees with the residual the solver reports;
+* a trajectory stays within 1e-5 of the float64 oracle, like the fp32 path.
+
+BF16 blocks (8 significant bits) stagnate on ill-conditioned systems: with
+per-row scales the refinement contracts only while cond(H) * 2^-9 < 1.  The
+test records that the solver reports this (MFEM_MAXITER and the residual it
+reached) rather than hiding it.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+from mfem_gb300 import Model, MixedFEMSolver, _lib, beams
+from oracle import mfem_oracle as O
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+def close(a, b, rtol):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    err = np.abs(a - b).max()
+    assert err <= rtol * np.abs(b).max(), f"max err {err:.3e} vs scale {np.abs(b).max():.3e}"
+
+
+def make(name, cells, precision, **kw):
+    mesh = beams.build_beam(name, cells=cells)
+    model = Model.from_beam(mesh, device=DEV)
+    solver = MixedFEMSolver(model, iterations=kw.pop("iterations", 8), energy=mesh.spec.energy,
+                            line_search=False, solver_precision=precision, **kw)
+    return mesh, model, solver
+
+
+def one_solve(mesh, solver):
+    """Predict, element stage, assembly and one global solve at q0; returns
+    the system (fp64 copies of the fp32 H and g) and the solution."""
+    q = torch.as_tensor(mesh.q0, device=DEV)
+    x = q.clone()
+    solver.predict(q, torch.zeros_like(q), mesh.spec.dt)
+    solver.update_system(x)
+    solver.assemble(x, mesh.spec.dt)
+    solver.global_solve(0)
+    torch.cuda.synchronize()
+    n = mesh.n
+    rp = solver.read_buffer("row_ptr").cpu().numpy()
+    ci = solver.read_buffer("col_idx").cpu().numpy()
+    vals = solver.read_buffer("h_values").cpu().numpy().astype(np.float64).reshape(-1, 3, 3)
+    H = sp.bsr_matrix((vals, ci, rp), shape=(3 * n, 3 * n)).tocsr()
+    g = solver.read_buffer("rhs").cpu().numpy().astype(np.float64)
+    dx64 = solver.read_buffer("mixed_dx").cpu().numpy()
+    dx32 = solver.read_buffer("dx").cpu().numpy()
+    return H, g, dx64, dx32
+
+
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+def test_mixed_solve_reaches_fp64_tolerance(precision):
+    mesh, _, solver = make("nh_beam", (16, 4, 4), precision)
+    H, g, dx64, dx32 = one_solve(mesh, solver)
+    rel = np.linalg.norm(g - H @ dx64) / np.linalg.norm(g)
+    st = solver.mixed_stats()[0]
+    assert st["status"] == _lib.MFEM_OK and 1 <= st["outer_iterations"] <= 10, st
+    assert rel <= 1e-8 and st["rel_residual"] <= 1e-8
+    assert rel == pytest.approx(st["rel_residual"], rel=1e-3, abs=1e-12)
+    np.testing.assert_array_equal(dx32, dx64.astype(np.float32))
+    # mfem_step_stats sees the same solve
+    s0 = solver.solve_stats()[0]
+    assert s0["iterations"] == st["inner_iterations"] and s0["status"] == st["status"]
+
+
+def test_fp16_reaches_tolerance_on_the_ill_conditioned_beam():
+    """E log-uniform in [1e4, 1e7] (the stiff beam's materials) at 32x8x8."""
+    mesh, _, solver = make("stiff_beam", (32, 8, 8), "fp16")
+    H, g, dx64, _ = one_solve(mesh, solver)
+    rel = np.linalg.norm(g - H @ dx64) / np.linalg.norm(g)
+    st = solver.mixed_stats()[0]
+    assert st["status"] == _lib.MFEM_OK and rel <= 1e-8, (st, rel)
+
+
+def test_bf16_stagnation_is_reported():
+    mesh, _, solver = make("stiff_beam", (32, 8, 8), "bf16", outer_max_iterations=4)
+    H, g, dx64, _ = one_solve(mesh, solver)
+    rel = np.linalg.norm(g - H @ dx64) / np.linalg.norm(g)
+    st = solver.mixed_stats()[0]
+    if st["status"] == _lib.MFEM_OK:
+        assert rel <= 1e-8
+    else:
+        assert st["status"] == _lib.MFEM_MAXITER and st["outer_iterations"] == 4
+        assert rel == pytest.approx(st["rel_residual"], rel=1e-3) and rel > 1e-8
+
+
+@pytest.mark.parametrize("precision,outer_tolerance", [("fp16", 1e-8), ("bf16", 1e-6)])
+def test_mixed_trajectory_matches_fp64_oracle(precision, outer_tolerance):
+    """BF16 targets 1e-6: on later Newton iterations it stagnates near 3e-7."""
+    mesh, model, solver = make("nh_beam", (16, 4, 4), precision, outer_tolerance=outer_tolerance,
+                               outer_max_iterations=12)
+    ref = O.OracleSolver(mesh, dtype=np.float64)
+    A, B = model.state(), model.state()
+    A.particle_q.copy_(torch.as_tensor(mesh.q0, device=DEV))
+    q, qd = mesh.q0, mesh.qd0
+    for _ in range(3):
+        solver.step(A, B, None, None, mesh.spec.dt)
+        A, B = B, A
+        q, qd = ref.step(q, qd, mesh.spec.dt)
+        assert all(s["status"] == _lib.MFEM_OK for s in solver.mixed_stats())
+        close(A.particle_q.cpu().numpy(), q, 1e-5)
+
+
+def test_mixed_graph_and_eager_agree_bitwise():
+    outs = []
+    for graph in (True, False):
+        mesh, model, solver = make("nh_beam", (16, 4, 4), "fp16", use_cuda_graph=graph)
+        A, B = model.state(), model.state()
+        for _ in range(2):
+            solver.step(A, B, None, None, mesh.spec.dt)
+            A, B = B, A
+        outs.append(A.particle_q.clone())
+    assert torch.equal(outs[0], outs[1])
+
+
+def test_set_solver_rejects_bad_config():
+    mesh = beams.build_beam("cantilever", cells=(2, 1, 1))
+    model = Model.from_beam(mesh, device=DEV)
+    with pytest.raises(_lib.MfemError):
+        MixedFEMSolver(model, iterations=1, solver_precision="fp16", inner_tolerance=2.0)
+    with pytest.raises(ValueError):
+        MixedFEMSolver(model, iterations=1, solver_precision="fp8")

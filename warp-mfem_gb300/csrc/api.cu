@@ -57,6 +57,10 @@ struct mfem_plan {
     std::vector<int32_t> h_tets, h_row_ptr, h_col_idx, h_tet_slots;
     const int32_t *base_chunk_ptr = nullptr, *base_code = nullptr, *base_slot = nullptr;
     int base_chunks = 0;
+    // mixed-precision global solve (mfem_plan_set_solver); mode 0 = the
+    // reference's float32 PCG
+    IrWork ir{};
+    std::vector<void *> ir_allocs;
     int32_t *tet_slots = nullptr;
     double *resid = nullptr;
     cudaStream_t capture_stream = nullptr;
@@ -149,6 +153,7 @@ bool buffer_ref(const mfem_plan *p, int which, BufferRef &ref) {
         case MFEM_BUF_TRI_CONTACT: ref = {p->cv.tri, p->cv.on ? (size_t)p->n_tris * kTriData * 4 : 0}; return true;
         case MFEM_BUF_FRICTION_NORMAL: ref = {p->cv.normal_lagged, p->cv.on ? n * 3 * 4 : 0}; return true;
         case MFEM_BUF_FRICTION_FORCE: ref = {p->cv.force_lagged, p->cv.on ? n * 4 : 0}; return true;
+        case MFEM_BUF_MIXED_DX: ref = {p->ir.dx_out, p->ir.mode ? n * 3 * 8 : 0}; return true;
         default: return false;
     }
 }
@@ -174,6 +179,14 @@ bool valid_config(const mfem_config *cfg, std::string &err) {
 }
 
 // The whole step as a launch sequence on one stream.
+// The reference's float32 PCG, or the mixed-precision iterative refinement.
+cudaError_t global_solve(mfem_plan *p, int slot, cudaStream_t s) {
+    if (p->ir.mode == 0)
+        return launch_pcg(p->bv, p->vv, p->pw, p->pl, p->pcg_ctas, slot, p->cfg.cg_tolerance,
+                          p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
+    return launch_mixed_solve(p->bv, p->vv, p->ir, p->pw, slot, p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
+}
+
 // Local solve then either the plain update x += dx, s += ds or the line
 // search (solver.py:539-557).
 cudaError_t local_update(mfem_plan *p, float *x, float dt, int slot, cudaStream_t s) {
@@ -202,9 +215,7 @@ cudaError_t run_step(mfem_plan *p, const float *q_in, const float *qd_in, float 
     for (int it = 0; err == cudaSuccess && it < p->cfg.iterations; ++it) {
         err = launch_element(q_out, p->cfg.energy, p->tv, s);
         if (err == cudaSuccess) err = contact_and_assemble(p, q_out, dt, s);
-        if (err == cudaSuccess)
-            err = launch_pcg(p->bv, p->vv, p->pw, p->pl, p->pcg_ctas, it, p->cfg.cg_tolerance,
-                             p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
+        if (err == cudaSuccess) err = global_solve(p, it, s);
         if (err == cudaSuccess) err = local_update(p, q_out, dt, it, s);
     }
     if (err == cudaSuccess) err = launch_velocity(q_out, qd_out, dt, p->vv, s);
@@ -293,6 +304,7 @@ void mfem_plan_destroy(mfem_plan *p) {
         if (p->capture_stream) cudaStreamDestroy(p->capture_stream);
         for (void *a : p->allocs) cudaFree(a);
         for (void *a : p->contact_allocs) cudaFree(a);
+        for (void *a : p->ir_allocs) cudaFree(a);
     }
     delete p;
 }
@@ -853,6 +865,110 @@ int mfem_set_body_poses(mfem_plan *p, const float *body_q, int32_t n_bodies, mfe
     return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "set_body_poses");
 }
 
+void mfem_solver_config_default(mfem_solver_config *cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->precision = MFEM_PRECISION_FP32;
+    cfg->inner_tolerance = 1.0e-3f;
+    cfg->outer_max_iterations = 10;
+    cfg->outer_tolerance = 1.0e-8;
+}
+
+int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
+    if (!p) return MFEM_BAD_ARG;
+    mfem_solver_config cfg;
+    if (cfg_in) cfg = *cfg_in;
+    else mfem_solver_config_default(&cfg);
+    if (cfg.precision != MFEM_PRECISION_FP32 && cfg.precision != MFEM_PRECISION_BF16 &&
+        cfg.precision != MFEM_PRECISION_FP16)
+        return fail(p, MFEM_BAD_ARG, "unknown precision");
+    if (!(cfg.inner_tolerance > 0.0f) || !(cfg.inner_tolerance < 1.0f))
+        return fail(p, MFEM_BAD_ARG, "inner_tolerance must be in (0, 1)");
+    if (!(cfg.outer_tolerance > 0.0) || !std::isfinite(cfg.outer_tolerance))
+        return fail(p, MFEM_BAD_ARG, "outer_tolerance must be finite and > 0");
+    if (cfg.outer_max_iterations < 1 || cfg.outer_max_iterations > 100)
+        return fail(p, MFEM_BAD_ARG, "outer_max_iterations must be in [1, 100]");
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaDeviceSynchronize();  // no step of this plan may still use the old buffers
+    if (e != cudaSuccess) return cuda_fail(p, e, "cudaDeviceSynchronize");
+    for (auto &ge : p->graphs) {
+        if (ge.exec) cudaGraphExecDestroy(ge.exec);
+        ge = mfem_plan::GraphEntry{};
+    }
+    for (void *a : p->ir_allocs) cudaFree(a);
+    p->ir_allocs.clear();
+    p->ir = IrWork{};
+    if (cfg.precision == MFEM_PRECISION_FP32) return MFEM_OK;
+
+    const size_t n3 = (size_t)p->n * 3, nz = (size_t)p->nnzb;
+    auto alloc = [&](auto **ptr, size_t bytes) {
+        if (e != cudaSuccess) return;
+        void *raw = nullptr;
+        e = cudaMalloc(&raw, std::max<size_t>(bytes, 16));
+        if (e == cudaSuccess) {
+            p->ir_allocs.push_back(raw);
+            *ptr = static_cast<std::remove_reference_t<decltype(*ptr)>>(raw);
+        }
+    };
+    IrWork w{};
+    w.mode = cfg.precision == MFEM_PRECISION_BF16 ? kIrBf16 : kIrFp16;
+    w.outer_max = cfg.outer_max_iterations;
+    w.inner_tol = cfg.inner_tolerance;
+    w.outer_tol = cfg.outer_tolerance;
+    alloc(&w.lowp, nz * 9 * 2);
+    alloc(&w.row_scale, (size_t)p->n * sizeof(float));
+    alloc(&w.dx64, 2 * n3 * sizeof(double));
+    alloc(&w.dx_out, n3 * sizeof(double));
+    alloc(&w.e, n3 * sizeof(float));
+    alloc(&w.res, n3 * sizeof(float));
+    alloc(&w.z, n3 * sizeof(float));
+    alloc(&w.p0, n3 * sizeof(float));
+    alloc(&w.p1, n3 * sizeof(float));
+    alloc(&w.r, n3 * sizeof(float));
+    alloc(&w.Ap, n3 * sizeof(float));
+    alloc(&w.partials, 2 * 256 * 4 * sizeof(float));
+    alloc(&w.counter, sizeof(unsigned long long));
+    alloc(&w.res_partials, (size_t)2 * ir_residual_blocks(p->n) * sizeof(double));
+    alloc(&w.ticket, sizeof(unsigned));
+    alloc(&w.state, 8 * sizeof(int));
+    alloc(&w.stats, (size_t)p->max_stats * sizeof(IrStats));
+    int max_ctas = 1;
+    if (e == cudaSuccess) e = ir_max_ctas(p->device, &max_ctas);
+    if (e == cudaSuccess) e = cudaMemset(w.counter, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(w.ticket, 0, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(w.state, 0, 8 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(w.stats, 0, (size_t)p->max_stats * sizeof(IrStats));
+    if (e == cudaSuccess) e = cudaMemset(w.e, 0, n3 * sizeof(float));
+    if (e != cudaSuccess) {
+        for (void *a : p->ir_allocs) cudaFree(a);
+        p->ir_allocs.clear();
+        return cuda_fail(p, e, "mixed-precision buffers");
+    }
+    w.ctas = std::max(1, std::min(max_ctas, (p->n + 63) / 64));
+    p->ir = w;
+    return MFEM_OK;
+}
+
+int mfem_step_mixed_stats(mfem_plan *p, mfem_mixed_solve_stats *h_stats, int32_t max_entries, int32_t *count,
+                          mfem_stream stream) {
+    static_assert(sizeof(mfem_mixed_solve_stats) == sizeof(IrStats), "stats layout");
+    if (!p || (max_entries > 0 && !h_stats)) return MFEM_BAD_ARG;
+    if (p->ir.mode == 0) {
+        if (count) *count = 0;
+        return MFEM_OK;
+    }
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(p, e, "cudaStreamSynchronize");
+    const int k = std::max(0, std::min<int>(max_entries, p->cfg.iterations));
+    std::vector<IrStats> tmp(p->max_stats);
+    e = cudaMemcpy(tmp.data(), p->ir.stats, sizeof(IrStats) * p->max_stats, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(p, e, "stats readback");
+    for (int i = 0; i < k; ++i) std::memcpy(&h_stats[i], &tmp[i], sizeof(IrStats));
+    if (count) *count = k;
+    return MFEM_OK;
+}
+
 int mfem_step_line_search_stats(mfem_plan *p, mfem_line_search_stats *h_stats, int32_t max_entries, int32_t *count,
                            mfem_stream stream) {
     static_assert(sizeof(mfem_line_search_stats) == sizeof(LineSearchStats), "stats layout");
@@ -902,8 +1018,7 @@ int mfem_global_solve(mfem_plan *p, int32_t slot, mfem_stream stream) {
     if (!p) return MFEM_BAD_ARG;
     if (slot < 0 || slot >= p->max_stats) return fail(p, MFEM_BAD_ARG, "stats slot out of range");
     DeviceGuard g(p->device);
-    cudaError_t e = launch_pcg(p->bv, p->vv, p->pw, p->pl, p->pcg_ctas, slot, p->cfg.cg_tolerance,
-                               p->cfg.cg_max_iterations, p->cfg.preconditioner, (cudaStream_t)stream);
+    cudaError_t e = global_solve(p, slot, (cudaStream_t)stream);
     p->stage_slot = slot;
     return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "global_solve");
 }

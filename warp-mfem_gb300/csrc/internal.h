@@ -149,6 +149,40 @@ struct ContactViews {
     int tri_code_base;        // assembly codes >= base are tri blocks
 };
 
+// Mixed-precision global solve (pcg_mixed.cu): iterative refinement with an
+// fp64 residual around a PCG on 16-bit blocks with per-row scales.
+constexpr int kIrBf16 = 1;
+constexpr int kIrFp16 = 2;
+
+struct IrStats {               // same layout as mfem_mixed_solve_stats
+    int32_t outer_iterations;
+    int32_t inner_iterations;
+    int32_t status;
+    int32_t reserved;
+    double rel_residual;       // fp64 ||g - H dx|| / ||g||
+};
+
+struct IrWork {
+    int mode;                  // kIrBf16 or kIrFp16
+    int ctas;                  // inner PCG CTAs
+    int outer_max;
+    float inner_tol;
+    double outer_tol;
+    void *lowp;                // [nnzb][9] bf16 / fp16, H / row scale
+    float *row_scale;          // [n]
+    double *dx64;              // [2][n][3] double-buffered solution
+    double *dx_out;            // [n][3] the latest iterate
+    float *e;                  // [n][3] inner correction
+    float *res;                // [n][3] fp32 copy of the fp64 residual (inner rhs)
+    float *z, *p0, *p1, *r, *Ap;  // inner PCG vectors [n][3]
+    float *partials;           // [2][256][4]
+    unsigned long long *counter;  // inner PCG grid barrier, never reset
+    double *res_partials;      // [residual blocks][2]
+    unsigned *ticket;          // last-block detection of the residual kernel
+    int *state;                // done, outer, inner, pending, parity, status
+    IrStats *stats;            // [max solves per step]
+};
+
 // Row partition and shared-memory plan of the persistent PCG.
 struct PcgLayout {
     enum { kAuto = 0, kStandard = 1, kSingleReduction = 2, kGather = 3 };
@@ -206,6 +240,10 @@ cudaError_t pcg_max_ctas(int device, int *ctas);
 cudaError_t pcg_plan_layout(int device, PcgLayout &L, const int32_t *row_ptr, const int32_t *col_idx, int n,
                             int ctas, int variant, std::vector<int4> &cta_info, std::string &err);
 cudaError_t launch_true_residual(const BsrViews &bv, const VertexViews &vv, double *out3, cudaStream_t s);
+cudaError_t ir_max_ctas(int device, int *ctas);
+int ir_residual_blocks(int n);
+cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const IrWork &w, const PcgWork &pw,
+                               int slot, int maxiter, int use_precond, cudaStream_t s);
 
 // Number of kernels launched by the launchers above (process-wide).
 void count_launches(uint64_t k);

@@ -29,7 +29,7 @@ BUF = {
     "h_lambda": 5, "hess_s_inv": 6, "g_lambda": 7, "element_hessian": 8, "element_rhs": 9,
     "row_ptr": 10, "col_idx": 11, "tet_slots": 12, "h_values": 13, "rhs": 14, "precond": 15,
     "x_tilde": 16, "dx": 17, "stretch_direction": 18, "contact_block": 19, "contact_gradient": 20,
-    "contact_energy": 21, "tri_contact": 22, "friction_normal": 23, "friction_force": 24,
+    "contact_energy": 21, "tri_contact": 22, "friction_normal": 23, "friction_force": 24, "mixed_dx": 25,
 }
 
 SHAPE_PLANE = 0
@@ -89,6 +89,30 @@ class MfemContactConfig(ctypes.Structure):
     ]
 
 
+class MfemSolverConfig(ctypes.Structure):
+    _fields_ = [
+        ("precision", ctypes.c_int32),
+        ("inner_tolerance", ctypes.c_float),
+        ("outer_max_iterations", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32),
+        ("outer_tolerance", ctypes.c_double),
+        ("reserved", ctypes.c_int32 * 4),
+    ]
+
+
+class MfemMixedSolveStats(ctypes.Structure):
+    _fields_ = [
+        ("outer_iterations", ctypes.c_int32),
+        ("inner_iterations", ctypes.c_int32),
+        ("status", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("rel_residual", ctypes.c_double),
+    ]
+
+
+PRECISION = {"fp32": 0, "bf16": 1, "fp16": 2}
+
+
 class MfemError(RuntimeError):
     def __init__(self, code: int, message: str):
         super().__init__(f"{message} (status {code})")
@@ -124,6 +148,10 @@ _SIGNATURES = {
     "mfem_plan_set_contact": (ctypes.c_int, [_P, ctypes.POINTER(MfemContactConfig), _I32, _P, _P, _P, _P, _P, _I32,
                                              _I32, _P]),
     "mfem_set_body_poses": (ctypes.c_int, [_P, _P, _I32, _P]),
+    "mfem_solver_config_default": (None, [ctypes.POINTER(MfemSolverConfig)]),
+    "mfem_plan_set_solver": (ctypes.c_int, [_P, ctypes.POINTER(MfemSolverConfig)]),
+    "mfem_step_mixed_stats": (ctypes.c_int, [_P, ctypes.POINTER(MfemMixedSolveStats), _I32, ctypes.POINTER(_I32),
+                                             _P]),
     "mfem_predict": (ctypes.c_int, [_P, _P, _P, _F32, _P]),
     "mfem_update_system": (ctypes.c_int, [_P, _P, _P]),
     "mfem_assemble": (ctypes.c_int, [_P, _P, _F32, _P]),

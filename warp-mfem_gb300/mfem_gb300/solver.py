@@ -39,6 +39,13 @@ class MixedFEMSolver:
     the model has shapes.  Refinement and the membrane shell are outside this
     solver: ``enable_refinement`` defaults to False here and raises if set
     True; ``shell_mu`` must be 0.
+
+    ``solver_precision`` ("fp32", the reference's float32 PCG and the
+    default; "bf16" or "fp16") selects the mixed-precision global solve:
+    16-bit BSR blocks with per-row scales in an inner PCG to
+    ``inner_tolerance`` (1e-3) inside an fp64-residual iterative refinement
+    to ``outer_tolerance`` (1e-8), at most ``outer_max_iterations`` (10)
+    corrections.
     """
 
     def __init__(self, model: Model, iterations: int, max_tets: Optional[int] = None,
@@ -111,6 +118,17 @@ class MixedFEMSolver:
         self.n_contact_tris = 0
         if getattr(model, "shape_count", 0) > 0:
             self._set_contact(model, kwargs)
+        self.solver_precision = kwargs.get("solver_precision", "fp32")
+        if self.solver_precision not in _lib.PRECISION:
+            raise ValueError(f"Unknown solver_precision {self.solver_precision!r}")
+        if self.solver_precision != "fp32":
+            scfg = _lib.MfemSolverConfig()
+            self._lib.mfem_solver_config_default(ctypes.byref(scfg))
+            scfg.precision = _lib.PRECISION[self.solver_precision]
+            scfg.inner_tolerance = float(kwargs.get("inner_tolerance", 1.0e-3))
+            scfg.outer_tolerance = float(kwargs.get("outer_tolerance", 1.0e-8))
+            scfg.outer_max_iterations = int(kwargs.get("outer_max_iterations", 10))
+            _lib.check(self._lib.mfem_plan_set_solver(self._plan, ctypes.byref(scfg)), self._plan)
 
     def _set_contact(self, model, kwargs) -> None:
         """Contact against the model's shapes (Contact.__init__,
@@ -208,6 +226,17 @@ class MixedFEMSolver:
         return [dict(iterations=buf[i].iterations, status=buf[i].status, rel_residual=buf[i].rel_residual)
                 for i in range(count.value)]
 
+    def mixed_stats(self) -> list[dict]:
+        """Mixed-precision solve outcome of each Newton iteration of the last
+        step (synchronises; empty with the fp32 solve)."""
+        buf = (_lib.MfemMixedSolveStats * max(1, self.iterations))()
+        count = ctypes.c_int32()
+        rc = self._lib.mfem_step_mixed_stats(self._plan, buf, max(1, self.iterations), ctypes.byref(count),
+                                             _stream_handle(self.device))
+        _lib.check(rc, self._plan)
+        return [dict(outer_iterations=buf[i].outer_iterations, inner_iterations=buf[i].inner_iterations,
+                     status=buf[i].status, rel_residual=buf[i].rel_residual) for i in range(count.value)]
+
     def line_search_stats(self) -> list[dict]:
         """Line-search outcome of each Newton iteration of the last step
         (synchronises; all zero with the line search off)."""
@@ -249,7 +278,8 @@ class MixedFEMSolver:
         return out.value
 
     # -- buffers ---------------------------------------------------------------
-    _BUF_DTYPE = {"row_ptr": torch.int32, "col_idx": torch.int32, "tet_slots": torch.int32}
+    _BUF_DTYPE = {"row_ptr": torch.int32, "col_idx": torch.int32, "tet_slots": torch.int32,
+                  "mixed_dx": torch.float64}
 
     def contact_tris(self) -> np.ndarray:
         """The per-tri contact record [m, 12] (d, k b, k b', k max(b'', 0),
@@ -262,7 +292,7 @@ class MixedFEMSolver:
         nbytes = ctypes.c_size_t()
         _lib.check(self._lib.mfem_plan_buffer_bytes(self._plan, which, ctypes.byref(nbytes)), self._plan)
         dt = self._BUF_DTYPE.get(name, torch.float32)
-        out = torch.empty(nbytes.value // 4, dtype=dt, device=self.device)
+        out = torch.empty(nbytes.value // (8 if dt == torch.float64 else 4), dtype=dt, device=self.device)
         _lib.check(self._lib.mfem_plan_copy_out(self._plan, which, ctypes.c_void_p(out.data_ptr()), nbytes.value,
                                                 _stream_handle(self.device)), self._plan)
         return out
