@@ -231,8 +231,10 @@ const char *mfem_plan_last_error(const mfem_plan *plan);
 int mfem_plan_sizes(const mfem_plan *plan, int32_t *n_particles, int32_t *n_tets, int64_t *nnzb);
 
 /* The persistent PCG the plan chose: variant (1 standard, 2 single-reduction,
- * 3 gather), CTAs, whether each CTA keeps its slice of H in shared memory,
- * and the dynamic shared memory per CTA.  Diagnostics; no reference
+ * 3 gather; 0 when the mesh is too large for their shared-memory slices and
+ * the global solve runs the global-memory PCG of mfem_plan_set_bodies as a
+ * one-body batch), CTAs, whether each CTA keeps its slice of H in shared
+ * memory, and the dynamic shared memory per CTA.  Diagnostics; no reference
  * counterpart. */
 int mfem_plan_pcg_layout(const mfem_plan *plan, int32_t *variant, int32_t *ctas, int32_t *cache_matrix,
                          int64_t *smem_bytes);
@@ -294,6 +296,35 @@ int mfem_plan_set_solver(mfem_plan *plan, const mfem_solver_config *cfg);
  * residual. */
 int mfem_step_mixed_stats(mfem_plan *plan, mfem_mixed_solve_stats *h_stats, int32_t max_entries,
                           int32_t *count, mfem_stream stream);
+
+/* ---- independent bodies in one plan ------------------------------------ */
+
+/* Declares the plan's mesh to be n_bodies independent bodies: the vertices
+ * of body b are [vertex_offsets[b], vertex_offsets[b+1]), its tets
+ * [tet_offsets[b], tet_offsets[b+1]), and no tet joins two bodies.  Each body
+ * has its own energy (mfem_energy) and gravity [3].  The step then solves one
+ * block-Jacobi PCG per body (own scalars and stopping test, the reference's
+ * solve applied to each body) in a single persistent launch; the other
+ * kernels run on the union.  Needs a plan created with line_search = 0 and
+ * the FP32 solve.  No reference counterpart: the benchmark spec's batch of
+ * uneven bodies.  Synchronises the device and drops captured graphs. */
+int mfem_plan_set_bodies(mfem_plan *plan, int32_t n_bodies, const int32_t *h_vertex_offsets,
+                         const int32_t *h_tet_offsets, const int32_t *h_body_energy,
+                         const float *h_body_gravity);
+
+/* CTAs and threads per CTA of the batched PCG's current schedule. */
+int mfem_plan_batch_layout(const mfem_plan *plan, int32_t *ctas, int32_t *threads);
+
+/* Times the batched PCG on the system at d_q (at rest) for each candidate
+ * schedule (threads per CTA 128/256/512; minimum blocks per CTA before a
+ * body is split over several CTAs 2048/8192/never) and keeps the fastest;
+ * *h_best_ms receives its solve time.  Synchronises the stream. */
+int mfem_plan_autotune_batch(mfem_plan *plan, const float *d_q, float dt, double *h_best_ms, mfem_stream stream);
+
+/* Per-body PCG outcomes of the last step, [iteration][body] (synchronises
+ * the stream; *count = 0 without bodies). */
+int mfem_step_body_stats(mfem_plan *plan, mfem_solve_stats *h_stats, int32_t max_entries, int32_t *count,
+                         mfem_stream stream);
 
 /* ---- the step and its stages ---------------------------------------- */
 

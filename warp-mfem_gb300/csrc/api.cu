@@ -61,6 +61,11 @@ struct mfem_plan {
     // reference's float32 PCG
     IrWork ir{};
     std::vector<void *> ir_allocs;
+    // independent bodies (mfem_plan_set_bodies): per-body PCGs in one launch
+    BatchViews bw{};
+    std::vector<void *> batch_allocs;
+    std::vector<int32_t> h_body_row, h_body_nnzb;
+    bool global_memory_pcg = false;  // the mesh is solved as a one-body batch
     int32_t *tet_slots = nullptr;
     double *resid = nullptr;
     cudaStream_t capture_stream = nullptr;
@@ -181,10 +186,14 @@ bool valid_config(const mfem_config *cfg, std::string &err) {
 // The whole step as a launch sequence on one stream.
 // The reference's float32 PCG, or the mixed-precision iterative refinement.
 cudaError_t global_solve(mfem_plan *p, int slot, cudaStream_t s) {
-    if (p->ir.mode == 0)
-        return launch_pcg(p->bv, p->vv, p->pw, p->pl, p->pcg_ctas, slot, p->cfg.cg_tolerance,
-                          p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
-    return launch_mixed_solve(p->bv, p->vv, p->ir, p->pw, slot, p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
+    if (p->ir.mode != 0)
+        return launch_mixed_solve(p->bv, p->vv, p->ir, p->pw, slot, p->cfg.cg_max_iterations, p->cfg.preconditioner,
+                                  s);
+    if (p->bw.n_bodies > 0)
+        return launch_batched_pcg(p->bv, p->vv, p->bw, p->pw.error, slot, p->cfg.cg_tolerance,
+                                  p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
+    return launch_pcg(p->bv, p->vv, p->pw, p->pl, p->pcg_ctas, slot, p->cfg.cg_tolerance, p->cfg.cg_max_iterations,
+                      p->cfg.preconditioner, s);
 }
 
 // Local solve then either the plain update x += dx, s += ds or the line
@@ -222,6 +231,62 @@ cudaError_t run_step(mfem_plan *p, const float *q_in, const float *qd_in, float 
     return err;
 }
 
+// CTA tasks for the batched PCG: every body gets one CTA; while CTAs are
+// left, the body with the most blocks per CTA gets another, as long as each
+// CTA keeps at least `min_blocks` blocks.  With more bodies than CTAs, bodies
+// are dealt to CTAs largest first onto the least-loaded CTA (each alone).
+void batch_schedule(const std::vector<int32_t> &nnzb, int capacity, int min_blocks, std::vector<int> &task_ptr,
+                    std::vector<int4> &tasks, int &ctas) {
+    const int B = (int)nnzb.size();
+    task_ptr.clear();
+    tasks.clear();
+    if (B <= capacity) {
+        std::vector<int> g(B, 1);
+        int spare = capacity - B;
+        while (spare > 0) {
+            int best = -1;
+            double best_load = 0.0;
+            for (int b = 0; b < B; ++b) {
+                const double load = (double)nnzb[b] / g[b];
+                if ((double)nnzb[b] / (g[b] + 1) >= min_blocks && load > best_load) {
+                    best_load = load;
+                    best = b;
+                }
+            }
+            if (best < 0) break;
+            ++g[best];
+            --spare;
+        }
+        int c = 0;
+        task_ptr.push_back(0);
+        for (int b = 0; b < B; ++b)
+            for (int r = 0; r < g[b]; ++r) {
+                tasks.push_back(make_int4(b, r, g[b], c - r));
+                task_ptr.push_back((int)tasks.size());
+                ++c;
+            }
+        ctas = c;
+        return;
+    }
+    std::vector<int> order(B);
+    for (int b = 0; b < B; ++b) order[b] = b;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nnzb[a] > nnzb[b]; });
+    std::vector<std::vector<int>> bins(capacity);
+    std::vector<double> load(capacity, 0.0);
+    for (int b : order) {
+        const int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        bins[c].push_back(b);
+        load[c] += nnzb[b];
+    }
+    task_ptr.push_back(0);
+    for (int c = 0; c < capacity; ++c) {
+        std::sort(bins[c].begin(), bins[c].end());
+        for (int b : bins[c]) tasks.push_back(make_int4(b, 0, 1, c));
+        task_ptr.push_back((int)tasks.size());
+    }
+    ctas = capacity;
+}
+
 uint64_t count_kernel_nodes(cudaGraph_t g) {
     size_t num = 0;
     if (cudaGraphGetNodes(g, nullptr, &num) != cudaSuccess || num == 0) return 0;
@@ -236,6 +301,9 @@ uint64_t count_kernel_nodes(cudaGraph_t g) {
 }
 
 }  // namespace
+
+int install_bodies(mfem_plan *p, int n_bodies, const int32_t *voff, const int32_t *toff, const int32_t *energy,
+                   const float *gravity);
 
 extern "C" {
 
@@ -305,6 +373,7 @@ void mfem_plan_destroy(mfem_plan *p) {
         for (void *a : p->allocs) cudaFree(a);
         for (void *a : p->contact_allocs) cudaFree(a);
         for (void *a : p->ir_allocs) cudaFree(a);
+        for (void *a : p->batch_allocs) cudaFree(a);
     }
     delete p;
 }
@@ -446,8 +515,18 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
         e = pcg_plan_layout(device, p->pl, sym.row_ptr.data(), sym.col_idx.data(), n, p->pcg_ctas, cfg.pcg_variant,
                             cta_info, lerr);
         if (e != cudaSuccess && !lerr.empty()) {
-            mfem_plan_destroy(p);
-            return fail(nullptr, MFEM_BAD_ARG, lerr);
+            if (cfg.pcg_variant != PcgLayout::kAuto) {
+                mfem_plan_destroy(p);
+                return fail(nullptr, MFEM_BAD_ARG, lerr);
+            }
+            // too large for the shared-memory PCG: the global solve runs the
+            // global-memory PCG of the batched kernel as a one-body batch
+            cudaGetLastError();
+            e = cudaSuccess;
+            p->pl = PcgLayout{};
+            p->pl.variant = 0;
+            p->global_memory_pcg = true;
+            cta_info.assign(1, make_int4(0, 0, 0, 0));
         }
     }
     int4 *d_cta = nullptr;
@@ -520,6 +599,15 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
         int rc = cuda_fail(nullptr, e, "plan initialisation");
         mfem_plan_destroy(p);
         return rc;
+    }
+    if (p->global_memory_pcg) {
+        const int32_t voff[2] = {0, n}, toff[2] = {0, T};
+        const int rc = install_bodies(p, 1, voff, toff, nullptr, nullptr);
+        if (rc != MFEM_OK) {
+            const std::string msg = p->last_error;
+            mfem_plan_destroy(p);
+            return fail(nullptr, rc, msg);
+        }
     }
     *out = p;
     return MFEM_OK;
@@ -888,6 +976,8 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
         return fail(p, MFEM_BAD_ARG, "outer_tolerance must be finite and > 0");
     if (cfg.outer_max_iterations < 1 || cfg.outer_max_iterations > 100)
         return fail(p, MFEM_BAD_ARG, "outer_max_iterations must be in [1, 100]");
+    if (p->bw.n_bodies > 1 && cfg.precision != MFEM_PRECISION_FP32)
+        return fail(p, MFEM_BAD_ARG, "batched bodies use the fp32 PCG");
     DeviceGuard g(p->device);
     cudaError_t e = cudaDeviceSynchronize();  // no step of this plan may still use the old buffers
     if (e != cudaSuccess) return cuda_fail(p, e, "cudaDeviceSynchronize");
@@ -966,6 +1056,268 @@ int mfem_step_mixed_stats(mfem_plan *p, mfem_mixed_solve_stats *h_stats, int32_t
     if (e != cudaSuccess) return cuda_fail(p, e, "stats readback");
     for (int i = 0; i < k; ++i) std::memcpy(&h_stats[i], &tmp[i], sizeof(IrStats));
     if (count) *count = k;
+    return MFEM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Uploads a schedule for `threads` threads per CTA and `min_blocks` blocks
+// per CTA of a multi-CTA body.
+int apply_batch_layout(mfem_plan *p, int threads, int min_blocks) {
+    int capacity = 0;
+    cudaError_t e = batch_capacity(p->device, threads, &capacity);
+    if (e != cudaSuccess) return cuda_fail(p, e, "batch capacity");
+    if (capacity < 1) return fail(p, MFEM_CUDA_ERROR, "the batched PCG does not fit on an SM");
+    std::vector<int> task_ptr;
+    std::vector<int4> tasks;
+    int ctas = 0;
+    batch_schedule(p->h_body_nnzb, capacity, min_blocks, task_ptr, tasks, ctas);
+    int *d_ptr = nullptr;
+    int4 *d_task = nullptr;
+    float *partials = nullptr;
+    e = cudaMalloc(&d_ptr, task_ptr.size() * sizeof(int));
+    if (e == cudaSuccess) p->batch_allocs.push_back(d_ptr);
+    if (e == cudaSuccess) e = cudaMalloc(&d_task, tasks.size() * sizeof(int4));
+    if (e == cudaSuccess) p->batch_allocs.push_back(d_task);
+    if (e == cudaSuccess) e = cudaMalloc(&partials, (size_t)2 * ctas * 4 * sizeof(float));
+    if (e == cudaSuccess) p->batch_allocs.push_back(partials);
+    if (e == cudaSuccess) e = upload(d_ptr, task_ptr.data(), task_ptr.size());
+    if (e == cudaSuccess) e = upload(d_task, tasks.data(), tasks.size());
+    // a group's barrier base is its counter rounded down to the group size,
+    // so the counters restart with every schedule (group sizes change)
+    if (e == cudaSuccess) e = cudaMemset(p->bw.counter, 0, (size_t)p->bw.n_bodies * sizeof(unsigned long long));
+    if (e != cudaSuccess) return cuda_fail(p, e, "batch schedule");
+    p->bw.task_ptr = d_ptr;
+    p->bw.task = d_task;
+    p->bw.partials = partials;
+    p->bw.ctas = ctas;
+    p->bw.threads = threads;
+    return MFEM_OK;
+}
+
+void drop_graphs(mfem_plan *p) {
+    for (auto &ge : p->graphs) {
+        if (ge.exec) cudaGraphExecDestroy(ge.exec);
+        ge = mfem_plan::GraphEntry{};
+    }
+}
+
+}  // namespace
+
+// Installs validated bodies: per-body rows, energies and gravity (null
+// energy / gravity: the plan's, for the one-body batch of a mesh too large for
+// the shared-memory PCG), the per-body work arrays and a first schedule.
+int install_bodies(mfem_plan *p, int n_bodies, const int32_t *voff, const int32_t *toff, const int32_t *energy,
+                   const float *gravity) {
+    std::vector<int32_t> vb, nnzb(n_bodies, 0);
+    std::vector<unsigned char> code;
+    if (gravity) {
+        vb.resize(p->n);
+        for (int b = 0; b < n_bodies; ++b)
+            for (int v = voff[b]; v < voff[b + 1]; ++v) vb[v] = b;
+    }
+    if (energy) {
+        code.resize(p->T);
+        for (int b = 0; b < n_bodies; ++b)
+            for (int t = toff[b]; t < toff[b + 1]; ++t) code[t] = (unsigned char)energy[b];
+    }
+    for (int b = 0; b < n_bodies; ++b) nnzb[b] = p->h_row_ptr[voff[b + 1]] - p->h_row_ptr[voff[b]];
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(p, e, "cudaDeviceSynchronize");
+    drop_graphs(p);
+    for (void *a : p->batch_allocs) cudaFree(a);
+    p->batch_allocs.clear();
+    p->bw = BatchViews{};
+    p->tv.energy_code = nullptr;
+    p->vv.vertex_body = nullptr;
+    p->vv.body_gravity = nullptr;
+    p->h_body_row.assign(voff, voff + n_bodies + 1);
+    p->h_body_nnzb = nnzb;
+    const size_t n3 = (size_t)p->n * 3;
+    auto alloc = [&](auto **ptr, size_t bytes) {
+        if (e != cudaSuccess) return;
+        void *raw = nullptr;
+        e = cudaMalloc(&raw, std::max<size_t>(bytes, 16));
+        if (e == cudaSuccess) {
+            p->batch_allocs.push_back(raw);
+            *ptr = static_cast<std::remove_reference_t<decltype(*ptr)>>(raw);
+        }
+    };
+    int *body_row = nullptr, *vbody = nullptr;
+    unsigned char *ecode = nullptr;
+    float *grav = nullptr;
+    BatchViews &bw = p->bw;
+    alloc(&body_row, (size_t)(n_bodies + 1) * sizeof(int));
+    if (gravity) {
+        alloc(&vbody, (size_t)p->n * sizeof(int));
+        alloc(&grav, (size_t)n_bodies * 3 * sizeof(float));
+    }
+    if (energy) alloc(&ecode, (size_t)p->T);
+    alloc(&bw.counter, (size_t)n_bodies * sizeof(unsigned long long));
+    alloc(&bw.z, n3 * sizeof(float));
+    alloc(&bw.p0, n3 * sizeof(float));
+    alloc(&bw.p1, n3 * sizeof(float));
+    alloc(&bw.r, n3 * sizeof(float));
+    alloc(&bw.Ap, n3 * sizeof(float));
+    alloc(&bw.stats, (size_t)p->max_stats * n_bodies * sizeof(SolveStats));
+    if (e == cudaSuccess) e = upload(body_row, voff, (size_t)n_bodies + 1);
+    if (e == cudaSuccess && gravity) e = upload(vbody, vb.data(), vb.size());
+    if (e == cudaSuccess && gravity) e = upload(grav, gravity, (size_t)n_bodies * 3);
+    if (e == cudaSuccess && energy && p->T > 0) e = upload(ecode, code.data(), code.size());
+    if (e == cudaSuccess) e = cudaMemset(bw.counter, 0, (size_t)n_bodies * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(bw.stats, 0, (size_t)p->max_stats * n_bodies * sizeof(SolveStats));
+    if (e != cudaSuccess) {
+        for (void *a : p->batch_allocs) cudaFree(a);
+        p->batch_allocs.clear();
+        p->bw = BatchViews{};
+        return cuda_fail(p, e, "batch buffers");
+    }
+    bw.n_bodies = n_bodies;
+    bw.body_row = body_row;
+    p->tv.energy_code = ecode;
+    p->vv.vertex_body = vbody;
+    p->vv.body_gravity = grav;
+    const int rc = apply_batch_layout(p, 256, 8192);
+    if (rc != MFEM_OK) {
+        for (void *a : p->batch_allocs) cudaFree(a);
+        p->batch_allocs.clear();
+        p->bw = BatchViews{};
+        p->tv.energy_code = nullptr;
+        p->vv.vertex_body = nullptr;
+        p->vv.body_gravity = nullptr;
+    }
+    return rc;
+}
+
+extern "C" {
+
+int mfem_plan_set_bodies(mfem_plan *p, int32_t n_bodies, const int32_t *h_vertex_offsets,
+                         const int32_t *h_tet_offsets, const int32_t *h_body_energy, const float *h_body_gravity) {
+    if (!p) return MFEM_BAD_ARG;
+    if (n_bodies < 1 || !h_vertex_offsets || !h_tet_offsets || !h_body_energy || !h_body_gravity)
+        return fail(p, MFEM_BAD_ARG, "need n_bodies >= 1 and every array");
+    if (p->cfg.line_search && n_bodies > 1)
+        return fail(p, MFEM_BAD_ARG, "batched bodies run the plain update: create the plan with line_search = 0");
+    if (p->ir.mode != 0) return fail(p, MFEM_BAD_ARG, "batched bodies use the fp32 PCG");
+    if (h_vertex_offsets[0] != 0 || h_vertex_offsets[n_bodies] != p->n || h_tet_offsets[0] != 0 ||
+        h_tet_offsets[n_bodies] != p->T)
+        return fail(p, MFEM_BAD_ARG, "body offsets must start at 0 and end at n / T");
+    for (int b = 0; b < n_bodies; ++b) {
+        if (h_vertex_offsets[b + 1] <= h_vertex_offsets[b] || h_tet_offsets[b + 1] < h_tet_offsets[b])
+            return fail(p, MFEM_BAD_ARG, "body offsets must increase (every body needs a vertex)");
+        if (h_body_energy[b] != MFEM_ENERGY_ARAP && h_body_energy[b] != MFEM_ENERGY_NEOHOOKEAN)
+            return fail(p, MFEM_BAD_ARG, "unknown body energy");
+        for (int i = 0; i < 3; ++i)
+            if (!std::isfinite(h_body_gravity[3 * b + i])) return fail(p, MFEM_BAD_ARG, "non-finite body gravity");
+        for (int t = h_tet_offsets[b]; t < h_tet_offsets[b + 1]; ++t)
+            for (int k = 0; k < 4; ++k) {
+                const int v = p->h_tets[4 * (size_t)t + k];
+                if (v < h_vertex_offsets[b] || v >= h_vertex_offsets[b + 1])
+                    return fail(p, MFEM_BAD_ARG, "tet " + std::to_string(t) + " uses a vertex of another body");
+            }
+    }
+    return install_bodies(p, n_bodies, h_vertex_offsets, h_tet_offsets, h_body_energy, h_body_gravity);
+}
+
+int mfem_plan_batch_layout(const mfem_plan *p, int32_t *ctas, int32_t *threads) {
+    if (!p) return MFEM_BAD_ARG;
+    if (ctas) *ctas = p->bw.ctas;
+    if (threads) *threads = p->bw.threads;
+    return MFEM_OK;
+}
+
+int mfem_plan_autotune_batch(mfem_plan *p, const float *d_q, float dt, double *h_best_ms, mfem_stream stream) {
+    if (!p) return MFEM_BAD_ARG;
+    if (p->bw.n_bodies == 0) return fail(p, MFEM_BAD_ARG, "no bodies: call mfem_plan_set_bodies first");
+    if (!d_q || !(dt > 0.0f)) return fail(p, MFEM_BAD_ARG, "need q and dt > 0");
+    DeviceGuard g(p->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    // one system at q (at rest), solved from the same warm start by every
+    // candidate layout
+    float *x = nullptr, *dx0 = nullptr;
+    const size_t bytes = (size_t)p->n * 3 * sizeof(float);
+    cudaError_t e = cudaMalloc(&x, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&dx0, bytes);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dx0, 0, bytes, s);
+    if (e == cudaSuccess) e = launch_predict(d_q, dx0, x, p->gravity, dt, p->vv, s);
+    if (e == cudaSuccess) e = launch_element(x, p->cfg.energy, p->tv, s);
+    if (e == cudaSuccess) e = contact_and_assemble(p, x, dt, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dx0, p->vv.dx, bytes, cudaMemcpyDeviceToDevice, s);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    const int threads_opts[3] = {128, 256, 512};
+    const int min_blocks_opts[3] = {2048, 8192, 1 << 30};
+    int best_t = 256, best_m = 8192;
+    float best = 1e30f;
+    for (int ti = 0; e == cudaSuccess && ti < 3; ++ti)
+        for (int mi = 0; e == cudaSuccess && mi < 3; ++mi) {
+            const int rc = apply_batch_layout(p, threads_opts[ti], min_blocks_opts[mi]);
+            if (rc != MFEM_OK) {
+                e = cudaErrorUnknown;
+                break;
+            }
+            float ms = 0.0f;
+            int flag = 0;
+            for (int rep = 0; e == cudaSuccess && rep < 2; ++rep) {
+                e = cudaMemcpyAsync(p->vv.dx, dx0, bytes, cudaMemcpyDeviceToDevice, s);
+                if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+                if (e == cudaSuccess) e = global_solve(p, 0, s);
+                if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            }
+            if (e == cudaSuccess) e = cudaMemcpy(&flag, p->pw.error, sizeof(int), cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess && flag) {
+                // a wait gave up: this schedule is not a candidate
+                e = cudaMemset(p->pw.error, 0, sizeof(int));
+                continue;
+            }
+            if (e == cudaSuccess && ms < best) {
+                best = ms;
+                best_t = threads_opts[ti];
+                best_m = min_blocks_opts[mi];
+            }
+        }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (x) cudaFree(x);
+    if (dx0) cudaFree(dx0);
+    if (e != cudaSuccess) return cuda_fail(p, e, "autotune");
+    drop_graphs(p);
+    const int rc = apply_batch_layout(p, best_t, best_m);
+    if (rc == MFEM_OK && h_best_ms) *h_best_ms = best;
+    return rc;
+}
+
+int mfem_step_body_stats(mfem_plan *p, mfem_solve_stats *h_stats, int32_t max_entries, int32_t *count,
+                         mfem_stream stream) {
+    if (!p || (max_entries > 0 && !h_stats)) return MFEM_BAD_ARG;
+    const int B = p->bw.n_bodies;
+    if (B == 0) {
+        if (count) *count = 0;
+        return MFEM_OK;
+    }
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(p, e, "cudaStreamSynchronize");
+    const int k = std::max(0, std::min<int>(max_entries, p->cfg.iterations * B));
+    std::vector<SolveStats> tmp((size_t)p->max_stats * B);
+    e = cudaMemcpy(tmp.data(), p->bw.stats, tmp.size() * sizeof(SolveStats), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(p, e, "stats readback");
+    for (int i = 0; i < k; ++i) std::memcpy(&h_stats[i], &tmp[i], sizeof(mfem_solve_stats));
+    if (count) *count = k;
+    int flag = 0;
+    e = cudaMemcpy(&flag, p->pw.error, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(p, e, "stats readback");
+    if (flag) {
+        for (int b = 0; b < B; ++b) cudaMemsetAsync(p->bw.counter + b, 0, sizeof(unsigned long long));
+        cudaMemset(p->pw.error, 0, sizeof(int));
+        return fail(p, MFEM_TIMEOUT, "a batched PCG barrier timed out");
+    }
     return MFEM_OK;
 }
 

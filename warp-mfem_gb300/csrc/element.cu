@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kElementThreads)
     const float vol = 1.0f / (6.0f * em::det3(Dm));
 
     float g_s[6], H_l[21], H_si[21];
-    em::energy_terms(energy, s, mu, lam, vol, g_s, H_l, H_si);
+    em::energy_terms(tv.energy_code ? (int)tv.energy_code[t] : energy, s, mu, lam, vol, g_s, H_l, H_si);
     float hsg[6];  // H_s^-1 g_s
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
@@ -151,7 +151,14 @@ __global__ void __launch_bounds__(kVertexThreads)
                    float gy, float gz, float dt, VertexViews vv) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= vv.n) return;
-    const float g[3] = {gx, gy, gz};
+    float g[3] = {gx, gy, gz};
+    if (vv.vertex_body) {
+        // batched bodies: each body falls along its own gravity
+        const float *bg = vv.body_gravity + 3 * vv.vertex_body[v];
+        g[0] = bg[0];
+        g[1] = bg[1];
+        g[2] = bg[2];
+    }
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const float q = q_in[3 * v + a];

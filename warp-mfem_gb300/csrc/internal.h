@@ -54,6 +54,7 @@ struct TetViews {
     // element contributions gathered by the assembly, tet-major
     float *Ke;                 // [T][90]
     float *fe;                 // [T][12]
+    const unsigned char *energy_code;  // [T] per-tet energy (batched bodies), or null: the plan's
 };
 
 struct VertexViews {
@@ -67,6 +68,26 @@ struct VertexViews {
     float *rhs;                // [n][3]
     float *dx;                 // [n][3]
     float *Minv;               // [n_pad][9]
+    const int *vertex_body;    // [n] body of each vertex (batched bodies), or null
+    const float *body_gravity; // [bodies][3]
+};
+
+// Independent bodies solved in one persistent launch (pcg_batched.cu): each
+// body's PCG runs on a group of CTAs with its own scalars, barrier and
+// stopping test.  A CTA runs the tasks [task_ptr[c], task_ptr[c+1]) in
+// order; a task is (body, rank in the group, group size, first CTA of the
+// group), and a group of more than one CTA is its CTAs' only task.
+struct BatchViews {
+    int n_bodies;
+    const int *body_row;       // [bodies + 1] vertex (block row) offsets
+    const int *task_ptr;       // [ctas + 1]
+    const int4 *task;          // [tasks]
+    int ctas;
+    int threads;               // threads per CTA
+    float *partials;           // [2][ctas][4]
+    unsigned long long *counter;  // [bodies] group barriers, never reset
+    float *z, *p0, *p1, *r, *Ap;  // [n][3]
+    SolveStats *stats;         // [max solves per step][bodies]
 };
 
 struct BsrViews {
@@ -241,6 +262,9 @@ cudaError_t pcg_plan_layout(int device, PcgLayout &L, const int32_t *row_ptr, co
                             int ctas, int variant, std::vector<int4> &cta_info, std::string &err);
 cudaError_t launch_true_residual(const BsrViews &bv, const VertexViews &vv, double *out3, cudaStream_t s);
 cudaError_t ir_max_ctas(int device, int *ctas);
+cudaError_t batch_capacity(int device, int threads, int *ctas);
+cudaError_t launch_batched_pcg(const BsrViews &bv, const VertexViews &vv, const BatchViews &bw, int *error, int slot,
+                               float tol, int maxiter, int use_precond, cudaStream_t s);
 int ir_residual_blocks(int n);
 cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const IrWork &w, const PcgWork &pw,
                                int slot, int maxiter, int use_precond, cudaStream_t s);

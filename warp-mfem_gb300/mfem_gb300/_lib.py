@@ -152,6 +152,10 @@ _SIGNATURES = {
     "mfem_plan_set_solver": (ctypes.c_int, [_P, ctypes.POINTER(MfemSolverConfig)]),
     "mfem_step_mixed_stats": (ctypes.c_int, [_P, ctypes.POINTER(MfemMixedSolveStats), _I32, ctypes.POINTER(_I32),
                                              _P]),
+    "mfem_plan_set_bodies": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P]),
+    "mfem_plan_batch_layout": (ctypes.c_int, [_P, ctypes.POINTER(_I32), ctypes.POINTER(_I32)]),
+    "mfem_plan_autotune_batch": (ctypes.c_int, [_P, _P, _F32, ctypes.POINTER(ctypes.c_double), _P]),
+    "mfem_step_body_stats": (ctypes.c_int, [_P, ctypes.POINTER(MfemSolveStats), _I32, ctypes.POINTER(_I32), _P]),
     "mfem_predict": (ctypes.c_int, [_P, _P, _P, _F32, _P]),
     "mfem_update_system": (ctypes.c_int, [_P, _P, _P]),
     "mfem_assemble": (ctypes.c_int, [_P, _P, _F32, _P]),

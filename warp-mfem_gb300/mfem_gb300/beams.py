@@ -199,3 +199,64 @@ def build_beam(spec: BeamSpec | str, cells: Optional[tuple[int, int, int]] = Non
         particle_inv_mass=inv_mass.astype(f32),
         gravity=np.asarray(spec.gravity, dtype=f32),
     )
+
+
+@dataclasses.dataclass
+class BodyBatch:
+    """Independent bodies concatenated into one mesh (vertices and tets of
+    body b contiguous), plus each body's own mesh for per-body checks."""
+
+    bodies: list                # [BeamMesh] per body
+    union: BeamMesh             # the concatenated mesh (tets renumbered)
+    vertex_offsets: np.ndarray  # [B+1] int32
+    tet_offsets: np.ndarray     # [B+1] int32
+    energies: list              # per body "arap" | "neohookean"
+    gravity: np.ndarray         # [B, 3] f32
+    dt: float = 1.0 / 60.0
+    iterations: int = 8
+
+    @property
+    def n_bodies(self) -> int:
+        return len(self.bodies)
+
+
+def concatenate(bodies: list) -> BodyBatch:
+    """The union of independent meshes: vertex and tet arrays stacked, tet
+    indices offset by each body's first vertex."""
+    voff = np.zeros(len(bodies) + 1, dtype=np.int64)
+    toff = np.zeros(len(bodies) + 1, dtype=np.int64)
+    for b, m in enumerate(bodies):
+        voff[b + 1] = voff[b] + m.n
+        toff[b + 1] = toff[b] + m.T
+    cat = lambda key: np.concatenate([getattr(m, key) for m in bodies])
+    tets = np.concatenate([m.tet_indices.astype(np.int64) + voff[b] for b, m in enumerate(bodies)])
+    first = bodies[0]
+    union = BeamMesh(spec=first.spec, rest_q=cat("rest_q"), q0=cat("q0"), qd0=cat("qd0"),
+                     tet_indices=tets.astype(np.int32), tet_poses=cat("tet_poses"),
+                     tet_materials=cat("tet_materials"), particle_mass=cat("particle_mass"),
+                     particle_inv_mass=cat("particle_inv_mass"), gravity=first.gravity)
+    return BodyBatch(bodies=bodies, union=union, vertex_offsets=voff.astype(np.int32),
+                     tet_offsets=toff.astype(np.int32), energies=[m.spec.energy for m in bodies],
+                     gravity=np.stack([m.gravity for m in bodies]).astype(np.float32), dt=first.spec.dt,
+                     iterations=first.spec.iterations)
+
+
+def batched_bodies(n_bodies: int = 512, seed: int = 4, cell: float = 0.05, nx=(4, 48), nyz=(2, 12),
+                   E=(1.0e4, 1.0e6), nu=(0.3, 0.48)) -> BodyBatch:
+    """The batch of uneven beams: per body nx ~ U{4..48}, ny, nz ~ U{2..12}
+    hex cells of `cell` m (6 tets each), ARAP or Neo-Hookean with p = 0.5,
+    per-tet E log-uniform in E, nu ~ U(nu), gravity 9.81 m/s^2 along a
+    direction uniform on the sphere, the x = 0 face pinned, at rest."""
+    rng = np.random.default_rng(seed)
+    bodies = []
+    for b in range(n_bodies):
+        cells = (int(rng.integers(nx[0], nx[1] + 1)), int(rng.integers(nyz[0], nyz[1] + 1)),
+                 int(rng.integers(nyz[0], nyz[1] + 1)))
+        energy = "arap" if rng.random() < 0.5 else "neohookean"
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        spec = BeamSpec(name=f"body{b}", cells=cells, extent=tuple(c * cell for c in cells), energy=energy,
+                        E=E, nu=float(rng.uniform(nu[0], nu[1])), gravity=tuple(9.81 * d),
+                        steps=10, seed=int(rng.integers(0, 2 ** 31 - 1)))
+        bodies.append(build_beam(spec))
+    return concatenate(bodies)

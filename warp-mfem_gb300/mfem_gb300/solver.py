@@ -180,7 +180,7 @@ class MixedFEMSolver:
         smem = ctypes.c_int64()
         _lib.check(self._lib.mfem_plan_pcg_layout(self._plan, ctypes.byref(v), ctypes.byref(c), ctypes.byref(m),
                                                   ctypes.byref(smem)), self._plan)
-        name = {1: "standard", 2: "single_reduction", 3: "gather"}[v.value]
+        name = {0: "global_memory", 1: "standard", 2: "single_reduction", 3: "gather"}[v.value]
         return dict(variant=name, ctas=c.value, cache_matrix=bool(m.value), smem_bytes=smem.value)
 
     # ------------------------------------------------------------------
