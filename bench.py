@@ -13,6 +13,9 @@ step; the timed run is the workload's 50 steps from its initial state.
   roofline  the persistent PCG kernel (the dominant kernel), from an eager
          stage-by-stage pass timed with CUDA events on the launch stream.
 
+--workload batched512 steps the batch of 512 uneven beams (per-body PCGs in
+one persistent launch): value = batch steps/s (every body advanced one step).
+
 --impl reference times the CPU oracle (the restatement of the reference's
 step, float32) on the host instead.  With --gpus N under torchrun every rank
 runs an independent replica (the step does not shard across GPUs).
@@ -208,6 +211,8 @@ def run_reference(args, rank, world):
     from mfem_gb300 import beams
     if rank != 0:
         return 0
+    if args.workload.startswith("batched"):
+        return run_reference_batched(args)
     mesh = beams.build_beam(args.workload)
     budget = max(10.0, min(150.0, args.cpu_budget_s * max(1, args.steps) / 10.0))
     rate, steps, el = cpu_oracle_rate(mesh, budget)
@@ -219,6 +224,216 @@ def run_reference(args, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(mesh, {"reference": "CPU oracle port (the reference's Warp path cannot run: "
                                                       "warp-lang / newton absent, Python >= 3.13 required)"}),
+        "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# batch of independent bodies
+# ---------------------------------------------------------------------------
+def batched_count(workload: str) -> int:
+    return int(workload[len("batched"):] or 512)
+
+
+def run_batched(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    from mfem_gb300 import beams, _lib
+    from mfem_gb300.batched import BatchedSolver
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    B = batched_count(args.workload)
+    batch = beams.batched_bodies(B, seed=4)
+    u = batch.union
+    bs = BatchedSolver(batch, device=dev)
+    tune_ms = bs.autotune()
+    layout = bs.layout()
+    s_init = bs.solver.tet_stretch.clone().reshape(-1)
+    lam0 = torch.zeros_like(s_init)
+    q0 = torch.as_tensor(u.q0, device=dev)
+    A, Bst = bs.model.state(), bs.model.state()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def reset():
+        A.particle_q.copy_(q0)
+        A.particle_qd.zero_()
+        bs.solver.write_buffer("tet_stretch", s_init)
+        bs.solver.write_buffer("tet_lambda", lam0)
+
+    reset()
+    for _ in range(args.warmup):
+        bs.step(A, Bst)
+        A, Bst = Bst, A
+    torch.cuda.synchronize(dev)
+    reset()
+    sampler = ClockSampler(local_rank)
+    torch.cuda.synchronize(dev)
+    sampler.start()
+    launches0 = _lib.kernel_launch_count()
+    total_ms = 0.0
+    its = []
+    statuses = set()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        bs.step(A, Bst)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        st = bs.body_stats()
+        its.append(st["iterations"])
+        statuses.update(int(x) for x in np.unique(st["status"]))
+        A, Bst = Bst, A
+    launches = _lib.kernel_launch_count() - launches0
+    torch.cuda.synchronize(dev)
+    clocks = sampler.stop()
+    t_max = max_over_ranks(total_ms / 1000.0, world, dev)
+    value = job_rate(args.steps, world, t_max)
+    q_final = A.particle_q.cpu().numpy()
+
+    # e2e: host-resident union state through the public API
+    reset()
+    hq = torch.empty((u.n, 3), dtype=torch.float32, pin_memory=True)
+    hqd = torch.empty_like(hq, pin_memory=True)
+    hq.copy_(q0.cpu())
+    hqd.zero_()
+    e2e_ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        A.particle_q.copy_(hq, non_blocking=True)
+        A.particle_qd.copy_(hqd, non_blocking=True)
+        bs.step(A, Bst)
+        hq.copy_(Bst.particle_q, non_blocking=True)
+        hqd.copy_(Bst.particle_qd, non_blocking=True)
+        e1.record(stream)
+        e1.synchronize()
+        e2e_ms += e0.elapsed_time(e1)
+    e2e_s = max_over_ranks(e2e_ms / 1000.0, world, dev)
+    e2e_value = job_rate(args.steps, world, e2e_s)
+    state_bytes = 2 * u.n * 3 * 4
+
+    # roofline of the batched PCG: eager stages of a few steps
+    reset()
+    solver = bs.solver
+    pcg_ms = 0.0
+    solves = 0
+    bytes_pcg = 0.0
+    row_ptr = solver.read_buffer("row_ptr").cpu().numpy()
+    voff = batch.vertex_offsets
+    nnzb_b = (row_ptr[voff[1:]] - row_ptr[voff[:-1]]).astype(np.float64)
+    n_b = np.diff(voff).astype(np.float64)
+    per_it_b = 40.0 * nnzb_b + 172.0 * n_b
+    x = Bst.particle_q
+    prof_steps = max(1, min(3, args.steps))
+    for _ in range(prof_steps):
+        flush.zero_()
+        solver.predict(A.particle_q, A.particle_qd, batch.dt)
+        x.copy_(A.particle_q)
+        for it in range(solver.iterations):
+            solver.update_system(x)
+            solver.assemble(x, batch.dt)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            solver.global_solve(it)
+            e1.record(stream)
+            solver.local_solve(x)
+            e1.synchronize()
+            pcg_ms += e0.elapsed_time(e1)
+            solves += 1
+        st = bs.body_stats()
+        bytes_pcg += float(((st["iterations"].astype(np.float64) + 1.0) * per_it_b[None, :]).sum())
+        Bst.particle_qd.copy_((x - A.particle_q) / batch.dt)
+        A, Bst = Bst, A
+        x = Bst.particle_q
+    achieved = bytes_pcg / (pcg_ms / 1000.0) / 1e9
+    peak, peak_src = hbm_peak()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "batched_pcg_kernel (per-body block-Jacobi PCGs, one launch)",
+                "algorithmic_bytes_per_launch": bytes_pcg / solves,
+                "bytes_per_body_iteration": "40 nnzb_b + 172 n_b, summed over bodies x (iterations_b + 1)",
+                "avg_launch_ms": pcg_ms / solves, "peak_source": peak_src}
+
+    if rank != 0:
+        return 0
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        # the float32 oracle stepping bodies one after another, within budget
+        from oracle import mfem_oracle
+        t0 = time.perf_counter()
+        done = 0
+        for m in batch.bodies:
+            ref = mfem_oracle.OracleSolver(m, dtype=np.float32)
+            ref.step(m.q0, m.qd0, m.spec.dt)
+            done += 1
+            if time.perf_counter() - t0 > args.cpu_budget_s:
+                break
+        el = time.perf_counter() - t0
+        cpu = {"value": done / el / B, "unit": "steps/s", "cores": 1, "kind": "port",
+               "sample": f"one step of the first {done} of {B} bodies by the float32 oracle in {el:.1f} s "
+                         "(batch steps/s = body steps/s / bodies)"}
+    it_all = np.stack(its)
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": (f"{B} uneven beams in one plan (seed 4): per body nx~U{{4..48}}, ny,nz~U{{2..12}} "
+                                f"hex cells of 0.05 m x 6 tets, ARAP or Neo-Hookean (p 0.5), E log-uniform [1e4, 1e6] "
+                                f"Pa, nu~U[0.3, 0.48], gravity on the unit sphere, x = 0 face pinned; "
+                                f"{u.T} tets, {u.n} vertices; 8 local/global iterations, per-body block-Jacobi "
+                                f"fp32 PCG to 1e-6"),
+                   "bodies": B, "tets": u.T, "vertices": u.n, "pcg_schedule": layout,
+                   "autotune_best_solve_ms": tune_ms, "parallelism": "replicas",
+                   "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write, outside the timed events)"},
+        "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
+                "d2h_bytes_per_step": state_bytes, "matches_resident_run": bool(np.array_equal(hq.numpy(), q_final))},
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "body_steps_per_s": B * value,
+        "pcg_iterations_per_body_step": {"mean": float(it_all.sum(1).mean()), "max": int(it_all.sum(1).max())},
+        "pcg_status_codes": sorted(statuses),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_reference_batched(args):
+    """The float32 oracle steps the bodies one after another (a bounded
+    sample); batch steps/s = body steps/s / bodies."""
+    import numpy as np
+    from mfem_gb300 import beams
+    from oracle import mfem_oracle
+    B = batched_count(args.workload)
+    batch = beams.batched_bodies(B, seed=4)
+    budget = max(10.0, min(150.0, args.cpu_budget_s * max(1, args.steps) / 10.0))
+    t0 = time.perf_counter()
+    done = 0
+    for m in batch.bodies:
+        mfem_oracle.OracleSolver(m, dtype=np.float32).step(m.q0, m.qd0, m.spec.dt)
+        done += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    rate = done / el / B
+    sample = f"one step of the first {done} of {B} bodies by the float32 oracle in {el:.1f} s"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": args.gpus,
+        "steps": 1, "warmup": 0, "ms_per_step": 1000.0 / rate, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{B} uneven beams (seed 4)", "bodies": B,
+                   "reference": "CPU oracle port (the reference's Warp path cannot run here)"},
         "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": 1, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -440,6 +655,8 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     try:
+        if args.workload.startswith("batched"):
+            return run_batched(args, rank, world, local_rank)
         return run_gb300(args, rank, world, local_rank)
     finally:
         if world > 1:

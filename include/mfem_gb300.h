@@ -315,10 +315,12 @@ int mfem_plan_set_bodies(mfem_plan *plan, int32_t n_bodies, const int32_t *h_ver
 /* CTAs and threads per CTA of the batched PCG's current schedule. */
 int mfem_plan_batch_layout(const mfem_plan *plan, int32_t *ctas, int32_t *threads);
 
-/* Times the batched PCG on the system at d_q (at rest) for each candidate
- * schedule (threads per CTA 128/256/512; minimum blocks per CTA before a
- * body is split over several CTAs 2048/8192/never) and keeps the fastest;
- * *h_best_ms receives its solve time.  Synchronises the stream. */
+/* Solves the system at d_q (at rest) once to learn each body's PCG
+ * iterations, then times the batched PCG for each candidate schedule
+ * (threads per CTA 128/256/512 x three costs of a group barrier; bodies get
+ * CTA groups while that shortens the longest modelled body time, iterations x
+ * blocks per CTA) and keeps the fastest; *h_best_ms receives its solve time.
+ * Synchronises the stream. */
 int mfem_plan_autotune_batch(mfem_plan *plan, const float *d_q, float dt, double *h_best_ms, mfem_stream stream);
 
 /* Per-body PCG outcomes of the last step, [iteration][body] (synchronises

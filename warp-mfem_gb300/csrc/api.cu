@@ -64,7 +64,7 @@ struct mfem_plan {
     // independent bodies (mfem_plan_set_bodies): per-body PCGs in one launch
     BatchViews bw{};
     std::vector<void *> batch_allocs;
-    std::vector<int32_t> h_body_row, h_body_nnzb;
+    std::vector<int32_t> h_body_row, h_body_nnzb, h_body_its;
     bool global_memory_pcg = false;  // the mesh is solved as a one-body batch
     int32_t *tet_slots = nullptr;
     double *resid = nullptr;
@@ -231,31 +231,37 @@ cudaError_t run_step(mfem_plan *p, const float *q_in, const float *qd_in, float 
     return err;
 }
 
-// CTA tasks for the batched PCG: every body gets one CTA; while CTAs are
-// left, the body with the most blocks per CTA gets another, as long as each
-// CTA keeps at least `min_blocks` blocks.  With more bodies than CTAs, bodies
-// are dealt to CTAs largest first onto the least-loaded CTA (each alone).
-void batch_schedule(const std::vector<int32_t> &nnzb, int capacity, int min_blocks, std::vector<int> &task_ptr,
-                    std::vector<int4> &tasks, int &ctas) {
+// CTA tasks for the batched PCG.  The time of body b on g CTAs is modelled
+// as its_b * (nnzb_b / g + c0 [g > 1]) (block products per iteration, plus
+// the cost of a group barrier pair in the same unit); starting from one CTA
+// per body, the body with the largest modelled time gets one more CTA while
+// CTAs are left and that shortens it.  With more bodies than CTAs, bodies are
+// dealt to CTAs largest first onto the least-loaded CTA (each alone).
+void batch_schedule(const std::vector<int32_t> &nnzb, const std::vector<int32_t> &its, int capacity, double c0,
+                    std::vector<int> &task_ptr, std::vector<int4> &tasks, int &ctas) {
     const int B = (int)nnzb.size();
     task_ptr.clear();
     tasks.clear();
+    auto work = [&](int b) { return (double)std::max(its[b], 1) * (double)nnzb[b]; };
     if (B <= capacity) {
         std::vector<int> g(B, 1);
+        auto model = [&](int b, int gb) {
+            return (double)std::max(its[b], 1) * ((double)nnzb[b] / gb + (gb > 1 ? c0 : 0.0));
+        };
+        std::vector<std::pair<double, int>> heap;
+        for (int b = 0; b < B; ++b) heap.push_back({model(b, 1), b});
+        std::make_heap(heap.begin(), heap.end());
         int spare = capacity - B;
-        while (spare > 0) {
-            int best = -1;
-            double best_load = 0.0;
-            for (int b = 0; b < B; ++b) {
-                const double load = (double)nnzb[b] / g[b];
-                if ((double)nnzb[b] / (g[b] + 1) >= min_blocks && load > best_load) {
-                    best_load = load;
-                    best = b;
-                }
-            }
-            if (best < 0) break;
-            ++g[best];
+        while (spare > 0 && !heap.empty()) {
+            std::pop_heap(heap.begin(), heap.end());
+            auto [t, b] = heap.back();
+            heap.pop_back();
+            const double t1 = model(b, g[b] + 1);
+            if (!(t1 < t)) break;  // the critical body gains nothing from another CTA
+            ++g[b];
             --spare;
+            heap.push_back({t1, b});
+            std::push_heap(heap.begin(), heap.end());
         }
         int c = 0;
         task_ptr.push_back(0);
@@ -270,13 +276,13 @@ void batch_schedule(const std::vector<int32_t> &nnzb, int capacity, int min_bloc
     }
     std::vector<int> order(B);
     for (int b = 0; b < B; ++b) order[b] = b;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nnzb[a] > nnzb[b]; });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work(a) > work(b); });
     std::vector<std::vector<int>> bins(capacity);
     std::vector<double> load(capacity, 0.0);
     for (int b : order) {
         const int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
         bins[c].push_back(b);
-        load[c] += nnzb[b];
+        load[c] += work(b);
     }
     task_ptr.push_back(0);
     for (int c = 0; c < capacity; ++c) {
@@ -1063,9 +1069,10 @@ int mfem_step_mixed_stats(mfem_plan *p, mfem_mixed_solve_stats *h_stats, int32_t
 
 namespace {
 
-// Uploads a schedule for `threads` threads per CTA and `min_blocks` blocks
-// per CTA of a multi-CTA body.
-int apply_batch_layout(mfem_plan *p, int threads, int min_blocks) {
+// Uploads a schedule for `threads` threads per CTA and a group-barrier cost
+// of `c0` block products (batch_schedule), with the plan's iteration
+// estimates per body.
+int apply_batch_layout(mfem_plan *p, int threads, double c0) {
     int capacity = 0;
     cudaError_t e = batch_capacity(p->device, threads, &capacity);
     if (e != cudaSuccess) return cuda_fail(p, e, "batch capacity");
@@ -1073,7 +1080,8 @@ int apply_batch_layout(mfem_plan *p, int threads, int min_blocks) {
     std::vector<int> task_ptr;
     std::vector<int4> tasks;
     int ctas = 0;
-    batch_schedule(p->h_body_nnzb, capacity, min_blocks, task_ptr, tasks, ctas);
+    if (p->h_body_its.size() != p->h_body_nnzb.size()) p->h_body_its.assign(p->h_body_nnzb.size(), 1);
+    batch_schedule(p->h_body_nnzb, p->h_body_its, capacity, c0, task_ptr, tasks, ctas);
     int *d_ptr = nullptr;
     int4 *d_task = nullptr;
     float *partials = nullptr;
@@ -1136,6 +1144,7 @@ int install_bodies(mfem_plan *p, int n_bodies, const int32_t *voff, const int32_
     p->vv.body_gravity = nullptr;
     p->h_body_row.assign(voff, voff + n_bodies + 1);
     p->h_body_nnzb = nnzb;
+    p->h_body_its.assign(n_bodies, 1);
     const size_t n3 = (size_t)p->n * 3;
     auto alloc = [&](auto **ptr, size_t bytes) {
         if (e != cudaSuccess) return;
@@ -1180,7 +1189,7 @@ int install_bodies(mfem_plan *p, int n_bodies, const int32_t *voff, const int32_
     p->tv.energy_code = ecode;
     p->vv.vertex_body = vbody;
     p->vv.body_gravity = grav;
-    const int rc = apply_batch_layout(p, 256, 8192);
+    const int rc = apply_batch_layout(p, 256, 2048.0);
     if (rc != MFEM_OK) {
         for (void *a : p->batch_allocs) cudaFree(a);
         p->batch_allocs.clear();
@@ -1249,13 +1258,25 @@ int mfem_plan_autotune_batch(mfem_plan *p, const float *d_q, float dt, double *h
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    // per-body iteration counts of this system weight the schedules
+    if (e == cudaSuccess) e = global_solve(p, 0, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) {
+        std::vector<SolveStats> st(p->bw.n_bodies);
+        e = cudaMemcpy(st.data(), p->bw.stats, st.size() * sizeof(SolveStats), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) {
+            p->h_body_its.resize(st.size());
+            for (size_t b = 0; b < st.size(); ++b) p->h_body_its[b] = std::max(1, st[b].iterations + 1);
+        }
+    }
     const int threads_opts[3] = {128, 256, 512};
-    const int min_blocks_opts[3] = {2048, 8192, 1 << 30};
-    int best_t = 256, best_m = 8192;
+    const double c0_opts[3] = {512.0, 2048.0, 8192.0};
+    int best_t = 256;
+    double best_m = 2048.0;
     float best = 1e30f;
     for (int ti = 0; e == cudaSuccess && ti < 3; ++ti)
         for (int mi = 0; e == cudaSuccess && mi < 3; ++mi) {
-            const int rc = apply_batch_layout(p, threads_opts[ti], min_blocks_opts[mi]);
+            const int rc = apply_batch_layout(p, threads_opts[ti], c0_opts[mi]);
             if (rc != MFEM_OK) {
                 e = cudaErrorUnknown;
                 break;
@@ -1279,7 +1300,7 @@ int mfem_plan_autotune_batch(mfem_plan *p, const float *d_q, float dt, double *h
             if (e == cudaSuccess && ms < best) {
                 best = ms;
                 best_t = threads_opts[ti];
-                best_m = min_blocks_opts[mi];
+                best_m = c0_opts[mi];
             }
         }
     if (e0) cudaEventDestroy(e0);

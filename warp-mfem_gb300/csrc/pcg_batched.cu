@@ -125,7 +125,16 @@ __device__ __forceinline__ void bt_precond(const float *Minv, int use, int row, 
     z[2] = m[6] * r[0] + m[7] * r[1] + m[8] * r[2];
 }
 
+// Loads of vectors other threads wrote during this launch: from L2 when a
+// group of CTAs shares them, through L1 when one CTA owns the whole body
+// (its own stores, ordered by __syncthreads).
+template <bool SHARED>
+__device__ __forceinline__ float bt_ld(const float *p) {
+    return SHARED ? __ldcg(p) : *p;
+}
+
 // y = sum_k H[k] (z[col] + beta p_old[col]) for one row, kBtGroup lanes.
+template <bool SHARED>
 __device__ __forceinline__ void bt_row_product(const BsrViews &bv, int row, const float *z, const float *p_old,
                                                float beta, float y[3]) {
     const int g_lane = threadIdx.x & (kBtGroup - 1);
@@ -137,8 +146,8 @@ __device__ __forceinline__ void bt_row_product(const BsrViews &bv, int row, cons
         float v[3];
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            const float zc = __ldcg(z + 3 * c + q);
-            v[q] = p_old ? __fmaf_rn(beta, __ldcg(p_old + 3 * c + q), zc) : zc;
+            const float zc = bt_ld<SHARED>(z + 3 * c + q);
+            v[q] = p_old ? __fmaf_rn(beta, bt_ld<SHARED>(p_old + 3 * c + q), zc) : zc;
         }
         const float *h = bv.values + (size_t)9 * k;
         a0 += __ldg(h + 0) * v[0] + __ldg(h + 1) * v[1] + __ldg(h + 2) * v[2];
@@ -193,7 +202,8 @@ __global__ void __launch_bounds__(kBtMaxThreads)
         // r = g - H x0 (x0: the warm start x~ - x), z = M r
         for (int row = lo + group; row < hi; row += ngroups) {
             float y[3];
-            bt_row_product(bv, row, vv.dx, nullptr, 0.0f, y);
+            if (tk.size > 1) bt_row_product<true>(bv, row, vv.dx, nullptr, 0.0f, y);
+            else bt_row_product<false>(bv, row, vv.dx, nullptr, 0.0f, y);
             if (g_lead)
 #pragma unroll
                 for (int q = 0; q < 3; ++q) bw.r[3 * row + q] = vv.rhs[3 * row + q] - y[q];
@@ -244,12 +254,13 @@ __global__ void __launch_bounds__(kBtMaxThreads)
             float pap[1] = {0.0f};
             for (int row = lo + group; row < hi; row += ngroups) {
                 float y[3];
-                bt_row_product(bv, row, bw.z, p_old, beta, y);
+                if (tk.size > 1) bt_row_product<true>(bv, row, bw.z, p_old, beta, y);
+                else bt_row_product<false>(bv, row, bw.z, p_old, beta, y);
                 if (g_lead) {
 #pragma unroll
                     for (int q = 0; q < 3; ++q) {
-                        const float zq = __ldcg(bw.z + 3 * row + q);
-                        const float pq = p_old ? __fmaf_rn(beta, __ldcg(p_old + 3 * row + q), zq) : zq;
+                        const float zq = bw.z[3 * row + q];
+                        const float pq = p_old ? __fmaf_rn(beta, p_old[3 * row + q], zq) : zq;
                         p_new[3 * row + q] = pq;
                         bw.Ap[3 * row + q] = y[q];
                         pap[0] = __fmaf_rn(pq, y[q], pap[0]);
