@@ -56,6 +56,8 @@ def parse_args():
                     help="global solve: fp32 PCG (the workload's) or mixed-precision iterative refinement")
     ap.add_argument("--outer-tolerance", type=float, default=1.0e-6,
                     help="fp64 relative residual of the mixed-precision solve")
+    ap.add_argument("--line-search", action="store_true",
+                    help="run the workload with the reference's backtracking line search")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget-s", type=float, default=30.0, help="CPU time budget of the oracle leg")
     return ap.parse_args()
@@ -458,7 +460,8 @@ def run_gb300(args, rank, world, local_rank):
     solver = MixedFEMSolver(model, iterations=spec.iterations, energy=spec.energy,
                             cg_tolerance=spec.cg_tolerance, cg_max_iterations=spec.cg_max_iterations,
                             pcg_ctas=args.pcg_ctas, pcg_variant=args.pcg_variant,
-                            line_search=False,  # the workload is the plain local/global step
+                            # the workload is the plain local/global step unless asked
+                            line_search=args.line_search,
                             solver_precision=args.precision, outer_tolerance=args.outer_tolerance)
     s_init = solver.tet_stretch.clone().reshape(-1)
     lam0 = torch.zeros_like(s_init)
@@ -623,7 +626,8 @@ def run_gb300(args, rank, world, local_rank):
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(mesh, precision=args.precision, outer_tolerance=args.outer_tolerance),
+        "config": workload_config(mesh, {"line_search": bool(args.line_search)}, precision=args.precision,
+                                  outer_tolerance=args.outer_tolerance),
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes, "matches_resident_run": e2e_match},
         "gpu_launches": int(launches),
