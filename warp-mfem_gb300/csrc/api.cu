@@ -64,6 +64,7 @@ struct mfem_plan {
     // independent bodies (mfem_plan_set_bodies): per-body PCGs in one launch
     BatchViews bw{};
     std::vector<void *> batch_allocs;
+    std::vector<void *> layout_allocs;  // the current schedule's task arrays and partials
     std::vector<int32_t> h_body_row, h_body_nnzb, h_body_its;
     bool global_memory_pcg = false;  // the mesh is solved as a one-body batch
     int32_t *tet_slots = nullptr;
@@ -380,6 +381,7 @@ void mfem_plan_destroy(mfem_plan *p) {
         for (void *a : p->contact_allocs) cudaFree(a);
         for (void *a : p->ir_allocs) cudaFree(a);
         for (void *a : p->batch_allocs) cudaFree(a);
+        for (void *a : p->layout_allocs) cudaFree(a);
     }
     delete p;
 }
@@ -1082,15 +1084,19 @@ int apply_batch_layout(mfem_plan *p, int threads, double c0) {
     int ctas = 0;
     if (p->h_body_its.size() != p->h_body_nnzb.size()) p->h_body_its.assign(p->h_body_nnzb.size(), 1);
     batch_schedule(p->h_body_nnzb, p->h_body_its, capacity, c0, task_ptr, tasks, ctas);
+    // the previous schedule's arrays: every caller has synchronised the
+    // device, so no launch still reads them
+    for (void *a : p->layout_allocs) cudaFree(a);
+    p->layout_allocs.clear();
     int *d_ptr = nullptr;
     int4 *d_task = nullptr;
     float *partials = nullptr;
     e = cudaMalloc(&d_ptr, task_ptr.size() * sizeof(int));
-    if (e == cudaSuccess) p->batch_allocs.push_back(d_ptr);
+    if (e == cudaSuccess) p->layout_allocs.push_back(d_ptr);
     if (e == cudaSuccess) e = cudaMalloc(&d_task, tasks.size() * sizeof(int4));
-    if (e == cudaSuccess) p->batch_allocs.push_back(d_task);
+    if (e == cudaSuccess) p->layout_allocs.push_back(d_task);
     if (e == cudaSuccess) e = cudaMalloc(&partials, (size_t)2 * ctas * 4 * sizeof(float));
-    if (e == cudaSuccess) p->batch_allocs.push_back(partials);
+    if (e == cudaSuccess) p->layout_allocs.push_back(partials);
     if (e == cudaSuccess) e = upload(d_ptr, task_ptr.data(), task_ptr.size());
     if (e == cudaSuccess) e = upload(d_task, tasks.data(), tasks.size());
     // a group's barrier base is its counter rounded down to the group size,
@@ -1244,6 +1250,9 @@ int mfem_plan_autotune_batch(mfem_plan *p, const float *d_q, float dt, double *h
     if (!d_q || !(dt > 0.0f)) return fail(p, MFEM_BAD_ARG, "need q and dt > 0");
     DeviceGuard g(p->device);
     cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t es = cudaStreamSynchronize(s);
+    if (es != cudaSuccess) return cuda_fail(p, es, "cudaStreamSynchronize");
+    drop_graphs(p);  // captured steps point at the schedule arrays replaced below
     // one system at q (at rest), solved from the same warm start by every
     // candidate layout
     float *x = nullptr, *dx0 = nullptr;
