@@ -56,6 +56,8 @@ def parse_args():
                     help="global solve: fp32 PCG (the workload's) or mixed-precision iterative refinement")
     ap.add_argument("--outer-tolerance", type=float, default=1.0e-6,
                     help="fp64 relative residual of the mixed-precision solve")
+    ap.add_argument("--preconditioner", default="block_jacobi", choices=["block_jacobi", "fsai"],
+                    help="PCG preconditioner: the workload's block-Jacobi, or FSAI (global-memory PCG)")
     ap.add_argument("--line-search", action="store_true",
                     help="run the workload with the reference's backtracking line search")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -251,7 +253,8 @@ def run_batched(args, rank, world, local_rank):
     B = batched_count(args.workload)
     batch = beams.batched_bodies(B, seed=4)
     u = batch.union
-    bs = BatchedSolver(batch, device=dev)
+    fsai = args.preconditioner == "fsai"
+    bs = BatchedSolver(batch, device=dev, preconditioner=args.preconditioner)
     tune_ms = bs.autotune()
     layout = bs.layout()
     s_init = bs.solver.tet_stretch.clone().reshape(-1)
@@ -334,7 +337,9 @@ def run_batched(args, rank, world, local_rank):
     voff = batch.vertex_offsets
     nnzb_b = (row_ptr[voff[1:]] - row_ptr[voff[:-1]]).astype(np.float64)
     n_b = np.diff(voff).astype(np.float64)
-    per_it_b = 40.0 * nnzb_b + 172.0 * n_b
+    # FSAI replaces the 36 n bytes of block-Jacobi blocks by two passes over
+    # G's lower blocks (G, col_idx, transposed slots, y and z)
+    per_it_b = (86.0 * nnzb_b + 222.0 * n_b) if fsai else (40.0 * nnzb_b + 172.0 * n_b)
     x = Bst.particle_q
     prof_steps = max(1, min(3, args.steps))
     for _ in range(prof_steps):
@@ -361,9 +366,12 @@ def run_batched(args, rank, world, local_rank):
     achieved = bytes_pcg / (pcg_ms / 1000.0) / 1e9
     peak, peak_src = hbm_peak()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "batched_pcg_kernel (per-body block-Jacobi PCGs, one launch)",
+                "traffic": None,
+                "kernel": ("batched_pcg_kernel (per-body " + ("FSAI" if fsai else "block-Jacobi") +
+                           " PCGs, one launch)"),
                 "algorithmic_bytes_per_launch": bytes_pcg / solves,
-                "bytes_per_body_iteration": "40 nnzb_b + 172 n_b, summed over bodies x (iterations_b + 1)",
+                "bytes_per_body_iteration": (("86 nnzb_b + 222 n_b" if fsai else "40 nnzb_b + 172 n_b") +
+                                             ", summed over bodies x (iterations_b + 1)"),
                 "avg_launch_ms": pcg_ms / solves, "peak_source": peak_src}
 
     if rank != 0:
@@ -392,8 +400,8 @@ def run_batched(args, rank, world, local_rank):
         "config": {"workload": (f"{B} uneven beams in one plan (seed 4): per body nx~U{{4..48}}, ny,nz~U{{2..12}} "
                                 f"hex cells of 0.05 m x 6 tets, ARAP or Neo-Hookean (p 0.5), E log-uniform [1e4, 1e6] "
                                 f"Pa, nu~U[0.3, 0.48], gravity on the unit sphere, x = 0 face pinned; "
-                                f"{u.T} tets, {u.n} vertices; 8 local/global iterations, per-body block-Jacobi "
-                                f"fp32 PCG to 1e-6"),
+                                f"{u.T} tets, {u.n} vertices; 8 local/global iterations, per-body "
+                                f"{'FSAI' if fsai else 'block-Jacobi'} fp32 PCG to 1e-6"),
                    "bodies": B, "tets": u.T, "vertices": u.n, "pcg_schedule": layout,
                    "autotune_best_solve_ms": tune_ms, "parallelism": "replicas",
                    "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write, outside the timed events)"},
@@ -461,7 +469,7 @@ def run_gb300(args, rank, world, local_rank):
                             cg_tolerance=spec.cg_tolerance, cg_max_iterations=spec.cg_max_iterations,
                             pcg_ctas=args.pcg_ctas, pcg_variant=args.pcg_variant,
                             # the workload is the plain local/global step unless asked
-                            line_search=args.line_search,
+                            line_search=args.line_search, preconditioner=args.preconditioner,
                             solver_precision=args.precision, outer_tolerance=args.outer_tolerance)
     s_init = solver.tet_stretch.clone().reshape(-1)
     lam0 = torch.zeros_like(s_init)
@@ -606,9 +614,10 @@ def run_gb300(args, rank, world, local_rank):
         "bytes_per_pcg_iteration": b_it, "pcg_iterations_per_launch": per_launch_iters - 1,
         "avg_launch_ms": stage_ms["pcg"] / stage_launches["pcg"], "peak_source": peak_src,
     }
-    if args.precision != "fp32":
-        # the persistent fp32 PCG does not run: the mixed-precision solves are
-        # reported as a whole (stage_ms_per_step["pcg"])
+    if args.precision != "fp32" or args.preconditioner != "block_jacobi":
+        # the persistent fp32 PCG does not run: the mixed-precision or
+        # global-memory FSAI solves are reported as a whole
+        # (stage_ms_per_step["pcg"])
         roofline = None
     total_stage = sum(stage_ms.values())
     shares = {k: v / total_stage for k, v in stage_ms.items()}
@@ -626,7 +635,8 @@ def run_gb300(args, rank, world, local_rank):
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(mesh, {"line_search": bool(args.line_search)}, precision=args.precision,
+        "config": workload_config(mesh, {"line_search": bool(args.line_search),
+                                         "preconditioner": args.preconditioner}, precision=args.precision,
                                   outer_tolerance=args.outer_tolerance),
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes, "matches_resident_run": e2e_match},

@@ -57,7 +57,9 @@ typedef struct mfem_config {
     float cg_tolerance;                   /* relative, ||r|| <= tol ||b|| (solver.py:91)         */
     float attachment_stiffness;           /* penalty on inv_mass==0 vertices (solver.py:106)     */
     float preconditioner_singular_threshold; /* |det| below -> identity block (solver.py:93)     */
-    int32_t preconditioner;               /* 1 block-Jacobi, 0 none (solver.py:128)              */
+    int32_t preconditioner;               /* 1 block-Jacobi, 0 none (solver.py:128), 2 FSAI:
+                                             M = G^T G, G lower block-triangular on H's pattern
+                                             (runs the global-memory PCG)                      */
     int32_t use_cuda_graph;               /* capture mfem_step once per argument set and replay  */
     int32_t pcg_ctas;                     /* persistent PCG CTAs; 0 = one per SM                 */
     int32_t pcg_variant;                  /* 0 auto, 1 standard (two reductions per iteration),
@@ -105,7 +107,10 @@ typedef enum mfem_buffer {
     MFEM_BUF_FRICTION_FORCE = 24,  /* f32 [n]    lagged normal force of the step                 */
     MFEM_BUF_MIXED_DX = 25,        /* f64 [n][3] solution of the last mixed-precision solve
                                       (empty with the FP32 solve)                              */
-    MFEM_BUF_COUNT = 26
+    MFEM_BUF_PRECOND_FACTOR = 26,  /* f32 [nnzl][3][3] factor F of preconditioner 2 on H's lower
+                                      block pattern: per row the blocks of columns <= row,
+                                      ascending (empty unless preconditioner >= 2)             */
+    MFEM_BUF_COUNT = 27
 } mfem_buffer;
 
 /* Rigid shapes that contact takes into account (Newton's GeoType PLANE and

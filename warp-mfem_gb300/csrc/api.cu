@@ -160,6 +160,7 @@ bool buffer_ref(const mfem_plan *p, int which, BufferRef &ref) {
         case MFEM_BUF_FRICTION_NORMAL: ref = {p->cv.normal_lagged, p->cv.on ? n * 3 * 4 : 0}; return true;
         case MFEM_BUF_FRICTION_FORCE: ref = {p->cv.force_lagged, p->cv.on ? n * 4 : 0}; return true;
         case MFEM_BUF_MIXED_DX: ref = {p->ir.dx_out, p->ir.mode ? n * 3 * 8 : 0}; return true;
+        case MFEM_BUF_PRECOND_FACTOR: ref = {(void *)p->bw.Lval, (size_t)p->bw.nnzl * 9 * 4}; return true;
         default: return false;
     }
 }
@@ -172,6 +173,10 @@ bool valid_config(const mfem_config *cfg, std::string &err) {
     else if (!std::isfinite(cfg->attachment_stiffness) || cfg->attachment_stiffness < 0.0f)
         err = "attachment_stiffness must be finite and >= 0";
     else if (!(cfg->preconditioner_singular_threshold >= 0.0f)) err = "preconditioner_singular_threshold must be >= 0";
+    else if (cfg->preconditioner < 0 || cfg->preconditioner > 2)
+        err = "preconditioner must be 0 (none), 1 (block-Jacobi) or 2 (FSAI)";
+    else if (cfg->preconditioner == 2 && cfg->pcg_variant != 0)
+        err = "the FSAI preconditioner runs the global-memory PCG: pcg_variant must be 0";
     else if (cfg->pcg_ctas < 0) err = "pcg_ctas must be >= 0";
     else if (cfg->pcg_variant < 0 || cfg->pcg_variant > 3) err = "pcg_variant must be 0 (auto), 1, 2 or 3";
     else if (cfg->line_search != 0 && cfg->line_search != 1) err = "line_search must be 0 or 1";
@@ -214,6 +219,8 @@ cudaError_t contact_and_assemble(mfem_plan *p, const float *x, float dt, cudaStr
     if (err == cudaSuccess)
         err = launch_assemble(x, dt, p->cfg.preconditioner_singular_threshold, p->cfg.preconditioner, p->tv, p->vv,
                               p->bv, p->cv, s);
+    if (err == cudaSuccess && p->cfg.preconditioner == 2) err = launch_fsai_setup(p->bv, p->bw, s);
+    if (err == cudaSuccess && p->cfg.preconditioner == 2) err = launch_factor_transpose(p->bw, s);
     return err;
 }
 
@@ -518,7 +525,13 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
         p->ls.c = cfg.line_search_c;
         p->ls.threshold = cfg.line_search_threshold;
     }
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess && cfg.preconditioner == 2) {
+        // FSAI is applied by the global-memory PCG only
+        p->pl = PcgLayout{};
+        p->pl.variant = 0;
+        p->global_memory_pcg = true;
+        cta_info.assign(1, make_int4(0, 0, 0, 0));
+    } else if (e == cudaSuccess) {
         std::string lerr;
         e = pcg_plan_layout(device, p->pl, sym.row_ptr.data(), sym.col_idx.data(), n, p->pcg_ctas, cfg.pcg_variant,
                             cta_info, lerr);
@@ -986,6 +999,8 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
         return fail(p, MFEM_BAD_ARG, "outer_max_iterations must be in [1, 100]");
     if (p->bw.n_bodies > 1 && cfg.precision != MFEM_PRECISION_FP32)
         return fail(p, MFEM_BAD_ARG, "batched bodies use the fp32 PCG");
+    if (p->cfg.preconditioner == 2 && cfg.precision != MFEM_PRECISION_FP32)
+        return fail(p, MFEM_BAD_ARG, "the FSAI preconditioner runs with the fp32 PCG");
     DeviceGuard g(p->device);
     cudaError_t e = cudaDeviceSynchronize();  // no step of this plan may still use the old buffers
     if (e != cudaSuccess) return cuda_fail(p, e, "cudaDeviceSynchronize");
@@ -1178,6 +1193,53 @@ int install_bodies(mfem_plan *p, int n_bodies, const int32_t *voff, const int32_
     alloc(&bw.r, n3 * sizeof(float));
     alloc(&bw.Ap, n3 * sizeof(float));
     alloc(&bw.stats, (size_t)p->max_stats * n_bodies * sizeof(SolveStats));
+    if (p->cfg.preconditioner >= 2) {
+        // factor preconditioner: H's lower block pattern (columns <= row) and
+        // its transpose as two CSRs; the pattern of tets is symmetric, so
+        // the upper CSR's row i lists the rows j >= i whose lower part holds
+        // column i, in ascending order
+        const int n = p->n;
+        std::vector<int32_t> lrow(n + 1, 0), lcol, urow(n + 1, 0), ucol, umap;
+        for (int r = 0; r < n; ++r) {
+            for (int k = p->h_row_ptr[r]; k < p->h_row_ptr[r + 1]; ++k)
+                if (p->h_col_idx[k] <= r) lcol.push_back(p->h_col_idx[k]);
+            lrow[r + 1] = (int32_t)lcol.size();
+        }
+        const size_t nnzl = lcol.size();
+        for (size_t l = 0; l < nnzl; ++l) ++urow[lcol[l] + 1];
+        for (int r = 0; r < n; ++r) urow[r + 1] += urow[r];
+        ucol.assign(nnzl, 0);
+        umap.assign(nnzl, 0);
+        std::vector<int32_t> fill(urow.begin(), urow.end() - 1);
+        for (int r = 0; r < n; ++r)  // rows ascending: each upper row fills in column order
+            for (int l = lrow[r]; l < lrow[r + 1]; ++l) {
+                const int u = fill[lcol[l]]++;
+                ucol[u] = r;
+                umap[u] = l;
+            }
+        int *d_lrow = nullptr, *d_lcol = nullptr, *d_urow = nullptr, *d_ucol = nullptr, *d_umap = nullptr;
+        alloc(&d_lrow, (size_t)(n + 1) * sizeof(int));
+        alloc(&d_urow, (size_t)(n + 1) * sizeof(int));
+        alloc(&d_lcol, nnzl * sizeof(int));
+        alloc(&d_ucol, nnzl * sizeof(int));
+        alloc(&d_umap, nnzl * sizeof(int));
+        alloc(&bw.Lval, nnzl * 9 * sizeof(float));
+        alloc(&bw.Uval, nnzl * 9 * sizeof(float));
+        alloc(&bw.y, n3 * sizeof(float));
+        if (e == cudaSuccess) e = upload(d_lrow, lrow.data(), lrow.size());
+        if (e == cudaSuccess) e = upload(d_urow, urow.data(), urow.size());
+        if (e == cudaSuccess) e = upload(d_lcol, lcol.data(), nnzl);
+        if (e == cudaSuccess) e = upload(d_ucol, ucol.data(), nnzl);
+        if (e == cudaSuccess) e = upload(d_umap, umap.data(), nnzl);
+        if (e == cudaSuccess) e = cudaMemset(bw.Lval, 0, nnzl * 9 * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemset(bw.Uval, 0, nnzl * 9 * sizeof(float));
+        bw.lrow = d_lrow;
+        bw.lcol = d_lcol;
+        bw.urow = d_urow;
+        bw.ucol = d_ucol;
+        bw.umap = d_umap;
+        bw.nnzl = (int)nnzl;
+    }
     if (e == cudaSuccess) e = upload(body_row, voff, (size_t)n_bodies + 1);
     if (e == cudaSuccess && gravity) e = upload(vbody, vb.data(), vb.size());
     if (e == cudaSuccess && gravity) e = upload(grav, gravity, (size_t)n_bodies * 3);

@@ -1,6 +1,7 @@
 // Internal definitions shared by the translation units of libmfem_gb300.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -88,7 +89,53 @@ struct BatchViews {
     unsigned long long *counter;  // [bodies] group barriers, never reset
     float *z, *p0, *p1, *r, *Ap;  // [n][3]
     SolveStats *stats;         // [max solves per step][bodies]
+    // Factor preconditioners on H's lower block pattern (columns <= row,
+    // ascending, the diagonal last): use_precond 2 applies M = F^T F (FSAI),
+    // 3 applies M = F F^T (learned).  F's blocks sit in the lower CSR; the
+    // upper CSR (columns >= row) holds the transposed blocks, (F^T)_ij =
+    // F_ji^T, so both passes are row-wise gathers.
+    const int *lrow, *lcol;    // [n + 1], [nnzl]
+    const int *urow, *ucol;    // [n + 1], [nnzl]
+    const int *umap;           // [nnzl] upper entry -> lower entry of the transposed block
+    float *Lval;               // [nnzl][9] F, row-major blocks
+    float *Uval;               // [nnzl][9] F^T in upper-CSR order
+    float *y;                  // [n][3] the first pass's output
+    int nnzl;
 };
+
+// The learned factor net (preconditioner 3): weights in device layout and
+// its per-vertex work arrays.  BF16 weight matrices are stored [out][in]
+// with the row padded by 8 elements (conflict-free fragment loads).
+constexpr int kNetWidth = 64;
+constexpr int kNetIn = 16;
+constexpr int kMpLd = 2 * kNetWidth + 8;  // message-passing layers: K = 128
+constexpr int kNodeLd = kNetWidth + 8;    // node and edge output layers: K = 64
+constexpr int kRLd = 16 + 8;              // edge-feature layer: K = 9, padded to 16
+constexpr int kNodeOut = 2 * kNetWidth + 8;  // P (64), Q (64), diagonal (6) + 2 zero rows
+struct FactorNetViews {
+    const float *w_in, *b_in;          // [64][16] (BF16-rounded values), [64]
+    const __nv_bfloat16 *w_mp[3];      // [64][kMpLd]
+    const float *b_mp[3];              // [64]
+    const __nv_bfloat16 *w_node;       // [kNodeOut][kNodeLd]
+    const float *b_node;               // [kNodeOut]
+    const __nv_bfloat16 *w_r;          // [64][kRLd]
+    const __nv_bfloat16 *w_o;          // [16][kNodeLd], rows 9..15 zero
+    const float *b_o;                  // [16]
+    const float *vstatic;              // [n][4] static vertex features
+    float *s, *ld;                     // [n] d^-1/2, log10 d
+    float *w;                          // [nnzb] aggregation weights (0 on the diagonal)
+    float *winv;                       // [n] 1 / sum of the row's weights
+    float *h;                          // [n][64]
+    __nv_bfloat16 *hb[2];              // [n][64] BF16 copies of h (ping-pong between layers)
+    __nv_bfloat16 *pb, *qb;            // [n][64] P h + b_p, Q h
+    const int *lslot;                  // [nnzl] H slot of each lower block
+    const int *erow, *elow;            // [n_edges] row and lower entry of each off-diagonal lower block
+    int n_edges;
+    int ready;                         // weights and static features are set
+};
+
+constexpr int kFsaiMaxCols = 16;  // lower block columns a row may have for FSAI
+constexpr int kFsaiDim = 3 * kFsaiMaxCols;
 
 struct BsrViews {
     int n;
@@ -262,6 +309,9 @@ cudaError_t pcg_plan_layout(int device, PcgLayout &L, const int32_t *row_ptr, co
                             int ctas, int variant, std::vector<int4> &cta_info, std::string &err);
 cudaError_t launch_true_residual(const BsrViews &bv, const VertexViews &vv, double *out3, cudaStream_t s);
 cudaError_t ir_max_ctas(int device, int *ctas);
+cudaError_t launch_fsai_setup(const BsrViews &bv, const BatchViews &bw, cudaStream_t s);
+cudaError_t launch_factor_transpose(const BatchViews &bw, cudaStream_t s);
+cudaError_t launch_factor_net(const BsrViews &bv, const BatchViews &bw, const FactorNetViews &fv, cudaStream_t s);
 cudaError_t batch_capacity(int device, int threads, int *ctas);
 cudaError_t launch_batched_pcg(const BsrViews &bv, const VertexViews &vv, const BatchViews &bw, int *error, int slot,
                                float tol, int maxiter, int use_precond, cudaStream_t s);

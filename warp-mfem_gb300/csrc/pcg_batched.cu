@@ -165,6 +165,72 @@ __device__ __forceinline__ void bt_row_product(const BsrViews &bv, int row, cons
     y[2] = a2;
 }
 
+// out = F in over this CTA's rows for one factor form (row pointers, columns,
+// row-major 3x3 blocks), kBtGroup lanes per row.
+template <bool SHARED>
+__device__ __forceinline__ void bt_factor_pass(const int *rp, const int *col, const float *val, const float *in,
+                                               float *out, int lo, int hi) {
+    const int g_lane = threadIdx.x & (kBtGroup - 1);
+    const unsigned gmask = ((1u << kBtGroup) - 1u) << (threadIdx.x & (32 - kBtGroup));
+    const int group = threadIdx.x / kBtGroup, ngroups = blockDim.x / kBtGroup;
+    for (int row = lo + group; row < hi; row += ngroups) {
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+        for (int k = __ldg(rp + row) + g_lane; k < __ldg(rp + row + 1); k += kBtGroup) {
+            const int c = __ldg(col + k);
+            const float v0 = bt_ld<SHARED>(in + 3 * c), v1 = bt_ld<SHARED>(in + 3 * c + 1),
+                        v2 = bt_ld<SHARED>(in + 3 * c + 2);
+            const float *f = val + (size_t)9 * k;
+            a0 += __ldg(f + 0) * v0 + __ldg(f + 1) * v1 + __ldg(f + 2) * v2;
+            a1 += __ldg(f + 3) * v0 + __ldg(f + 4) * v1 + __ldg(f + 5) * v2;
+            a2 += __ldg(f + 6) * v0 + __ldg(f + 7) * v1 + __ldg(f + 8) * v2;
+        }
+#pragma unroll
+        for (int off = kBtGroup / 2; off > 0; off >>= 1) {
+            a0 += __shfl_xor_sync(gmask, a0, off);
+            a1 += __shfl_xor_sync(gmask, a1, off);
+            a2 += __shfl_xor_sync(gmask, a2, off);
+        }
+        if (g_lane == 0) {
+            out[3 * row] = a0;
+            out[3 * row + 1] = a1;
+            out[3 * row + 2] = a2;
+        }
+    }
+}
+
+// The barrier of the body between factor passes and before reading vectors
+// other CTAs of the group wrote: __syncthreads for a one-CTA body, the
+// group's counter barrier otherwise.
+__device__ __forceinline__ bool bt_sync(const BatchViews &bw, const Task &tk, int *error, unsigned &k,
+                                        unsigned long long &target, float *s_tot, float (*s_redf)[32], int *s_ok) {
+    if (tk.size == 1) {
+        __syncthreads();
+        return true;
+    }
+    float d[1] = {0.0f};
+    return bt_reduce<1>(d, bw, tk, error, k++, target, s_tot, s_redf, s_ok);
+}
+
+// z = M r for the CTA's rows with a factor preconditioner: M = F^T F
+// (mode 2: y = F r, z = F^T y) or M = F F^T (mode 3: y = F^T r, z = F y).
+// r of every row of the body is in place on entry (after a barrier); z of
+// the CTA's own rows on return.
+__device__ __forceinline__ bool bt_apply_factor(const BatchViews &bw, int mode, const Task &tk, int lo, int hi,
+                                                int *error, unsigned &k, unsigned long long &target, float *s_tot,
+                                                float (*s_redf)[32], int *s_ok) {
+    const bool lower_first = mode == 2;
+    const int *rp0 = lower_first ? bw.lrow : bw.urow, *c0 = lower_first ? bw.lcol : bw.ucol;
+    const int *rp1 = lower_first ? bw.urow : bw.lrow, *c1 = lower_first ? bw.ucol : bw.lcol;
+    const float *v0 = lower_first ? bw.Lval : bw.Uval, *v1 = lower_first ? bw.Uval : bw.Lval;
+    if (tk.size > 1) bt_factor_pass<true>(rp0, c0, v0, bw.r, bw.y, lo, hi);
+    else bt_factor_pass<false>(rp0, c0, v0, bw.r, bw.y, lo, hi);
+    if (!bt_sync(bw, tk, error, k, target, s_tot, s_redf, s_ok)) return false;
+    if (tk.size > 1) bt_factor_pass<true>(rp1, c1, v1, bw.y, bw.z, lo, hi);
+    else bt_factor_pass<false>(rp1, c1, v1, bw.y, bw.z, lo, hi);
+    __syncthreads();
+    return true;
+}
+
 struct BtScalars {
     float alpha, beta, rz, rr, bb, thr2;
     int status, done;
@@ -209,12 +275,25 @@ __global__ void __launch_bounds__(kBtMaxThreads)
                 for (int q = 0; q < 3; ++q) bw.r[3 * row + q] = vv.rhs[3 * row + q] - y[q];
         }
         __syncthreads();
+        const bool factor = use_precond >= 2;  // a factor preconditioner
+        // every row's r must be in place before G r gathers it
+        if (factor && !(bt_sync(bw, tk, error, k, target, s_tot, s_redf, &s_ok) &&
+                      bt_apply_factor(bw, use_precond, tk, lo, hi, error, k, target, s_tot, s_redf, &s_ok))) {
+            if (tk.rank == 0 && threadIdx.x == 0) *st = SolveStats{0, MFEM_TIMEOUT, 0.0f, 0.0f};
+            __syncthreads();
+            continue;
+        }
         float acc3[3] = {0.0f, 0.0f, 0.0f};
         for (int row = lo + threadIdx.x; row < hi; row += blockDim.x) {
             float r[3], z[3];
 #pragma unroll
             for (int q = 0; q < 3; ++q) r[q] = bw.r[3 * row + q];
-            bt_precond(vv.Minv, use_precond, row, r, z);
+            if (factor) {
+#pragma unroll
+                for (int q = 0; q < 3; ++q) z[q] = bw.z[3 * row + q];
+            } else {
+                bt_precond(vv.Minv, use_precond, row, r, z);
+            }
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
                 bw.z[3 * row + q] = z[q];
@@ -286,15 +365,36 @@ __global__ void __launch_bounds__(kBtMaxThreads)
             if (sc.done) break;
             const float alpha = sc.alpha;
             float acc2[2] = {0.0f, 0.0f};
+            if (factor) {
+                for (int row = lo + threadIdx.x; row < hi; row += blockDim.x)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        vv.dx[3 * row + q] = __fmaf_rn(alpha, p_new[3 * row + q], vv.dx[3 * row + q]);
+                        bw.r[3 * row + q] = __fmaf_rn(-alpha, bw.Ap[3 * row + q], bw.r[3 * row + q]);
+                    }
+                if (!(bt_sync(bw, tk, error, k, target, s_tot, s_redf, &s_ok) &&
+                      bt_apply_factor(bw, use_precond, tk, lo, hi, error, k, target, s_tot, s_redf, &s_ok))) {
+                    if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+                    break;
+                }
+            }
             for (int row = lo + threadIdx.x; row < hi; row += blockDim.x) {
                 float r[3], z[3];
+                if (factor) {
 #pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    vv.dx[3 * row + q] = __fmaf_rn(alpha, p_new[3 * row + q], vv.dx[3 * row + q]);
-                    r[q] = __fmaf_rn(-alpha, bw.Ap[3 * row + q], bw.r[3 * row + q]);
-                    bw.r[3 * row + q] = r[q];
+                    for (int q = 0; q < 3; ++q) {
+                        r[q] = bw.r[3 * row + q];
+                        z[q] = bw.z[3 * row + q];
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        vv.dx[3 * row + q] = __fmaf_rn(alpha, p_new[3 * row + q], vv.dx[3 * row + q]);
+                        r[q] = __fmaf_rn(-alpha, bw.Ap[3 * row + q], bw.r[3 * row + q]);
+                        bw.r[3 * row + q] = r[q];
+                    }
+                    bt_precond(vv.Minv, use_precond, row, r, z);
                 }
-                bt_precond(vv.Minv, use_precond, row, r, z);
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
                     bw.z[3 * row + q] = z[q];

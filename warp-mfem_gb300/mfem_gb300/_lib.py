@@ -30,6 +30,7 @@ BUF = {
     "row_ptr": 10, "col_idx": 11, "tet_slots": 12, "h_values": 13, "rhs": 14, "precond": 15,
     "x_tilde": 16, "dx": 17, "stretch_direction": 18, "contact_block": 19, "contact_gradient": 20,
     "contact_energy": 21, "tri_contact": 22, "friction_normal": 23, "friction_force": 24, "mixed_dx": 25,
+    "precond_factor": 26,
 }
 
 SHAPE_PLANE = 0

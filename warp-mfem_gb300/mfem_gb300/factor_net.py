@@ -1,0 +1,344 @@
+"""The learned factor preconditioner: a message-passing net on the vertex
+graph that writes a lower block-triangular L on H's lower block pattern;
+the PCG applies M = L L^T (preconditioner="learned").
+
+The net (width 64, BF16 weights, FP32 accumulation):
+
+* Per-vertex scale d_i = tr(H_ii) / 3 and s_i = d_i^-1/2; every quantity the
+  net sees is of the scaled system S H S (S = diag(s)), and L = S L~ with L~
+  the net's output, so that M = S L~ L~^T S.
+* Inputs x_i (16, zero padded): the scaled diagonal block (its diagonal
+  minus 1 and its three off-diagonal entries), log10 d_i minus the mean of
+  log10 d over the neighbours, the incident-tet mean of log10 E minus 5, the
+  rest position minus the body's centroid, and the block count of row i / 15.
+* h = relu(W_in x + b_in); three layers h += relu(W_l [h, a] + b_l), with
+  a_i = sum_j w_ij h_j / sum_j w_ij over the off-diagonal blocks of row i,
+  w_ij = ||(S H S)_ij||_F.
+* Diagonal block: o = W_d h_i + b_d, L~_ii = [[sp(o0), 0, 0], [o3, sp(o1), 0],
+  [o4, o5, sp(o2)]] with sp = softplus (a positive diagonal: L is
+  nonsingular, so M is symmetric positive definite whatever L's rounding).
+* Off-diagonal block (i, j), j < i: z = relu(P h_i + b_p + Q h_j + R e_ij),
+  e_ij = (S H S)_ij as 9 values; L~_ij = W_o z + b_o (row-major 3x3).
+
+The device computes the GEMMs from BF16 operands: h, a, P h, Q h, e and z
+are rounded to BF16 where they enter a tensor-core product, which
+``reference_factor`` reproduces.
+
+Training (``train``) minimises ||r - K M r||^2 / ||r||^2 over (K, r) pairs of
+the scaled systems that this library's solver assembles along trajectories
+with random initial velocities N(0, 0.1 m/s) and random gravity directions;
+r is the scaled right-hand side or a random normal vector.
+"""
+from __future__ import annotations
+
+import math
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+import torch
+import torch.nn as nn
+
+WIDTH = 64
+N_IN = 16
+WEIGHTS_FILE = Path(__file__).with_name("factor_net_weights.npz")
+
+# packed parameter order of mfem_plan_set_factor_net
+LAYOUT = [
+    ("inp.weight", (WIDTH, N_IN)), ("inp.bias", (WIDTH,)),
+    ("mp.0.weight", (WIDTH, 2 * WIDTH)), ("mp.0.bias", (WIDTH,)),
+    ("mp.1.weight", (WIDTH, 2 * WIDTH)), ("mp.1.bias", (WIDTH,)),
+    ("mp.2.weight", (WIDTH, 2 * WIDTH)), ("mp.2.bias", (WIDTH,)),
+    ("diag.weight", (6, WIDTH)), ("diag.bias", (6,)),
+    ("P.weight", (WIDTH, WIDTH)), ("P.bias", (WIDTH,)),
+    ("Q.weight", (WIDTH, WIDTH)),
+    ("R.weight", (WIDTH, 9)),
+    ("out.weight", (9, WIDTH)), ("out.bias", (9,)),
+]
+N_PARAMS = sum(int(np.prod(s)) for _, s in LAYOUT)
+
+
+class FactorNet(nn.Module):
+    def __init__(self):
+        super().__init__()
+        W = WIDTH
+        self.inp = nn.Linear(N_IN, W)
+        self.mp = nn.ModuleList([nn.Linear(2 * W, W) for _ in range(3)])
+        self.diag = nn.Linear(W, 6)
+        self.P = nn.Linear(W, W)
+        self.Q = nn.Linear(W, W, bias=False)
+        self.R = nn.Linear(9, W, bias=False)
+        self.out = nn.Linear(W, 9)
+        # start from block-Jacobi-like factors: L~ = I, no off-diagonal blocks
+        nn.init.zeros_(self.out.weight)
+        nn.init.zeros_(self.out.bias)
+        nn.init.zeros_(self.diag.weight)
+        with torch.no_grad():
+            self.diag.bias.zero_()
+            self.diag.bias[:3] = math.log(math.e - 1.0)
+
+    def pack(self) -> np.ndarray:
+        sd = self.state_dict()
+        return np.concatenate([sd[k].detach().cpu().numpy().astype(np.float32).reshape(-1) for k, _ in LAYOUT])
+
+    def unpack(self, flat: np.ndarray) -> "FactorNet":
+        flat = np.asarray(flat, dtype=np.float32).reshape(-1)
+        if flat.size != N_PARAMS:
+            raise ValueError(f"expected {N_PARAMS} parameters, got {flat.size}")
+        sd = self.state_dict()
+        o = 0
+        for k, shape in LAYOUT:
+            m = int(np.prod(shape))
+            sd[k] = torch.as_tensor(flat[o:o + m].reshape(shape))
+            o += m
+        self.load_state_dict(sd)
+        return self
+
+
+def load_weights(path: Optional[Path] = None) -> np.ndarray:
+    """The packed float32 parameters shipped with the package."""
+    with np.load(path or WEIGHTS_FILE) as z:
+        return z["params"].astype(np.float32)
+
+
+def static_features(rest_q: np.ndarray, tets: np.ndarray, materials: np.ndarray,
+                    vertex_offsets: Optional[np.ndarray] = None) -> np.ndarray:
+    """[n, 4] float32: incident-tet mean of log10 E minus 5, and the rest
+    position minus its body's centroid.  E = mu (3 lambda + 2 mu) / (lambda +
+    mu) from the tets' Lame parameters."""
+    rest = np.asarray(rest_q, dtype=np.float64)
+    n = rest.shape[0]
+    mu = materials[:, 0].astype(np.float64)
+    lam = materials[:, 1].astype(np.float64)
+    E = mu * (3.0 * lam + 2.0 * mu) / np.maximum(lam + mu, 1e-30)
+    logE = np.log10(np.maximum(E, 1e-30))
+    acc = np.zeros(n)
+    cnt = np.zeros(n)
+    tv = np.asarray(tets, dtype=np.int64).reshape(-1)
+    np.add.at(acc, tv, np.repeat(logE, 4))
+    np.add.at(cnt, tv, 1.0)
+    out = np.zeros((n, 4), dtype=np.float64)
+    out[:, 0] = np.where(cnt > 0, acc / np.maximum(cnt, 1.0), 5.0) - 5.0
+    offs = np.asarray(vertex_offsets if vertex_offsets is not None else [0, n], dtype=np.int64)
+    for b in range(len(offs) - 1):
+        sl = slice(offs[b], offs[b + 1])
+        out[sl, 1:4] = rest[sl] - rest[sl].mean(axis=0)
+    return out.astype(np.float32)
+
+
+# -- graph of one system ------------------------------------------------------
+class Graph:
+    """Index arrays of H's block pattern that the net and its loss use."""
+
+    def __init__(self, row_ptr, col_idx, device="cpu"):
+        rp = np.asarray(row_ptr, dtype=np.int64)
+        ci = np.asarray(col_idx, dtype=np.int64)
+        n = rp.size - 1
+        rows = np.repeat(np.arange(n), np.diff(rp))
+        self.n = n
+        self.rows = torch.as_tensor(rows, device=device)
+        self.cols = torch.as_tensor(ci, device=device)
+        self.diag = torch.as_tensor(np.flatnonzero(rows == ci), device=device)
+        off = np.flatnonzero(rows != ci)
+        self.off = torch.as_tensor(off, device=device)
+        lo = np.flatnonzero(rows > ci)
+        self.lo = torch.as_tensor(lo, device=device)
+        self.deg = torch.as_tensor(np.diff(rp).astype(np.float32), device=device)
+        # the lower pattern (columns <= row, ascending): entry index of each
+        # diagonal and off-diagonal lower block
+        lmask = rows >= ci
+        lidx = np.cumsum(lmask) - 1
+        self.nnzl = int(lmask.sum())
+        self.l_of_diag = torch.as_tensor(lidx[rows == ci], device=device)
+        self.l_of_lo = torch.as_tensor(lidx[lo], device=device)
+
+
+def _bf16(t: torch.Tensor) -> torch.Tensor:
+    return t.to(torch.bfloat16).to(torch.float32)
+
+
+def scaled_system(G: Graph, values: torch.Tensor):
+    """(s [n], scaled blocks [nnzb, 3, 3]) of S H S, s = (tr(H_ii)/3)^-1/2."""
+    Hd = values[G.diag]
+    d = (Hd[:, 0, 0] + Hd[:, 1, 1] + Hd[:, 2, 2]) / 3.0
+    ok = torch.isfinite(d) & (d > 0)
+    s = torch.where(ok, torch.rsqrt(torch.where(ok, d, torch.ones_like(d))), torch.ones_like(d))
+    Ks = values * (s[G.rows] * s[G.cols])[:, None, None]
+    return s, d, Ks
+
+
+def forward(net: FactorNet, G: Graph, values: torch.Tensor, vstatic: torch.Tensor, emulate_bf16: bool = False):
+    """(s, L~ diagonal blocks [n, 3, 3], L~ off-diagonal lower blocks
+    [n_lo, 3, 3]) for one system.  ``emulate_bf16`` rounds weights and GEMM
+    operands as the device does."""
+    r = _bf16 if emulate_bf16 else (lambda t: t)
+    n = G.n
+    s, d, Ks = scaled_system(G, values)
+    Kd = Ks[G.diag]
+    ld = torch.log10(torch.where(d > 0, d, torch.ones_like(d)))
+    offr, offc = G.rows[G.off], G.cols[G.off]
+    cnt = torch.zeros(n, device=values.device).index_add_(0, offr, torch.ones_like(offr, dtype=torch.float32))
+    ldn = torch.zeros(n, device=values.device).index_add_(0, offr, ld[offc]) / cnt.clamp_min(1.0)
+    x = torch.zeros(n, N_IN, device=values.device)
+    x[:, 0] = Kd[:, 0, 0] - 1.0
+    x[:, 1] = Kd[:, 1, 1] - 1.0
+    x[:, 2] = Kd[:, 2, 2] - 1.0
+    x[:, 3] = Kd[:, 0, 1]
+    x[:, 4] = Kd[:, 0, 2]
+    x[:, 5] = Kd[:, 1, 2]
+    x[:, 6] = torch.where(cnt > 0, ld - ldn, torch.zeros_like(ld))
+    x[:, 7:11] = vstatic
+    x[:, 11] = G.deg / 15.0
+    w = torch.linalg.vector_norm(Ks[G.off].reshape(-1, 9), dim=1)
+    wsum = torch.zeros(n, device=values.device).index_add_(0, offr, w)
+    winv = torch.where(wsum > 0, 1.0 / wsum.clamp_min(1e-30), torch.zeros_like(wsum))
+    h = torch.relu(x @ r(net.inp.weight).t() + net.inp.bias)
+    for lin in net.mp:
+        hb = r(h)
+        a = torch.zeros_like(h).index_add_(0, offr, w[:, None] * hb[offc]) * winv[:, None]
+        h = h + torch.relu(torch.cat([hb, r(a)], 1) @ r(lin.weight).t() + lin.bias)
+    hb = r(h)
+    o = hb @ r(net.diag.weight).t() + net.diag.bias
+    sp = nn.functional.softplus
+    z0 = torch.zeros(n, device=values.device)
+    Ld = torch.stack([torch.stack([sp(o[:, 0]), z0, z0], 1),
+                      torch.stack([o[:, 3], sp(o[:, 1]), z0], 1),
+                      torch.stack([o[:, 4], o[:, 5], sp(o[:, 2])], 1)], 1)
+    Ph = r(hb @ r(net.P.weight).t() + net.P.bias)
+    Qh = r(hb @ r(net.Q.weight).t())
+    li, lj = G.rows[G.lo], G.cols[G.lo]
+    e = r(Ks[G.lo].reshape(-1, 9))
+    z = torch.relu(Ph[li] + Qh[lj] + e @ r(net.R.weight).t())
+    Lo = (r(z) @ r(net.out.weight).t() + net.out.bias).reshape(-1, 3, 3)
+    return s, Ld, Lo
+
+
+def reference_factor(net: FactorNet, row_ptr, col_idx, values, vstatic, emulate_bf16: bool = True) -> np.ndarray:
+    """L = S L~ on the lower pattern [nnzl, 3, 3], float64 numpy: what the
+    device writes into the factor buffer."""
+    G = Graph(row_ptr, col_idx)
+    with torch.no_grad():
+        vals = torch.as_tensor(np.asarray(values, dtype=np.float32).reshape(-1, 3, 3))
+        s, Ld, Lo = forward(net, G, vals, torch.as_tensor(np.asarray(vstatic, dtype=np.float32)), emulate_bf16)
+        L = torch.zeros(G.nnzl, 3, 3)
+        L[G.l_of_diag] = Ld * s[:, None, None]
+        L[G.l_of_lo] = Lo * s[G.rows[G.lo]][:, None, None]
+    return L.numpy().astype(np.float64)
+
+
+def apply_scaled_M(G: Graph, Ld, Lo, r):
+    """z = L~ (L~^T r) for r [n, 3, k]."""
+    li, lj = G.rows[G.lo], G.cols[G.lo]
+    y = torch.einsum("nji,njk->nik", Ld, r)
+    y = y.index_add(0, lj, torch.einsum("eji,ejk->eik", Lo, r[li]))
+    z = torch.einsum("nij,njk->nik", Ld, y)
+    return z.index_add(0, li, torch.einsum("eij,ejk->eik", Lo, y[lj]))
+
+
+def apply_blocks(G: Graph, Ks, v):
+    return torch.zeros_like(v).index_add_(0, G.rows, torch.einsum("kij,kjm->kim", Ks, v[G.cols]))
+
+
+def loss(net: FactorNet, G: Graph, values, vstatic, rhs, k: int = 8, generator=None):
+    s, Ld, Lo = forward(net, G, values, vstatic)
+    _, _, Ks = scaled_system(G, values)
+    r = torch.randn(G.n, 3, k, device=values.device, generator=generator)
+    r[:, :, 0] = rhs * s[:, None]
+    r = r / torch.linalg.vector_norm(r.reshape(-1, k), dim=0).clamp_min(1e-30)
+    res = r - apply_blocks(G, Ks, apply_scaled_M(G, Ld, Lo, r))
+    return (torch.linalg.vector_norm(res.reshape(-1, k), dim=0) ** 2).mean()
+
+
+# -- training data from this library's solver --------------------------------
+def solver_systems(mesh, n_steps: int, seed: int, device: str = "cuda:0", velocity_std: float = 0.1):
+    """(row_ptr, col_idx, [(H values, rhs)], static features) along a
+    trajectory of ``mesh`` with random initial velocities and a random
+    gravity direction (|g| = 9.81)."""
+    import dataclasses
+    from .model import Model
+    from .solver import MixedFEMSolver
+    rng = np.random.default_rng(seed)
+    free = mesh.particle_inv_mass > 0
+    qd = (rng.normal(0.0, velocity_std, size=(mesh.n, 3)) * free[:, None]).astype(np.float32)
+    g = rng.normal(size=3)
+    g = (9.81 * g / np.linalg.norm(g)).astype(np.float32)
+    mesh = dataclasses.replace(mesh, qd0=qd, gravity=g)
+    model = Model.from_beam(mesh, device=device)
+    solver = MixedFEMSolver(model, iterations=mesh.spec.iterations, energy=mesh.spec.energy, line_search=False,
+                            cg_tolerance=mesh.spec.cg_tolerance, cg_max_iterations=mesh.spec.cg_max_iterations)
+    q = torch.as_tensor(mesh.q0, device=device)
+    v = torch.as_tensor(qd, device=device)
+    x = q.clone()
+    out = []
+    for _ in range(n_steps):
+        solver.predict(q, v, mesh.spec.dt)
+        x.copy_(q)
+        for it in range(solver.iterations):
+            solver.update_system(x)
+            solver.assemble(x, mesh.spec.dt)
+            out.append((solver.read_buffer("h_values").reshape(-1, 3, 3).clone(),
+                        solver.read_buffer("rhs").reshape(-1, 3).clone()))
+            solver.global_solve(it)
+            solver.local_solve(x)
+        v = (x - q) / mesh.spec.dt
+        q = x.clone()
+    rp = solver.read_buffer("row_ptr").cpu().numpy()
+    ci = solver.read_buffer("col_idx").cpu().numpy()
+    vs = static_features(mesh.rest_q, mesh.tet_indices, mesh.tet_materials)
+    solver.close()
+    return rp, ci, out, vs
+
+
+def train(meshes, pairs: int = 2000, r_per_system: int = 8, epochs: int = 12, seed: int = 5,
+          device: str = "cuda:0", log=print) -> FactorNet:
+    """Trains on about ``pairs`` (K, r) pairs: pairs / r_per_system systems
+    drawn along trajectories of ``meshes``."""
+    torch.manual_seed(seed)
+    systems = []
+    per_mesh = max(1, pairs // r_per_system // len(meshes))
+    for m_i, mesh in enumerate(meshes):
+        its = mesh.spec.iterations
+        steps = max(1, (per_mesh + its - 1) // its)
+        rp, ci, sysl, vs = solver_systems(mesh, steps, seed + 17 * m_i, device)
+        G = Graph(rp, ci, device)
+        vst = torch.as_tensor(vs, device=device)
+        for vals, rhs in sysl[:per_mesh]:
+            systems.append((G, vals, vst, rhs))
+        log(f"mesh {mesh.spec.name} {mesh.spec.cells}: {min(per_mesh, len(sysl))} systems")
+    net = FactorNet().to(device)
+    opt = torch.optim.Adam(net.parameters(), lr=2e-3)
+    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, epochs)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    for ep in range(epochs):
+        perm = np.random.default_rng(seed + ep).permutation(len(systems))
+        tot = 0.0
+        for i in perm:
+            G, vals, vst, rhs = systems[i]
+            opt.zero_grad()
+            lv = loss(net, G, vals, vst, rhs, r_per_system, gen)
+            lv.backward()
+            opt.step()
+            tot += float(lv)
+        sched.step()
+        log(f"epoch {ep}: loss {tot / len(systems):.4f}")
+    return net.cpu()
+
+
+def main(argv=None):
+    import argparse
+    from . import beams
+    ap = argparse.ArgumentParser(description="train the learned factor preconditioner")
+    ap.add_argument("--out", default=str(WEIGHTS_FILE))
+    ap.add_argument("--pairs", type=int, default=2000)
+    ap.add_argument("--epochs", type=int, default=12)
+    ap.add_argument("--device", default="cuda:0")
+    args = ap.parse_args(argv)
+    meshes = [beams.build_beam("nh_beam"), beams.build_beam("stiff_beam")]
+    net = train(meshes, pairs=args.pairs, epochs=args.epochs, device=args.device)
+    np.savez(args.out, params=net.pack())
+    print(f"wrote {args.out} ({N_PARAMS} parameters)")
+
+
+if __name__ == "__main__":
+    main()

@@ -46,6 +46,11 @@ class MixedFEMSolver:
     ``inner_tolerance`` (1e-3) inside an fp64-residual iterative refinement
     to ``outer_tolerance`` (1e-8), at most ``outer_max_iterations`` (10)
     corrections.
+
+    ``preconditioner`` is the reference's flag (True: block-Jacobi, False:
+    none) or "fsai": a factorized sparse approximate inverse M = G^T G with G
+    lower block-triangular on H's block pattern, recomputed after every
+    assembly and applied by the global-memory PCG (fp32 solve only).
     """
 
     def __init__(self, model: Model, iterations: int, max_tets: Optional[int] = None,
@@ -78,7 +83,13 @@ class MixedFEMSolver:
         cfg.cg_tolerance = float(kwargs.get("cg_tolerance", 1.0e-6))
         cfg.attachment_stiffness = float(kwargs.get("attachment_stiffness", 10.0))
         cfg.preconditioner_singular_threshold = float(kwargs.get("preconditioner_singular_threshold", 1.0e-20))
-        cfg.preconditioner = 1 if kwargs.get("preconditioner", True) else 0
+        pc = kwargs.get("preconditioner", True)
+        if isinstance(pc, str):
+            if pc not in ("block_jacobi", "fsai"):
+                raise ValueError(f"unknown preconditioner {pc!r}")
+            cfg.preconditioner = 2 if pc == "fsai" else 1
+        else:
+            cfg.preconditioner = 1 if pc else 0
         cfg.use_cuda_graph = 1 if kwargs.get("use_cuda_graph", True) else 0
         cfg.pcg_ctas = int(kwargs.get("pcg_ctas", 0))
         cfg.pcg_variant = {"auto": 0, "standard": 1, "single_reduction": 2,
