@@ -56,8 +56,9 @@ def parse_args():
                     help="global solve: fp32 PCG (the workload's) or mixed-precision iterative refinement")
     ap.add_argument("--outer-tolerance", type=float, default=1.0e-6,
                     help="fp64 relative residual of the mixed-precision solve")
-    ap.add_argument("--preconditioner", default="block_jacobi", choices=["block_jacobi", "fsai"],
-                    help="PCG preconditioner: the workload's block-Jacobi, or FSAI (global-memory PCG)")
+    ap.add_argument("--preconditioner", default="block_jacobi", choices=["block_jacobi", "fsai", "learned"],
+                    help="PCG preconditioner: the workload's block-Jacobi, or the FSAI / learned factor "
+                         "(global-memory PCG)")
     ap.add_argument("--line-search", action="store_true",
                     help="run the workload with the reference's backtracking line search")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -253,7 +254,7 @@ def run_batched(args, rank, world, local_rank):
     B = batched_count(args.workload)
     batch = beams.batched_bodies(B, seed=4)
     u = batch.union
-    fsai = args.preconditioner == "fsai"
+    fsai = args.preconditioner in ("fsai", "learned")  # a factor preconditioner
     bs = BatchedSolver(batch, device=dev, preconditioner=args.preconditioner)
     tune_ms = bs.autotune()
     layout = bs.layout()
@@ -367,8 +368,7 @@ def run_batched(args, rank, world, local_rank):
     peak, peak_src = hbm_peak()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": None,
-                "kernel": ("batched_pcg_kernel (per-body " + ("FSAI" if fsai else "block-Jacobi") +
-                           " PCGs, one launch)"),
+                "kernel": f"batched_pcg_kernel (per-body {args.preconditioner} PCGs, one launch)",
                 "algorithmic_bytes_per_launch": bytes_pcg / solves,
                 "bytes_per_body_iteration": (("86 nnzb_b + 222 n_b" if fsai else "40 nnzb_b + 172 n_b") +
                                              ", summed over bodies x (iterations_b + 1)"),
@@ -401,7 +401,7 @@ def run_batched(args, rank, world, local_rank):
                                 f"hex cells of 0.05 m x 6 tets, ARAP or Neo-Hookean (p 0.5), E log-uniform [1e4, 1e6] "
                                 f"Pa, nu~U[0.3, 0.48], gravity on the unit sphere, x = 0 face pinned; "
                                 f"{u.T} tets, {u.n} vertices; 8 local/global iterations, per-body "
-                                f"{'FSAI' if fsai else 'block-Jacobi'} fp32 PCG to 1e-6"),
+                                f"{args.preconditioner} fp32 PCG to 1e-6"),
                    "bodies": B, "tets": u.T, "vertices": u.n, "pcg_schedule": layout,
                    "autotune_best_solve_ms": tune_ms, "parallelism": "replicas",
                    "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write, outside the timed events)"},

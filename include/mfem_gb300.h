@@ -58,8 +58,10 @@ typedef struct mfem_config {
     float attachment_stiffness;           /* penalty on inv_mass==0 vertices (solver.py:106)     */
     float preconditioner_singular_threshold; /* |det| below -> identity block (solver.py:93)     */
     int32_t preconditioner;               /* 1 block-Jacobi, 0 none (solver.py:128), 2 FSAI:
-                                             M = G^T G, G lower block-triangular on H's pattern
-                                             (runs the global-memory PCG)                      */
+                                             M = G^T G, G lower block-triangular on H's pattern,
+                                             3 learned: M = L L^T from the factor net
+                                             (mfem_plan_set_factor_net); 2 and 3 run the
+                                             global-memory PCG                                 */
     int32_t use_cuda_graph;               /* capture mfem_step once per argument set and replay  */
     int32_t pcg_ctas;                     /* persistent PCG CTAs; 0 = one per SM                 */
     int32_t pcg_variant;                  /* 0 auto, 1 standard (two reductions per iteration),
@@ -107,9 +109,10 @@ typedef enum mfem_buffer {
     MFEM_BUF_FRICTION_FORCE = 24,  /* f32 [n]    lagged normal force of the step                 */
     MFEM_BUF_MIXED_DX = 25,        /* f64 [n][3] solution of the last mixed-precision solve
                                       (empty with the FP32 solve)                              */
-    MFEM_BUF_PRECOND_FACTOR = 26,  /* f32 [nnzl][3][3] factor F of preconditioner 2 on H's lower
-                                      block pattern: per row the blocks of columns <= row,
-                                      ascending (empty unless preconditioner >= 2)             */
+    MFEM_BUF_PRECOND_FACTOR = 26,  /* f32 [nnzl][3][3] factor of preconditioners 2 (G) and 3 (L)
+                                      on H's lower block pattern: per row the blocks of
+                                      columns <= row, ascending (empty unless
+                                      preconditioner >= 2)                                     */
     MFEM_BUF_COUNT = 27
 } mfem_buffer;
 
@@ -302,6 +305,29 @@ int mfem_plan_set_solver(mfem_plan *plan, const mfem_solver_config *cfg);
 int mfem_step_mixed_stats(mfem_plan *plan, mfem_mixed_solve_stats *h_stats, int32_t max_entries,
                           int32_t *count, mfem_stream stream);
 
+/* ---- the learned factor preconditioner (preconditioner = 3) -------------- */
+
+/* Parameters of the factor net, packed as float32 in this order ([out][in]
+ * row-major matrices): W_in [64][16], b_in [64]; for l = 0..2: W_l [64][128],
+ * b_l [64]; W_d [6][64], b_d [6]; W_p [64][64], b_p [64]; W_q [64][64];
+ * W_r [64][9]; W_o [9][64], b_o [9].  Matrices are rounded to BF16 here. */
+#define MFEM_FACTOR_NET_PARAMS 35663
+
+/* Loads the net's parameters and the static per-vertex inputs
+ * h_vertex_static [n][4] (incident-tet mean log10 E minus 5; rest position
+ * minus the body's centroid).  After every assembly the net writes L (lower
+ * block-triangular on H's lower block pattern, positive-diagonal diagonal
+ * blocks) into MFEM_BUF_PRECOND_FACTOR and the PCG applies M = L L^T; a
+ * body whose factor-preconditioned solve breaks down (non-finite values or
+ * p.Ap <= 0) is solved again with block-Jacobi.  Net: width 64, three
+ * message-passing layers over H's block graph with weights ||(S H S)_ij||_F,
+ * S = diag(tr(H_ii)/3)^-1/2; L = S L~ with L~ the net's output.  Needs a plan
+ * created with preconditioner = 3.  No reference counterpart: the north
+ * star's learned preconditioner.  Synchronises the device and drops
+ * captured graphs. */
+int mfem_plan_set_factor_net(mfem_plan *plan, const float *h_params, int64_t n_params,
+                             const float *h_vertex_static);
+
 /* ---- independent bodies in one plan ------------------------------------ */
 
 /* Declares the plan's mesh to be n_bodies independent bodies: the vertices
@@ -347,7 +373,10 @@ int mfem_step(mfem_plan *plan, const float *d_q_in, const float *d_qd_in,
               float *d_q_out, float *d_qd_out, float dt, mfem_stream stream);
 
 /* Outcome of the global solves of the last step (synchronises the stream).
- * Writes min(max_entries, iterations) entries; *count = entries written. */
+ * Writes min(max_entries, iterations) entries; *count = entries written.
+ * With several bodies (mfem_plan_set_bodies) each entry summarises the
+ * bodies: the most iterations, the largest residual and the first failing
+ * body's status; mfem_step_body_stats gives them one by one. */
 int mfem_step_stats(mfem_plan *plan, mfem_solve_stats *h_stats, int32_t max_entries,
                     int32_t *count, mfem_stream stream);
 

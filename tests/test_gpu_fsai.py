@@ -129,7 +129,7 @@ def test_fewer_iterations_than_block_jacobi(name, cells):
         st = one_solve(mesh, solver)
         assert st["status"] == _lib.MFEM_OK, (pc, st)
         its[pc] = st["iterations"]
-    assert its["fsai"] < its["block_jacobi"], its
+    assert 0 < its["fsai"] < its["block_jacobi"], its
 
 
 def test_trajectory_matches_fp64_oracle():
@@ -186,3 +186,10 @@ def test_bad_combinations_are_refused():
         MixedFEMSolver(model, iterations=1, preconditioner="fsai", pcg_variant="standard")
     with pytest.raises(_lib.MfemError):
         MixedFEMSolver(model, iterations=1, preconditioner="fsai", solver_precision="fp16")
+
+
+def test_step_stats_report_the_global_memory_solve():
+    """mfem_step_stats of a one-body global-memory plan is the body's record."""
+    mesh, _, solver = make("nh_beam", (16, 4, 4), preconditioner="fsai")
+    st = one_solve(mesh, solver)
+    assert st["status"] == _lib.MFEM_OK and st["iterations"] > 0 and 0.0 < st["rel_residual"] <= 1e-6, st

@@ -1,0 +1,158 @@
+"""The learned factor preconditioner (preconditioner="learned") on the GPU.
+
+It has no reference counterpart: the reference's PCG is block-Jacobi.  The
+bar is:
+* the factor L the net's CUDA kernels write equals the float32 torch
+  reference of the same net (``factor_net.reference_factor``, which rounds
+  weights and tensor-core operands to BF16 as the device does), on the same
+  H: within 2e-2 of the largest |L| of the block row -- the two differ in
+  FP32 summation order, which can move a value across a BF16 rounding
+  boundary;
+* with the shipped weights the solve takes fewer iterations than
+  block-Jacobi and a trajectory stays within 1e-5 of the float64 oracle;
+* a factor that breaks the PCG down (here: one that overflows to inf) is
+  replaced by block-Jacobi for that solve, which then converges.
+"""
+import numpy as np
+import pytest
+import torch
+
+from mfem_gb300 import Model, MixedFEMSolver, _lib, beams, factor_net as F
+from mfem_gb300.batched import BatchedSolver
+from oracle import mfem_oracle as O
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+def make(name, cells, **kw):
+    mesh = beams.build_beam(name, cells=cells)
+    model = Model.from_beam(mesh, device=DEV)
+    solver = MixedFEMSolver(model, iterations=kw.pop("iterations", 8), energy=mesh.spec.energy,
+                            line_search=False, **kw)
+    return mesh, model, solver
+
+
+def one_solve(mesh, solver):
+    q = torch.as_tensor(mesh.q0, device=DEV)
+    x = q.clone()
+    solver.predict(q, torch.zeros_like(q), mesh.spec.dt)
+    solver.update_system(x)
+    solver.assemble(x, mesh.spec.dt)
+    solver.global_solve(0)
+    torch.cuda.synchronize()
+    return solver.solve_stats()[0]
+
+
+def random_net(seed):
+    torch.manual_seed(seed)
+    net = F.FactorNet()
+    with torch.no_grad():
+        for p in net.parameters():
+            p.add_(0.1 * torch.randn_like(p))
+    return net
+
+
+@pytest.mark.parametrize("name,cells", [("nh_beam", (16, 4, 4)), ("stiff_beam", (12, 4, 4))])
+def test_factor_matches_torch_reference(name, cells):
+    net = random_net(7)
+    mesh, _, solver = make(name, cells, preconditioner="learned", factor_net_params=net.pack())
+    assert solver.pcg_layout()["variant"] == "global_memory"
+    one_solve(mesh, solver)
+    rp = solver.read_buffer("row_ptr").cpu().numpy()
+    ci = solver.read_buffer("col_idx").cpu().numpy()
+    vals = solver.read_buffer("h_values").cpu().numpy().reshape(-1, 3, 3)
+    L = solver.read_buffer("precond_factor").cpu().numpy().astype(np.float64).reshape(-1, 3, 3)
+    vs = F.static_features(mesh.rest_q, mesh.tet_indices, mesh.tet_materials)
+    ref = F.reference_factor(net, rp, ci, vals, vs)
+    assert L.shape == ref.shape
+    G = F.Graph(rp, ci)
+    lrow = np.concatenate([[0], np.cumsum(np.bincount(G.rows.numpy()[G.rows.numpy() >= ci], minlength=mesh.n))])
+    worst = 0.0
+    for i in range(mesh.n):
+        blk = slice(lrow[i], lrow[i + 1])
+        scale = np.abs(ref[blk]).max()
+        worst = max(worst, np.abs(L[blk] - ref[blk]).max() / scale)
+    assert worst <= 2e-2, worst
+    # the bulk agrees far more closely than the worst element
+    rel = np.abs(L - ref).max(axis=(1, 2)) / np.abs(ref).max(axis=(1, 2)).clip(1e-30)
+    assert np.median(rel) <= 2e-3
+
+
+def test_overflowing_factor_falls_back_to_block_jacobi():
+    net = F.FactorNet()
+    with torch.no_grad():
+        net.diag.bias[:3] = 1.0e30  # softplus(1e30) = 1e30: M r overflows
+    mesh, _, solver = make("nh_beam", (16, 4, 4), preconditioner="learned", factor_net_params=net.pack())
+    st = one_solve(mesh, solver)
+    _, _, bj = make("nh_beam", (16, 4, 4))
+    st_bj = one_solve(mesh, bj)
+    # the retry is a block-Jacobi solve from the same warm start (in the
+    # global-memory PCG, whose sums run in another order than the default
+    # plan's persistent PCG)
+    assert st["status"] == _lib.MFEM_OK and st["iterations"] > 0, st
+    assert abs(st["iterations"] - st_bj["iterations"]) <= 2, (st, st_bj)
+    dx = solver.read_buffer("dx").cpu().numpy()
+    dx_bj = bj.read_buffer("dx").cpu().numpy()
+    assert np.abs(dx - dx_bj).max() <= 1e-4 * np.abs(dx_bj).max()
+
+
+@pytest.mark.parametrize("name,cells", [("nh_beam", (16, 4, 4)), ("stiff_beam", (16, 4, 4))])
+def test_shipped_weights_take_fewer_iterations_than_block_jacobi(name, cells):
+    its = {}
+    for pc in ("block_jacobi", "learned"):
+        mesh, _, solver = make(name, cells, preconditioner=pc)
+        st = one_solve(mesh, solver)
+        assert st["status"] == _lib.MFEM_OK, (pc, st)
+        its[pc] = st["iterations"]
+    assert 0 < its["learned"] < its["block_jacobi"], its
+
+
+def test_trajectory_matches_fp64_oracle():
+    mesh, model, solver = make("nh_beam", (16, 4, 4), preconditioner="learned")
+    ref = O.OracleSolver(mesh, dtype=np.float64)
+    A, B = model.state(), model.state()
+    A.particle_q.copy_(torch.as_tensor(mesh.q0, device=DEV))
+    q, qd = mesh.q0, mesh.qd0
+    for _ in range(3):
+        solver.step(A, B, None, None, mesh.spec.dt)
+        A, B = B, A
+        q, qd = ref.step(q, qd, mesh.spec.dt)
+        assert all(s["status"] == _lib.MFEM_OK for s in solver.solve_stats())
+        got = A.particle_q.cpu().numpy().astype(np.float64)
+        assert np.abs(got - q).max() <= 1e-5 * np.abs(q).max()
+
+
+def test_batched_bodies_with_learned_factor_match_the_oracle():
+    batch = beams.batched_bodies(6, seed=5, nx=(2, 7), nyz=(1, 3))
+    bs = BatchedSolver(batch, device=DEV, preconditioner="learned")
+    A, B = bs.state(), bs.model.state()
+    for _ in range(2):
+        bs.step(A, B)
+        A, B = B, A
+        assert (bs.body_stats()["status"] == _lib.MFEM_OK).all()
+    q = A.particle_q.cpu().numpy()
+    for k, m in enumerate(batch.bodies):
+        S = O.OracleSolver(m, dtype=np.float64)
+        qq, vv = m.q0, m.qd0
+        for _ in range(2):
+            qq, vv = S.step(qq, vv, m.spec.dt)
+        got = q[batch.vertex_offsets[k]:batch.vertex_offsets[k + 1]]
+        assert np.abs(got - qq).max() <= 1e-5 * np.abs(qq).max(), k
+
+
+def test_set_factor_net_refuses_bad_input():
+    mesh = beams.build_beam("cantilever", cells=(2, 1, 1))
+    model = Model.from_beam(mesh, device=DEV)
+    good = F.FactorNet().pack()
+    with pytest.raises(_lib.MfemError):  # a plan without preconditioner 3
+        MixedFEMSolver(model, iterations=1).set_factor_net(good)
+    with pytest.raises(_lib.MfemError):
+        MixedFEMSolver(model, iterations=1, preconditioner="learned", factor_net_params=good[:-1])
+    bad = good.copy()
+    bad[3] = np.nan
+    with pytest.raises(_lib.MfemError):
+        MixedFEMSolver(model, iterations=1, preconditioner="learned", factor_net_params=bad)
+    with pytest.raises(_lib.MfemError):
+        MixedFEMSolver(model, iterations=1, preconditioner="learned", factor_net_params=good,
+                       solver_precision="fp16")

@@ -64,6 +64,9 @@ struct mfem_plan {
     // independent bodies (mfem_plan_set_bodies): per-body PCGs in one launch
     BatchViews bw{};
     std::vector<void *> batch_allocs;
+    // the learned factor net (preconditioner 3)
+    FactorNetViews fv{};
+    std::vector<void *> net_allocs;
     std::vector<void *> layout_allocs;  // the current schedule's task arrays and partials
     std::vector<int32_t> h_body_row, h_body_nnzb, h_body_its;
     bool global_memory_pcg = false;  // the mesh is solved as a one-body batch
@@ -173,10 +176,10 @@ bool valid_config(const mfem_config *cfg, std::string &err) {
     else if (!std::isfinite(cfg->attachment_stiffness) || cfg->attachment_stiffness < 0.0f)
         err = "attachment_stiffness must be finite and >= 0";
     else if (!(cfg->preconditioner_singular_threshold >= 0.0f)) err = "preconditioner_singular_threshold must be >= 0";
-    else if (cfg->preconditioner < 0 || cfg->preconditioner > 2)
-        err = "preconditioner must be 0 (none), 1 (block-Jacobi) or 2 (FSAI)";
-    else if (cfg->preconditioner == 2 && cfg->pcg_variant != 0)
-        err = "the FSAI preconditioner runs the global-memory PCG: pcg_variant must be 0";
+    else if (cfg->preconditioner < 0 || cfg->preconditioner > 3)
+        err = "preconditioner must be 0 (none), 1 (block-Jacobi), 2 (FSAI) or 3 (learned)";
+    else if (cfg->preconditioner >= 2 && cfg->pcg_variant != 0)
+        err = "factor preconditioners run the global-memory PCG: pcg_variant must be 0";
     else if (cfg->pcg_ctas < 0) err = "pcg_ctas must be >= 0";
     else if (cfg->pcg_variant < 0 || cfg->pcg_variant > 3) err = "pcg_variant must be 0 (auto), 1, 2 or 3";
     else if (cfg->line_search != 0 && cfg->line_search != 1) err = "line_search must be 0 or 1";
@@ -188,6 +191,9 @@ bool valid_config(const mfem_config *cfg, std::string &err) {
     else return true;
     return false;
 }
+
+// A plan with the learned preconditioner needs its net before any assembly.
+bool net_ready(const mfem_plan *p) { return p->cfg.preconditioner != 3 || p->fv.ready; }
 
 // The whole step as a launch sequence on one stream.
 // The reference's float32 PCG, or the mixed-precision iterative refinement.
@@ -221,6 +227,7 @@ cudaError_t contact_and_assemble(mfem_plan *p, const float *x, float dt, cudaStr
                               p->bv, p->cv, s);
     if (err == cudaSuccess && p->cfg.preconditioner == 2) err = launch_fsai_setup(p->bv, p->bw, s);
     if (err == cudaSuccess && p->cfg.preconditioner == 2) err = launch_factor_transpose(p->bw, s);
+    if (err == cudaSuccess && p->cfg.preconditioner == 3) err = launch_factor_net(p->bv, p->bw, p->fv, s);
     return err;
 }
 
@@ -389,6 +396,7 @@ void mfem_plan_destroy(mfem_plan *p) {
         for (void *a : p->ir_allocs) cudaFree(a);
         for (void *a : p->batch_allocs) cudaFree(a);
         for (void *a : p->layout_allocs) cudaFree(a);
+        for (void *a : p->net_allocs) cudaFree(a);
     }
     delete p;
 }
@@ -525,8 +533,8 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
         p->ls.c = cfg.line_search_c;
         p->ls.threshold = cfg.line_search_threshold;
     }
-    if (e == cudaSuccess && cfg.preconditioner == 2) {
-        // FSAI is applied by the global-memory PCG only
+    if (e == cudaSuccess && cfg.preconditioner >= 2) {
+        // factor preconditioners are applied by the global-memory PCG only
         p->pl = PcgLayout{};
         p->pl.variant = 0;
         p->global_memory_pcg = true;
@@ -694,6 +702,7 @@ int mfem_step(mfem_plan *p, const float *q_in, const float *qd_in, float *q_out,
     if (!p) return MFEM_BAD_ARG;
     if (!q_in || !qd_in || !q_out || !qd_out) return fail(p, MFEM_BAD_ARG, "NULL state pointer");
     if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(p, MFEM_BAD_ARG, "dt must be finite and > 0");
+    if (!net_ready(p)) return fail(p, MFEM_BAD_ARG, "preconditioner 3 needs mfem_plan_set_factor_net");
     if ((const void *)qd_in == (const void *)q_out || (const void *)q_in == (const void *)qd_out)
         return fail(p, MFEM_BAD_ARG, "positions and velocities must not alias");
     cudaStream_t stream = (cudaStream_t)stream_;
@@ -762,7 +771,26 @@ int mfem_step_stats(mfem_plan *p, mfem_solve_stats *h_stats, int32_t max_entries
     if (e != cudaSuccess) return cuda_fail(p, e, "cudaStreamSynchronize");
     const int k = std::max(0, std::min<int>(max_entries, p->cfg.iterations));
     std::vector<SolveStats> tmp(p->max_stats);
-    e = cudaMemcpy(tmp.data(), p->pw.stats, sizeof(SolveStats) * p->max_stats, cudaMemcpyDeviceToHost);
+    if (p->bw.n_bodies > 0 && p->ir.mode == 0) {
+        // the global-memory PCG's per-body records, [slot][body]: a single
+        // body's own, else per slot the most iterations, the largest
+        // residual and the first body's failure
+        const int B = p->bw.n_bodies;
+        std::vector<SolveStats> all((size_t)p->max_stats * B);
+        e = cudaMemcpy(all.data(), p->bw.stats, all.size() * sizeof(SolveStats), cudaMemcpyDeviceToHost);
+        for (int i = 0; e == cudaSuccess && i < p->max_stats; ++i) {
+            SolveStats agg = all[(size_t)i * B];
+            for (int b = 1; b < B; ++b) {
+                const SolveStats &sb = all[(size_t)i * B + b];
+                agg.iterations = std::max(agg.iterations, sb.iterations);
+                agg.rel_residual = std::max(agg.rel_residual, sb.rel_residual);
+                if (agg.status == MFEM_OK && sb.status != MFEM_OK) agg.status = sb.status;
+            }
+            tmp[i] = agg;
+        }
+    } else {
+        e = cudaMemcpy(tmp.data(), p->pw.stats, sizeof(SolveStats) * p->max_stats, cudaMemcpyDeviceToHost);
+    }
     int flag = 0;
     if (e == cudaSuccess) e = cudaMemcpy(&flag, p->pw.error, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(p, e, "stats readback");
@@ -999,8 +1027,8 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
         return fail(p, MFEM_BAD_ARG, "outer_max_iterations must be in [1, 100]");
     if (p->bw.n_bodies > 1 && cfg.precision != MFEM_PRECISION_FP32)
         return fail(p, MFEM_BAD_ARG, "batched bodies use the fp32 PCG");
-    if (p->cfg.preconditioner == 2 && cfg.precision != MFEM_PRECISION_FP32)
-        return fail(p, MFEM_BAD_ARG, "the FSAI preconditioner runs with the fp32 PCG");
+    if (p->cfg.preconditioner >= 2 && cfg.precision != MFEM_PRECISION_FP32)
+        return fail(p, MFEM_BAD_ARG, "factor preconditioners run with the fp32 PCG");
     DeviceGuard g(p->device);
     cudaError_t e = cudaDeviceSynchronize();  // no step of this plan may still use the old buffers
     if (e != cudaSuccess) return cuda_fail(p, e, "cudaDeviceSynchronize");
@@ -1226,6 +1254,7 @@ int install_bodies(mfem_plan *p, int n_bodies, const int32_t *voff, const int32_
         alloc(&bw.Lval, nnzl * 9 * sizeof(float));
         alloc(&bw.Uval, nnzl * 9 * sizeof(float));
         alloc(&bw.y, n3 * sizeof(float));
+        alloc(&bw.dx0, n3 * sizeof(float));
         if (e == cudaSuccess) e = upload(d_lrow, lrow.data(), lrow.size());
         if (e == cudaSuccess) e = upload(d_urow, urow.data(), urow.size());
         if (e == cudaSuccess) e = upload(d_lcol, lcol.data(), nnzl);
@@ -1299,6 +1328,132 @@ int mfem_plan_set_bodies(mfem_plan *p, int32_t n_bodies, const int32_t *h_vertex
     return install_bodies(p, n_bodies, h_vertex_offsets, h_tet_offsets, h_body_energy, h_body_gravity);
 }
 
+int mfem_plan_set_factor_net(mfem_plan *p, const float *h_params, int64_t n_params, const float *h_vertex_static) {
+    if (!p) return MFEM_BAD_ARG;
+    if (p->cfg.preconditioner != 3)
+        return fail(p, MFEM_BAD_ARG, "the factor net needs a plan created with preconditioner = 3");
+    if (!h_params || n_params != MFEM_FACTOR_NET_PARAMS)
+        return fail(p, MFEM_BAD_ARG, "need MFEM_FACTOR_NET_PARAMS parameters");
+    if (!h_vertex_static && p->n > 0) return fail(p, MFEM_BAD_ARG, "h_vertex_static is NULL");
+    for (int64_t i = 0; i < n_params; ++i)
+        if (!std::isfinite(h_params[i])) return fail(p, MFEM_BAD_ARG, "non-finite net parameter");
+    for (int64_t i = 0; i < (int64_t)p->n * 4; ++i)
+        if (!std::isfinite(h_vertex_static[i])) return fail(p, MFEM_BAD_ARG, "non-finite static vertex feature");
+    constexpr int W = kNetWidth;
+    // unpack in the documented order
+    const float *q = h_params;
+    auto take = [&](int64_t count) {
+        const float *r = q;
+        q += count;
+        return r;
+    };
+    const float *w_in = take(W * kNetIn), *b_in = take(W);
+    const float *w_mp[3], *b_mp[3];
+    for (int l = 0; l < 3; ++l) {
+        w_mp[l] = take(W * 2 * W);
+        b_mp[l] = take(W);
+    }
+    const float *w_d = take(6 * W), *b_d = take(6), *w_p = take(W * W), *b_p = take(W), *w_q = take(W * W);
+    const float *w_r = take(W * 9), *w_o = take(9 * W), *b_o = take(9);
+    auto bf = [](float v) { return __float2bfloat16_rn(v); };
+    std::vector<float> h_w_in(W * kNetIn);
+    for (int i = 0; i < W * kNetIn; ++i) h_w_in[i] = __bfloat162float(bf(w_in[i]));
+    const __nv_bfloat16 zero = bf(0.0f);
+    std::vector<__nv_bfloat16> h_mp[3];
+    for (int l = 0; l < 3; ++l) {
+        h_mp[l].assign((size_t)W * kMpLd, zero);
+        for (int o = 0; o < W; ++o)
+            for (int k = 0; k < 2 * W; ++k) h_mp[l][(size_t)o * kMpLd + k] = bf(w_mp[l][o * 2 * W + k]);
+    }
+    std::vector<__nv_bfloat16> h_node((size_t)kNodeOut * kNodeLd, zero);
+    std::vector<float> h_bnode(kNodeOut, 0.0f);
+    for (int o = 0; o < W; ++o) {
+        for (int k = 0; k < W; ++k) {
+            h_node[(size_t)o * kNodeLd + k] = bf(w_p[o * W + k]);
+            h_node[(size_t)(W + o) * kNodeLd + k] = bf(w_q[o * W + k]);
+        }
+        h_bnode[o] = b_p[o];
+    }
+    for (int o = 0; o < 6; ++o) {
+        for (int k = 0; k < W; ++k) h_node[(size_t)(2 * W + o) * kNodeLd + k] = bf(w_d[o * W + k]);
+        h_bnode[2 * W + o] = b_d[o];
+    }
+    std::vector<__nv_bfloat16> h_r((size_t)W * kRLd, zero), h_o((size_t)16 * kNodeLd, zero);
+    std::vector<float> h_bo(16, 0.0f);
+    for (int o = 0; o < W; ++o)
+        for (int k = 0; k < 9; ++k) h_r[(size_t)o * kRLd + k] = bf(w_r[o * 9 + k]);
+    for (int o = 0; o < 9; ++o) {
+        for (int k = 0; k < W; ++k) h_o[(size_t)o * kNodeLd + k] = bf(w_o[o * W + k]);
+        h_bo[o] = b_o[o];
+    }
+    // lower pattern: H slot of each lower block, and the off-diagonal ones
+    std::vector<int32_t> lslot, erow, elow;
+    for (int r = 0; r < p->n; ++r)
+        for (int k = p->h_row_ptr[r]; k < p->h_row_ptr[r + 1]; ++k) {
+            const int c = p->h_col_idx[k];
+            if (c > r) continue;
+            if (c < r) {
+                erow.push_back(r);
+                elow.push_back((int32_t)lslot.size());
+            }
+            lslot.push_back(k);
+        }
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(p, e, "cudaDeviceSynchronize");
+    drop_graphs(p);
+    for (void *a : p->net_allocs) cudaFree(a);
+    p->net_allocs.clear();
+    p->fv = FactorNetViews{};
+    FactorNetViews fv{};
+    const size_t n = (size_t)p->n;
+    auto put = [&](auto **dst, const auto *src, size_t count) {
+        if (e != cudaSuccess) return;
+        void *raw = nullptr;
+        const size_t bytes = std::max<size_t>(count * sizeof(**dst), 16);
+        e = cudaMalloc(&raw, bytes);
+        if (e != cudaSuccess) return;
+        p->net_allocs.push_back(raw);
+        if (src && count) e = cudaMemcpy(raw, src, count * sizeof(**dst), cudaMemcpyHostToDevice);
+        *dst = static_cast<std::remove_reference_t<decltype(*dst)>>(raw);
+    };
+    const float *nf = nullptr;
+    const __nv_bfloat16 *nb = nullptr;
+    put(&fv.w_in, h_w_in.data(), h_w_in.size());
+    put(&fv.b_in, b_in, W);
+    for (int l = 0; l < 3; ++l) {
+        put(&fv.w_mp[l], h_mp[l].data(), h_mp[l].size());
+        put(&fv.b_mp[l], b_mp[l], W);
+    }
+    put(&fv.w_node, h_node.data(), h_node.size());
+    put(&fv.b_node, h_bnode.data(), h_bnode.size());
+    put(&fv.w_r, h_r.data(), h_r.size());
+    put(&fv.w_o, h_o.data(), h_o.size());
+    put(&fv.b_o, h_bo.data(), h_bo.size());
+    put(&fv.vstatic, h_vertex_static, n * 4);
+    put(&fv.s, nf, n);
+    put(&fv.ld, nf, n);
+    put(&fv.w, nf, (size_t)p->nnzb);
+    put(&fv.winv, nf, n);
+    put(&fv.h, nf, n * W);
+    put(&fv.hb[0], nb, n * W);
+    put(&fv.hb[1], nb, n * W);
+    put(&fv.pb, nb, n * W);
+    put(&fv.qb, nb, n * W);
+    put(&fv.lslot, lslot.data(), lslot.size());
+    put(&fv.erow, erow.data(), erow.size());
+    put(&fv.elow, elow.data(), elow.size());
+    if (e != cudaSuccess) {
+        for (void *a : p->net_allocs) cudaFree(a);
+        p->net_allocs.clear();
+        return cuda_fail(p, e, "factor net buffers");
+    }
+    fv.n_edges = (int)erow.size();
+    fv.ready = 1;
+    p->fv = fv;
+    return MFEM_OK;
+}
+
 int mfem_plan_batch_layout(const mfem_plan *p, int32_t *ctas, int32_t *threads) {
     if (!p) return MFEM_BAD_ARG;
     if (ctas) *ctas = p->bw.ctas;
@@ -1310,6 +1465,7 @@ int mfem_plan_autotune_batch(mfem_plan *p, const float *d_q, float dt, double *h
     if (!p) return MFEM_BAD_ARG;
     if (p->bw.n_bodies == 0) return fail(p, MFEM_BAD_ARG, "no bodies: call mfem_plan_set_bodies first");
     if (!d_q || !(dt > 0.0f)) return fail(p, MFEM_BAD_ARG, "need q and dt > 0");
+    if (!net_ready(p)) return fail(p, MFEM_BAD_ARG, "preconditioner 3 needs mfem_plan_set_factor_net");
     DeviceGuard g(p->device);
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t es = cudaStreamSynchronize(s);
@@ -1450,6 +1606,7 @@ int mfem_update_system(mfem_plan *p, const float *x, mfem_stream stream) {
 
 int mfem_assemble(mfem_plan *p, const float *x, float dt, mfem_stream stream) {
     if (!p) return MFEM_BAD_ARG;
+    if (!net_ready(p)) return fail(p, MFEM_BAD_ARG, "preconditioner 3 needs mfem_plan_set_factor_net");
     if (!x) return fail(p, MFEM_BAD_ARG, "x is NULL");
     if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(p, MFEM_BAD_ARG, "dt must be finite and > 0");
     DeviceGuard g(p->device);

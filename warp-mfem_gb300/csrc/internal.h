@@ -100,6 +100,7 @@ struct BatchViews {
     float *Lval;               // [nnzl][9] F, row-major blocks
     float *Uval;               // [nnzl][9] F^T in upper-CSR order
     float *y;                  // [n][3] the first pass's output
+    float *dx0;                // [n][3] warm start kept for a block-Jacobi retry
     int nnzl;
 };
 

@@ -264,165 +264,182 @@ __global__ void __launch_bounds__(kBtMaxThreads)
         }
         unsigned long long target = s_base;
         unsigned k = 0;
-        int it = 0;
-        // r = g - H x0 (x0: the warm start x~ - x), z = M r
-        for (int row = lo + group; row < hi; row += ngroups) {
-            float y[3];
-            if (tk.size > 1) bt_row_product<true>(bv, row, vv.dx, nullptr, 0.0f, y);
-            else bt_row_product<false>(bv, row, vv.dx, nullptr, 0.0f, y);
-            if (g_lead)
-#pragma unroll
-                for (int q = 0; q < 3; ++q) bw.r[3 * row + q] = vv.rhs[3 * row + q] - y[q];
-        }
-        __syncthreads();
-        const bool factor = use_precond >= 2;  // a factor preconditioner
-        // every row's r must be in place before G r gathers it
-        if (factor && !(bt_sync(bw, tk, error, k, target, s_tot, s_redf, &s_ok) &&
-                      bt_apply_factor(bw, use_precond, tk, lo, hi, error, k, target, s_tot, s_redf, &s_ok))) {
-            if (tk.rank == 0 && threadIdx.x == 0) *st = SolveStats{0, MFEM_TIMEOUT, 0.0f, 0.0f};
-            __syncthreads();
-            continue;
-        }
-        float acc3[3] = {0.0f, 0.0f, 0.0f};
-        for (int row = lo + threadIdx.x; row < hi; row += blockDim.x) {
-            float r[3], z[3];
-#pragma unroll
-            for (int q = 0; q < 3; ++q) r[q] = bw.r[3 * row + q];
-            if (factor) {
-#pragma unroll
-                for (int q = 0; q < 3; ++q) z[q] = bw.z[3 * row + q];
-            } else {
-                bt_precond(vv.Minv, use_precond, row, r, z);
-            }
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                bw.z[3 * row + q] = z[q];
-                const float bq = vv.rhs[3 * row + q];
-                acc3[0] = __fmaf_rn(r[q], z[q], acc3[0]);
-                acc3[1] = __fmaf_rn(r[q], r[q], acc3[1]);
-                acc3[2] = __fmaf_rn(bq, bq, acc3[2]);
-            }
-        }
-        bool ok = bt_reduce<3>(acc3, bw, tk, error, k++, target, s_tot, s_redf, &s_ok);
-        if (threadIdx.x == 0) {
-            if (!ok) {
-                sc.status = MFEM_TIMEOUT;
-                sc.done = 1;
-                sc.rr = 0.0f;
-                sc.bb = 1.0f;
-            } else {
-                sc.rz = s_tot[0];
-                sc.rr = s_tot[1];
-                sc.bb = s_tot[2];
-                sc.thr2 = tol * tol * s_tot[2];
-                sc.beta = 0.0f;
-                sc.status =
-                    (isfinite(s_tot[0]) && isfinite(s_tot[1]) && isfinite(s_tot[2])) ? MFEM_OK : MFEM_NONFINITE;
-                sc.done = sc.status != MFEM_OK || s_tot[1] <= sc.thr2;
-            }
-        }
-        __syncthreads();
-        while (!sc.done) {
-            if (it >= maxiter) {
-                if (threadIdx.x == 0) sc.status = MFEM_MAXITER;
-                break;
-            }
-            float *p_new = (it & 1) ? bw.p1 : bw.p0;
-            const float *p_old = it == 0 ? nullptr : ((it & 1) ? bw.p0 : bw.p1);
-            const float beta = sc.beta;
-            float pap[1] = {0.0f};
+        int mode = use_precond, it = 0, it_done = 0;
+        bool timed_out = false;
+        if (mode >= 2)  // the warm start, for a block-Jacobi retry
+            for (int t3 = 3 * lo + threadIdx.x; t3 < 3 * hi; t3 += blockDim.x) bw.dx0[t3] = vv.dx[t3];
+        for (;;) {  // one attempt; a factor solve that breaks down is retried with block-Jacobi
+            it = 0;
+            // r = g - H x0 (x0: the warm start x~ - x), z = M r
             for (int row = lo + group; row < hi; row += ngroups) {
                 float y[3];
-                if (tk.size > 1) bt_row_product<true>(bv, row, bw.z, p_old, beta, y);
-                else bt_row_product<false>(bv, row, bw.z, p_old, beta, y);
-                if (g_lead) {
+                if (tk.size > 1) bt_row_product<true>(bv, row, vv.dx, nullptr, 0.0f, y);
+                else bt_row_product<false>(bv, row, vv.dx, nullptr, 0.0f, y);
+                if (g_lead)
 #pragma unroll
-                    for (int q = 0; q < 3; ++q) {
-                        const float zq = bw.z[3 * row + q];
-                        const float pq = p_old ? __fmaf_rn(beta, p_old[3 * row + q], zq) : zq;
-                        p_new[3 * row + q] = pq;
-                        bw.Ap[3 * row + q] = y[q];
-                        pap[0] = __fmaf_rn(pq, y[q], pap[0]);
-                    }
-                }
-            }
-            if (!bt_reduce<1>(pap, bw, tk, error, k++, target, s_tot, s_redf, &s_ok)) {
-                if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
-                break;
-            }
-            if (threadIdx.x == 0) {
-                if (!isfinite(s_tot[0])) {
-                    sc.status = MFEM_NONFINITE;
-                    sc.done = 1;
-                } else if (!(s_tot[0] > 0.0f)) {
-                    sc.status = MFEM_STAGNATION;
-                    sc.done = 1;
-                } else {
-                    sc.alpha = sc.rz / s_tot[0];
-                }
+                    for (int q = 0; q < 3; ++q) bw.r[3 * row + q] = vv.rhs[3 * row + q] - y[q];
             }
             __syncthreads();
-            if (sc.done) break;
-            const float alpha = sc.alpha;
-            float acc2[2] = {0.0f, 0.0f};
-            if (factor) {
-                for (int row = lo + threadIdx.x; row < hi; row += blockDim.x)
-#pragma unroll
-                    for (int q = 0; q < 3; ++q) {
-                        vv.dx[3 * row + q] = __fmaf_rn(alpha, p_new[3 * row + q], vv.dx[3 * row + q]);
-                        bw.r[3 * row + q] = __fmaf_rn(-alpha, bw.Ap[3 * row + q], bw.r[3 * row + q]);
-                    }
-                if (!(bt_sync(bw, tk, error, k, target, s_tot, s_redf, &s_ok) &&
-                      bt_apply_factor(bw, use_precond, tk, lo, hi, error, k, target, s_tot, s_redf, &s_ok))) {
-                    if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
-                    break;
-                }
+            const bool factor = mode >= 2;  // a factor preconditioner
+            // every row's r must be in place before the factor's first pass gathers it
+            if (factor && !(bt_sync(bw, tk, error, k, target, s_tot, s_redf, &s_ok) &&
+                          bt_apply_factor(bw, mode, tk, lo, hi, error, k, target, s_tot, s_redf, &s_ok))) {
+                timed_out = true;
+                break;
             }
+            float acc3[3] = {0.0f, 0.0f, 0.0f};
             for (int row = lo + threadIdx.x; row < hi; row += blockDim.x) {
                 float r[3], z[3];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) r[q] = bw.r[3 * row + q];
                 if (factor) {
 #pragma unroll
-                    for (int q = 0; q < 3; ++q) {
-                        r[q] = bw.r[3 * row + q];
-                        z[q] = bw.z[3 * row + q];
-                    }
+                    for (int q = 0; q < 3; ++q) z[q] = bw.z[3 * row + q];
                 } else {
-#pragma unroll
-                    for (int q = 0; q < 3; ++q) {
-                        vv.dx[3 * row + q] = __fmaf_rn(alpha, p_new[3 * row + q], vv.dx[3 * row + q]);
-                        r[q] = __fmaf_rn(-alpha, bw.Ap[3 * row + q], bw.r[3 * row + q]);
-                        bw.r[3 * row + q] = r[q];
-                    }
-                    bt_precond(vv.Minv, use_precond, row, r, z);
+                    bt_precond(vv.Minv, mode, row, r, z);
                 }
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
                     bw.z[3 * row + q] = z[q];
-                    acc2[0] = __fmaf_rn(r[q], z[q], acc2[0]);
-                    acc2[1] = __fmaf_rn(r[q], r[q], acc2[1]);
+                    const float bq = vv.rhs[3 * row + q];
+                    acc3[0] = __fmaf_rn(r[q], z[q], acc3[0]);
+                    acc3[1] = __fmaf_rn(r[q], r[q], acc3[1]);
+                    acc3[2] = __fmaf_rn(bq, bq, acc3[2]);
                 }
             }
-            if (!bt_reduce<2>(acc2, bw, tk, error, k++, target, s_tot, s_redf, &s_ok)) {
-                if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
-                break;
-            }
-            ++it;
+            bool ok = bt_reduce<3>(acc3, bw, tk, error, k++, target, s_tot, s_redf, &s_ok);
             if (threadIdx.x == 0) {
-                sc.rr = s_tot[1];
-                if (!isfinite(s_tot[0]) || !isfinite(s_tot[1])) {
-                    sc.status = MFEM_NONFINITE;
+                if (!ok) {
+                    sc.status = MFEM_TIMEOUT;
                     sc.done = 1;
+                    sc.rr = 0.0f;
+                    sc.bb = 1.0f;
                 } else {
-                    sc.beta = s_tot[0] / sc.rz;
                     sc.rz = s_tot[0];
-                    sc.done = s_tot[1] <= sc.thr2;
+                    sc.rr = s_tot[1];
+                    sc.bb = s_tot[2];
+                    sc.thr2 = tol * tol * s_tot[2];
+                    sc.beta = 0.0f;
+                    sc.status =
+                        (isfinite(s_tot[0]) && isfinite(s_tot[1]) && isfinite(s_tot[2])) ? MFEM_OK : MFEM_NONFINITE;
+                    sc.done = sc.status != MFEM_OK || s_tot[1] <= sc.thr2;
                 }
             }
             __syncthreads();
+            while (!sc.done) {
+                if (it >= maxiter) {
+                    if (threadIdx.x == 0) sc.status = MFEM_MAXITER;
+                    break;
+                }
+                float *p_new = (it & 1) ? bw.p1 : bw.p0;
+                const float *p_old = it == 0 ? nullptr : ((it & 1) ? bw.p0 : bw.p1);
+                const float beta = sc.beta;
+                float pap[1] = {0.0f};
+                for (int row = lo + group; row < hi; row += ngroups) {
+                    float y[3];
+                    if (tk.size > 1) bt_row_product<true>(bv, row, bw.z, p_old, beta, y);
+                    else bt_row_product<false>(bv, row, bw.z, p_old, beta, y);
+                    if (g_lead) {
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            const float zq = bw.z[3 * row + q];
+                            const float pq = p_old ? __fmaf_rn(beta, p_old[3 * row + q], zq) : zq;
+                            p_new[3 * row + q] = pq;
+                            bw.Ap[3 * row + q] = y[q];
+                            pap[0] = __fmaf_rn(pq, y[q], pap[0]);
+                        }
+                    }
+                }
+                if (!bt_reduce<1>(pap, bw, tk, error, k++, target, s_tot, s_redf, &s_ok)) {
+                    if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+                    break;
+                }
+                if (threadIdx.x == 0) {
+                    if (!isfinite(s_tot[0])) {
+                        sc.status = MFEM_NONFINITE;
+                        sc.done = 1;
+                    } else if (!(s_tot[0] > 0.0f)) {
+                        sc.status = MFEM_STAGNATION;
+                        sc.done = 1;
+                    } else {
+                        sc.alpha = sc.rz / s_tot[0];
+                    }
+                }
+                __syncthreads();
+                if (sc.done) break;
+                const float alpha = sc.alpha;
+                float acc2[2] = {0.0f, 0.0f};
+                if (factor) {
+                    for (int row = lo + threadIdx.x; row < hi; row += blockDim.x)
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            vv.dx[3 * row + q] = __fmaf_rn(alpha, p_new[3 * row + q], vv.dx[3 * row + q]);
+                            bw.r[3 * row + q] = __fmaf_rn(-alpha, bw.Ap[3 * row + q], bw.r[3 * row + q]);
+                        }
+                    if (!(bt_sync(bw, tk, error, k, target, s_tot, s_redf, &s_ok) &&
+                          bt_apply_factor(bw, mode, tk, lo, hi, error, k, target, s_tot, s_redf, &s_ok))) {
+                        if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+                        break;
+                    }
+                }
+                for (int row = lo + threadIdx.x; row < hi; row += blockDim.x) {
+                    float r[3], z[3];
+                    if (factor) {
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            r[q] = bw.r[3 * row + q];
+                            z[q] = bw.z[3 * row + q];
+                        }
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            vv.dx[3 * row + q] = __fmaf_rn(alpha, p_new[3 * row + q], vv.dx[3 * row + q]);
+                            r[q] = __fmaf_rn(-alpha, bw.Ap[3 * row + q], bw.r[3 * row + q]);
+                            bw.r[3 * row + q] = r[q];
+                        }
+                        bt_precond(vv.Minv, mode, row, r, z);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        bw.z[3 * row + q] = z[q];
+                        acc2[0] = __fmaf_rn(r[q], z[q], acc2[0]);
+                        acc2[1] = __fmaf_rn(r[q], r[q], acc2[1]);
+                    }
+                }
+                if (!bt_reduce<2>(acc2, bw, tk, error, k++, target, s_tot, s_redf, &s_ok)) {
+                    if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+                    break;
+                }
+                ++it;
+                if (threadIdx.x == 0) {
+                    sc.rr = s_tot[1];
+                    if (!isfinite(s_tot[0]) || !isfinite(s_tot[1])) {
+                        sc.status = MFEM_NONFINITE;
+                        sc.done = 1;
+                    } else {
+                        sc.beta = s_tot[0] / sc.rz;
+                        sc.rz = s_tot[0];
+                        sc.done = s_tot[1] <= sc.thr2;
+                    }
+                }
+                __syncthreads();
+            }
+            if (mode >= 2 && (sc.status == MFEM_STAGNATION || sc.status == MFEM_NONFINITE)) {
+                for (int t3 = 3 * lo + threadIdx.x; t3 < 3 * hi; t3 += blockDim.x) vv.dx[t3] = bw.dx0[t3];
+                // every row's warm start is back before the retry's product reads it
+                if (!bt_sync(bw, tk, error, k, target, s_tot, s_redf, &s_ok)) {
+                    timed_out = true;
+                    break;
+                }
+                it_done += it;
+                mode = 1;
+                continue;
+            }
+            break;
         }
         if (tk.rank == 0 && threadIdx.x == 0) {
             const float rel = sc.bb > 0.0f ? sqrtf(sc.rr / sc.bb) : sqrtf(sc.rr);
-            *st = SolveStats{it, sc.status, rel, 0.0f};
+            *st = timed_out ? SolveStats{0, MFEM_TIMEOUT, 0.0f, 0.0f} : SolveStats{it_done + it, sc.status, rel, 0.0f};
         }
         __syncthreads();  // sc and s_ok are reused by the next task
     }

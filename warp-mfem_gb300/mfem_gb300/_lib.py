@@ -23,6 +23,8 @@ MFEM_CUDA_ERROR = 5
 MFEM_TIMEOUT = 6
 
 ENERGY = {"arap": 0, "neohookean": 1}
+PRECONDITIONER = {"none": 0, "block_jacobi": 1, "fsai": 2, "learned": 3}
+FACTOR_NET_PARAMS = 35663
 
 BUF = {
     "tet_stretch": 0, "tet_lambda": 1, "constraint": 2, "grad_constraint": 3, "grad_s": 4,
@@ -154,6 +156,7 @@ _SIGNATURES = {
     "mfem_step_mixed_stats": (ctypes.c_int, [_P, ctypes.POINTER(MfemMixedSolveStats), _I32, ctypes.POINTER(_I32),
                                              _P]),
     "mfem_plan_set_bodies": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P]),
+    "mfem_plan_set_factor_net": (ctypes.c_int, [_P, _P, _I64, _P]),
     "mfem_plan_batch_layout": (ctypes.c_int, [_P, ctypes.POINTER(_I32), ctypes.POINTER(_I32)]),
     "mfem_plan_autotune_batch": (ctypes.c_int, [_P, _P, _F32, ctypes.POINTER(ctypes.c_double), _P]),
     "mfem_step_body_stats": (ctypes.c_int, [_P, ctypes.POINTER(MfemSolveStats), _I32, ctypes.POINTER(_I32), _P]),

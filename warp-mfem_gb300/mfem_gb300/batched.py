@@ -40,6 +40,9 @@ class BatchedSolver:
         P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
         _lib.check(self._lib.mfem_plan_set_bodies(self._plan, batch.n_bodies, P(h["voff"]), P(h["toff"]),
                                                   P(h["energy"]), P(h["gravity"])), self._plan)
+        if kwargs.get("preconditioner") == "learned":
+            # rest positions relative to each body's centroid
+            self.solver.set_factor_net(kwargs.get("factor_net_params"), vertex_offsets=h["voff"])
 
     @property
     def n_bodies(self) -> int:

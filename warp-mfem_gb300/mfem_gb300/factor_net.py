@@ -158,7 +158,8 @@ def _bf16(t: torch.Tensor) -> torch.Tensor:
 
 
 def scaled_system(G: Graph, values: torch.Tensor):
-    """(s [n], scaled blocks [nnzb, 3, 3]) of S H S, s = (tr(H_ii)/3)^-1/2."""
+    """(s [n], d [n], scaled blocks [nnzb, 3, 3]) of S H S: d = tr(H_ii)/3,
+    s = d^-1/2 (1 where d is not positive and finite)."""
     Hd = values[G.diag]
     d = (Hd[:, 0, 0] + Hd[:, 1, 1] + Hd[:, 2, 2]) / 3.0
     ok = torch.isfinite(d) & (d > 0)
@@ -319,7 +320,7 @@ def train(meshes, pairs: int = 2000, r_per_system: int = 8, epochs: int = 12, se
             lv = loss(net, G, vals, vst, rhs, r_per_system, gen)
             lv.backward()
             opt.step()
-            tot += float(lv)
+            tot += float(lv.detach())
         sched.step()
         log(f"epoch {ep}: loss {tot / len(systems):.4f}")
     return net.cpu()

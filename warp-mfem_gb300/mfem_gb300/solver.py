@@ -48,9 +48,12 @@ class MixedFEMSolver:
     corrections.
 
     ``preconditioner`` is the reference's flag (True: block-Jacobi, False:
-    none) or "fsai": a factorized sparse approximate inverse M = G^T G with G
+    none), "fsai": a factorized sparse approximate inverse M = G^T G with G
     lower block-triangular on H's block pattern, recomputed after every
-    assembly and applied by the global-memory PCG (fp32 solve only).
+    assembly, or "learned": M = L L^T with L written by the factor net
+    (``factor_net``; parameters ``factor_net_params`` or the shipped
+    weights).  Both factor forms run the global-memory PCG (fp32 solve
+    only).
     """
 
     def __init__(self, model: Model, iterations: int, max_tets: Optional[int] = None,
@@ -85,9 +88,9 @@ class MixedFEMSolver:
         cfg.preconditioner_singular_threshold = float(kwargs.get("preconditioner_singular_threshold", 1.0e-20))
         pc = kwargs.get("preconditioner", True)
         if isinstance(pc, str):
-            if pc not in ("block_jacobi", "fsai"):
+            if pc not in _lib.PRECONDITIONER:
                 raise ValueError(f"unknown preconditioner {pc!r}")
-            cfg.preconditioner = 2 if pc == "fsai" else 1
+            cfg.preconditioner = _lib.PRECONDITIONER[pc]
         else:
             cfg.preconditioner = 1 if pc else 0
         cfg.use_cuda_graph = 1 if kwargs.get("use_cuda_graph", True) else 0
@@ -129,6 +132,8 @@ class MixedFEMSolver:
         self.n_contact_tris = 0
         if getattr(model, "shape_count", 0) > 0:
             self._set_contact(model, kwargs)
+        if cfg.preconditioner == _lib.PRECONDITIONER["learned"]:
+            self.set_factor_net(kwargs.get("factor_net_params"))
         self.solver_precision = kwargs.get("solver_precision", "fp32")
         if self.solver_precision not in _lib.PRECISION:
             raise ValueError(f"Unknown solver_precision {self.solver_precision!r}")
@@ -140,6 +145,23 @@ class MixedFEMSolver:
             scfg.outer_tolerance = float(kwargs.get("outer_tolerance", 1.0e-8))
             scfg.outer_max_iterations = int(kwargs.get("outer_max_iterations", 10))
             _lib.check(self._lib.mfem_plan_set_solver(self._plan, ctypes.byref(scfg)), self._plan)
+
+    def set_factor_net(self, params=None, vertex_offsets=None) -> None:
+        """Loads the learned preconditioner's parameters (packed float32,
+        ``factor_net.LAYOUT``; None: the weights shipped with the package)
+        and the static vertex inputs of the model (per-body centroids for
+        ``vertex_offsets``)."""
+        from . import factor_net
+        if params is None:
+            params = factor_net.load_weights()
+        params = np.ascontiguousarray(params, dtype=np.float32).reshape(-1)
+        h = self._host
+        vs = np.ascontiguousarray(factor_net.static_features(
+            h["rest"], h["tets"].reshape(-1, 4), h["materials"].reshape(-1, 3), vertex_offsets), dtype=np.float32)
+        self._factor_net = (params, vs)  # kept alive while the call copies them
+        _lib.check(self._lib.mfem_plan_set_factor_net(self._plan, params.ctypes.data_as(ctypes.c_void_p),
+                                                      params.size, vs.ctypes.data_as(ctypes.c_void_p)),
+                   self._plan)
 
     def _set_contact(self, model, kwargs) -> None:
         """Contact against the model's shapes (Contact.__init__,
