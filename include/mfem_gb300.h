@@ -347,11 +347,14 @@ int mfem_plan_set_bodies(mfem_plan *plan, int32_t n_bodies, const int32_t *h_ver
 int mfem_plan_batch_layout(const mfem_plan *plan, int32_t *ctas, int32_t *threads);
 
 /* Solves the system at d_q (at rest) once to learn each body's PCG
- * iterations, then times the batched PCG for each candidate schedule
- * (threads per CTA 128/256/512 x three costs of a group barrier; bodies get
- * CTA groups while that shortens the longest modelled body time, iterations x
- * blocks per CTA) and keeps the fastest; *h_best_ms receives its solve time.
- * Synchronises the stream. */
+ * iterations, then times the batched PCG for each distinct candidate
+ * schedule (threads per CTA 128/256/512 x three costs of a group barrier,
+ * and for one body x five caps on its group's CTAs, from unbounded to a
+ * quarter of the SMs; bodies
+ * get CTA groups while that shortens the longest modelled body time,
+ * iterations x blocks per CTA) and keeps the fastest; *h_best_ms receives its
+ * solve time.  Also serves a one-body plan (a mesh too large for the
+ * persistent PCG, or a factor preconditioner).  Synchronises the stream. */
 int mfem_plan_autotune_batch(mfem_plan *plan, const float *d_q, float dt, double *h_best_ms, mfem_stream stream);
 
 /* Per-body PCG outcomes of the last step, [iteration][body] (synchronises

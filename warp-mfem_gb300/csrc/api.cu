@@ -2,6 +2,7 @@
 // buffer/diagnostic accessors declared in include/mfem_gb300.h.
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -64,6 +65,8 @@ struct mfem_plan {
     // independent bodies (mfem_plan_set_bodies): per-body PCGs in one launch
     BatchViews bw{};
     std::vector<void *> batch_allocs;
+    int bw_max_group = INT_MAX;  // the schedule's group cap and barrier cost
+    double bw_c0 = 2048.0;
     // the learned factor net (preconditioner 3)
     FactorNetViews fv{};
     std::vector<void *> net_allocs;
@@ -253,7 +256,7 @@ cudaError_t run_step(mfem_plan *p, const float *q_in, const float *qd_in, float 
 // CTAs are left and that shortens it.  With more bodies than CTAs, bodies are
 // dealt to CTAs largest first onto the least-loaded CTA (each alone).
 void batch_schedule(const std::vector<int32_t> &nnzb, const std::vector<int32_t> &its, int capacity, double c0,
-                    std::vector<int> &task_ptr, std::vector<int4> &tasks, int &ctas) {
+                    int max_group, std::vector<int> &task_ptr, std::vector<int4> &tasks, int &ctas) {
     const int B = (int)nnzb.size();
     task_ptr.clear();
     tasks.clear();
@@ -271,7 +274,9 @@ void batch_schedule(const std::vector<int32_t> &nnzb, const std::vector<int32_t>
             std::pop_heap(heap.begin(), heap.end());
             auto [t, b] = heap.back();
             heap.pop_back();
-            const double t1 = model(b, g[b] + 1);
+            // a group's barrier serialises its arrivals: groups stay at most
+            // max_group CTAs
+            const double t1 = g[b] < max_group ? model(b, g[b] + 1) : t;
             if (!(t1 < t)) break;  // the critical body gains nothing from another CTA
             ++g[b];
             --spare;
@@ -1117,16 +1122,16 @@ namespace {
 // Uploads a schedule for `threads` threads per CTA and a group-barrier cost
 // of `c0` block products (batch_schedule), with the plan's iteration
 // estimates per body.
-int apply_batch_layout(mfem_plan *p, int threads, double c0) {
+int apply_batch_layout(mfem_plan *p, int threads, double c0, int max_group) {
     int capacity = 0;
-    cudaError_t e = batch_capacity(p->device, threads, &capacity);
+    cudaError_t e = batch_capacity(p->device, threads, p->cfg.preconditioner >= 2, &capacity);
     if (e != cudaSuccess) return cuda_fail(p, e, "batch capacity");
     if (capacity < 1) return fail(p, MFEM_CUDA_ERROR, "the batched PCG does not fit on an SM");
     std::vector<int> task_ptr;
     std::vector<int4> tasks;
     int ctas = 0;
     if (p->h_body_its.size() != p->h_body_nnzb.size()) p->h_body_its.assign(p->h_body_nnzb.size(), 1);
-    batch_schedule(p->h_body_nnzb, p->h_body_its, capacity, c0, task_ptr, tasks, ctas);
+    batch_schedule(p->h_body_nnzb, p->h_body_its, capacity, c0, std::max(1, max_group), task_ptr, tasks, ctas);
     // the previous schedule's arrays: every caller has synchronised the
     // device, so no launch still reads them
     for (void *a : p->layout_allocs) cudaFree(a);
@@ -1151,6 +1156,8 @@ int apply_batch_layout(mfem_plan *p, int threads, double c0) {
     p->bw.partials = partials;
     p->bw.ctas = ctas;
     p->bw.threads = threads;
+    p->bw_max_group = max_group;
+    p->bw_c0 = c0;
     return MFEM_OK;
 }
 
@@ -1255,6 +1262,34 @@ int install_bodies(mfem_plan *p, int n_bodies, const int32_t *voff, const int32_
         alloc(&bw.Uval, nnzl * 9 * sizeof(float));
         alloc(&bw.y, n3 * sizeof(float));
         alloc(&bw.dx0, n3 * sizeof(float));
+        if (p->cfg.preconditioner == 2) {
+            // the H slot of every pair of a row's lower columns (FSAI setup)
+            std::vector<int64_t> pptr(n + 1, 0);
+            std::vector<int32_t> pairs;
+            for (int r = 0; r < n; ++r) {
+                const int m = lrow[r + 1] - lrow[r];
+                if (m <= kFsaiMaxCols)
+                    for (int a = 0; a < m; ++a) {
+                        const int ca = lcol[lrow[r] + a];
+                        const int32_t *b0 = p->h_col_idx.data() + p->h_row_ptr[ca];
+                        const int32_t *b1 = p->h_col_idx.data() + p->h_row_ptr[ca + 1];
+                        for (int b = 0; b <= a; ++b) {
+                            const int32_t *q = std::lower_bound(b0, b1, lcol[lrow[r] + b]);
+                            pairs.push_back(q != b1 && *q == lcol[lrow[r] + b] ? (int32_t)(q - p->h_col_idx.data())
+                                                                               : -1);
+                        }
+                    }
+                pptr[r + 1] = (int64_t)pairs.size();
+            }
+            int64_t *d_pptr = nullptr;
+            int *d_pairs = nullptr;
+            alloc(&d_pptr, pptr.size() * sizeof(int64_t));
+            alloc(&d_pairs, pairs.size() * sizeof(int));
+            if (e == cudaSuccess) e = upload(d_pptr, pptr.data(), pptr.size());
+            if (e == cudaSuccess) e = upload(d_pairs, pairs.data(), pairs.size());
+            bw.fsai_pair_ptr = d_pptr;
+            bw.fsai_pairs = d_pairs;
+        }
         if (e == cudaSuccess) e = upload(d_lrow, lrow.data(), lrow.size());
         if (e == cudaSuccess) e = upload(d_urow, urow.data(), urow.size());
         if (e == cudaSuccess) e = upload(d_lcol, lcol.data(), nnzl);
@@ -1286,7 +1321,12 @@ int install_bodies(mfem_plan *p, int n_bodies, const int32_t *voff, const int32_
     p->tv.energy_code = ecode;
     p->vv.vertex_body = vbody;
     p->vv.body_gravity = grav;
-    const int rc = apply_batch_layout(p, 256, 2048.0);
+    // one body: one 512-thread CTA per SM, like the persistent PCG; many
+    // bodies: the work-weighted schedule, groups as large as helps
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
+    const int rc = n_bodies == 1 ? apply_batch_layout(p, 512, 2048.0, std::max(1, sms))
+                                 : apply_batch_layout(p, 256, 2048.0, INT_MAX);
     if (rc != MFEM_OK) {
         for (void *a : p->batch_allocs) cudaFree(a);
         p->batch_allocs.clear();
@@ -1498,45 +1538,74 @@ int mfem_plan_autotune_batch(mfem_plan *p, const float *d_q, float dt, double *h
     }
     const int threads_opts[3] = {128, 256, 512};
     const double c0_opts[3] = {512.0, 2048.0, 8192.0};
-    int best_t = 256;
-    double best_m = 2048.0;
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
+    // group caps for one body: unbounded, and 2, 1, 1/2 and 1/4 CTAs per
+    // SM; many bodies keep unbounded groups (a capped schedule timed best on
+    // the tuning system but not along trajectories)
+    const int group_opts[5] = {INT_MAX, 2 * sms, sms, std::max(1, sms / 2), std::max(1, sms / 4)};
+    const int n_caps = p->bw.n_bodies == 1 ? 5 : 1;
+    int best_t = p->bw.threads, best_g = p->bw_max_group;
+    double best_m = p->bw_c0;
     float best = 1e30f;
-    for (int ti = 0; e == cudaSuccess && ti < 3; ++ti)
-        for (int mi = 0; e == cudaSuccess && mi < 3; ++mi) {
-            const int rc = apply_batch_layout(p, threads_opts[ti], c0_opts[mi]);
-            if (rc != MFEM_OK) {
-                e = cudaErrorUnknown;
-                break;
-            }
-            float ms = 0.0f;
-            int flag = 0;
-            for (int rep = 0; e == cudaSuccess && rep < 2; ++rep) {
-                e = cudaMemcpyAsync(p->vv.dx, dx0, bytes, cudaMemcpyDeviceToDevice, s);
-                if (e == cudaSuccess) e = cudaEventRecord(e0, s);
-                if (e == cudaSuccess) e = global_solve(p, 0, s);
-                if (e == cudaSuccess) e = cudaEventRecord(e1, s);
-                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-            }
-            if (e == cudaSuccess) e = cudaMemcpy(&flag, p->pw.error, sizeof(int), cudaMemcpyDeviceToHost);
-            if (e == cudaSuccess && flag) {
-                // a wait gave up: this schedule is not a candidate
-                e = cudaMemset(p->pw.error, 0, sizeof(int));
-                continue;
-            }
-            if (e == cudaSuccess && ms < best) {
-                best = ms;
-                best_t = threads_opts[ti];
-                best_m = c0_opts[mi];
-            }
+    std::vector<std::vector<int4>> tried;
+    for (int cand = 0; e == cudaSuccess && cand < 3 * 3 * n_caps; ++cand) {
+        const int threads = threads_opts[cand / (3 * n_caps)], cap = group_opts[cand % n_caps];
+        const double c0 = c0_opts[(cand / n_caps) % 3];
+        // skip a schedule already timed (c0 and the cap often do not change it)
+        int capacity = 0;
+        if (batch_capacity(p->device, threads, p->cfg.preconditioner >= 2, &capacity) != cudaSuccess ||
+            capacity < 1)
+            continue;
+        std::vector<int> tp;
+        std::vector<int4> tk;
+        int nc = 0;
+        batch_schedule(p->h_body_nnzb, p->h_body_its, capacity, c0, cap, tp, tk, nc);
+        tk.push_back(make_int4(threads, nc, 0, 0));
+        bool seen = false;
+        for (const auto &t : tried) {
+            seen = t.size() == tk.size();
+            for (size_t q = 0; seen && q < t.size(); ++q)
+                seen = t[q].x == tk[q].x && t[q].y == tk[q].y && t[q].z == tk[q].z && t[q].w == tk[q].w;
+            if (seen) break;
         }
+        if (seen) continue;
+        tried.push_back(std::move(tk));
+        const int rc = apply_batch_layout(p, threads, c0, cap);
+        if (rc != MFEM_OK) {
+            e = cudaErrorUnknown;
+            break;
+        }
+        float ms = 0.0f;
+        int flag = 0;
+        for (int rep = 0; e == cudaSuccess && rep < 2; ++rep) {
+            e = cudaMemcpyAsync(p->vv.dx, dx0, bytes, cudaMemcpyDeviceToDevice, s);
+            if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+            if (e == cudaSuccess) e = global_solve(p, 0, s);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        }
+        if (e == cudaSuccess) e = cudaMemcpy(&flag, p->pw.error, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && flag) {
+            // a wait gave up: this schedule is not a candidate
+            e = cudaMemset(p->pw.error, 0, sizeof(int));
+            continue;
+        }
+        if (e == cudaSuccess && ms < best) {
+            best = ms;
+            best_t = threads;
+            best_m = c0;
+            best_g = cap;
+        }
+    }
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     if (x) cudaFree(x);
     if (dx0) cudaFree(dx0);
     if (e != cudaSuccess) return cuda_fail(p, e, "autotune");
     drop_graphs(p);
-    const int rc = apply_batch_layout(p, best_t, best_m);
+    const int rc = apply_batch_layout(p, best_t, best_m, best_g);
     if (rc == MFEM_OK && h_best_ms) *h_best_ms = best;
     return rc;
 }

@@ -176,45 +176,50 @@ __global__ void __launch_bounds__(kNetThreads) fn_mp_kernel(BsrViews bv, FactorN
     const int tiles = (bv.n + 15) / 16;
     for (int tile = blockIdx.x * kNetWarps + wid; tile < tiles; tile += gridDim.x * kNetWarps) {
         const int base = tile * 16;
-        // rows [h_i, a_i] in BF16; a lane owns channels 2 lane, 2 lane + 1
-        for (int r = 0; r < 16; ++r) {
-            const int i = base + r;
-            uint32_t hpair = 0u, apair = 0u;
+        // rows [h_i, a_i] in BF16: a quarter-warp per vertex (four at a
+        // time), a lane owns 8 channels and gathers them with 16-byte loads
+        const int quarter = lane >> 3, ql = lane & 7;
+        for (int r0 = 0; r0 < 16; r0 += 4) {
+            const int r = r0 + quarter, i = base + r;
+            uint4 hq = make_uint4(0u, 0u, 0u, 0u), aq = hq;
             if (i < bv.n) {
-                hpair = ld_u32(hin + (size_t)kNetWidth * i + 2 * lane);
-                float a0 = 0.0f, a1 = 0.0f;
+                hq = *reinterpret_cast<const uint4 *>(hin + (size_t)kNetWidth * i + 8 * ql);
+                float a[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) a[q] = 0.0f;
                 const int kb = bv.row_ptr[i], ke = bv.row_ptr[i + 1];
                 int k = kb;
-                for (; k + 4 <= ke; k += 4) {
-                    int c[4];
-                    float wk[4];
-                    uint32_t v[4];
+                for (; k + 2 <= ke; k += 2) {
+                    const int c0 = __ldg(bv.col_idx + k), c1 = __ldg(bv.col_idx + k + 1);
+                    const float w0 = __ldg(fv.w + k), w1 = __ldg(fv.w + k + 1);
+                    const uint4 v0 = *reinterpret_cast<const uint4 *>(hin + (size_t)kNetWidth * c0 + 8 * ql);
+                    const uint4 v1 = *reinterpret_cast<const uint4 *>(hin + (size_t)kNetWidth * c1 + 8 * ql);
+                    const uint32_t u0[4] = {v0.x, v0.y, v0.z, v0.w}, u1[4] = {v1.x, v1.y, v1.z, v1.w};
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        c[u] = __ldg(bv.col_idx + k + u);
-                        wk[u] = __ldg(fv.w + k + u);
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) v[u] = ld_u32(hin + (size_t)kNetWidth * c[u] + 2 * lane);
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const float2 f = unpack_bf16(v[u]);
-                        a0 = fmaf(wk[u], f.x, a0);
-                        a1 = fmaf(wk[u], f.y, a1);
+                    for (int q = 0; q < 4; ++q) {
+                        const float2 f0 = unpack_bf16(u0[q]), f1 = unpack_bf16(u1[q]);
+                        a[2 * q] = fmaf(w1, f1.x, fmaf(w0, f0.x, a[2 * q]));
+                        a[2 * q + 1] = fmaf(w1, f1.y, fmaf(w0, f0.y, a[2 * q + 1]));
                     }
                 }
-                for (; k < ke; ++k) {
-                    const int c = __ldg(bv.col_idx + k);
-                    const float wk = __ldg(fv.w + k);
-                    const float2 f = unpack_bf16(ld_u32(hin + (size_t)kNetWidth * c + 2 * lane));
-                    a0 = fmaf(wk, f.x, a0);
-                    a1 = fmaf(wk, f.y, a1);
+                if (k < ke) {
+                    const int c0 = __ldg(bv.col_idx + k);
+                    const float w0 = __ldg(fv.w + k);
+                    const uint4 v0 = *reinterpret_cast<const uint4 *>(hin + (size_t)kNetWidth * c0 + 8 * ql);
+                    const uint32_t u0[4] = {v0.x, v0.y, v0.z, v0.w};
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const float2 f0 = unpack_bf16(u0[q]);
+                        a[2 * q] = fmaf(w0, f0.x, a[2 * q]);
+                        a[2 * q + 1] = fmaf(w0, f0.y, a[2 * q + 1]);
+                    }
                 }
                 const float wi = fv.winv[i];
-                apair = pack_bf16(a0 * wi, a1 * wi);
+                aq = make_uint4(pack_bf16(a[0] * wi, a[1] * wi), pack_bf16(a[2] * wi, a[3] * wi),
+                                pack_bf16(a[4] * wi, a[5] * wi), pack_bf16(a[6] * wi, a[7] * wi));
             }
-            st_u32(A + r * kMpLd + 2 * lane, hpair);
-            st_u32(A + r * kMpLd + kNetWidth + 2 * lane, apair);
+            *reinterpret_cast<uint4 *>(A + r * kMpLd + 8 * ql) = hq;
+            *reinterpret_cast<uint4 *>(A + r * kMpLd + kNetWidth + 8 * ql) = aq;
         }
         __syncwarp();
         float acc[8][4];
@@ -400,9 +405,11 @@ __global__ void __launch_bounds__(kNetThreads) fn_edge_kernel(BsrViews bv, Batch
     }
 }
 
+// CTAs for `tiles` warp tiles: the kernels stride over tiles, so the grid
+// is only bounded (a few waves of the GPU's resident CTAs)
 int grid_for(int tiles, int per_cta) {
     const int ctas = (tiles + per_cta - 1) / per_cta;
-    return std::max(1, std::min(ctas, 152 * 8));
+    return std::max(1, std::min(ctas, 1 << 14));
 }
 
 }  // namespace

@@ -85,11 +85,15 @@ __global__ void __launch_bounds__(kFsaiThreads) fsai_setup_kernel(BsrViews bv, B
     const int S = N | 1;  // odd row stride: the rows lanes own fall in distinct banks
     bool ok = m >= 1 && m <= kFsaiMaxCols;
     if (ok) {
-        // A = H[P, P], lower block triangle
-        for (int t = lane; t < m * m; t += 32) {
-            const int a = t / m, b = t - a * m;
-            if (b > a) continue;
-            const int s = find_slot(bv.row_ptr, bv.col_idx, cols[a], cols[b]);
+        // A = H[P, P], lower block triangle; pair (a, b), b <= a, is entry
+        // a (a + 1) / 2 + b of the row's precomputed slot list
+        const int *pslot = bw.fsai_pairs + bw.fsai_pair_ptr[row];
+        for (int t = lane; t < m * (m + 1) / 2; t += 32) {
+            int a = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+            while (a * (a + 1) / 2 > t) --a;
+            while ((a + 1) * (a + 2) / 2 <= t) ++a;
+            const int b = t - a * (a + 1) / 2;
+            const int s = pslot[t];
 #pragma unroll
             for (int p = 0; p < 3; ++p)
 #pragma unroll
@@ -107,15 +111,25 @@ __global__ void __launch_bounds__(kFsaiThreads) fsai_setup_kernel(BsrViews bv, B
             const int r0 = j + lane, r1 = j + 32 + lane;
             if (r0 < N) {
                 const float *lr = A + r0 * S;
-                float acc = lr[j];
-                for (int k = 0; k < j; ++k) acc = fmaf(-lr[k], lj[k], acc);
-                v0 = acc;
+                float acc = lr[j], acc2 = 0.0f;
+                int k = 0;
+                for (; k + 2 <= j; k += 2) {
+                    acc = fmaf(-lr[k], lj[k], acc);
+                    acc2 = fmaf(-lr[k + 1], lj[k + 1], acc2);
+                }
+                if (k < j) acc = fmaf(-lr[k], lj[k], acc);
+                v0 = acc + acc2;
             }
             if (r1 < N) {
                 const float *lr = A + r1 * S;
-                float acc = lr[j];
-                for (int k = 0; k < j; ++k) acc = fmaf(-lr[k], lj[k], acc);
-                v1 = acc;
+                float acc = lr[j], acc2 = 0.0f;
+                int k = 0;
+                for (; k + 2 <= j; k += 2) {
+                    acc = fmaf(-lr[k], lj[k], acc);
+                    acc2 = fmaf(-lr[k + 1], lj[k + 1], acc2);
+                }
+                if (k < j) acc = fmaf(-lr[k], lj[k], acc);
+                v1 = acc + acc2;
             }
             float d = __shfl_sync(0xffffffffu, v0, 0);
             if (!(d > 0.0f) || !isfinite(d)) {

@@ -101,6 +101,11 @@ struct BatchViews {
     float *Uval;               // [nnzl][9] F^T in upper-CSR order
     float *y;                  // [n][3] the first pass's output
     float *dx0;                // [n][3] warm start kept for a block-Jacobi retry
+    // FSAI setup: per row, the H slot (or -1) of every pair (a, b), b <= a,
+    // of the row's lower columns, a-major; rows with more than kFsaiMaxCols
+    // lower blocks have none
+    const int64_t *fsai_pair_ptr;  // [n + 1]
+    const int *fsai_pairs;
     int nnzl;
 };
 
@@ -313,7 +318,7 @@ cudaError_t ir_max_ctas(int device, int *ctas);
 cudaError_t launch_fsai_setup(const BsrViews &bv, const BatchViews &bw, cudaStream_t s);
 cudaError_t launch_factor_transpose(const BatchViews &bw, cudaStream_t s);
 cudaError_t launch_factor_net(const BsrViews &bv, const BatchViews &bw, const FactorNetViews &fv, cudaStream_t s);
-cudaError_t batch_capacity(int device, int threads, int *ctas);
+cudaError_t batch_capacity(int device, int threads, bool factor, int *ctas);
 cudaError_t launch_batched_pcg(const BsrViews &bv, const VertexViews &vv, const BatchViews &bw, int *error, int slot,
                                float tol, int maxiter, int use_precond, cudaStream_t s);
 int ir_residual_blocks(int n);

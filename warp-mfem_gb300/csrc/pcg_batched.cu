@@ -141,18 +141,27 @@ __device__ __forceinline__ void bt_row_product(const BsrViews &bv, int row, cons
     const unsigned gmask = ((1u << kBtGroup) - 1u) << (threadIdx.x & (32 - kBtGroup));
     const int kb = bv.row_ptr[row], ke = bv.row_ptr[row + 1];
     float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-    for (int k = kb + g_lane; k < ke; k += kBtGroup) {
-        const int c = __ldg(bv.col_idx + k);
-        float v[3];
+    // two blocks per lane and trip: their loads are in flight together
+    for (int k = kb + g_lane; k < ke; k += 2 * kBtGroup) {
+        const int k2 = k + kBtGroup;
+        const bool two = k2 < ke;
+        const int c = __ldg(bv.col_idx + k), c2 = two ? __ldg(bv.col_idx + k2) : c;
+        float v[3], v2[3];
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            const float zc = bt_ld<SHARED>(z + 3 * c + q);
+            const float zc = bt_ld<SHARED>(z + 3 * c + q), zc2 = bt_ld<SHARED>(z + 3 * c2 + q);
             v[q] = p_old ? __fmaf_rn(beta, bt_ld<SHARED>(p_old + 3 * c + q), zc) : zc;
+            v2[q] = p_old ? __fmaf_rn(beta, bt_ld<SHARED>(p_old + 3 * c2 + q), zc2) : zc2;
         }
+        if (!two) v2[0] = v2[1] = v2[2] = 0.0f;
         const float *h = bv.values + (size_t)9 * k;
+        const float *h2 = bv.values + (size_t)9 * (two ? k2 : k);
         a0 += __ldg(h + 0) * v[0] + __ldg(h + 1) * v[1] + __ldg(h + 2) * v[2];
         a1 += __ldg(h + 3) * v[0] + __ldg(h + 4) * v[1] + __ldg(h + 5) * v[2];
         a2 += __ldg(h + 6) * v[0] + __ldg(h + 7) * v[1] + __ldg(h + 8) * v[2];
+        a0 += __ldg(h2 + 0) * v2[0] + __ldg(h2 + 1) * v2[1] + __ldg(h2 + 2) * v2[2];
+        a1 += __ldg(h2 + 3) * v2[0] + __ldg(h2 + 4) * v2[1] + __ldg(h2 + 5) * v2[2];
+        a2 += __ldg(h2 + 6) * v2[0] + __ldg(h2 + 7) * v2[1] + __ldg(h2 + 8) * v2[2];
     }
 #pragma unroll
     for (int off = kBtGroup / 2; off > 0; off >>= 1) {
@@ -175,14 +184,24 @@ __device__ __forceinline__ void bt_factor_pass(const int *rp, const int *col, co
     const int group = threadIdx.x / kBtGroup, ngroups = blockDim.x / kBtGroup;
     for (int row = lo + group; row < hi; row += ngroups) {
         float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-        for (int k = __ldg(rp + row) + g_lane; k < __ldg(rp + row + 1); k += kBtGroup) {
-            const int c = __ldg(col + k);
+        const int ke = __ldg(rp + row + 1);
+        for (int k = __ldg(rp + row) + g_lane; k < ke; k += 2 * kBtGroup) {
+            const int k2 = k + kBtGroup;
+            const bool two = k2 < ke;
+            const int c = __ldg(col + k), c2 = two ? __ldg(col + k2) : c;
             const float v0 = bt_ld<SHARED>(in + 3 * c), v1 = bt_ld<SHARED>(in + 3 * c + 1),
                         v2 = bt_ld<SHARED>(in + 3 * c + 2);
+            float w0 = bt_ld<SHARED>(in + 3 * c2), w1 = bt_ld<SHARED>(in + 3 * c2 + 1),
+                  w2 = bt_ld<SHARED>(in + 3 * c2 + 2);
+            if (!two) w0 = w1 = w2 = 0.0f;
             const float *f = val + (size_t)9 * k;
+            const float *f2 = val + (size_t)9 * (two ? k2 : k);
             a0 += __ldg(f + 0) * v0 + __ldg(f + 1) * v1 + __ldg(f + 2) * v2;
             a1 += __ldg(f + 3) * v0 + __ldg(f + 4) * v1 + __ldg(f + 5) * v2;
             a2 += __ldg(f + 6) * v0 + __ldg(f + 7) * v1 + __ldg(f + 8) * v2;
+            a0 += __ldg(f2 + 0) * w0 + __ldg(f2 + 1) * w1 + __ldg(f2 + 2) * w2;
+            a1 += __ldg(f2 + 3) * w0 + __ldg(f2 + 4) * w1 + __ldg(f2 + 5) * w2;
+            a2 += __ldg(f2 + 6) * w0 + __ldg(f2 + 7) * w1 + __ldg(f2 + 8) * w2;
         }
 #pragma unroll
         for (int off = kBtGroup / 2; off > 0; off >>= 1) {
@@ -236,6 +255,10 @@ struct BtScalars {
     int status, done;
 };
 
+// FACTOR: the instantiation for the factor preconditioners (use_precond 2
+// or 3, with the block-Jacobi retry); the other one, for use_precond 0 or 1,
+// carries none of that code (fewer registers, more resident CTAs).
+template <bool FACTOR>
 __global__ void __launch_bounds__(kBtMaxThreads)
     batched_pcg_kernel(BsrViews bv, VertexViews vv, BatchViews bw, int *error, int slot, float tol, int maxiter,
                        int use_precond) {
@@ -266,7 +289,7 @@ __global__ void __launch_bounds__(kBtMaxThreads)
         unsigned k = 0;
         int mode = use_precond, it = 0, it_done = 0;
         bool timed_out = false;
-        if (mode >= 2)  // the warm start, for a block-Jacobi retry
+        if (FACTOR && mode >= 2)  // the warm start, for a block-Jacobi retry
             for (int t3 = 3 * lo + threadIdx.x; t3 < 3 * hi; t3 += blockDim.x) bw.dx0[t3] = vv.dx[t3];
         for (;;) {  // one attempt; a factor solve that breaks down is retried with block-Jacobi
             it = 0;
@@ -280,7 +303,7 @@ __global__ void __launch_bounds__(kBtMaxThreads)
                     for (int q = 0; q < 3; ++q) bw.r[3 * row + q] = vv.rhs[3 * row + q] - y[q];
             }
             __syncthreads();
-            const bool factor = mode >= 2;  // a factor preconditioner
+            const bool factor = FACTOR && mode >= 2;  // a factor preconditioner
             // every row's r must be in place before the factor's first pass gathers it
             if (factor && !(bt_sync(bw, tk, error, k, target, s_tot, s_redf, &s_ok) &&
                           bt_apply_factor(bw, mode, tk, lo, hi, error, k, target, s_tot, s_redf, &s_ok))) {
@@ -424,7 +447,7 @@ __global__ void __launch_bounds__(kBtMaxThreads)
                 }
                 __syncthreads();
             }
-            if (mode >= 2 && (sc.status == MFEM_STAGNATION || sc.status == MFEM_NONFINITE)) {
+            if (FACTOR && mode >= 2 && (sc.status == MFEM_STAGNATION || sc.status == MFEM_NONFINITE)) {
                 for (int t3 = 3 * lo + threadIdx.x; t3 < 3 * hi; t3 += blockDim.x) vv.dx[t3] = bw.dx0[t3];
                 // every row's warm start is back before the retry's product reads it
                 if (!bt_sync(bw, tk, error, k, target, s_tot, s_redf, &s_ok)) {
@@ -447,10 +470,12 @@ __global__ void __launch_bounds__(kBtMaxThreads)
 
 }  // namespace
 
-cudaError_t batch_capacity(int device, int threads, int *ctas) {
+cudaError_t batch_capacity(int device, int threads, bool factor, int *ctas) {
     int sms = 0, occ = 0;
     cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_pcg_kernel, threads, 0);
+    if (e == cudaSuccess)
+        e = factor ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_pcg_kernel<true>, threads, 0)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_pcg_kernel<false>, threads, 0);
     if (e != cudaSuccess) return e;
     *ctas = sms * std::max(occ, 0);
     return cudaSuccess;
@@ -467,7 +492,11 @@ cudaError_t launch_batched_pcg(const BsrViews &bv, const VertexViews &vv, const 
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e = cudaLaunchKernelEx(&cfg, batched_pcg_kernel, bv, vv, bw, error, slot, tol, maxiter, use_precond);
+    cudaError_t e = use_precond >= 2
+                        ? cudaLaunchKernelEx(&cfg, batched_pcg_kernel<true>, bv, vv, bw, error, slot, tol, maxiter,
+                                             use_precond)
+                        : cudaLaunchKernelEx(&cfg, batched_pcg_kernel<false>, bv, vv, bw, error, slot, tol, maxiter,
+                                             use_precond);
     count_launches(1);
     return e;
 }

@@ -206,6 +206,18 @@ class MixedFEMSolver:
         _lib.check(self._lib.mfem_set_body_poses(self._plan, ctypes.c_void_p(body_q.data_ptr()), self.n_bodies,
                                                  _stream_handle(self.device)), self._plan)
 
+    def autotune(self, q: torch.Tensor, dt: float) -> float:
+        """For a plan on the global-memory PCG (a factor preconditioner, or a
+        mesh too large for the persistent PCG): picks the fastest schedule
+        on the system at q (at rest); returns that solve's time in ms."""
+        if self.pcg_layout()["variant"] != "global_memory":
+            raise ValueError("autotune serves plans on the global-memory PCG")
+        best = ctypes.c_double()
+        _lib.check(self._lib.mfem_plan_autotune_batch(self._plan, ctypes.c_void_p(self._check_state(q, "q")),
+                                                      float(dt), ctypes.byref(best), _stream_handle(self.device)),
+                   self._plan)
+        return best.value
+
     def pcg_layout(self) -> dict:
         """The persistent PCG this plan uses (variant, CTAs, matrix cached in
         shared memory, dynamic shared memory per CTA)."""
