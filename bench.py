@@ -59,6 +59,8 @@ def parse_args():
     ap.add_argument("--preconditioner", default="block_jacobi", choices=["block_jacobi", "fsai", "learned"],
                     help="PCG preconditioner: the workload's block-Jacobi, or the FSAI / learned factor "
                          "(global-memory PCG)")
+    ap.add_argument("--factor-refresh", type=int, default=1,
+                    help="factor preconditioners: recompute the factor every this many Newton iterations")
     ap.add_argument("--line-search", action="store_true",
                     help="run the workload with the reference's backtracking line search")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -255,7 +257,7 @@ def run_batched(args, rank, world, local_rank):
     batch = beams.batched_bodies(B, seed=4)
     u = batch.union
     fsai = args.preconditioner in ("fsai", "learned")  # a factor preconditioner
-    bs = BatchedSolver(batch, device=dev, preconditioner=args.preconditioner)
+    bs = BatchedSolver(batch, device=dev, preconditioner=args.preconditioner, factor_refresh=args.factor_refresh)
     tune_ms = bs.autotune()
     layout = bs.layout()
     s_init = bs.solver.tet_stretch.clone().reshape(-1)
@@ -406,6 +408,7 @@ def run_batched(args, rank, world, local_rank):
                                 f"Pa, nu~U[0.3, 0.48], gravity on the unit sphere, x = 0 face pinned; "
                                 f"{u.T} tets, {u.n} vertices; 8 local/global iterations, per-body "
                                 f"{args.preconditioner} fp32 PCG to 1e-6"),
+                   "preconditioner": args.preconditioner, "factor_refresh": args.factor_refresh,
                    "bodies": B, "tets": u.T, "vertices": u.n, "pcg_schedule": layout,
                    "autotune_best_solve_ms": tune_ms, "parallelism": "replicas",
                    "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write, outside the timed events)"},
@@ -476,6 +479,7 @@ def run_gb300(args, rank, world, local_rank):
                             pcg_ctas=args.pcg_ctas, pcg_variant=args.pcg_variant,
                             # the workload is the plain local/global step unless asked
                             line_search=args.line_search, preconditioner=args.preconditioner,
+                            factor_refresh=args.factor_refresh,
                             solver_precision=args.precision, outer_tolerance=args.outer_tolerance)
     s_init = solver.tet_stretch.clone().reshape(-1)
     lam0 = torch.zeros_like(s_init)
@@ -645,6 +649,7 @@ def run_gb300(args, rank, world, local_rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(mesh, {"line_search": bool(args.line_search),
                                          "preconditioner": args.preconditioner,
+                                         "factor_refresh": args.factor_refresh,
                                          "global_memory_autotune_ms": tune_ms}, precision=args.precision,
                                   outer_tolerance=args.outer_tolerance),
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,

@@ -159,7 +159,12 @@ typedef struct mfem_solver_config {
     int32_t precision;              /* mfem_precision                                   */
     float inner_tolerance;          /* inner PCG: ||r|| <= tol ||rhs||, default 1e-3     */
     int32_t outer_max_iterations;   /* corrections per solve, default 10                */
-    int32_t reserved0;
+    int32_t factor_refresh;         /* preconditioners 2 and 3 (FP32 solve): recompute the
+                                       factor at the Newton iterations it of a step with
+                                       it % factor_refresh == 0 and reuse it in between
+                                       (an older factor still gives an SPD M); 0 or 1:
+                                       every assembly.  Staged mfem_assemble calls always
+                                       recompute it                                      */
     double outer_tolerance;         /* fp64 ||g - H dx|| <= tol ||g||, default 1e-8     */
     int32_t reserved[4];
 } mfem_solver_config;

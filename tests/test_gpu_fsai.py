@@ -193,3 +193,22 @@ def test_step_stats_report_the_global_memory_solve():
     mesh, _, solver = make("nh_beam", (16, 4, 4), preconditioner="fsai")
     st = one_solve(mesh, solver)
     assert st["status"] == _lib.MFEM_OK and st["iterations"] > 0 and 0.0 < st["rel_residual"] <= 1e-6, st
+
+
+@pytest.mark.parametrize("pc", ["fsai", "learned"])
+def test_lagged_factor_matches_the_oracle(pc):
+    """factor_refresh=8: one factor per step, reused by its eight solves."""
+    mesh, model, solver = make("nh_beam", (16, 4, 4), preconditioner=pc, factor_refresh=8)
+    ref = O.OracleSolver(mesh, dtype=np.float64)
+    A, B = model.state(), model.state()
+    A.particle_q.copy_(torch.as_tensor(mesh.q0, device=DEV))
+    q, qd = mesh.q0, mesh.qd0
+    for _ in range(2):
+        solver.step(A, B, None, None, mesh.spec.dt)
+        A, B = B, A
+        q, qd = ref.step(q, qd, mesh.spec.dt)
+        assert all(s["status"] == _lib.MFEM_OK and s["iterations"] > 0 for s in solver.solve_stats())
+        got = A.particle_q.cpu().numpy().astype(np.float64)
+        assert np.abs(got - q).max() <= 1e-5 * np.abs(q).max()
+    with pytest.raises(_lib.MfemError):
+        make("nh_beam", (4, 2, 2), preconditioner=pc, factor_refresh=-1)

@@ -65,6 +65,7 @@ struct mfem_plan {
     // independent bodies (mfem_plan_set_bodies): per-body PCGs in one launch
     BatchViews bw{};
     std::vector<void *> batch_allocs;
+    int factor_refresh = 1;      // recompute a factor preconditioner every this many Newton iterations
     int bw_max_group = INT_MAX;  // the schedule's group cap and barrier cost
     double bw_c0 = 2048.0;
     // the learned factor net (preconditioner 3)
@@ -223,14 +224,16 @@ cudaError_t local_update(mfem_plan *p, float *x, float dt, int slot, cudaStream_
 
 // Contact terms at x, then the assembly (Contact.evaluate runs in
 // _update_system, solver.py:637; it needs dt for the friction threshold).
-cudaError_t contact_and_assemble(mfem_plan *p, const float *x, float dt, cudaStream_t s) {
+cudaError_t contact_and_assemble(mfem_plan *p, const float *x, float dt, cudaStream_t s, bool factor_setup = true) {
     cudaError_t err = launch_contact(x, dt, p->cv, p->vv, s);
     if (err == cudaSuccess)
         err = launch_assemble(x, dt, p->cfg.preconditioner_singular_threshold, p->cfg.preconditioner, p->tv, p->vv,
                               p->bv, p->cv, s);
-    if (err == cudaSuccess && p->cfg.preconditioner == 2) err = launch_fsai_setup(p->bv, p->bw, s);
-    if (err == cudaSuccess && p->cfg.preconditioner == 2) err = launch_factor_transpose(p->bw, s);
-    if (err == cudaSuccess && p->cfg.preconditioner == 3) err = launch_factor_net(p->bv, p->bw, p->fv, s);
+    if (factor_setup) {
+        if (err == cudaSuccess && p->cfg.preconditioner == 2) err = launch_fsai_setup(p->bv, p->bw, s);
+        if (err == cudaSuccess && p->cfg.preconditioner == 2) err = launch_factor_transpose(p->bw, s);
+        if (err == cudaSuccess && p->cfg.preconditioner == 3) err = launch_factor_net(p->bv, p->bw, p->fv, s);
+    }
     return err;
 }
 
@@ -241,7 +244,7 @@ cudaError_t run_step(mfem_plan *p, const float *q_in, const float *qd_in, float 
     if (err == cudaSuccess) err = launch_contact_begin(p->cv, p->vv, s);
     for (int it = 0; err == cudaSuccess && it < p->cfg.iterations; ++it) {
         err = launch_element(q_out, p->cfg.energy, p->tv, s);
-        if (err == cudaSuccess) err = contact_and_assemble(p, q_out, dt, s);
+        if (err == cudaSuccess) err = contact_and_assemble(p, q_out, dt, s, it % p->factor_refresh == 0);
         if (err == cudaSuccess) err = global_solve(p, it, s);
         if (err == cudaSuccess) err = local_update(p, q_out, dt, it, s);
     }
@@ -1013,6 +1016,7 @@ void mfem_solver_config_default(mfem_solver_config *cfg) {
     cfg->precision = MFEM_PRECISION_FP32;
     cfg->inner_tolerance = 1.0e-3f;
     cfg->outer_max_iterations = 10;
+    cfg->factor_refresh = 1;
     cfg->outer_tolerance = 1.0e-8;
 }
 
@@ -1044,6 +1048,8 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
     for (void *a : p->ir_allocs) cudaFree(a);
     p->ir_allocs.clear();
     p->ir = IrWork{};
+    if (cfg.factor_refresh < 0) return fail(p, MFEM_BAD_ARG, "factor_refresh must be >= 0");
+    p->factor_refresh = std::max(1, cfg.factor_refresh);
     if (cfg.precision == MFEM_PRECISION_FP32) return MFEM_OK;
 
     const size_t n3 = (size_t)p->n * 3, nz = (size_t)p->nnzb;
@@ -1281,14 +1287,22 @@ int install_bodies(mfem_plan *p, int n_bodies, const int32_t *voff, const int32_
                     }
                 pptr[r + 1] = (int64_t)pairs.size();
             }
+            // rows the register kernel does not take (more than 8 lower blocks)
+            std::vector<int32_t> big;
+            for (int r = 0; r < n; ++r)
+                if (lrow[r + 1] - lrow[r] > 8) big.push_back(r);
             int64_t *d_pptr = nullptr;
-            int *d_pairs = nullptr;
+            int *d_pairs = nullptr, *d_big = nullptr;
             alloc(&d_pptr, pptr.size() * sizeof(int64_t));
             alloc(&d_pairs, pairs.size() * sizeof(int));
+            alloc(&d_big, big.size() * sizeof(int));
             if (e == cudaSuccess) e = upload(d_pptr, pptr.data(), pptr.size());
             if (e == cudaSuccess) e = upload(d_pairs, pairs.data(), pairs.size());
+            if (e == cudaSuccess) e = upload(d_big, big.data(), big.size());
             bw.fsai_pair_ptr = d_pptr;
             bw.fsai_pairs = d_pairs;
+            bw.fsai_big_rows = d_big;
+            bw.n_fsai_big = (int)big.size();
         }
         if (e == cudaSuccess) e = upload(d_lrow, lrow.data(), lrow.size());
         if (e == cudaSuccess) e = upload(d_urow, urow.data(), urow.size());

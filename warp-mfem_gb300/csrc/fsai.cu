@@ -42,7 +42,7 @@ __device__ int find_slot(const int *row_ptr, const int *col_idx, int row, int co
 
 // 3x3 lower Cholesky factor of a symmetric 3x3 (row-major a); false if not
 // positive definite.
-__device__ bool chol3(const float a[9], float l[9]) {
+__device__ __forceinline__ bool chol3(const float a[9], float l[9]) {
     for (int i = 0; i < 9; ++i) l[i] = 0.0f;
     const float d0 = a[0];
     if (!(d0 > 0.0f)) return false;
@@ -60,7 +60,7 @@ __device__ bool chol3(const float a[9], float l[9]) {
 }
 
 // inverse of a 3x3 lower-triangular matrix
-__device__ void inv_lower3(const float l[9], float m[9]) {
+__device__ __forceinline__ void inv_lower3(const float l[9], float m[9]) {
     for (int i = 0; i < 9; ++i) m[i] = 0.0f;
     m[0] = 1.0f / l[0];
     m[4] = 1.0f / l[4];
@@ -70,12 +70,136 @@ __device__ void inv_lower3(const float l[9], float m[9]) {
     m[6] = -(l[6] * m[0] + l[7] * m[3]) * m[8];
 }
 
+// Rows with at most kFsaiSmallCols lower blocks (every vertex of a Kuhn tet
+// grid): one thread per row.  The local matrix, padded to kFsaiSmall with an
+// identity block at its top left (which leaves the last block row of L^-1
+// unchanged), is factored in place as a packed lower triangle in shared
+// memory (row stride odd, so the threads of a warp hit distinct banks);
+// every loop is unrolled, so addresses are constant offsets and row j of L
+// sits in registers while column j is formed.  The last block row of L^-1
+// comes from w L = E^T, solved column by column from the last.
+constexpr int kFsaiSmallCols = 8;
+constexpr int kFsaiSmall = 3 * kFsaiSmallCols;
+constexpr int kFsaiPacked = kFsaiSmall * (kFsaiSmall + 1) / 2;
+constexpr int kFsaiThreadStride = kFsaiPacked + 1;
+constexpr int kFsaiRowThreads = 32;
+
+__device__ __forceinline__ constexpr int pk(int r, int c) { return r * (r + 1) / 2 + c; }
+
+__global__ void __launch_bounds__(kFsaiRowThreads) fsai_setup_small_kernel(BsrViews bv, BatchViews bw) {
+    extern __shared__ float s_mat[];
+    const int row = blockIdx.x * kFsaiRowThreads + threadIdx.x;
+    if (row >= bv.n) return;
+    const int lb = bw.lrow[row], m = bw.lrow[row + 1] - lb;
+    if (m < 1 || m > kFsaiSmallCols) return;  // the shared-memory warp kernel's rows
+    float *L = s_mat + threadIdx.x * kFsaiThreadStride;
+    float *G = bw.Lval + (size_t)9 * lb;
+    const int pad = kFsaiSmall - 3 * m;
+    const int *pslot = bw.fsai_pairs + bw.fsai_pair_ptr[row];
+#pragma unroll
+    for (int r = 0; r < kFsaiSmall; ++r)
+#pragma unroll
+        for (int c = 0; c <= r; ++c) {
+            float v;
+            if (r < pad) {
+                v = r == c ? 1.0f : 0.0f;
+            } else if (c < pad) {
+                v = 0.0f;
+            } else {
+                const int rr = r - pad, cc = c - pad, a = rr / 3, b = cc / 3;
+                const int sl = pslot[a * (a + 1) / 2 + b];
+                v = sl >= 0 ? bv.values[(size_t)9 * sl + 3 * (rr - 3 * a) + (cc - 3 * b)] : 0.0f;
+            }
+            L[pk(r, c)] = v;
+        }
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < kFsaiSmall; ++j) {
+        float lj[kFsaiSmall];
+        float d = L[pk(j, j)];
+#pragma unroll
+        for (int k = 0; k < j; ++k) {
+            lj[k] = L[pk(j, k)];
+            d = fmaf(-lj[k], lj[k], d);
+        }
+        if (!(d > 0.0f) || !isfinite(d)) {
+            ok = false;
+            d = 1.0f;
+        }
+        const float ljj = sqrtf(d), inv = 1.0f / ljj;
+        L[pk(j, j)] = ljj;
+#pragma unroll
+        for (int r = j + 1; r < kFsaiSmall; ++r) {
+            float a0 = L[pk(r, j)], a1 = 0.0f;
+#pragma unroll
+            for (int k = 0; k + 1 < j; k += 2) {
+                a0 = fmaf(-L[pk(r, k)], lj[k], a0);
+                a1 = fmaf(-L[pk(r, k + 1)], lj[k + 1], a1);
+            }
+            if (j & 1) a0 = fmaf(-L[pk(r, j - 1)], lj[j - 1], a0);
+            L[pk(r, j)] = (a0 + a1) * inv;
+        }
+    }
+    if (ok) {
+        // w L = E^T: w[t][c] = (E[t][c] - sum_{r > c} w[t][r] L[r][c]) / L[c][c]
+        float w0[kFsaiSmall], w1[kFsaiSmall], w2[kFsaiSmall];
+#pragma unroll
+        for (int c = kFsaiSmall - 1; c >= 0; --c) {
+            float a0 = c == kFsaiSmall - 3 ? 1.0f : 0.0f;
+            float a1 = c == kFsaiSmall - 2 ? 1.0f : 0.0f;
+            float a2 = c == kFsaiSmall - 1 ? 1.0f : 0.0f;
+#pragma unroll
+            for (int r = c + 1; r < kFsaiSmall; ++r) {
+                const float l = L[pk(r, c)];
+                a0 = fmaf(-w0[r], l, a0);
+                a1 = fmaf(-w1[r], l, a1);
+                a2 = fmaf(-w2[r], l, a2);
+            }
+            const float inv = 1.0f / L[pk(c, c)];
+            w0[c] = a0 * inv;
+            w1[c] = a1 * inv;
+            w2[c] = a2 * inv;
+        }
+        // G[i, P] = w restricted to the real columns: block a, entry (p, q)
+        // = w[p][pad + 3a + q]
+#pragma unroll
+        for (int c = 0; c < kFsaiSmall; ++c)
+            if (c >= pad) {
+                const int cc = c - pad, a = cc / 3, q = cc - 3 * a;
+                float *g = G + 9 * a + q;
+                g[0] = w0[c];
+                g[3] = w1[c];
+                g[6] = w2[c];
+            }
+        return;
+    }
+    // fallback: G_ii = chol(H_ii)^-1, the other blocks zero
+    for (int t = 0; t < 9 * m; ++t) G[t] = 0.0f;
+    const int sl = find_slot(bv.row_ptr, bv.col_idx, row, row);
+    float h[9], l[9], li[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) h[q] = bv.values[(size_t)9 * sl + q];
+    float *gd = G + 9 * (m - 1);
+    if (chol3(h, l)) {
+        inv_lower3(l, li);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) gd[q] = li[q];
+    } else {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) gd[q] = (q % 4 == 0) ? 1.0f : 0.0f;
+    }
+}
+
+// Rows with more lower blocks (kFsaiSmallCols < m <= kFsaiMaxCols, and the
+// fallback of longer ones), one warp per listed row, the local matrix in
+// shared memory.
 __global__ void __launch_bounds__(kFsaiThreads) fsai_setup_kernel(BsrViews bv, BatchViews bw) {
     __shared__ float s_A[kFsaiWarps][kFsaiDim * (kFsaiDim + 1)];
     __shared__ float s_X[kFsaiWarps][kFsaiDim * 3];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row = blockIdx.x * kFsaiWarps + wid;
-    if (row >= bv.n) return;  // uniform per warp
+    const int t_row = blockIdx.x * kFsaiWarps + wid;
+    if (t_row >= bw.n_fsai_big) return;  // uniform per warp
+    const int row = bw.fsai_big_rows[t_row];
     float *A = s_A[wid];
     float *X = s_X[wid];
     const int lb = bw.lrow[row], m = bw.lrow[row + 1] - lb;
@@ -201,8 +325,13 @@ __global__ void factor_transpose_kernel(BatchViews bw) {
 
 cudaError_t launch_fsai_setup(const BsrViews &bv, const BatchViews &bw, cudaStream_t s) {
     if (bv.n == 0) return cudaSuccess;
-    fsai_setup_kernel<<<(bv.n + kFsaiWarps - 1) / kFsaiWarps, kFsaiThreads, 0, s>>>(bv, bw);
+    const size_t smem = (size_t)kFsaiRowThreads * kFsaiThreadStride * sizeof(float);
+    fsai_setup_small_kernel<<<(bv.n + kFsaiRowThreads - 1) / kFsaiRowThreads, kFsaiRowThreads, smem, s>>>(bv, bw);
     count_launches(1);
+    if (bw.n_fsai_big > 0) {
+        fsai_setup_kernel<<<(bw.n_fsai_big + kFsaiWarps - 1) / kFsaiWarps, kFsaiThreads, 0, s>>>(bv, bw);
+        count_launches(1);
+    }
     return cudaGetLastError();
 }
 

@@ -106,6 +106,8 @@ struct BatchViews {
     // lower blocks have none
     const int64_t *fsai_pair_ptr;  // [n + 1]
     const int *fsai_pairs;
+    const int *fsai_big_rows;  // [n_fsai_big] rows with more than 8 lower blocks
+    int n_fsai_big;
     int nnzl;
 };
 

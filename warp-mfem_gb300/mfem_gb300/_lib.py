@@ -97,7 +97,7 @@ class MfemSolverConfig(ctypes.Structure):
         ("precision", ctypes.c_int32),
         ("inner_tolerance", ctypes.c_float),
         ("outer_max_iterations", ctypes.c_int32),
-        ("reserved0", ctypes.c_int32),
+        ("factor_refresh", ctypes.c_int32),
         ("outer_tolerance", ctypes.c_double),
         ("reserved", ctypes.c_int32 * 4),
     ]

@@ -53,7 +53,8 @@ class MixedFEMSolver:
     assembly, or "learned": M = L L^T with L written by the factor net
     (``factor_net``; parameters ``factor_net_params`` or the shipped
     weights).  Both factor forms run the global-memory PCG (fp32 solve
-    only).
+    only); ``factor_refresh`` k recomputes the factor at every k-th Newton
+    iteration of a step (default 1: every assembly).
     """
 
     def __init__(self, model: Model, iterations: int, max_tets: Optional[int] = None,
@@ -137,10 +138,11 @@ class MixedFEMSolver:
         self.solver_precision = kwargs.get("solver_precision", "fp32")
         if self.solver_precision not in _lib.PRECISION:
             raise ValueError(f"Unknown solver_precision {self.solver_precision!r}")
-        if self.solver_precision != "fp32":
+        if self.solver_precision != "fp32" or "factor_refresh" in kwargs:
             scfg = _lib.MfemSolverConfig()
             self._lib.mfem_solver_config_default(ctypes.byref(scfg))
             scfg.precision = _lib.PRECISION[self.solver_precision]
+            scfg.factor_refresh = int(kwargs.get("factor_refresh", 1))
             scfg.inner_tolerance = float(kwargs.get("inner_tolerance", 1.0e-3))
             scfg.outer_tolerance = float(kwargs.get("outer_tolerance", 1.0e-8))
             scfg.outer_max_iterations = int(kwargs.get("outer_max_iterations", 10))
