@@ -257,9 +257,11 @@ struct BtScalars {
 
 // FACTOR: the instantiation for the factor preconditioners (use_precond 2
 // or 3, with the block-Jacobi retry); the other one, for use_precond 0 or 1,
-// carries none of that code (fewer registers, more resident CTAs).
+// carries none of that code.  Register caps (no spills at either): 48 lets
+// 10 CTAs of 128 threads share an SM, 56 lets 9 (the kernel waits on gather
+// latency, so resident warps matter); up to kBtMaxThreads threads a CTA.
 template <bool FACTOR>
-__global__ void __launch_bounds__(kBtMaxThreads)
+__global__ void __maxnreg__(FACTOR ? 56 : 48)
     batched_pcg_kernel(BsrViews bv, VertexViews vv, BatchViews bw, int *error, int slot, float tol, int maxiter,
                        int use_precond) {
     __shared__ float s_redf[3][32];
