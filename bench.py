@@ -68,10 +68,14 @@ def parse_args():
     return ap.parse_args()
 
 
-def workload_config(mesh, extra=None, precision="fp32", outer_tolerance=1e-6):
+def workload_config(mesh, extra=None, precision="fp32", outer_tolerance=1e-6, preconditioner="block_jacobi",
+                    factor_refresh=1):
     spec = mesh.spec
-    if precision == "fp32":
-        pcg = "plain fp32 block-Jacobi (the learned + mixed-precision variant is not built)"
+    if precision == "fp32" and preconditioner == "block_jacobi":
+        pcg = "plain fp32 block-Jacobi, the reference's (persistent PCG)"
+    elif precision == "fp32":
+        pcg = (f"fp32 PCG with the {preconditioner} factor preconditioner (global-memory PCG), factor recomputed "
+               f"every {factor_refresh} Newton iteration(s); the learned factor is not combined with mixed precision")
     else:
         pcg = (f"{precision} blocks with per-row scales, fp32 block-Jacobi inner PCG to 1e-3, fp64 iterative "
                f"refinement to {outer_tolerance:g}")
@@ -650,8 +654,9 @@ def run_gb300(args, rank, world, local_rank):
         "config": workload_config(mesh, {"line_search": bool(args.line_search),
                                          "preconditioner": args.preconditioner,
                                          "factor_refresh": args.factor_refresh,
-                                         "global_memory_autotune_ms": tune_ms}, precision=args.precision,
-                                  outer_tolerance=args.outer_tolerance),
+                                         "global_memory_autotune_ms": tune_ms},
+                                  precision=args.precision, outer_tolerance=args.outer_tolerance,
+                                  preconditioner=args.preconditioner, factor_refresh=args.factor_refresh),
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes, "matches_resident_run": e2e_match},
         "gpu_launches": int(launches),
