@@ -174,7 +174,9 @@ typedef struct mfem_mixed_solve_stats {
     int32_t outer_iterations;       /* corrections applied                              */
     int32_t inner_iterations;       /* PCG iterations over all corrections              */
     int32_t status;                 /* MFEM_OK, MFEM_MAXITER (outer cap), ...           */
-    int32_t reserved;
+    int32_t fp32_inner;             /* 1: the refinement diverged (residual above 4x its
+                                       best) and the solve restarted from the warm
+                                       start with the fp32 H in the inner PCG          */
     double rel_residual;            /* fp64 ||g - H dx|| / ||g|| of the returned dx     */
 } mfem_mixed_solve_stats;
 

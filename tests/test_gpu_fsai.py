@@ -184,8 +184,6 @@ def test_bad_combinations_are_refused():
         MixedFEMSolver(model, iterations=1, preconditioner="ilu")
     with pytest.raises(_lib.MfemError):
         MixedFEMSolver(model, iterations=1, preconditioner="fsai", pcg_variant="standard")
-    with pytest.raises(_lib.MfemError):
-        MixedFEMSolver(model, iterations=1, preconditioner="fsai", solver_precision="fp16")
 
 
 def test_step_stats_report_the_global_memory_solve():

@@ -153,6 +153,3 @@ def test_set_factor_net_refuses_bad_input():
     bad[3] = np.nan
     with pytest.raises(_lib.MfemError):
         MixedFEMSolver(model, iterations=1, preconditioner="learned", factor_net_params=bad)
-    with pytest.raises(_lib.MfemError):
-        MixedFEMSolver(model, iterations=1, preconditioner="learned", factor_net_params=good,
-                       solver_precision="fp16")

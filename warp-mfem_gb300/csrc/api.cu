@@ -203,7 +203,8 @@ bool net_ready(const mfem_plan *p) { return p->cfg.preconditioner != 3 || p->fv.
 // The reference's float32 PCG, or the mixed-precision iterative refinement.
 cudaError_t global_solve(mfem_plan *p, int slot, cudaStream_t s) {
     if (p->ir.mode != 0)
-        return launch_mixed_solve(p->bv, p->vv, p->ir, p->pw, slot, p->cfg.cg_max_iterations, p->cfg.preconditioner,
+        return launch_mixed_solve(p->bv, p->vv, p->ir, p->pw, p->bw, slot, p->cfg.cg_max_iterations,
+                                  p->cfg.preconditioner,
                                   s);
     if (p->bw.n_bodies > 0)
         return launch_batched_pcg(p->bv, p->vv, p->bw, p->pw.error, slot, p->cfg.cg_tolerance,
@@ -1036,8 +1037,7 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
         return fail(p, MFEM_BAD_ARG, "outer_max_iterations must be in [1, 100]");
     if (p->bw.n_bodies > 1 && cfg.precision != MFEM_PRECISION_FP32)
         return fail(p, MFEM_BAD_ARG, "batched bodies use the fp32 PCG");
-    if (p->cfg.preconditioner >= 2 && cfg.precision != MFEM_PRECISION_FP32)
-        return fail(p, MFEM_BAD_ARG, "factor preconditioners run with the fp32 PCG");
+
     DeviceGuard g(p->device);
     cudaError_t e = cudaDeviceSynchronize();  // no step of this plan may still use the old buffers
     if (e != cudaSuccess) return cuda_fail(p, e, "cudaDeviceSynchronize");
@@ -1078,11 +1078,13 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
     alloc(&w.p1, n3 * sizeof(float));
     alloc(&w.r, n3 * sizeof(float));
     alloc(&w.Ap, n3 * sizeof(float));
-    alloc(&w.partials, 2 * 256 * 4 * sizeof(float));
+    alloc(&w.partials, 2 * 256 * 4 * sizeof(double));
     alloc(&w.counter, sizeof(unsigned long long));
     alloc(&w.res_partials, (size_t)2 * ir_residual_blocks(p->n) * sizeof(double));
     alloc(&w.ticket, sizeof(unsigned));
     alloc(&w.state, 8 * sizeof(int));
+    alloc(&w.dx_init, n3 * sizeof(float));
+    alloc(&w.best, sizeof(double));
     alloc(&w.stats, (size_t)p->max_stats * sizeof(IrStats));
     int max_ctas = 1;
     if (e == cudaSuccess) e = ir_max_ctas(p->device, &max_ctas);

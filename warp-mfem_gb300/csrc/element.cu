@@ -83,6 +83,17 @@ __global__ void __launch_bounds__(kElementThreads)
 #pragma unroll
         for (int col = 0; col < 12; ++col) tv.G[(size_t)(r * 12 + col) * T + t] = G[r][col];
 
+    // H_l g_l = H_l c + INV_SYM g_s: the reference's product, without the
+    // cancellation of H_l SYM H_s^-1 g_s (H_l = INV_SYM H_s INV_SYM), which
+    // loses fp32 accuracy on tets whose H_s is nearly singular
+    float w[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        float acc = em::inv_sym_w(i) * g_s[i];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) acc += H_l[em::p21(i, j)] * c[j];
+        w[i] = acc;
+    }
     float *Ke = tv.Ke + (size_t)t * kKeFloats;
     float *fe = tv.fe + (size_t)t * kFeFloats;
 #pragma unroll
@@ -101,7 +112,7 @@ __global__ void __launch_bounds__(kElementThreads)
         for (int b = 0; b < 3; ++b) {
             float acc = 0.0f;
 #pragma unroll
-            for (int i = 0; i < 6; ++i) acc += P[i][b] * g_l[i];
+            for (int i = 0; i < 6; ++i) acc += G[i][3 * l + b] * w[i];
             fe[3 * l + b] = acc;
         }
 #pragma unroll
@@ -170,20 +181,27 @@ __global__ void __launch_bounds__(kVertexThreads)
 }
 
 // lambda and ds of tet t (local_solve_lambda, local_solve_stretch,
-// kernels.py:252-283):  lambda = -H_l (g_l - G dx), ds = -H_s^-1 (SYM lambda
-// + g_s); gdx = G dx, accumulated block by block as it is subtracted.
+// kernels.py:252-283): the reference computes lambda = -H_l (g_l - G dx) and
+// ds = -H_s^-1 (SYM lambda + g_s) with g_l = c + SYM H_s^-1 g_s and H_l =
+// INV_SYM H_s INV_SYM.  With u = c - G dx these are exactly
+//     lambda = -(H_l u + INV_SYM g_s),   ds = INV_SYM u,
+// which is what is evaluated here: the reference's order forms SYM lambda +
+// g_s as a difference of two large, nearly equal terms and multiplies it by
+// H_s^-1, which amplifies fp32 rounding by cond(H_s) (above 1e4 for strongly
+// stretched Neo-Hookean tets, where the trajectory then drifts from the exact
+// one and diverges).  gdx = G dx.
 __device__ __forceinline__ void local_tet(const TetViews &tv, const float *__restrict__ dx, int t, float nl[6],
                                           float ds[6], float gdx[6]) {
     const int T = tv.n_tets;
     const int4 tt = tv.tets[t];
     const int vid[4] = {tt.x, tt.y, tt.z, tt.w};
-    float lam[6];
+    float u[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
-        lam[i] = tv.g_l[(size_t)i * T + t];
+        u[i] = tv.c[(size_t)i * T + t];
         gdx[i] = 0.0f;
     }
-    // lambda -= G_k dx[v_k], block by block (kernels.py:266-268)
+    // u = c - G dx, block by block (kernels.py:266-268)
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         float d[3];
@@ -192,7 +210,7 @@ __device__ __forceinline__ void local_tet(const TetViews &tv, const float *__res
         for (int i = 0; i < 6; ++i) {
             const float *g = tv.G + (size_t)(i * 12 + 3 * k) * T + t;
             const float gd = g[0] * d[0] + g[(size_t)T] * d[1] + g[(size_t)2 * T] * d[2];
-            lam[i] -= gd;
+            u[i] -= gd;
             gdx[i] += gd;
         }
     }
@@ -201,21 +219,11 @@ __device__ __forceinline__ void local_tet(const TetViews &tv, const float *__res
     for (int k = 0; k < 21; ++k) Hl[k] = tv.H_l[(size_t)k * T + t];
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
-        float acc = 0.0f;
+        float acc = em::inv_sym_w(i) * tv.g_s[(size_t)i * T + t];
 #pragma unroll
-        for (int j = 0; j < 6; ++j) acc += Hl[em::p21(i, j)] * lam[j];
+        for (int j = 0; j < 6; ++j) acc += Hl[em::p21(i, j)] * u[j];
         nl[i] = -acc;
-    }
-    // ds = -H_s^-1 (SYM lambda + g_s) (kernels.py:271-283)
-    float rhs[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) rhs[i] = em::sym_w(i) * nl[i] + tv.g_s[(size_t)i * T + t];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        float acc = 0.0f;
-#pragma unroll
-        for (int j = 0; j < 6; ++j) acc += tv.H_si[(size_t)em::p21(i, j) * T + t] * rhs[j];
-        ds[i] = -acc;
+        ds[i] = em::inv_sym_w(i) * u[i];
     }
 }
 

@@ -1,0 +1,72 @@
+// One pass of a factor preconditioner, shared by the global-memory PCGs: out
+// = F in over rows [lo, hi) for one form of the factor (row pointers,
+// columns, row-major 3x3 blocks), `group` lanes per row.  `in` is read with
+// __ldcg (other CTAs wrote it during this launch) unless LOCAL says this
+// CTA's own stores, ordered by __syncthreads, are the only writers.
+#pragma once
+
+#include "internal.h"
+
+namespace mfem {
+
+template <bool LOCAL, int GROUP>
+__device__ __forceinline__ void factor_pass(const int *rp, const int *col, const float *val, const float *in,
+                                            float *out, int lo, int hi) {
+    const int g_lane = threadIdx.x & (GROUP - 1);
+    const unsigned gmask = ((1u << GROUP) - 1u) << (threadIdx.x & (32 - GROUP));
+    const int group = threadIdx.x / GROUP, ngroups = blockDim.x / GROUP;
+    auto ld = [](const float *p) { return LOCAL ? *p : __ldcg(p); };
+    for (int row = lo + group; row < hi; row += ngroups) {
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+        const int ke = __ldg(rp + row + 1);
+        // two blocks per lane and trip: their loads are in flight together
+        for (int k = __ldg(rp + row) + g_lane; k < ke; k += 2 * GROUP) {
+            const int k2 = k + GROUP;
+            const bool two = k2 < ke;
+            const int c = __ldg(col + k), c2 = two ? __ldg(col + k2) : c;
+            const float v0 = ld(in + 3 * c), v1 = ld(in + 3 * c + 1), v2 = ld(in + 3 * c + 2);
+            float w0 = ld(in + 3 * c2), w1 = ld(in + 3 * c2 + 1), w2 = ld(in + 3 * c2 + 2);
+            if (!two) w0 = w1 = w2 = 0.0f;
+            const float *f = val + (size_t)9 * k;
+            const float *f2 = val + (size_t)9 * (two ? k2 : k);
+            a0 += __ldg(f + 0) * v0 + __ldg(f + 1) * v1 + __ldg(f + 2) * v2;
+            a1 += __ldg(f + 3) * v0 + __ldg(f + 4) * v1 + __ldg(f + 5) * v2;
+            a2 += __ldg(f + 6) * v0 + __ldg(f + 7) * v1 + __ldg(f + 8) * v2;
+            a0 += __ldg(f2 + 0) * w0 + __ldg(f2 + 1) * w1 + __ldg(f2 + 2) * w2;
+            a1 += __ldg(f2 + 3) * w0 + __ldg(f2 + 4) * w1 + __ldg(f2 + 5) * w2;
+            a2 += __ldg(f2 + 6) * w0 + __ldg(f2 + 7) * w1 + __ldg(f2 + 8) * w2;
+        }
+#pragma unroll
+        for (int off = GROUP / 2; off > 0; off >>= 1) {
+            a0 += __shfl_xor_sync(gmask, a0, off);
+            a1 += __shfl_xor_sync(gmask, a1, off);
+            a2 += __shfl_xor_sync(gmask, a2, off);
+        }
+        if (g_lane == 0) {
+            out[3 * row] = a0;
+            out[3 * row + 1] = a1;
+            out[3 * row + 2] = a2;
+        }
+    }
+}
+
+// The two passes of M r for mode 2 (M = F^T F: lower form first) or mode 3
+// (M = F F^T: upper form first), as (row pointers, columns, values) pairs.
+struct FactorForms {
+    const int *rp0, *c0, *rp1, *c1;
+    const float *v0, *v1;
+};
+
+__device__ __forceinline__ FactorForms factor_forms(const BatchViews &bw, int mode) {
+    const bool lower_first = mode == 2;
+    FactorForms f;
+    f.rp0 = lower_first ? bw.lrow : bw.urow;
+    f.c0 = lower_first ? bw.lcol : bw.ucol;
+    f.v0 = lower_first ? bw.Lval : bw.Uval;
+    f.rp1 = lower_first ? bw.urow : bw.lrow;
+    f.c1 = lower_first ? bw.ucol : bw.lcol;
+    f.v1 = lower_first ? bw.Uval : bw.Lval;
+    return f;
+}
+
+}  // namespace mfem

@@ -234,7 +234,7 @@ struct IrStats {               // same layout as mfem_mixed_solve_stats
     int32_t outer_iterations;
     int32_t inner_iterations;
     int32_t status;
-    int32_t reserved;
+    int32_t fp32_inner;        // the solve restarted with the fp32 H in the inner PCG
     double rel_residual;       // fp64 ||g - H dx|| / ||g||
 };
 
@@ -251,11 +251,13 @@ struct IrWork {
     float *e;                  // [n][3] inner correction
     float *res;                // [n][3] fp32 copy of the fp64 residual (inner rhs)
     float *z, *p0, *p1, *r, *Ap;  // inner PCG vectors [n][3]
-    float *partials;           // [2][256][4]
+    double *partials;          // [2][256][4] fp64 partial sums of the inner PCG
     unsigned long long *counter;  // inner PCG grid barrier, never reset
     double *res_partials;      // [residual blocks][2]
     unsigned *ticket;          // last-block detection of the residual kernel
-    int *state;                // done, outer, inner, pending, parity, status
+    int *state;                // done, outer, inner, pending, parity, status, fp32 inner, restart
+    float *dx_init;            // [n][3] the warm start, for a restart
+    double *best;              // [1] smallest fp64 relative residual of the solve so far
     IrStats *stats;            // [max solves per step]
 };
 
@@ -325,7 +327,7 @@ cudaError_t launch_batched_pcg(const BsrViews &bv, const VertexViews &vv, const 
                                float tol, int maxiter, int use_precond, cudaStream_t s);
 int ir_residual_blocks(int n);
 cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const IrWork &w, const PcgWork &pw,
-                               int slot, int maxiter, int use_precond, cudaStream_t s);
+                               const BatchViews &fb, int slot, int maxiter, int use_precond, cudaStream_t s);
 
 // Number of kernels launched by the launchers above (process-wide).
 void count_launches(uint64_t k);

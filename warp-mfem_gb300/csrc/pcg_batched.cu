@@ -20,6 +20,7 @@
 // a given schedule.  Every wait is bounded.
 #include <algorithm>
 
+#include "factor_apply.cuh"
 #include "internal.h"
 
 namespace mfem {
@@ -174,49 +175,6 @@ __device__ __forceinline__ void bt_row_product(const BsrViews &bv, int row, cons
     y[2] = a2;
 }
 
-// out = F in over this CTA's rows for one factor form (row pointers, columns,
-// row-major 3x3 blocks), kBtGroup lanes per row.
-template <bool SHARED>
-__device__ __forceinline__ void bt_factor_pass(const int *rp, const int *col, const float *val, const float *in,
-                                               float *out, int lo, int hi) {
-    const int g_lane = threadIdx.x & (kBtGroup - 1);
-    const unsigned gmask = ((1u << kBtGroup) - 1u) << (threadIdx.x & (32 - kBtGroup));
-    const int group = threadIdx.x / kBtGroup, ngroups = blockDim.x / kBtGroup;
-    for (int row = lo + group; row < hi; row += ngroups) {
-        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-        const int ke = __ldg(rp + row + 1);
-        for (int k = __ldg(rp + row) + g_lane; k < ke; k += 2 * kBtGroup) {
-            const int k2 = k + kBtGroup;
-            const bool two = k2 < ke;
-            const int c = __ldg(col + k), c2 = two ? __ldg(col + k2) : c;
-            const float v0 = bt_ld<SHARED>(in + 3 * c), v1 = bt_ld<SHARED>(in + 3 * c + 1),
-                        v2 = bt_ld<SHARED>(in + 3 * c + 2);
-            float w0 = bt_ld<SHARED>(in + 3 * c2), w1 = bt_ld<SHARED>(in + 3 * c2 + 1),
-                  w2 = bt_ld<SHARED>(in + 3 * c2 + 2);
-            if (!two) w0 = w1 = w2 = 0.0f;
-            const float *f = val + (size_t)9 * k;
-            const float *f2 = val + (size_t)9 * (two ? k2 : k);
-            a0 += __ldg(f + 0) * v0 + __ldg(f + 1) * v1 + __ldg(f + 2) * v2;
-            a1 += __ldg(f + 3) * v0 + __ldg(f + 4) * v1 + __ldg(f + 5) * v2;
-            a2 += __ldg(f + 6) * v0 + __ldg(f + 7) * v1 + __ldg(f + 8) * v2;
-            a0 += __ldg(f2 + 0) * w0 + __ldg(f2 + 1) * w1 + __ldg(f2 + 2) * w2;
-            a1 += __ldg(f2 + 3) * w0 + __ldg(f2 + 4) * w1 + __ldg(f2 + 5) * w2;
-            a2 += __ldg(f2 + 6) * w0 + __ldg(f2 + 7) * w1 + __ldg(f2 + 8) * w2;
-        }
-#pragma unroll
-        for (int off = kBtGroup / 2; off > 0; off >>= 1) {
-            a0 += __shfl_xor_sync(gmask, a0, off);
-            a1 += __shfl_xor_sync(gmask, a1, off);
-            a2 += __shfl_xor_sync(gmask, a2, off);
-        }
-        if (g_lane == 0) {
-            out[3 * row] = a0;
-            out[3 * row + 1] = a1;
-            out[3 * row + 2] = a2;
-        }
-    }
-}
-
 // The barrier of the body between factor passes and before reading vectors
 // other CTAs of the group wrote: __syncthreads for a one-CTA body, the
 // group's counter barrier otherwise.
@@ -237,15 +195,12 @@ __device__ __forceinline__ bool bt_sync(const BatchViews &bw, const Task &tk, in
 __device__ __forceinline__ bool bt_apply_factor(const BatchViews &bw, int mode, const Task &tk, int lo, int hi,
                                                 int *error, unsigned &k, unsigned long long &target, float *s_tot,
                                                 float (*s_redf)[32], int *s_ok) {
-    const bool lower_first = mode == 2;
-    const int *rp0 = lower_first ? bw.lrow : bw.urow, *c0 = lower_first ? bw.lcol : bw.ucol;
-    const int *rp1 = lower_first ? bw.urow : bw.lrow, *c1 = lower_first ? bw.ucol : bw.lcol;
-    const float *v0 = lower_first ? bw.Lval : bw.Uval, *v1 = lower_first ? bw.Uval : bw.Lval;
-    if (tk.size > 1) bt_factor_pass<true>(rp0, c0, v0, bw.r, bw.y, lo, hi);
-    else bt_factor_pass<false>(rp0, c0, v0, bw.r, bw.y, lo, hi);
+    const FactorForms f = factor_forms(bw, mode);
+    if (tk.size > 1) factor_pass<false, kBtGroup>(f.rp0, f.c0, f.v0, bw.r, bw.y, lo, hi);
+    else factor_pass<true, kBtGroup>(f.rp0, f.c0, f.v0, bw.r, bw.y, lo, hi);
     if (!bt_sync(bw, tk, error, k, target, s_tot, s_redf, s_ok)) return false;
-    if (tk.size > 1) bt_factor_pass<true>(rp1, c1, v1, bw.y, bw.z, lo, hi);
-    else bt_factor_pass<false>(rp1, c1, v1, bw.y, bw.z, lo, hi);
+    if (tk.size > 1) factor_pass<false, kBtGroup>(f.rp1, f.c1, f.v1, bw.y, bw.z, lo, hi);
+    else factor_pass<true, kBtGroup>(f.rp1, f.c1, f.v1, bw.y, bw.z, lo, hi);
     __syncthreads();
     return true;
 }

@@ -8,6 +8,9 @@
 //   iteration forms r = g - H dx in fp64 from the fp32 H, stops when
 //   ||r|| <= outer_tol ||g||, else solves Hq e = r to inner_tol with the PCG
 //   (fp32 vectors, the fp32 block-Jacobi inverse) and sets dx += e.
+//   If the refinement diverges (the relative residual rises above 4x its
+//   best, or turns non-finite), the 16-bit H is too coarse for this system:
+//   the solve restarts from the warm start with the fp32 H in the inner PCG.
 //
 // This is the benchmark spec's mixed-precision variant of the global solve (the
 // reference solves H dx = g with one float32 PCG, src/mfem/refinement/
@@ -28,6 +31,7 @@
 
 #include <algorithm>
 
+#include "factor_apply.cuh"
 #include "internal.h"
 
 namespace mfem {
@@ -74,8 +78,14 @@ __global__ void ir_convert_kernel(BsrViews bv, IrWork w) {
 
 __global__ void ir_begin_kernel(VertexViews vv, IrWork w) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < 3 * vv.n) w.dx64[i] = (double)vv.dx[i];
+    if (i < 3 * vv.n) {
+        w.dx64[i] = (double)vv.dx[i];
+        w.dx_init[i] = vv.dx[i];
+    }
     if (i == 0) {
+        w.state[6] = 0;  // inner PCG on the fp32 H
+        w.state[7] = 0;  // restart from the warm start at the next residual
+        *w.best = __longlong_as_double(0x7ff0000000000000ll);  // +inf
         w.state[0] = 0;  // done
         w.state[1] = 0;  // outer iterations
         w.state[2] = 0;  // inner iterations
@@ -91,7 +101,8 @@ __global__ void __launch_bounds__(kResThreads)
     __shared__ int s_last;
     if (*(volatile int *)&w.state[0]) return;  // converged or capped
     const int par = w.state[4];
-    const bool pending = w.state[3] != 0;
+    const bool restart = w.state[7] != 0;
+    const bool pending = !restart && w.state[3] != 0;
     const size_t vec = (size_t)3 * vv.n;
     const double *xo = w.dx64 + (size_t)par * vec;
     double *xn = w.dx64 + (size_t)(par ^ 1) * vec;
@@ -105,7 +116,9 @@ __global__ void __launch_bounds__(kResThreads)
             const int c = bv.col_idx[k];
             double xc[3];
 #pragma unroll
-            for (int q = 0; q < 3; ++q) xc[q] = xo[3 * c + q] + (pending ? (double)w.e[3 * c + q] : 0.0);
+            for (int q = 0; q < 3; ++q)
+                xc[q] = restart ? (double)w.dx_init[3 * c + q]
+                                : xo[3 * c + q] + (pending ? (double)w.e[3 * c + q] : 0.0);
             const float *h = bv.values + (size_t)9 * k;
 #pragma unroll
             for (int a = 0; a < 3; ++a)
@@ -118,7 +131,8 @@ __global__ void __launch_bounds__(kResThreads)
         if (g_lane == 0) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                const double xr = xo[3 * row + a] + (pending ? (double)w.e[3 * row + a] : 0.0);
+                const double xr = restart ? (double)w.dx_init[3 * row + a]
+                                          : xo[3 * row + a] + (pending ? (double)w.e[3 * row + a] : 0.0);
                 xn[3 * row + a] = xr;
                 w.dx_out[3 * row + a] = xr;
                 vv.dx[3 * row + a] = (float)xr;
@@ -166,7 +180,15 @@ __global__ void __launch_bounds__(kResThreads)
         const int outer = w.state[1];
         int status = MFEM_OK;
         int done = 0;
-        if (!isfinite(rel)) {
+        const double best = *w.best;
+        w.state[7] = 0;
+        if (w.state[6] == 0 && isfinite(best) && !(rel <= 4.0 * best) && outer < w.outer_max) {
+            // diverging on the 16-bit H: restart from the warm start with
+            // the fp32 H (the next inner PCG is skipped; the next residual
+            // pass reads the warm start)
+            w.state[6] = 1;
+            w.state[7] = 1;
+        } else if (!isfinite(rel)) {
             status = MFEM_NONFINITE;
             done = 1;
         } else if (rel <= w.outer_tol) {
@@ -175,12 +197,13 @@ __global__ void __launch_bounds__(kResThreads)
             status = MFEM_MAXITER;
             done = 1;
         }
+        if (isfinite(rel) && rel < best && w.state[7] == 0) *w.best = rel;
         w.state[1] = outer + 1;
         w.state[3] = 0;
         w.state[4] = par ^ 1;
         w.state[0] = done;
         if (w.state[5] == MFEM_OK) w.state[5] = status;
-        w.stats[slot] = IrStats{outer, w.state[2], w.state[5], 0, rel};
+        w.stats[slot] = IrStats{outer, w.state[2], w.state[5], w.state[6], rel};
         pw.stats[slot] = SolveStats{w.state[2], w.state[5], (float)rel, 0.0f};
         *w.ticket = 0u;
     }
@@ -193,10 +216,12 @@ __device__ __forceinline__ unsigned long long ir_ld_relaxed(const unsigned long 
 }
 
 // Block-reduce NV partials, store them for barrier k, wait at the grid
-// barrier, sum all CTAs' partials in a fixed order into tot[].
+// barrier, sum all CTAs' partials in a fixed order into tot[].  In fp64:
+// the inner right-hand side is a residual that can be tiny, and fp32
+// products of its entries would underflow (0/0 in the recurrence).
 template <int NV>
-__device__ bool ir_reduce(float (&v)[NV], const IrWork &w, int *error, unsigned k, unsigned long long &target,
-                          float *tot, float (*s_redf)[32], float *s_val, int *s_ok) {
+__device__ bool ir_reduce(double (&v)[NV], const IrWork &w, int *error, unsigned k, unsigned long long &target,
+                          double *tot, double (*s_redf)[32], double *s_val, int *s_ok) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nb = gridDim.x;
 #pragma unroll
     for (int i = 0; i < NV; ++i)
@@ -206,13 +231,13 @@ __device__ bool ir_reduce(float (&v)[NV], const IrWork &w, int *error, unsigned 
 #pragma unroll
         for (int i = 0; i < NV; ++i) s_redf[i][wid] = v[i];
     __syncthreads();
-    float *buf = w.partials + (size_t)(k & 1u) * 256 * 4;
+    double *buf = w.partials + (size_t)(k & 1u) * 256 * 4;
     if (wid == 0) {
         const int nw = blockDim.x >> 5;
-        float part[NV];
+        double part[NV];
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
-            part[i] = lane < nw ? s_redf[i][lane] : 0.0f;
+            part[i] = lane < nw ? s_redf[i][lane] : 0.0;
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) part[i] += __shfl_down_sync(0xffffffffu, part[i], off);
         }
@@ -244,9 +269,9 @@ __device__ bool ir_reduce(float (&v)[NV], const IrWork &w, int *error, unsigned 
     }
     __syncthreads();
     if (wid == 0) {
-        float acc[NV];
+        double acc[NV];
 #pragma unroll
-        for (int i = 0; i < NV; ++i) acc[i] = 0.0f;
+        for (int i = 0; i < NV; ++i) acc[i] = 0.0;
         for (int b = lane; b < nb; b += 32)
 #pragma unroll
             for (int i = 0; i < NV; ++i) acc[i] += s_val[b * 4 + i];
@@ -275,10 +300,26 @@ __device__ __forceinline__ void ir_precond(const float *Minv, int use, int row, 
     z[2] = m[6] * r[0] + m[7] * r[1] + m[8] * r[2];
 }
 
-// y_row = s_row sum_k Hq[k] (z[col] + beta p_old[col]), fp32 accumulation.
+// z = M r over this CTA's rows with the plan's factor (every row's r is in
+// place on entry): the first pass into fb.y, a grid barrier, the second into
+// w.z; z of the CTA's own rows on return.
+__device__ __forceinline__ bool ir_apply_factor(const BatchViews &fb, int mode, const IrWork &w, int *error,
+                                                unsigned &k, unsigned long long &target, double *s_tot,
+                                                double (*s_redf)[32], double *s_val, int *s_ok, int lo, int hi) {
+    const FactorForms f = factor_forms(fb, mode);
+    factor_pass<false, kIrGroup>(f.rp0, f.c0, f.v0, w.r, fb.y, lo, hi);
+    double d[1] = {0.0};
+    if (!ir_reduce<1>(d, w, error, k++, target, s_tot, s_redf, s_val, s_ok)) return false;
+    factor_pass<false, kIrGroup>(f.rp1, f.c1, f.v1, fb.y, w.z, lo, hi);
+    __syncthreads();
+    return true;
+}
+
+// y_row = s_row sum_k Hq[k] (z[col] + beta p_old[col]), fp32 accumulation;
+// with `full`, the fp32 H instead (after a restart).
 template <class T>
 __device__ __forceinline__ void ir_row_product(const BsrViews &bv, const IrWork &w, int row, const float *z,
-                                               const float *p_old, float beta, float y[3]) {
+                                               const float *p_old, float beta, bool full, float y[3]) {
     const int g_lane = threadIdx.x & (kIrGroup - 1);
     const unsigned gmask = ((1u << kIrGroup) - 1u) << (threadIdx.x & (32 - kIrGroup));
     const int kb = bv.row_ptr[row], ke = bv.row_ptr[row + 1];
@@ -292,10 +333,17 @@ __device__ __forceinline__ void ir_row_product(const BsrViews &bv, const IrWork 
             const float zc = __ldcg(z + 3 * c + i);
             v[i] = p_old ? __fmaf_rn(beta, __ldcg(p_old + 3 * c + i), zc) : zc;
         }
-        const T *h = q + (size_t)9 * k;
-        a0 += from_lowp(h[0]) * v[0] + from_lowp(h[1]) * v[1] + from_lowp(h[2]) * v[2];
-        a1 += from_lowp(h[3]) * v[0] + from_lowp(h[4]) * v[1] + from_lowp(h[5]) * v[2];
-        a2 += from_lowp(h[6]) * v[0] + from_lowp(h[7]) * v[1] + from_lowp(h[8]) * v[2];
+        if (full) {
+            const float *h = bv.values + (size_t)9 * k;
+            a0 += __ldg(h + 0) * v[0] + __ldg(h + 1) * v[1] + __ldg(h + 2) * v[2];
+            a1 += __ldg(h + 3) * v[0] + __ldg(h + 4) * v[1] + __ldg(h + 5) * v[2];
+            a2 += __ldg(h + 6) * v[0] + __ldg(h + 7) * v[1] + __ldg(h + 8) * v[2];
+        } else {
+            const T *h = q + (size_t)9 * k;
+            a0 += from_lowp(h[0]) * v[0] + from_lowp(h[1]) * v[1] + from_lowp(h[2]) * v[2];
+            a1 += from_lowp(h[3]) * v[0] + from_lowp(h[4]) * v[1] + from_lowp(h[5]) * v[2];
+            a2 += from_lowp(h[6]) * v[0] + from_lowp(h[7]) * v[1] + from_lowp(h[8]) * v[2];
+        }
     }
 #pragma unroll
     for (int off = kIrGroup / 2; off > 0; off >>= 1) {
@@ -303,27 +351,33 @@ __device__ __forceinline__ void ir_row_product(const BsrViews &bv, const IrWork 
         a1 += __shfl_xor_sync(gmask, a1, off);
         a2 += __shfl_xor_sync(gmask, a2, off);
     }
-    const float s = w.row_scale[row];
+    const float s = full ? 1.0f : w.row_scale[row];
     y[0] = s * a0;
     y[1] = s * a1;
     y[2] = s * a2;
 }
 
 struct IrScalars {
-    float alpha, beta, rz, thr2;
+    double alpha, beta, rz, thr2;
     int status, done;
 };
 
-template <class T>
+// FACTOR: the instantiation for the factor preconditioners (use_precond 2
+// or 3: M r = F^T (F r) or F (F^T r) from the plan's factor fb, two more grid
+// barriers per iteration; an inner solve that breaks down is restarted from
+// e = 0 with block-Jacobi).
+template <class T, bool FACTOR>
 __global__ void __launch_bounds__(kIrThreads, 1)
-    ir_pcg_kernel(BsrViews bv, VertexViews vv, IrWork w, int *error, int maxiter, int use_precond) {
-    __shared__ float s_redf[3][32];
-    __shared__ float s_val[4 * 256];
-    __shared__ float s_tot[3];
+    ir_pcg_kernel(BsrViews bv, VertexViews vv, IrWork w, BatchViews fb, int *error, int maxiter, int use_precond) {
+    __shared__ double s_redf[3][32];
+    __shared__ double s_val[4 * 256];
+    __shared__ double s_tot[3];
     __shared__ IrScalars sc;
     __shared__ int s_ok;
     __shared__ unsigned long long s_base;
     if (*(volatile int *)&w.state[0]) return;  // the outer loop has finished
+    if (*(volatile int *)&w.state[7]) return;  // a restart: no correction this round
+    const bool full = *(volatile int *)&w.state[6] != 0;  // the fp32 H
     const int n = vv.n, nb = gridDim.x, cta = blockIdx.x;
     const int lo = (int)(((long long)n * cta) / nb), hi = (int)(((long long)n * (cta + 1)) / nb);
     const int group = threadIdx.x / kIrGroup, ngroups = blockDim.x / kIrGroup;
@@ -343,117 +397,178 @@ __global__ void __launch_bounds__(kIrThreads, 1)
     unsigned long long target = s_base;
     unsigned k = 0;
     int it = 0;
-    // e0 = 0: r = rhs, z = M r
-    float acc3[3] = {0.0f, 0.0f, 0.0f};
-    for (int row = lo + threadIdx.x; row < hi; row += blockDim.x) {
-        float r[3], z[3];
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            r[q] = w.res[3 * row + q];
-            w.e[3 * row + q] = 0.0f;
-            w.r[3 * row + q] = r[q];
-        }
-        ir_precond(vv.Minv, use_precond, row, r, z);
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            w.z[3 * row + q] = z[q];
-            acc3[0] = __fmaf_rn(r[q], z[q], acc3[0]);
-            acc3[1] = __fmaf_rn(r[q], r[q], acc3[1]);
-        }
-    }
-    acc3[2] = acc3[1];  // ||rhs||^2 = ||r0||^2
-    bool ok = ir_reduce<3>(acc3, w, error, k++, target, s_tot, s_redf, s_val, &s_ok);
-    if (threadIdx.x == 0) {
-        if (!ok) {
-            sc.status = MFEM_TIMEOUT;
-            sc.done = 1;
-        } else {
-            sc.rz = s_tot[0];
-            sc.thr2 = w.inner_tol * w.inner_tol * s_tot[2];
-            sc.beta = 0.0f;
-            sc.status = (isfinite(s_tot[0]) && isfinite(s_tot[1])) ? MFEM_OK : MFEM_NONFINITE;
-            sc.done = sc.status != MFEM_OK || s_tot[1] <= sc.thr2;
-        }
-    }
-    __syncthreads();
-    while (!sc.done) {
-        if (it >= maxiter) break;
-        float *p_new = (it & 1) ? w.p1 : w.p0;
-        const float *p_old = it == 0 ? nullptr : ((it & 1) ? w.p0 : w.p1);
-        const float beta = sc.beta;
-        float pap[1] = {0.0f};
-        for (int row = lo + group; row < hi; row += ngroups) {
-            float y[3];
-            ir_row_product<T>(bv, w, row, w.z, p_old, beta, y);
-            if (g_lead) {
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    const float zq = __ldcg(w.z + 3 * row + q);
-                    const float pq = p_old ? __fmaf_rn(beta, __ldcg(p_old + 3 * row + q), zq) : zq;
-                    p_new[3 * row + q] = pq;
-                    w.Ap[3 * row + q] = y[q];
-                    pap[0] = __fmaf_rn(pq, y[q], pap[0]);
-                }
-            }
-        }
-        if (!ir_reduce<1>(pap, w, error, k++, target, s_tot, s_redf, s_val, &s_ok)) {
-            if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
-            break;
-        }
-        if (threadIdx.x == 0) {
-            if (!isfinite(s_tot[0])) {
-                sc.status = MFEM_NONFINITE;
-                sc.done = 1;
-            } else if (!(s_tot[0] > 0.0f)) {
-                sc.status = MFEM_STAGNATION;
-                sc.done = 1;
-            } else {
-                sc.alpha = sc.rz / s_tot[0];
-            }
-        }
-        __syncthreads();
-        if (sc.done) break;
-        const float alpha = sc.alpha;
-        float acc2[2] = {0.0f, 0.0f};
+    int mode = use_precond, it_done = 0;
+    bool timed_out = false;
+    for (;;) {  // one attempt; a factor solve that breaks down restarts with block-Jacobi
+        const bool factor = FACTOR && mode >= 2;
+        it = 0;
+        // e0 = 0: r = rhs, z = M r
+        double acc3[3] = {0.0, 0.0, 0.0};
         for (int row = lo + threadIdx.x; row < hi; row += blockDim.x) {
             float r[3], z[3];
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
-                w.e[3 * row + q] = __fmaf_rn(alpha, p_new[3 * row + q], w.e[3 * row + q]);
-                r[q] = __fmaf_rn(-alpha, w.Ap[3 * row + q], w.r[3 * row + q]);
+                r[q] = w.res[3 * row + q];
+                w.e[3 * row + q] = 0.0f;
                 w.r[3 * row + q] = r[q];
             }
-            ir_precond(vv.Minv, use_precond, row, r, z);
+            if (factor) continue;  // z comes from the factor passes below
+            ir_precond(vv.Minv, mode, row, r, z);
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
                 w.z[3 * row + q] = z[q];
-                acc2[0] = __fmaf_rn(r[q], z[q], acc2[0]);
-                acc2[1] = __fmaf_rn(r[q], r[q], acc2[1]);
+                acc3[0] = fma((double)r[q], (double)z[q], acc3[0]);
+                acc3[1] = fma((double)r[q], (double)r[q], acc3[1]);
             }
         }
-        if (!ir_reduce<2>(acc2, w, error, k++, target, s_tot, s_redf, s_val, &s_ok)) {
-            if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
-            break;
+        if (factor) {
+            // every row's r in place, then z = M r, then (r, z) and (r, r)
+            double d[1] = {0.0};
+            if (!ir_reduce<1>(d, w, error, k++, target, s_tot, s_redf, s_val, &s_ok) ||
+                !ir_apply_factor(fb, mode, w, error, k, target, s_tot, s_redf, s_val, &s_ok, lo, hi)) {
+                timed_out = true;
+                break;
+            }
+            for (int row = lo + threadIdx.x; row < hi; row += blockDim.x)
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    const float rq = w.r[3 * row + q], zq = w.z[3 * row + q];
+                    acc3[0] = fma((double)rq, (double)zq, acc3[0]);
+                    acc3[1] = fma((double)rq, (double)rq, acc3[1]);
+                }
         }
-        ++it;
+        acc3[2] = acc3[1];  // ||rhs||^2 = ||r0||^2
+        bool ok = ir_reduce<3>(acc3, w, error, k++, target, s_tot, s_redf, s_val, &s_ok);
         if (threadIdx.x == 0) {
-            if (!isfinite(s_tot[0]) || !isfinite(s_tot[1])) {
-                sc.status = MFEM_NONFINITE;
+            if (!ok) {
+                sc.status = MFEM_TIMEOUT;
                 sc.done = 1;
             } else {
-                sc.beta = s_tot[0] / sc.rz;
                 sc.rz = s_tot[0];
-                sc.done = s_tot[1] <= sc.thr2;
+                sc.thr2 = w.inner_tol * w.inner_tol * s_tot[2];
+                sc.beta = 0.0;
+                sc.status = (isfinite(s_tot[0]) && isfinite(s_tot[1])) ? MFEM_OK : MFEM_NONFINITE;
+                sc.done = sc.status != MFEM_OK || s_tot[1] <= sc.thr2;
             }
         }
         __syncthreads();
+        while (!sc.done) {
+            if (it >= maxiter) break;
+            float *p_new = (it & 1) ? w.p1 : w.p0;
+            const float *p_old = it == 0 ? nullptr : ((it & 1) ? w.p0 : w.p1);
+            const float beta = (float)sc.beta;
+            double pap[1] = {0.0};
+            for (int row = lo + group; row < hi; row += ngroups) {
+                float y[3];
+                ir_row_product<T>(bv, w, row, w.z, p_old, beta, full, y);
+                if (g_lead) {
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        const float zq = __ldcg(w.z + 3 * row + q);
+                        const float pq = p_old ? __fmaf_rn(beta, __ldcg(p_old + 3 * row + q), zq) : zq;
+                        p_new[3 * row + q] = pq;
+                        w.Ap[3 * row + q] = y[q];
+                        pap[0] = fma((double)pq, (double)y[q], pap[0]);
+                    }
+                }
+            }
+            if (!ir_reduce<1>(pap, w, error, k++, target, s_tot, s_redf, s_val, &s_ok)) {
+                if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+                break;
+            }
+            if (threadIdx.x == 0) {
+                if (!isfinite(s_tot[0])) {
+                    sc.status = MFEM_NONFINITE;
+                    sc.done = 1;
+                } else if (!(s_tot[0] > 0.0)) {
+                    sc.status = MFEM_STAGNATION;
+                    sc.done = 1;
+                } else {
+                    sc.alpha = sc.rz / s_tot[0];
+                }
+            }
+            __syncthreads();
+            if (sc.done) break;
+            const float alpha = (float)sc.alpha;
+            double acc2[2] = {0.0, 0.0};
+            if (factor) {
+                for (int row = lo + threadIdx.x; row < hi; row += blockDim.x)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        w.e[3 * row + q] = __fmaf_rn(alpha, p_new[3 * row + q], w.e[3 * row + q]);
+                        w.r[3 * row + q] = __fmaf_rn(-alpha, w.Ap[3 * row + q], w.r[3 * row + q]);
+                    }
+                double d[1] = {0.0};
+                if (!ir_reduce<1>(d, w, error, k++, target, s_tot, s_redf, s_val, &s_ok) ||
+                    !ir_apply_factor(fb, mode, w, error, k, target, s_tot, s_redf, s_val, &s_ok, lo, hi)) {
+                    if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+                    break;
+                }
+            }
+            for (int row = lo + threadIdx.x; row < hi; row += blockDim.x) {
+                float r[3], z[3];
+                if (factor) {
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        r[q] = w.r[3 * row + q];
+                        z[q] = w.z[3 * row + q];
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        w.e[3 * row + q] = __fmaf_rn(alpha, p_new[3 * row + q], w.e[3 * row + q]);
+                        r[q] = __fmaf_rn(-alpha, w.Ap[3 * row + q], w.r[3 * row + q]);
+                        w.r[3 * row + q] = r[q];
+                    }
+                    ir_precond(vv.Minv, mode, row, r, z);
+                }
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    w.z[3 * row + q] = z[q];
+                    acc2[0] = fma((double)r[q], (double)z[q], acc2[0]);
+                    acc2[1] = fma((double)r[q], (double)r[q], acc2[1]);
+                }
+            }
+            if (!ir_reduce<2>(acc2, w, error, k++, target, s_tot, s_redf, s_val, &s_ok)) {
+                if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+                break;
+            }
+            ++it;
+            if (threadIdx.x == 0) {
+                if (!isfinite(s_tot[0]) || !isfinite(s_tot[1])) {
+                    sc.status = MFEM_NONFINITE;
+                    sc.done = 1;
+                } else {
+                    sc.beta = s_tot[0] / sc.rz;
+                    sc.rz = s_tot[0];
+                    sc.done = s_tot[1] <= sc.thr2;
+                }
+            }
+            __syncthreads();
+        }
+        if (FACTOR && mode >= 2 && (sc.status == MFEM_STAGNATION || sc.status == MFEM_NONFINITE)) {
+            // no barrier needed: the restart writes e = 0 and r = rhs for
+            // its own rows before its first grid barrier
+            it_done += it;
+            mode = 1;
+            __syncthreads();
+            continue;
+        }
+        break;
     }
+    if (timed_out && threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+    it += it_done;
     if (cta == 0 && threadIdx.x == 0) {
         // the outer loop adds the correction at its next residual; a broken
         // inner solve still hands over its iterate, as the reference's CG does
         w.state[2] += it;
         w.state[3] = 1;
-        if (sc.status == MFEM_TIMEOUT || sc.status == MFEM_NONFINITE) {
+        if (sc.status == MFEM_NONFINITE && !full) {
+            // the 16-bit H broke the inner solve: restart on the fp32 H
+            w.state[3] = 0;
+            w.state[6] = 1;
+            w.state[7] = 1;
+        } else if (sc.status == MFEM_TIMEOUT || sc.status == MFEM_NONFINITE) {
             w.state[5] = sc.status;
             w.state[0] = 1;
         }
@@ -463,8 +578,8 @@ __global__ void __launch_bounds__(kIrThreads, 1)
 inline int blocks_for(int n, int threads) { return (n + threads - 1) / threads; }
 
 template <class T>
-cudaError_t launch_ir_pcg(const BsrViews &bv, const VertexViews &vv, const IrWork &w, int *error, int maxiter,
-                          int use_precond, cudaStream_t s) {
+cudaError_t launch_ir_pcg(const BsrViews &bv, const VertexViews &vv, const IrWork &w, const BatchViews &fb,
+                          int *error, int maxiter, int use_precond, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(w.ctas);
     cfg.blockDim = dim3(kIrThreads);
@@ -474,7 +589,10 @@ cudaError_t launch_ir_pcg(const BsrViews &bv, const VertexViews &vv, const IrWor
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e = cudaLaunchKernelEx(&cfg, ir_pcg_kernel<T>, bv, vv, w, error, maxiter, use_precond);
+    cudaError_t e = use_precond >= 2
+                        ? cudaLaunchKernelEx(&cfg, ir_pcg_kernel<T, true>, bv, vv, w, fb, error, maxiter, use_precond)
+                        : cudaLaunchKernelEx(&cfg, ir_pcg_kernel<T, false>, bv, vv, w, fb, error, maxiter,
+                                             use_precond);
     count_launches(1);
     return e;
 }
@@ -484,8 +602,17 @@ cudaError_t launch_ir_pcg(const BsrViews &bv, const VertexViews &vv, const IrWor
 cudaError_t ir_max_ctas(int device, int *ctas) {
     int sms = 0, occ = 0;
     cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ir_pcg_kernel<__half>, kIrThreads, 0);
+    // the smallest residency of the four instantiations
+    occ = 1 << 30;
+    auto take = [&](const void *fn) {
+        int o = 0;
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, kIrThreads, 0);
+        occ = std::min(occ, o);
+    };
+    take((const void *)ir_pcg_kernel<__half, false>);
+    take((const void *)ir_pcg_kernel<__half, true>);
+    take((const void *)ir_pcg_kernel<__nv_bfloat16, false>);
+    take((const void *)ir_pcg_kernel<__nv_bfloat16, true>);
     if (e != cudaSuccess) return e;
     *ctas = std::max(1, std::min(256, sms * std::max(1, occ)));
     return cudaSuccess;
@@ -494,7 +621,7 @@ cudaError_t ir_max_ctas(int device, int *ctas) {
 int ir_residual_blocks(int n) { return std::max(1, blocks_for(n * kIrGroup, kResThreads)); }
 
 cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const IrWork &w, const PcgWork &pw,
-                               int slot, int maxiter, int use_precond, cudaStream_t s) {
+                               const BatchViews &fb, int slot, int maxiter, int use_precond, cudaStream_t s) {
     if (bv.n == 0) return cudaSuccess;
     const bool bf16 = w.mode == kIrBf16;
     cudaError_t e;
@@ -510,8 +637,8 @@ cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const 
         count_launches(1);
         e = cudaGetLastError();
         if (e == cudaSuccess)
-            e = bf16 ? launch_ir_pcg<__nv_bfloat16>(bv, vv, w, pw.error, maxiter, use_precond, s)
-                     : launch_ir_pcg<__half>(bv, vv, w, pw.error, maxiter, use_precond, s);
+            e = bf16 ? launch_ir_pcg<__nv_bfloat16>(bv, vv, w, fb, pw.error, maxiter, use_precond, s)
+                     : launch_ir_pcg<__half>(bv, vv, w, fb, pw.error, maxiter, use_precond, s);
     }
     if (e == cudaSuccess) {
         // the last correction and the final fp64 residual

@@ -108,7 +108,7 @@ class MfemMixedSolveStats(ctypes.Structure):
         ("outer_iterations", ctypes.c_int32),
         ("inner_iterations", ctypes.c_int32),
         ("status", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("fp32_inner", ctypes.c_int32),
         ("rel_residual", ctypes.c_double),
     ]
 

@@ -282,7 +282,8 @@ class MixedFEMSolver:
                                              _stream_handle(self.device))
         _lib.check(rc, self._plan)
         return [dict(outer_iterations=buf[i].outer_iterations, inner_iterations=buf[i].inner_iterations,
-                     status=buf[i].status, rel_residual=buf[i].rel_residual) for i in range(count.value)]
+                     status=buf[i].status, fp32_inner=bool(buf[i].fp32_inner), rel_residual=buf[i].rel_residual)
+                for i in range(count.value)]
 
     def line_search_stats(self) -> list[dict]:
         """Line-search outcome of each Newton iteration of the last step
