@@ -64,6 +64,8 @@ def parse_args():
     ap.add_argument("--line-search", action="store_true",
                     help="run the workload with the reference's backtracking line search")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the north-star solve variants (learned / FSAI factors, fp16) of the default line")
     ap.add_argument("--cpu-budget-s", type=float, default=30.0, help="CPU time budget of the oracle leg")
     return ap.parse_args()
 
@@ -467,6 +469,67 @@ def run_reference_batched(args):
 # ---------------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------------
+def north_star_solves(mesh, dev, steps=20, warmup=2):
+    """steps/s over the workload's first `steps` steps with the benchmark spec's
+    solves -- learned (or FSAI) factor preconditioners, fp16 mixed precision,
+    every solve to the workload's 1e-6 -- beside the plain fp32 block-Jacobi
+    PCG over the same steps (graph replays, L2 flushed between steps)."""
+    import torch
+    from mfem_gb300 import Model, MixedFEMSolver
+    spec = mesh.spec
+    q0 = torch.as_tensor(mesh.q0, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    out = {"steps": steps, "tolerance": spec.cg_tolerance, "factor_refresh": 8}
+    for precision, pc in (("fp32", "block_jacobi"), ("fp32", "fsai"), ("fp32", "learned"), ("fp16", "block_jacobi"),
+                          ("fp16", "fsai"), ("fp16", "learned")):
+        model = Model.from_beam(mesh, device=dev)
+        kw = dict(iterations=spec.iterations, energy=spec.energy, cg_tolerance=spec.cg_tolerance,
+                  cg_max_iterations=spec.cg_max_iterations, line_search=False, preconditioner=pc,
+                  solver_precision=precision, outer_tolerance=spec.cg_tolerance)
+        if pc != "block_jacobi":
+            kw["factor_refresh"] = 8
+        solver = MixedFEMSolver(model, **kw)
+        if solver.pcg_layout()["variant"] == "global_memory":
+            solver.autotune(q0, spec.dt)
+        s_init = solver.tet_stretch.clone().reshape(-1)
+        st = [model.state(), model.state()]
+
+        def reset():
+            st[0].particle_q.copy_(q0)
+            st[0].particle_qd.zero_()
+            solver.write_buffer("tet_stretch", s_init)
+            solver.write_buffer("tet_lambda", torch.zeros_like(s_init))
+
+        reset()
+        for _ in range(warmup):
+            solver.step(st[0], st[1], None, None, spec.dt)
+            st.reverse()
+        reset()
+        total_ms, its, codes = 0.0, 0, set()
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            solver.step(st[0], st[1], None, None, spec.dt)
+            e1.record(stream)
+            e1.synchronize()
+            total_ms += e0.elapsed_time(e1)
+            if precision == "fp32":
+                rec = solver.solve_stats()
+                its += sum(r["iterations"] for r in rec)
+            else:
+                rec = solver.mixed_stats()
+                its += sum(r["inner_iterations"] for r in rec)
+            codes.update(int(r["status"]) for r in rec)
+            st.reverse()
+        out[f"{precision}+{pc}"] = {"steps_per_s": 1000.0 * steps / total_ms, "pcg_iterations_per_step": its / steps,
+                                    "status_codes": sorted(codes)}
+        solver.close()
+    return out
+
+
 def run_gb300(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -640,6 +703,10 @@ def run_gb300(args, rank, world, local_rank):
 
     if rank != 0:
         return 0
+    variants = None
+    if (world == 1 and not args.no_variants and args.precision == "fp32" and args.preconditioner == "block_jacobi"
+            and not args.line_search):
+        variants = north_star_solves(mesh, dev)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         rate, steps, el = cpu_oracle_rate(mesh, args.cpu_budget_s)
@@ -668,6 +735,7 @@ def run_gb300(args, rank, world, local_rank):
         "pcg_status_codes": sorted(statuses),
         "stage_share": shares,
         "stage_ms_per_step": {k: v / prof_steps for k, v in stage_ms.items()},
+        "north_star_solves": variants,
     }
     print(json.dumps(line), flush=True)
     return 0
