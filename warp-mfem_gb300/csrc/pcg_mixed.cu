@@ -325,24 +325,34 @@ __device__ __forceinline__ void ir_row_product(const BsrViews &bv, const IrWork 
     const int kb = bv.row_ptr[row], ke = bv.row_ptr[row + 1];
     const T *q = reinterpret_cast<const T *>(w.lowp);
     float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-    for (int k = kb + g_lane; k < ke; k += kIrGroup) {
-        const int c = __ldg(bv.col_idx + k);
-        float v[3];
+    // two blocks per lane and trip: their loads are in flight together
+    for (int k = kb + g_lane; k < ke; k += 2 * kIrGroup) {
+        const int k2 = k + kIrGroup;
+        const bool two = k2 < ke;
+        const int kk[2] = {k, two ? k2 : k};
+        const int cc[2] = {__ldg(bv.col_idx + kk[0]), __ldg(bv.col_idx + kk[1])};
+        float v[2][3];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            const float zc = __ldcg(z + 3 * c + i);
-            v[i] = p_old ? __fmaf_rn(beta, __ldcg(p_old + 3 * c + i), zc) : zc;
-        }
-        if (full) {
-            const float *h = bv.values + (size_t)9 * k;
-            a0 += __ldg(h + 0) * v[0] + __ldg(h + 1) * v[1] + __ldg(h + 2) * v[2];
-            a1 += __ldg(h + 3) * v[0] + __ldg(h + 4) * v[1] + __ldg(h + 5) * v[2];
-            a2 += __ldg(h + 6) * v[0] + __ldg(h + 7) * v[1] + __ldg(h + 8) * v[2];
-        } else {
-            const T *h = q + (size_t)9 * k;
-            a0 += from_lowp(h[0]) * v[0] + from_lowp(h[1]) * v[1] + from_lowp(h[2]) * v[2];
-            a1 += from_lowp(h[3]) * v[0] + from_lowp(h[4]) * v[1] + from_lowp(h[5]) * v[2];
-            a2 += from_lowp(h[6]) * v[0] + from_lowp(h[7]) * v[1] + from_lowp(h[8]) * v[2];
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float zc = __ldcg(z + 3 * cc[u] + i);
+                v[u][i] = p_old ? __fmaf_rn(beta, __ldcg(p_old + 3 * cc[u] + i), zc) : zc;
+            }
+        if (!two) v[1][0] = v[1][1] = v[1][2] = 0.0f;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (full) {
+                const float *h = bv.values + (size_t)9 * kk[u];
+                a0 += __ldg(h + 0) * v[u][0] + __ldg(h + 1) * v[u][1] + __ldg(h + 2) * v[u][2];
+                a1 += __ldg(h + 3) * v[u][0] + __ldg(h + 4) * v[u][1] + __ldg(h + 5) * v[u][2];
+                a2 += __ldg(h + 6) * v[u][0] + __ldg(h + 7) * v[u][1] + __ldg(h + 8) * v[u][2];
+            } else {
+                const T *h = q + (size_t)9 * kk[u];
+                a0 += from_lowp(h[0]) * v[u][0] + from_lowp(h[1]) * v[u][1] + from_lowp(h[2]) * v[u][2];
+                a1 += from_lowp(h[3]) * v[u][0] + from_lowp(h[4]) * v[u][1] + from_lowp(h[5]) * v[u][2];
+                a2 += from_lowp(h[6]) * v[u][0] + from_lowp(h[7]) * v[u][1] + from_lowp(h[8]) * v[u][2];
+            }
         }
     }
 #pragma unroll
