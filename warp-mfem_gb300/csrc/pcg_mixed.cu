@@ -39,6 +39,7 @@ namespace {
 
 constexpr int kIrThreads = 512;
 constexpr int kIrGroup = 4;  // lanes per block row in the product
+constexpr int kIrDepth = 4;  // blocks per lane and loop trip in the product
 constexpr int kResThreads = 256;
 constexpr long long kIrWaitCycles = 8000000000ll;
 
@@ -325,23 +326,27 @@ __device__ __forceinline__ void ir_row_product(const BsrViews &bv, const IrWork 
     const int kb = bv.row_ptr[row], ke = bv.row_ptr[row + 1];
     const T *q = reinterpret_cast<const T *>(w.lowp);
     float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-    // two blocks per lane and trip: their loads are in flight together
-    for (int k = kb + g_lane; k < ke; k += 2 * kIrGroup) {
-        const int k2 = k + kIrGroup;
-        const bool two = k2 < ke;
-        const int kk[2] = {k, two ? k2 : k};
-        const int cc[2] = {__ldg(bv.col_idx + kk[0]), __ldg(bv.col_idx + kk[1])};
-        float v[2][3];
+    // kIrDepth blocks per lane and trip: their loads are in flight together
+    for (int k = kb + g_lane; k < ke; k += kIrDepth * kIrGroup) {
+        int kk[kIrDepth], cc[kIrDepth];
+        bool ok[kIrDepth];
 #pragma unroll
-        for (int u = 0; u < 2; ++u)
+        for (int u = 0; u < kIrDepth; ++u) {
+            ok[u] = k + u * kIrGroup < ke;
+            kk[u] = ok[u] ? k + u * kIrGroup : k;
+            cc[u] = __ldg(bv.col_idx + kk[u]);
+        }
+        float v[kIrDepth][3];
+#pragma unroll
+        for (int u = 0; u < kIrDepth; ++u)
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
                 const float zc = __ldcg(z + 3 * cc[u] + i);
                 v[u][i] = p_old ? __fmaf_rn(beta, __ldcg(p_old + 3 * cc[u] + i), zc) : zc;
+                if (!ok[u]) v[u][i] = 0.0f;
             }
-        if (!two) v[1][0] = v[1][1] = v[1][2] = 0.0f;
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
+        for (int u = 0; u < kIrDepth; ++u) {
             if (full) {
                 const float *h = bv.values + (size_t)9 * kk[u];
                 a0 += __ldg(h + 0) * v[u][0] + __ldg(h + 1) * v[u][1] + __ldg(h + 2) * v[u][2];
