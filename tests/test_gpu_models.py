@@ -46,3 +46,41 @@ def test_fem_beam_npz_model_steps_match_oracle(tmp_path, energy):
         got = s1.particle_q.cpu().numpy()
         assert np.abs(got - q).max() <= 1e-5 * np.abs(q).max()
         s0, s1 = s1, s0
+
+
+@pytest.mark.parametrize("pc", ["fsai", "learned"])
+def test_fem_beam_with_factor_preconditioner(tmp_path, pc):
+    """The 5-tet grid has rows with 9 and 10 lower blocks: FSAI sets them up
+    with the warp kernel (the per-thread kernel takes rows of up to 8).  The
+    factor equals a float64 FSAI of the same H, and a trajectory stays within
+    1e-5 of the oracle."""
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).parent))
+    from test_gpu_fsai import fsai_numpy, lower_pattern
+    mesh = _fem_beam_mesh(tmp_path, mu=100.0, energy="neohookean")
+    model = Model.from_beam(mesh, device=DEV)
+    solver = MixedFEMSolver(model, iterations=8, energy="neohookean", line_search=False, preconditioner=pc)
+    ref = O.OracleSolver(mesh, dtype=np.float64)
+    s0, s1 = model.state(), model.state()
+    q, qd = mesh.q0, mesh.qd0
+    for _ in range(3):
+        solver.step(s0, s1, None, None, mesh.spec.dt)
+        q, qd = ref.step(q, qd, mesh.spec.dt)
+        assert all(st["status"] == 0 and st["iterations"] > 0 for st in solver.solve_stats())
+        got = s1.particle_q.cpu().numpy()
+        assert np.abs(got - q).max() <= 1e-5 * np.abs(q).max()
+        s0, s1 = s1, s0
+    if pc == "fsai":
+        rp = solver.read_buffer("row_ptr").cpu().numpy()
+        ci = solver.read_buffer("col_idx").cpu().numpy()
+        vals = solver.read_buffer("h_values").cpu().numpy().astype(np.float64).reshape(-1, 3, 3)
+        G = solver.read_buffer("precond_factor").cpu().numpy().astype(np.float64).reshape(-1, 3, 3)
+        lrow, _, _ = lower_pattern(rp, ci)
+        assert (np.diff(lrow) > 8).any()
+        # the factor of the last assembly (the step's 8th Newton iteration)
+        ref_G, fallback = fsai_numpy(rp, ci, vals)
+        assert not fallback
+        for i in range(mesh.n):
+            blk = slice(lrow[i], lrow[i + 1])
+            assert np.abs(G[blk] - ref_G[blk]).max() <= 1e-3 * np.abs(ref_G[blk]).max(), i
