@@ -65,7 +65,7 @@ def parse_args():
                     help="run the workload with the reference's backtracking line search")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true",
-                    help="skip the north-star solve variants (learned / FSAI factors, fp16) of the default line")
+                    help="skip the solve variants (learned / FSAI factors, fp16) of the default line")
     ap.add_argument("--cpu-budget-s", type=float, default=30.0, help="CPU time budget of the oracle leg")
     return ap.parse_args()
 
@@ -469,9 +469,9 @@ def run_reference_batched(args):
 # ---------------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------------
-def north_star_solves(mesh, dev, steps=20, warmup=2):
-    """steps/s over the workload's first `steps` steps with the benchmark spec's
-    solves -- learned (or FSAI) factor preconditioners, fp16 mixed precision,
+def solve_variants(mesh, dev, steps=20, warmup=2):
+    """steps/s over the workload's first `steps` steps with the other solves
+    -- learned (or FSAI) factor preconditioners, fp16 mixed precision,
     every solve to the workload's 1e-6 -- beside the plain fp32 block-Jacobi
     PCG over the same steps (graph replays, L2 flushed between steps)."""
     import torch
@@ -706,7 +706,7 @@ def run_gb300(args, rank, world, local_rank):
     variants = None
     if (world == 1 and not args.no_variants and args.precision == "fp32" and args.preconditioner == "block_jacobi"
             and not args.line_search):
-        variants = north_star_solves(mesh, dev)
+        variants = solve_variants(mesh, dev)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         rate, steps, el = cpu_oracle_rate(mesh, args.cpu_budget_s)
@@ -735,7 +735,7 @@ def run_gb300(args, rank, world, local_rank):
         "pcg_status_codes": sorted(statuses),
         "stage_share": shares,
         "stage_ms_per_step": {k: v / prof_steps for k, v in stage_ms.items()},
-        "north_star_solves": variants,
+        "solve_variants": variants,
     }
     print(json.dumps(line), flush=True)
     return 0

@@ -329,8 +329,8 @@ int mfem_step_mixed_stats(mfem_plan *plan, mfem_mixed_solve_stats *h_stats, int3
  * p.Ap <= 0) is solved again with block-Jacobi.  Net: width 64, three
  * message-passing layers over H's block graph with weights ||(S H S)_ij||_F,
  * S = diag(tr(H_ii)/3)^-1/2; L = S L~ with L~ the net's output.  Needs a plan
- * created with preconditioner = 3.  No reference counterpart: the north
- * star's learned preconditioner.  Synchronises the device and drops
+ * created with preconditioner = 3.  No reference counterpart (the
+ * reference's PCG is block-Jacobi).  Synchronises the device and drops
  * captured graphs. */
 int mfem_plan_set_factor_net(mfem_plan *plan, const float *h_params, int64_t n_params,
                              const float *h_vertex_static);
@@ -344,8 +344,8 @@ int mfem_plan_set_factor_net(mfem_plan *plan, const float *h_params, int64_t n_p
  * block-Jacobi PCG per body (own scalars and stopping test, the reference's
  * solve applied to each body) in a single persistent launch; the other
  * kernels run on the union.  Needs a plan created with line_search = 0 and
- * the FP32 solve.  No reference counterpart: the benchmark spec's batch of
- * uneven bodies.  Synchronises the device and drops captured graphs. */
+ * the FP32 solve.  No reference counterpart (the reference steps one body
+ * per solver).  Synchronises the device and drops captured graphs. */
 int mfem_plan_set_bodies(mfem_plan *plan, int32_t n_bodies, const int32_t *h_vertex_offsets,
                          const int32_t *h_tet_offsets, const int32_t *h_body_energy,
                          const float *h_body_gravity);

@@ -1,7 +1,7 @@
 """The mixed-precision global solve (16-bit blocks with per-row scales, fp32
 inner PCG, fp64 iterative refinement) on the GPU.
 
-It has no reference counterpart.  Its bar is the benchmark spec's:
+It has no reference counterpart.  Its bar:
 * the fp64 residual ||g - H dx|| / ||g|| of the returned fp64 solution,
   recomputed here in numpy from the same fp32 H and g, is below the outer
   tolerance, and agrees with the residual the solver reports;

@@ -3,8 +3,8 @@
 Tolerances (float32 kernels against the float64 oracle on the same float32
 inputs): per-tet terms 2e-5 of each quantity's largest magnitude; assembled
 blocks and rhs 1e-5; positions after a step or a trajectory 1e-5 relative to
-the largest position (the bar of the benchmark spec: per-step positions within
-1e-5 relative in float32).  Sparsity and scatter maps are compared bit for bit.
+the largest position (per-step positions within 1e-5 relative in
+float32).  Sparsity and scatter maps are compared bit for bit.
 """
 import os
 

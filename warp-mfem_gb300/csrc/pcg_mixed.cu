@@ -12,8 +12,8 @@
 //   best, or turns non-finite), the 16-bit H is too coarse for this system:
 //   the solve restarts from the warm start with the fp32 H in the inner PCG.
 //
-// This is the benchmark spec's mixed-precision variant of the global solve (the
-// reference solves H dx = g with one float32 PCG, src/mfem/refinement/
+// This is a mixed-precision variant of the global solve (the reference
+// solves H dx = g with one float32 PCG, src/mfem/refinement/
 // solver.py:581-609).  Every launch is unconditional so the sequence can be
 // captured: a device flag written by the residual kernel turns the later
 // kernels of a converged solve into no-ops.

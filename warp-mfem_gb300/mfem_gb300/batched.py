@@ -4,8 +4,8 @@
 mesh and one plan: the element, assembly and local-solve kernels run on the
 union, while the global solve is one block-Jacobi PCG per body (its own
 scalars and stopping test, as if each body were stepped alone with the
-reference's ``RefinementSolver.step``) in a single persistent launch.  It is
-the benchmark spec's batch of uneven bodies; the reference has no counterpart.
+reference's ``RefinementSolver.step``) in a single persistent launch.  The
+reference has no counterpart: it steps one body per solver.
 The plain update is used (no line search), with the fp32 PCG.
 """
 from __future__ import annotations
