@@ -347,9 +347,11 @@ def run_batched(args, rank, world, local_rank):
     voff = batch.vertex_offsets
     nnzb_b = (row_ptr[voff[1:]] - row_ptr[voff[:-1]]).astype(np.float64)
     n_b = np.diff(voff).astype(np.float64)
-    # FSAI replaces the 36 n bytes of block-Jacobi blocks by two passes over
-    # G's lower blocks (G, col_idx, transposed slots, y and z)
-    per_it_b = (86.0 * nnzb_b + 222.0 * n_b) if fsai else (40.0 * nnzb_b + 172.0 * n_b)
+    # a factor preconditioner replaces the 36 n bytes of block-Jacobi blocks
+    # by two passes over the factor's nnzl = (nnzb + n)/2 blocks (20 B BF16
+    # block + 4 B column each, plus the pass's 12 B vector in and 12 B out
+    # per row): 40 nnzb + 136 n + 24 (nnzb + n) + 48 n
+    per_it_b = (64.0 * nnzb_b + 208.0 * n_b) if fsai else (40.0 * nnzb_b + 172.0 * n_b)
     x = Bst.particle_q
     prof_steps = max(1, min(3, args.steps))
     for _ in range(prof_steps):
@@ -382,7 +384,7 @@ def run_batched(args, rank, world, local_rank):
                 "traffic": None,
                 "kernel": f"batched_pcg_kernel (per-body {args.preconditioner} PCGs, one launch)",
                 "algorithmic_bytes_per_launch": bytes_pcg / solves,
-                "bytes_per_body_iteration": (("86 nnzb_b + 222 n_b" if fsai else "40 nnzb_b + 172 n_b") +
+                "bytes_per_body_iteration": (("64 nnzb_b + 208 n_b" if fsai else "40 nnzb_b + 172 n_b") +
                                              ", summed over bodies x (iterations_b + 1)"),
                 "avg_launch_ms": pcg_ms / solves, "peak_source": peak_src}
 

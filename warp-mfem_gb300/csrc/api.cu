@@ -1268,6 +1268,8 @@ int install_bodies(mfem_plan *p, int n_bodies, const int32_t *voff, const int32_
         alloc(&d_umap, nnzl * sizeof(int));
         alloc(&bw.Lval, nnzl * 9 * sizeof(float));
         alloc(&bw.Uval, nnzl * 9 * sizeof(float));
+        alloc(&bw.Lb, nnzl * kFactorLd * sizeof(__nv_bfloat16));
+        alloc(&bw.Ub, nnzl * kFactorLd * sizeof(__nv_bfloat16));
         alloc(&bw.y, n3 * sizeof(float));
         alloc(&bw.dx0, n3 * sizeof(float));
         if (p->cfg.preconditioner == 2) {

@@ -1,16 +1,33 @@
 // One pass of a factor preconditioner, shared by the global-memory PCGs: out
 // = F in over rows [lo, hi) for one form of the factor (row pointers,
-// columns, row-major 3x3 blocks), `group` lanes per row.  `in` is read with
-// __ldcg (other CTAs wrote it during this launch) unless LOCAL says this
-// CTA's own stores, ordered by __syncthreads, are the only writers.
+// columns, row-major 3x3 blocks in BF16, kFactorLd values per block), `group`
+// lanes per row.  `in` is read with __ldcg (other CTAs wrote it during this
+// launch) unless LOCAL says this CTA's own stores, ordered by __syncthreads,
+// are the only writers.
 #pragma once
+
+#include <cstring>
 
 #include "internal.h"
 
 namespace mfem {
 
+// the 3x3 block k of a BF16 factor form (kFactorLd values per block)
+__device__ __forceinline__ void factor_block(const __nv_bfloat16 *val, int k, float f[9]) {
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(val + (size_t)kFactorLd * k);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const uint32_t u = __ldg(w + i);
+        __nv_bfloat162 b;
+        memcpy(&b, &u, 4);
+        const float2 t = __bfloat1622float2(b);
+        f[2 * i] = t.x;
+        if (2 * i + 1 < 9) f[2 * i + 1] = t.y;
+    }
+}
+
 template <bool LOCAL, int GROUP>
-__device__ __forceinline__ void factor_pass(const int *rp, const int *col, const float *val, const float *in,
+__device__ __forceinline__ void factor_pass(const int *rp, const int *col, const __nv_bfloat16 *val, const float *in,
                                             float *out, int lo, int hi) {
     const int g_lane = threadIdx.x & (GROUP - 1);
     const unsigned gmask = ((1u << GROUP) - 1u) << (threadIdx.x & (32 - GROUP));
@@ -27,14 +44,15 @@ __device__ __forceinline__ void factor_pass(const int *rp, const int *col, const
             const float v0 = ld(in + 3 * c), v1 = ld(in + 3 * c + 1), v2 = ld(in + 3 * c + 2);
             float w0 = ld(in + 3 * c2), w1 = ld(in + 3 * c2 + 1), w2 = ld(in + 3 * c2 + 2);
             if (!two) w0 = w1 = w2 = 0.0f;
-            const float *f = val + (size_t)9 * k;
-            const float *f2 = val + (size_t)9 * (two ? k2 : k);
-            a0 += __ldg(f + 0) * v0 + __ldg(f + 1) * v1 + __ldg(f + 2) * v2;
-            a1 += __ldg(f + 3) * v0 + __ldg(f + 4) * v1 + __ldg(f + 5) * v2;
-            a2 += __ldg(f + 6) * v0 + __ldg(f + 7) * v1 + __ldg(f + 8) * v2;
-            a0 += __ldg(f2 + 0) * w0 + __ldg(f2 + 1) * w1 + __ldg(f2 + 2) * w2;
-            a1 += __ldg(f2 + 3) * w0 + __ldg(f2 + 4) * w1 + __ldg(f2 + 5) * w2;
-            a2 += __ldg(f2 + 6) * w0 + __ldg(f2 + 7) * w1 + __ldg(f2 + 8) * w2;
+            float f[9], f2[9];
+            factor_block(val, k, f);
+            factor_block(val, two ? k2 : k, f2);
+            a0 += f[0] * v0 + f[1] * v1 + f[2] * v2;
+            a1 += f[3] * v0 + f[4] * v1 + f[5] * v2;
+            a2 += f[6] * v0 + f[7] * v1 + f[8] * v2;
+            a0 += f2[0] * w0 + f2[1] * w1 + f2[2] * w2;
+            a1 += f2[3] * w0 + f2[4] * w1 + f2[5] * w2;
+            a2 += f2[6] * w0 + f2[7] * w1 + f2[8] * w2;
         }
 #pragma unroll
         for (int off = GROUP / 2; off > 0; off >>= 1) {
@@ -54,7 +72,7 @@ __device__ __forceinline__ void factor_pass(const int *rp, const int *col, const
 // (M = F F^T: upper form first), as (row pointers, columns, values) pairs.
 struct FactorForms {
     const int *rp0, *c0, *rp1, *c1;
-    const float *v0, *v1;
+    const __nv_bfloat16 *v0, *v1;
 };
 
 __device__ __forceinline__ FactorForms factor_forms(const BatchViews &bw, int mode) {
@@ -62,10 +80,10 @@ __device__ __forceinline__ FactorForms factor_forms(const BatchViews &bw, int mo
     FactorForms f;
     f.rp0 = lower_first ? bw.lrow : bw.urow;
     f.c0 = lower_first ? bw.lcol : bw.ucol;
-    f.v0 = lower_first ? bw.Lval : bw.Uval;
+    f.v0 = lower_first ? bw.Lb : bw.Ub;
     f.rp1 = lower_first ? bw.urow : bw.lrow;
     f.c1 = lower_first ? bw.ucol : bw.lcol;
-    f.v1 = lower_first ? bw.Uval : bw.Lval;
+    f.v1 = lower_first ? bw.Ub : bw.Lb;
     return f;
 }
 

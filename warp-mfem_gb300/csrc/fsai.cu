@@ -306,19 +306,29 @@ __global__ void __launch_bounds__(kFsaiThreads) fsai_setup_kernel(BsrViews bv, B
     }
 }
 
-// F^T in upper-CSR order: Uval[u] = Lval[umap[u]]^T
+// F^T in upper-CSR order, Uval[u] = Lval[umap[u]]^T, and the BF16 copies
+// of both forms
 __global__ void factor_transpose_kernel(BatchViews bw) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= bw.nnzl) return;
     const float *src = bw.Lval + (size_t)9 * bw.umap[u];
+    const float *own = bw.Lval + (size_t)9 * u;
     float *dst = bw.Uval + (size_t)9 * u;
+    __nv_bfloat16 *ub = bw.Ub + (size_t)kFactorLd * u;
+    __nv_bfloat16 *lb = bw.Lb + (size_t)kFactorLd * u;
     float v[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) v[q] = src[q];
 #pragma unroll
     for (int p = 0; p < 3; ++p)
 #pragma unroll
-        for (int q = 0; q < 3; ++q) dst[3 * p + q] = v[3 * q + p];
+        for (int q = 0; q < 3; ++q) {
+            dst[3 * p + q] = v[3 * q + p];
+            ub[3 * p + q] = __float2bfloat16_rn(v[3 * q + p]);
+        }
+#pragma unroll
+    for (int q = 0; q < 9; ++q) lb[q] = __float2bfloat16_rn(own[q]);
+    ub[9] = lb[9] = __float2bfloat16_rn(0.0f);
 }
 
 }  // namespace

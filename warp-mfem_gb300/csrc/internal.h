@@ -97,8 +97,12 @@ struct BatchViews {
     const int *lrow, *lcol;    // [n + 1], [nnzl]
     const int *urow, *ucol;    // [n + 1], [nnzl]
     const int *umap;           // [nnzl] upper entry -> lower entry of the transposed block
-    float *Lval;               // [nnzl][9] F, row-major blocks
+    float *Lval;               // [nnzl][9] F, row-major blocks (the setup's output)
     float *Uval;               // [nnzl][9] F^T in upper-CSR order
+    // BF16 copies the PCG passes read, kFactorLd values per block (the 10th
+    // is padding: 20-byte blocks keep 4-byte loads aligned); M = F^T F or
+    // F F^T stays symmetric positive definite whatever F's rounding
+    __nv_bfloat16 *Lb, *Ub;
     float *y;                  // [n][3] the first pass's output
     float *dx0;                // [n][3] warm start kept for a block-Jacobi retry
     // FSAI setup: per row, the H slot (or -1) of every pair (a, b), b <= a,
@@ -142,6 +146,7 @@ struct FactorNetViews {
     int ready;                         // weights and static features are set
 };
 
+constexpr int kFactorLd = 10;
 constexpr int kFsaiMaxCols = 16;  // lower block columns a row may have for FSAI
 constexpr int kFsaiDim = 3 * kFsaiMaxCols;
 
