@@ -70,3 +70,25 @@ def test_beam_stays_on_its_trajectory_past_step_20():
         assert all(s["status"] == _lib.MFEM_OK for s in st), (step, st)
         q = A.particle_q
         assert bool(torch.isfinite(q).all()) and float(q.abs().max()) < 1.1 * extent, step
+
+
+@pytest.mark.parametrize("line_search", [False, True])
+def test_full_beam_fifty_steps_converge(line_search):
+    """The nh_beam workload's whole 50-step run (64x16x16 cells): every solve
+    converges and the beam stays bounded, with the plain update and with the
+    reference's default line search."""
+    mesh = beams.build_beam("nh_beam")
+    model = Model.from_beam(mesh, device=DEV)
+    solver = MixedFEMSolver(model, iterations=mesh.spec.iterations, energy=mesh.spec.energy,
+                            line_search=line_search)
+    A, B = model.state(), model.state()
+    A.particle_q.copy_(torch.as_tensor(mesh.q0, device=DEV))
+    extent = float(np.abs(mesh.q0).max())
+    for step in range(50):
+        solver.step(A, B, None, None, mesh.spec.dt)
+        A, B = B, A
+        assert all(s["status"] == _lib.MFEM_OK for s in solver.solve_stats()), step
+        if line_search:
+            assert all(e["status"] == _lib.MFEM_OK for e in solver.line_search_stats()), step
+    q = A.particle_q
+    assert bool(torch.isfinite(q).all()) and float(q.abs().max()) < 1.1 * extent

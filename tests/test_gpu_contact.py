@@ -47,7 +47,7 @@ def tool_pose(k):
     return np.array([[0.85, 0.245 - 0.002 * k, 0.1, 0.0, 0.0, 0.0, 1.0]], dtype=np.float32)
 
 
-def scene(line_search=False, iterations=8, use_cuda_graph=True, shapes=True):
+def scene(line_search=False, iterations=8, use_cuda_graph=True, shapes=True, **extra):
     mesh = beams.build_beam("cantilever")
     tris = C.boundary_tris(mesh.tet_indices, mesh.rest_q.astype(np.float64))
     model = Model.from_beam(mesh, device=DEV)
@@ -57,7 +57,7 @@ def scene(line_search=False, iterations=8, use_cuda_graph=True, shapes=True):
         model.add_shape_capsule(0.03, 0.15, body=0)
         model.set_tri_indices(tris)
     solver = MixedFEMSolver(model, iterations=iterations, line_search=line_search, use_cuda_graph=use_cuda_graph,
-                            **(PARAMS if shapes else {}))
+                            **(PARAMS if shapes else {}), **extra)
     oshapes = [dict(type=C.SHAPE_PLANE, transform=PLANE_POSE, scale=[0, 0, 0], body=-1),
                dict(type=C.SHAPE_CAPSULE, transform=[0, 0, 0, 0, 0, 0, 1], scale=[0.03, 0.15, 0.0], body=0)]
     co = C.ContactOracle(oshapes, d0=PARAMS["contact_d0"], d1=PARAMS["contact_d1"],
@@ -194,6 +194,23 @@ def test_contact_trajectory_matches_oracle(line_search, steps):
         assert all(st["status"] == 0 for st in solver.solve_stats())
         close(A.particle_q.cpu().numpy(), q, 1e-5)
     assert q[:, 1].min() < -0.015  # the tool pushed the tip onto the plane
+
+
+@pytest.mark.parametrize("pc", ["fsai", "learned"])
+def test_contact_trajectory_with_factor_preconditioner(pc):
+    """Contact blocks enter H before the factor is built from it."""
+    mesh, model, solver, co = scene(preconditioner=pc)
+    ref = O.OracleSolver(mesh, dtype=np.float64, contact=co)
+    A, B = model.state(), model.state()
+    q, qd = mesh.q0.astype(np.float64), mesh.qd0.astype(np.float64)
+    for k in range(12):
+        B.body_q.copy_(torch.as_tensor(tool_pose(k), device=DEV))
+        solver.step(A, B, None, None, mesh.spec.dt)
+        ref.body_q = tool_pose(k).astype(np.float64)
+        q, qd = ref.step(q, qd, mesh.spec.dt)
+        A, B = B, A
+        assert all(st["status"] == 0 for st in solver.solve_stats())
+        close(A.particle_q.cpu().numpy(), q, 1e-5)
 
 
 def test_graph_and_eager_agree_bitwise_with_contact():

@@ -122,6 +122,23 @@ def test_line_search_trajectory_matches_oracle(name, cells, steps):
         close(A.particle_q.cpu().numpy(), q_ref, 1e-5)
 
 
+@pytest.mark.parametrize("pc", ["fsai", "learned"])
+def test_line_search_with_factor_preconditioner(pc):
+    mesh, model, solver = make("nh_beam", (16, 4, 4), preconditioner=pc)
+    dt = mesh.spec.dt
+    ref = O.OracleSolver(mesh, dtype=np.float64, line_search=True)
+    A, B = model.state(), model.state()
+    A.particle_q.copy_(torch.as_tensor(mesh.q0, device=DEV))
+    q_ref, qd_ref = mesh.q0.astype(np.float64), mesh.qd0.astype(np.float64)
+    for k in range(4):
+        solver.step(A, B, None, None, dt)
+        A, B = B, A
+        q_ref, qd_ref = ref.step(q_ref, qd_ref, dt)
+        assert all(e["status"] == 0 for e in solver.line_search_stats())
+        assert all(s["status"] == 0 for s in solver.solve_stats())
+        close(A.particle_q.cpu().numpy(), q_ref, 1e-5)
+
+
 def test_iteration_cap_leaves_state_unchanged():
     """line_search_max_iterations=1: the counter after the first trial is
     already at the cap, so nothing is ever written and x stays at q_in."""
