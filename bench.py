@@ -51,7 +51,7 @@ def parse_args():
     ap.add_argument("--workload", default="nh_beam")
     ap.add_argument("--profile-steps", type=int, default=10, help="steps of the eager stage profile")
     ap.add_argument("--pcg-ctas", type=int, default=0, help="persistent PCG CTAs (0: one per SM)")
-    ap.add_argument("--pcg-variant", default="auto", choices=["auto", "standard", "single_reduction"])
+    ap.add_argument("--pcg-variant", default="auto", choices=["auto", "standard", "single_reduction", "gather"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16", "fp16"],
                     help="global solve: fp32 PCG (the workload's) or mixed-precision iterative refinement")
     ap.add_argument("--outer-tolerance", type=float, default=1.0e-6,

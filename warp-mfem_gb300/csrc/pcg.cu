@@ -57,6 +57,7 @@ namespace {
 
 constexpr int kPcgThreads = 512;
 constexpr int kGroup = 4;                         // lanes per block row in the product
+constexpr int kGatherDepth = 4;                   // blocks per lane and trip in the gather product
 constexpr int kMaxCtas = 256;
 constexpr long long kWaitCycles = 8000000000ll;   // ~4 s at 2 GHz per wait
 constexpr size_t kStaticSmem = 12 * 1024;         // static shared memory reserve
@@ -761,25 +762,33 @@ __device__ __forceinline__ void gather_product(const PcgArgs &a, const int *rowo
     for (int i = group; i < nrows; i += ngroups) {
         const int kb = rowoff[i], ke = rowoff[i + 1];
         float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-        for (int k = kb + g_lane; k < ke; k += kGroup) {
-            const float *h;
-            int c;
-            if (CACHE) {
-                h = sH + (size_t)k * 9;
-                c = sCol[k];
-            } else {
-                h = a.values + (size_t)(blk_lo + k) * 9;
-                c = __ldg(a.col_idx + blk_lo + k);
-            }
-            float v[3];
+        // kGatherDepth blocks per lane and trip: their L2 gathers are in
+        // flight together
+        for (int k = kb + g_lane; k < ke; k += kGatherDepth * kGroup) {
+            int c[kGatherDepth], kk[kGatherDepth];
+            bool ok[kGatherDepth];
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                const float zc = __ldcg(z + 3 * c + q);
-                v[q] = p_old ? __fmaf_rn(beta, __ldcg(p_old + 3 * c + q), zc) : zc;
+            for (int u = 0; u < kGatherDepth; ++u) {
+                ok[u] = k + u * kGroup < ke;
+                kk[u] = ok[u] ? k + u * kGroup : k;
+                c[u] = CACHE ? sCol[kk[u]] : __ldg(a.col_idx + blk_lo + kk[u]);
             }
-            a0 += h[0] * v[0] + h[1] * v[1] + h[2] * v[2];
-            a1 += h[3] * v[0] + h[4] * v[1] + h[5] * v[2];
-            a2 += h[6] * v[0] + h[7] * v[1] + h[8] * v[2];
+            float v[kGatherDepth][3];
+#pragma unroll
+            for (int u = 0; u < kGatherDepth; ++u)
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    const float zc = __ldcg(z + 3 * c[u] + q);
+                    v[u][q] = p_old ? __fmaf_rn(beta, __ldcg(p_old + 3 * c[u] + q), zc) : zc;
+                    if (!ok[u]) v[u][q] = 0.0f;
+                }
+#pragma unroll
+            for (int u = 0; u < kGatherDepth; ++u) {
+                const float *h = CACHE ? sH + (size_t)kk[u] * 9 : a.values + (size_t)(blk_lo + kk[u]) * 9;
+                a0 += h[0] * v[u][0] + h[1] * v[u][1] + h[2] * v[u][2];
+                a1 += h[3] * v[u][0] + h[4] * v[u][1] + h[5] * v[u][2];
+                a2 += h[6] * v[u][0] + h[7] * v[u][1] + h[8] * v[u][2];
+            }
         }
 #pragma unroll
         for (int off = kGroup / 2; off > 0; off >>= 1) {
