@@ -4,7 +4,9 @@ import sys
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-for p in (os.path.join(ROOT, "warp-mfem_gb300"), ROOT):
+# the package, the repository root (oracle/) and tests/ (shared references
+# such as fsai_reference)
+for p in (os.path.join(ROOT, "warp-mfem_gb300"), ROOT, os.path.join(ROOT, "tests")):
     if p not in sys.path:
         sys.path.insert(0, p)
 

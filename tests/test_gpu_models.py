@@ -54,10 +54,7 @@ def test_fem_beam_with_factor_preconditioner(tmp_path, pc):
     with the warp kernel (the per-thread kernel takes rows of up to 8).  The
     factor equals a float64 FSAI of the same H, and a trajectory stays within
     1e-5 of the oracle."""
-    import sys
-    from pathlib import Path
-    sys.path.insert(0, str(Path(__file__).parent))
-    from test_gpu_fsai import fsai_numpy, lower_pattern
+    from fsai_reference import fsai_numpy, lower_pattern
     mesh = _fem_beam_mesh(tmp_path, mu=100.0, energy="neohookean")
     model = Model.from_beam(mesh, device=DEV)
     solver = MixedFEMSolver(model, iterations=8, energy="neohookean", line_search=False, preconditioner=pc)
