@@ -51,7 +51,8 @@ def parse_args():
     ap.add_argument("--workload", default="nh_beam")
     ap.add_argument("--profile-steps", type=int, default=10, help="steps of the eager stage profile")
     ap.add_argument("--pcg-ctas", type=int, default=0, help="persistent PCG CTAs (0: one per SM)")
-    ap.add_argument("--pcg-variant", default="auto", choices=["auto", "standard", "single_reduction", "gather"])
+    ap.add_argument("--pcg-variant", default="auto",
+                    choices=["auto", "standard", "single_reduction", "gather", "factor", "global_memory"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16", "fp16"],
                     help="global solve: fp32 PCG (the workload's) or mixed-precision iterative refinement")
     ap.add_argument("--outer-tolerance", type=float, default=1.0e-6,
@@ -71,15 +72,16 @@ def parse_args():
 
 
 def workload_config(mesh, extra=None, precision="fp32", outer_tolerance=1e-6, preconditioner="block_jacobi",
-                    factor_refresh=1):
+                    factor_refresh=1, pcg_variant="global_memory"):
     spec = mesh.spec
     if precision == "fp32" and preconditioner == "block_jacobi":
         pcg = "plain fp32 block-Jacobi, the reference's (persistent PCG)"
     elif precision == "fp32":
-        pcg = (f"fp32 PCG with the {preconditioner} factor preconditioner (global-memory PCG), factor recomputed "
-               f"every {factor_refresh} Newton iteration(s); the learned factor is not combined with mixed precision")
+        kind = "persistent factor PCG" if pcg_variant == "factor" else "global-memory PCG"
+        pcg = (f"fp32 PCG with the {preconditioner} factor preconditioner ({kind}), factor recomputed "
+               f"every {factor_refresh} Newton iteration(s)")
     else:
-        pcg = (f"{precision} blocks with per-row scales, fp32 block-Jacobi inner PCG to 1e-3, fp64 iterative "
+        pcg = (f"{precision} blocks with per-row scales, fp32 {preconditioner} inner PCG to 1e-3, fp64 iterative "
                f"refinement to {outer_tolerance:g}")
     cfg = {
         "workload": (f"{spec.name}: {spec.cells[0]}x{spec.cells[1]}x{spec.cells[2]} hex cells x 6 tets "
@@ -527,7 +529,9 @@ def solve_variants(mesh, dev, steps=20, warmup=2):
             codes.update(int(r["status"]) for r in rec)
             st.reverse()
         out[f"{precision}+{pc}"] = {"steps_per_s": 1000.0 * steps / total_ms, "pcg_iterations_per_step": its / steps,
-                                    "status_codes": sorted(codes)}
+                                    "status_codes": sorted(codes),
+                                    "pcg": ("mixed-precision refinement" if precision != "fp32"
+                                            else solver.pcg_layout()["variant"])}
         solver.close()
     return out
 
@@ -695,9 +699,22 @@ def run_gb300(args, rank, world, local_rank):
         "bytes_per_pcg_iteration": b_it, "pcg_iterations_per_launch": per_launch_iters - 1,
         "avg_launch_ms": stage_ms["pcg"] / stage_launches["pcg"], "peak_source": peak_src,
     }
-    if args.precision != "fp32" or args.preconditioner != "block_jacobi":
+    variant = solver.pcg_layout()["variant"]
+    if args.precision == "fp32" and args.preconditioner != "block_jacobi" and variant == "factor":
+        # the persistent factor PCG: two BF16 factor passes (20 B block + 4 B
+        # column each, over the lower and the upper pattern) replace the
+        # block-Jacobi block, plus the y and published Ap vectors
+        b_it = 64 * nnzb + 208 * mesh.n
+        roofline.update({
+            "achieved": b_it * (prof_iters + prof_solves) / (stage_ms["pcg"] / 1000.0) / 1e9,
+            "traffic": None, "traffic_note": None,
+            "kernel": f"pcg_factor_kernel (persistent cooperative {args.preconditioner} PCG)",
+            "algorithmic_bytes_per_launch": b_it * per_launch_iters, "bytes_per_pcg_iteration": b_it,
+            "bytes_per_pcg_iteration_formula": "64 nnzb + 208 n"})
+        roofline["frac"] = roofline["achieved"] / peak
+    elif args.precision != "fp32" or args.preconditioner != "block_jacobi":
         # the persistent fp32 PCG does not run: the mixed-precision or
-        # global-memory FSAI solves are reported as a whole
+        # global-memory factor solves are reported as a whole
         # (stage_ms_per_step["pcg"])
         roofline = None
     total_stage = sum(stage_ms.values())
@@ -725,7 +742,8 @@ def run_gb300(args, rank, world, local_rank):
                                          "factor_refresh": args.factor_refresh,
                                          "global_memory_autotune_ms": tune_ms},
                                   precision=args.precision, outer_tolerance=args.outer_tolerance,
-                                  preconditioner=args.preconditioner, factor_refresh=args.factor_refresh),
+                                  preconditioner=args.preconditioner, factor_refresh=args.factor_refresh,
+                                  pcg_variant=solver.pcg_layout()["variant"]),
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes, "matches_resident_run": e2e_match},
         "gpu_launches": int(launches),

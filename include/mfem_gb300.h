@@ -61,12 +61,17 @@ typedef struct mfem_config {
                                              M = G^T G, G lower block-triangular on H's pattern,
                                              3 learned: M = L L^T from the factor net
                                              (mfem_plan_set_factor_net); 2 and 3 run the
+                                             persistent factor PCG (pcg_variant 4) when its
+                                             ranges fit in shared memory, else the
                                              global-memory PCG                                 */
     int32_t use_cuda_graph;               /* capture mfem_step once per argument set and replay  */
     int32_t pcg_ctas;                     /* persistent PCG CTAs; 0 = one per SM                 */
     int32_t pcg_variant;                  /* 0 auto, 1 standard (two reductions per iteration),
                                              2 single-reduction (Chronopoulos-Gear), 3 gather
-                                             (standard, no column windows: any vertex order)    */
+                                             (standard, no column windows: any vertex order),
+                                             4 standard with a factor preconditioner (2 or 3
+                                             only), 5 the global-memory PCG as a one-body batch;
+                                             factor preconditioners take 0, 4 or 5              */
     /* backtracking line search on the merit function in place of x += dx,
      * s += ds (solver.py:99-103, 185, 539-557; src/mfem/line_search.py:76-163) */
     int32_t line_search;                  /* 1 on (the reference's default), 0 plain update      */
@@ -246,9 +251,10 @@ const char *mfem_plan_last_error(const mfem_plan *plan);
 int mfem_plan_sizes(const mfem_plan *plan, int32_t *n_particles, int32_t *n_tets, int64_t *nnzb);
 
 /* The persistent PCG the plan chose: variant (1 standard, 2 single-reduction,
- * 3 gather; 0 when the mesh is too large for their shared-memory slices and
- * the global solve runs the global-memory PCG of mfem_plan_set_bodies as a
- * one-body batch), CTAs, whether each CTA keeps its slice of H in shared
+ * 3 gather, 4 standard with a factor preconditioner; 0 when the global solve
+ * runs the global-memory PCG of mfem_plan_set_bodies as a one-body batch: a
+ * mesh too large for the shared-memory slices, pcg_variant 5, or bodies
+ * set), CTAs, whether each CTA keeps its slice of H in shared
  * memory, and the dynamic shared memory per CTA.  Diagnostics; no reference
  * counterpart. */
 int mfem_plan_pcg_layout(const mfem_plan *plan, int32_t *variant, int32_t *ctas, int32_t *cache_matrix,

@@ -1,4 +1,6 @@
-"""The FSAI preconditioner (preconditioner="fsai") of the global-memory PCG.
+"""The FSAI preconditioner (preconditioner="fsai"), in the persistent factor
+PCG (pcg_variant "factor", the default where it fits) and in the
+global-memory PCG.
 
 It has no reference counterpart: the reference's PCG is block-Jacobi.  The
 bar is:
@@ -56,7 +58,7 @@ def read_system(solver, n):
 @pytest.mark.parametrize("name,cells", [("nh_beam", (16, 4, 4)), ("stiff_beam", (12, 4, 4))])
 def test_factor_matches_float64_fsai(name, cells):
     mesh, _, solver = make(name, cells, preconditioner="fsai")
-    assert solver.pcg_layout()["variant"] == "global_memory"
+    assert solver.pcg_layout()["variant"] == "factor"
     st = one_solve(mesh, solver)
     assert st["status"] == _lib.MFEM_OK, st
     rp, ci, vals, G = read_system(solver, mesh.n)
@@ -89,8 +91,10 @@ def test_fewer_iterations_than_block_jacobi(name, cells):
     assert 0 < its["fsai"] < its["block_jacobi"], its
 
 
-def test_trajectory_matches_fp64_oracle():
-    mesh, model, solver = make("nh_beam", (16, 4, 4), preconditioner="fsai")
+@pytest.mark.parametrize("variant", ["factor", "global_memory"])
+def test_trajectory_matches_fp64_oracle(variant):
+    mesh, model, solver = make("nh_beam", (16, 4, 4), preconditioner="fsai", pcg_variant=variant)
+    assert solver.pcg_layout()["variant"] == variant
     ref = O.OracleSolver(mesh, dtype=np.float64)
     A, B = model.state(), model.state()
     A.particle_q.copy_(torch.as_tensor(mesh.q0, device=DEV))
@@ -141,11 +145,42 @@ def test_bad_combinations_are_refused():
         MixedFEMSolver(model, iterations=1, preconditioner="ilu")
     with pytest.raises(_lib.MfemError):
         MixedFEMSolver(model, iterations=1, preconditioner="fsai", pcg_variant="standard")
+    with pytest.raises(_lib.MfemError):
+        MixedFEMSolver(model, iterations=1, preconditioner="block_jacobi", pcg_variant="factor")
 
 
-def test_step_stats_report_the_global_memory_solve():
-    """mfem_step_stats of a one-body global-memory plan is the body's record."""
-    mesh, _, solver = make("nh_beam", (16, 4, 4), preconditioner="fsai")
+@pytest.mark.parametrize("pc", ["fsai", "learned"])
+@pytest.mark.parametrize("name,cells", [("nh_beam", (16, 4, 4)), ("stiff_beam", (12, 4, 4))])
+def test_persistent_and_global_memory_pcg_agree(pc, name, cells):
+    """The same system through both factor PCGs: the iterates are equal in
+    exact arithmetic; the float32 sums run in different orders."""
+    out = {}
+    for variant in ("factor", "global_memory"):
+        mesh, _, solver = make(name, cells, preconditioner=pc, pcg_variant=variant)
+        assert solver.pcg_layout()["variant"] == variant
+        st = one_solve(mesh, solver)
+        assert st["status"] == _lib.MFEM_OK and st["iterations"] > 0, (variant, st)
+        out[variant] = (st, solver.read_buffer("dx").cpu().numpy().astype(np.float64))
+    (sa, da), (sb, db) = out["factor"], out["global_memory"]
+    assert abs(sa["iterations"] - sb["iterations"]) <= max(2, sb["iterations"] // 50), (sa, sb)
+    assert np.abs(da - db).max() <= 1e-4 * np.abs(db).max()
+
+
+def test_mesh_too_large_for_the_persistent_factor_pcg():
+    """One CTA cannot hold nh_beam's rows: auto falls back to the
+    global-memory PCG, an explicit "factor" is refused."""
+    mesh = beams.build_beam("nh_beam", cells=(64, 16, 16))
+    model = Model.from_beam(mesh, device=DEV)
+    solver = MixedFEMSolver(model, iterations=1, preconditioner="fsai", pcg_ctas=1)
+    assert solver.pcg_layout()["variant"] == "global_memory"
+    with pytest.raises(_lib.MfemError):
+        MixedFEMSolver(model, iterations=1, preconditioner="fsai", pcg_ctas=1, pcg_variant="factor")
+
+
+@pytest.mark.parametrize("variant", ["factor", "global_memory"])
+def test_step_stats_report_the_factor_solve(variant):
+    """mfem_step_stats of a one-body factor plan is the body's record."""
+    mesh, _, solver = make("nh_beam", (16, 4, 4), preconditioner="fsai", pcg_variant=variant)
     st = one_solve(mesh, solver)
     assert st["status"] == _lib.MFEM_OK and st["iterations"] > 0 and 0.0 < st["rel_residual"] <= 1e-6, st
 

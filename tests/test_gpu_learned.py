@@ -57,7 +57,7 @@ def random_net(seed):
 def test_factor_matches_torch_reference(name, cells):
     net = random_net(7)
     mesh, _, solver = make(name, cells, preconditioner="learned", factor_net_params=net.pack())
-    assert solver.pcg_layout()["variant"] == "global_memory"
+    assert solver.pcg_layout()["variant"] == "factor"
     one_solve(mesh, solver)
     rp = solver.read_buffer("row_ptr").cpu().numpy()
     ci = solver.read_buffer("col_idx").cpu().numpy()
@@ -79,17 +79,20 @@ def test_factor_matches_torch_reference(name, cells):
     assert np.median(rel) <= 2e-3
 
 
-def test_overflowing_factor_falls_back_to_block_jacobi():
+@pytest.mark.parametrize("variant", ["factor", "global_memory"])
+def test_overflowing_factor_falls_back_to_block_jacobi(variant):
     net = F.FactorNet()
     with torch.no_grad():
         net.diag.bias[:3] = 1.0e30  # softplus(1e30) = 1e30: M r overflows
-    mesh, _, solver = make("nh_beam", (16, 4, 4), preconditioner="learned", factor_net_params=net.pack())
+    mesh, _, solver = make("nh_beam", (16, 4, 4), preconditioner="learned", factor_net_params=net.pack(),
+                           pcg_variant=variant)
+    assert solver.pcg_layout()["variant"] == variant
     st = one_solve(mesh, solver)
     _, _, bj = make("nh_beam", (16, 4, 4))
     st_bj = one_solve(mesh, bj)
-    # the retry is a block-Jacobi solve from the same warm start (in the
-    # global-memory PCG, whose sums run in another order than the default
-    # plan's persistent PCG)
+    # the retry is a block-Jacobi solve from the same warm start (in a
+    # kernel whose sums run in another order than the default plan's
+    # single-reduction PCG)
     assert st["status"] == _lib.MFEM_OK and st["iterations"] > 0, st
     assert abs(st["iterations"] - st_bj["iterations"]) <= 2, (st, st_bj)
     dx = solver.read_buffer("dx").cpu().numpy()
@@ -108,8 +111,9 @@ def test_shipped_weights_take_fewer_iterations_than_block_jacobi(name, cells):
     assert 0 < its["learned"] < its["block_jacobi"], its
 
 
-def test_trajectory_matches_fp64_oracle():
-    mesh, model, solver = make("nh_beam", (16, 4, 4), preconditioner="learned")
+@pytest.mark.parametrize("variant", ["factor", "global_memory"])
+def test_trajectory_matches_fp64_oracle(variant):
+    mesh, model, solver = make("nh_beam", (16, 4, 4), preconditioner="learned", pcg_variant=variant)
     ref = O.OracleSolver(mesh, dtype=np.float64)
     A, B = model.state(), model.state()
     A.particle_q.copy_(torch.as_tensor(mesh.q0, device=DEV))

@@ -182,10 +182,12 @@ bool valid_config(const mfem_config *cfg, std::string &err) {
     else if (!(cfg->preconditioner_singular_threshold >= 0.0f)) err = "preconditioner_singular_threshold must be >= 0";
     else if (cfg->preconditioner < 0 || cfg->preconditioner > 3)
         err = "preconditioner must be 0 (none), 1 (block-Jacobi), 2 (FSAI) or 3 (learned)";
-    else if (cfg->preconditioner >= 2 && cfg->pcg_variant != 0)
-        err = "factor preconditioners run the global-memory PCG: pcg_variant must be 0";
+    else if (cfg->pcg_variant < 0 || cfg->pcg_variant > 5) err = "pcg_variant must be in [0, 5]";
+    else if (cfg->preconditioner >= 2 && cfg->pcg_variant != 0 && cfg->pcg_variant != 4 && cfg->pcg_variant != 5)
+        err = "factor preconditioners take pcg_variant 0 (auto), 4 (persistent) or 5 (global memory)";
+    else if (cfg->preconditioner < 2 && cfg->pcg_variant == 4)
+        err = "pcg_variant 4 needs a factor preconditioner (2 or 3)";
     else if (cfg->pcg_ctas < 0) err = "pcg_ctas must be >= 0";
-    else if (cfg->pcg_variant < 0 || cfg->pcg_variant > 3) err = "pcg_variant must be 0 (auto), 1, 2 or 3";
     else if (cfg->line_search != 0 && cfg->line_search != 1) err = "line_search must be 0 or 1";
     else if (cfg->line_search_max_iterations < 0 || cfg->line_search_max_iterations > (1 << 20))
         err = "line_search_max_iterations must be in [0, 2^20]";
@@ -206,6 +208,9 @@ cudaError_t global_solve(mfem_plan *p, int slot, cudaStream_t s) {
         return launch_mixed_solve(p->bv, p->vv, p->ir, p->pw, p->bw, slot, p->cfg.cg_max_iterations,
                                   p->cfg.preconditioner,
                                   s);
+    if (p->pl.variant == PcgLayout::kFactor)
+        return launch_pcg_factor(p->bv, p->vv, p->pw, p->bw, p->pl, p->pcg_ctas, slot, p->cfg.cg_tolerance,
+                                 p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
     if (p->bw.n_bodies > 0)
         return launch_batched_pcg(p->bv, p->vv, p->bw, p->pw.error, slot, p->cfg.cg_tolerance,
                                   p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
@@ -542,12 +547,34 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
         p->ls.c = cfg.line_search_c;
         p->ls.threshold = cfg.line_search_threshold;
     }
-    if (e == cudaSuccess && cfg.preconditioner >= 2) {
-        // factor preconditioners are applied by the global-memory PCG only
+    std::vector<int4> factor_info;
+    if (e == cudaSuccess && (cfg.preconditioner >= 2 || cfg.pcg_variant == PcgLayout::kGlobalMemory)) {
+        // the factor structures and the block-Jacobi retry live in the
+        // one-body batch views; the persistent factor PCG runs when its
+        // ranges fit in shared memory, else the global-memory PCG
         p->pl = PcgLayout{};
         p->pl.variant = 0;
         p->global_memory_pcg = true;
         cta_info.assign(1, make_int4(0, 0, 0, 0));
+        if (cfg.preconditioner >= 2 && cfg.pcg_variant != PcgLayout::kGlobalMemory) {
+            std::string lerr;
+            PcgLayout fl{};
+            std::vector<int4> fcta;
+            e = pcg_factor_layout(device, fl, sym.row_ptr.data(), sym.col_idx.data(), n, p->pcg_ctas,
+                                  cfg.preconditioner, fcta, factor_info, lerr);
+            if (e == cudaSuccess) {
+                p->pl = fl;
+                cta_info = fcta;
+            } else if (!lerr.empty()) {
+                if (cfg.pcg_variant == PcgLayout::kFactor) {
+                    mfem_plan_destroy(p);
+                    return fail(nullptr, MFEM_BAD_ARG, lerr);
+                }
+                cudaGetLastError();
+                e = cudaSuccess;
+                factor_info.clear();
+            }
+        }
     } else if (e == cudaSuccess) {
         std::string lerr;
         e = pcg_plan_layout(device, p->pl, sym.row_ptr.data(), sym.col_idx.data(), n, p->pcg_ctas, cfg.pcg_variant,
@@ -571,6 +598,12 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
     if (e == cudaSuccess) e = dev_alloc(p, &d_cta, cta_info.size());
     if (e == cudaSuccess) e = upload(d_cta, cta_info.data(), cta_info.size());
     p->pl.cta_info = d_cta;
+    if (e == cudaSuccess && !factor_info.empty()) {
+        int4 *d_fcta = nullptr;
+        e = dev_alloc(p, &d_fcta, factor_info.size());
+        if (e == cudaSuccess) e = upload(d_fcta, factor_info.data(), factor_info.size());
+        p->pl.factor_info = d_fcta;
+    }
     if (e == cudaSuccess) e = upload(tets, reinterpret_cast<const int4 *>(h_tets), nT);
     if (e == cudaSuccess) e = upload(dminv, h_poses, nT * 9);
     if (e == cudaSuccess) e = upload(materials, h_materials, nT * 3);
@@ -1383,6 +1416,12 @@ int mfem_plan_set_bodies(mfem_plan *p, int32_t n_bodies, const int32_t *h_vertex
                     return fail(p, MFEM_BAD_ARG, "tet " + std::to_string(t) + " uses a vertex of another body");
             }
     }
+    if (p->pl.variant == PcgLayout::kFactor) {
+        // per-body solves run in the global-memory PCG
+        p->pl.variant = 0;
+        p->pl.cache_matrix = 0;
+        p->pl.smem = 0;
+    }
     return install_bodies(p, n_bodies, h_vertex_offsets, h_tet_offsets, h_body_energy, h_body_gravity);
 }
 
@@ -1522,6 +1561,8 @@ int mfem_plan_batch_layout(const mfem_plan *p, int32_t *ctas, int32_t *threads) 
 int mfem_plan_autotune_batch(mfem_plan *p, const float *d_q, float dt, double *h_best_ms, mfem_stream stream) {
     if (!p) return MFEM_BAD_ARG;
     if (p->bw.n_bodies == 0) return fail(p, MFEM_BAD_ARG, "no bodies: call mfem_plan_set_bodies first");
+    if (p->pl.variant == PcgLayout::kFactor)
+        return fail(p, MFEM_BAD_ARG, "the plan runs the persistent factor PCG: nothing to tune");
     if (!d_q || !(dt > 0.0f)) return fail(p, MFEM_BAD_ARG, "need q and dt > 0");
     if (!net_ready(p)) return fail(p, MFEM_BAD_ARG, "preconditioner 3 needs mfem_plan_set_factor_net");
     DeviceGuard g(p->device);

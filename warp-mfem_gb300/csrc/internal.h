@@ -268,10 +268,17 @@ struct IrWork {
 
 // Row partition and shared-memory plan of the persistent PCG.
 struct PcgLayout {
-    enum { kAuto = 0, kStandard = 1, kSingleReduction = 2, kGather = 3 };
+    // kFactor: the persistent PCG with a factor preconditioner (pcg_factor.cu);
+    // kGlobalMemory: requested in the config only, the mesh then runs the
+    // global-memory PCG as a one-body batch (reported as variant 0)
+    enum { kAuto = 0, kStandard = 1, kSingleReduction = 2, kGather = 3, kFactor = 4, kGlobalMemory = 5 };
     const int4 *cta_info;      // device [ctas]: (row_lo, row_hi, win_lo, win_hi)
+    const int4 *factor_info = nullptr;  // kFactor, device [ctas]: (y_lo, y_hi, r_lo, r_hi)
     int variant = kSingleReduction;
     int rows_max = 0, blk_max = 0, win_max = 0;
+    int y_max = 0, r_max = 0;  // kFactor: longest row ranges Y and R of a CTA
+    int f0_max = 0, f1_max = 0;  // kFactor: most first- / second-pass factor blocks of a CTA
+    int factor_cache = 0;      // kFactor: 1: each CTA keeps its factor rows in shared memory
     int cache_matrix = 0;      // 1: each CTA keeps its slice of H in shared memory
     size_t smem = 0;           // dynamic shared memory per CTA
 };
@@ -322,6 +329,15 @@ cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork 
 cudaError_t pcg_max_ctas(int device, int *ctas);
 cudaError_t pcg_plan_layout(int device, PcgLayout &L, const int32_t *row_ptr, const int32_t *col_idx, int n,
                             int ctas, int variant, std::vector<int4> &cta_info, std::string &err);
+// The persistent PCG with a factor preconditioner (mode 2: M = F^T F, 3: M =
+// F F^T; the factor in bw's lower / upper CSR).  The layout fails (err set)
+// when a CTA's rows and ranges do not fit in shared memory.
+cudaError_t pcg_factor_layout(int device, PcgLayout &L, const int32_t *row_ptr, const int32_t *col_idx, int n,
+                              int ctas, int mode, std::vector<int4> &cta_info, std::vector<int4> &factor_info,
+                              std::string &err);
+cudaError_t launch_pcg_factor(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const BatchViews &bw,
+                              const PcgLayout &L, int ctas, int slot, float tol, int maxiter, int mode,
+                              cudaStream_t s);
 cudaError_t launch_true_residual(const BsrViews &bv, const VertexViews &vv, double *out3, cudaStream_t s);
 cudaError_t ir_max_ctas(int device, int *ctas);
 cudaError_t launch_fsai_setup(const BsrViews &bv, const BatchViews &bw, cudaStream_t s);

@@ -50,301 +50,10 @@
 // Every wait (barrier, mbarrier) is bounded; after a timeout the kernel sets
 // the sticky error flag, waits (bounded) for its own copies in flight and
 // leaves, reporting MFEM_TIMEOUT.
-#include "internal.h"
+#include "pcg_common.cuh"
 
 namespace mfem {
 namespace {
-
-constexpr int kPcgThreads = 512;
-constexpr int kGroup = 4;                         // lanes per block row in the product
-constexpr int kGatherDepth = 4;                   // blocks per lane and trip in the gather product
-constexpr int kMaxCtas = 256;
-constexpr long long kWaitCycles = 8000000000ll;   // ~4 s at 2 GHz per wait
-constexpr size_t kStaticSmem = 12 * 1024;         // static shared memory reserve
-
-struct PcgArgs {
-    int n;
-    const int *row_ptr;
-    const int *col_idx;
-    const float *values;
-    const float *Minv;   // [n_pad][9]
-    const float *b;
-    float *x;            // [n_pad][3] warm start in, solution out
-    float *pub;          // published vectors, 6 x [n_pad][3]
-    int n_pad;
-    const int4 *cta;     // [ctas] (row_lo, row_hi, win_lo, win_hi)
-    int rows_max, blk_max, win_max;
-    float *partials;            // [2][kMaxCtas][4] per-CTA partial sums
-    unsigned long long *counter;  // grid barrier arrivals (never reset)
-    int *error;
-    SolveStats *stats;
-    int slot;
-    float tol;
-    int maxiter;
-    int use_precond;
-};
-
-__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *p) {
-    unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
-
-__device__ __forceinline__ uint32_t smem_addr(const void *p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-// ---- reduction barrier --------------------------------------------------------
-// Block-reduces NV per-thread float partials, stores the CTA's sums for
-// barrier `k` (parity buffer) and waits at the grid barrier.  Returns false
-// if the wait gave up.  CTA-uniform.
-template <int NV>
-__device__ bool reduce_arrive(float (&v)[NV], float *partials, unsigned k, unsigned long long *counter,
-                              unsigned long long &target, int *error, float (*s_redf)[32], int *s_ok) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int i = 0; i < NV; ++i) {
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v[i] += __shfl_down_sync(0xffffffffu, v[i], off);
-    }
-    if (lane == 0) {
-#pragma unroll
-        for (int i = 0; i < NV; ++i) s_redf[i][wid] = v[i];
-    }
-    __syncthreads();
-    if (wid == 0) {
-        const int nw = blockDim.x >> 5;
-        float part[NV];
-#pragma unroll
-        for (int i = 0; i < NV; ++i) {
-            part[i] = lane < nw ? s_redf[i][lane] : 0.0f;
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) part[i] += __shfl_down_sync(0xffffffffu, part[i], off);
-        }
-        if (lane == 0) {
-            float *buf = partials + (size_t)(k & 1u) * kMaxCtas * 4 + (size_t)blockIdx.x * 4;
-#pragma unroll
-            for (int i = 0; i < NV; ++i) buf[i] = part[i];
-            // arrive: every earlier store of this CTA (published vectors,
-            // partials) is released before the counter moves
-            target += gridDim.x;
-            __threadfence();
-            atomicAdd(counter, 1ull);
-            int ok = 1;
-            const long long t0 = clock64();
-            unsigned spins = 0;
-            while (ld_relaxed(counter) < target) {
-                if ((++spins & 1023u) == 0 && (ld_volatile(error) != 0 || clock64() - t0 > kWaitCycles)) {
-                    atomicExch(error, 1);
-                    ok = 0;
-                    break;
-                }
-            }
-            __threadfence();
-            *s_ok = ok;
-        }
-    }
-    __syncthreads();
-    return *s_ok != 0;
-}
-
-// Sums the partials of barrier `k` over all CTAs (after reduce_arrive):
-// threads 0..nb*NV-1 fetch one each (one round trip), warp 0 adds them in a
-// fixed order.  tot[] is valid for every thread on return.
-template <int NV>
-__device__ void reduce_totals(const float *partials, unsigned k, float *s_val, float *tot) {
-    const int nb = gridDim.x;
-    const float *buf = partials + (size_t)(k & 1u) * kMaxCtas * 4;
-    for (int t = threadIdx.x; t < nb * NV; t += blockDim.x) {
-        const int b = t / NV, i = t - b * NV;
-        s_val[b * 4 + i] = __ldcg(buf + (size_t)b * 4 + i);
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        float acc[NV];
-#pragma unroll
-        for (int i = 0; i < NV; ++i) acc[i] = 0.0f;
-        for (int b = lane; b < nb; b += 32) {
-#pragma unroll
-            for (int i = 0; i < NV; ++i) acc[i] += s_val[b * 4 + i];
-        }
-#pragma unroll
-        for (int i = 0; i < NV; ++i) {
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) acc[i] += __shfl_down_sync(0xffffffffu, acc[i], off);
-        }
-        if (lane == 0) {
-#pragma unroll
-            for (int i = 0; i < NV; ++i) tot[i] = acc[i];
-        }
-    }
-    __syncthreads();
-}
-
-// Scalars of the iteration, decided by thread 0 and broadcast.
-struct Scalars {
-    float alpha, beta, gamma, rr, bb, thr2;
-    int status, done;
-};
-
-// ---- bulk copies -----------------------------------------------------------
-// Issued by thread 0 after a __syncthreads that ended every read of the
-// destinations and after the reduction that published the sources.
-__device__ __forceinline__ void tma_expect(uint64_t *mbar, uint32_t bytes) {
-    asm volatile("fence.proxy.async.global;" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ void tma_copy(void *dst, const void *src, uint32_t bytes, uint64_t *mbar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_addr(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_addr(mbar))
-                 : "memory");
-}
-
-// Waits for the mbarrier phase `parity` (bounded; a second bounded wait after
-// a timeout so no copy is still writing when the CTA leaves).  CTA-uniform.
-__device__ bool tma_wait(uint64_t *mbar, uint32_t &parity, int *error) {
-    const uint32_t mb = smem_addr(mbar);
-    bool ok = true;
-    for (int attempt = 0; attempt < 2; ++attempt) {
-        uint32_t done = 0;
-        const long long t0 = clock64();
-        unsigned spins = 0;
-        while (!done) {
-            asm volatile(
-                "{\n\t.reg .pred p;\n\t"
-                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                "selp.u32 %0, 1, 0, p;\n\t}"
-                : "=r"(done)
-                : "r"(mb), "r"(parity)
-                : "memory");
-            if (!done && (++spins & 255u) == 0 && clock64() - t0 > kWaitCycles / 2) break;
-        }
-        if (done) break;
-        ok = false;
-    }
-    ok = __syncthreads_and(ok) != 0;
-    if (!ok && threadIdx.x == 0) atomicExch(error, 1);
-    parity ^= 1u;
-    return ok;
-}
-
-// out[i] = sum_k H[k] win[col_k] over the CTA's rows, kGroup lanes per row.
-template <bool CACHE>
-__device__ __forceinline__ void window_product(const PcgArgs &a, const int *rowoff, const float *sH, const int *sCol,
-                                               int blk_lo, int win_lo, int nrows, const float *win, float *out) {
-    const int g_lane = threadIdx.x & (kGroup - 1);
-    const int group = threadIdx.x / kGroup;
-    const int ngroups = blockDim.x / kGroup;
-    const unsigned gmask = ((1u << kGroup) - 1u) << (threadIdx.x & (32 - kGroup));
-    for (int i = group; i < nrows; i += ngroups) {
-        const int kb = rowoff[i], ke = rowoff[i + 1];
-        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-#pragma unroll 4
-        for (int k = kb + g_lane; k < ke; k += kGroup) {
-            const float *h;
-            int c;
-            if (CACHE) {
-                h = sH + (size_t)k * 9;
-                c = sCol[k];
-            } else {
-                h = a.values + (size_t)(blk_lo + k) * 9;
-                c = __ldg(a.col_idx + blk_lo + k) - win_lo;
-            }
-            const float v0 = win[3 * c + 0], v1 = win[3 * c + 1], v2 = win[3 * c + 2];
-            a0 += h[0] * v0 + h[1] * v1 + h[2] * v2;
-            a1 += h[3] * v0 + h[4] * v1 + h[5] * v2;
-            a2 += h[6] * v0 + h[7] * v1 + h[8] * v2;
-        }
-#pragma unroll
-        for (int off = kGroup / 2; off > 0; off >>= 1) {
-            a0 += __shfl_xor_sync(gmask, a0, off);
-            a1 += __shfl_xor_sync(gmask, a1, off);
-            a2 += __shfl_xor_sync(gmask, a2, off);
-        }
-        if (g_lane == 0) {
-            out[3 * i + 0] = a0;
-            out[3 * i + 1] = a1;
-            out[3 * i + 2] = a2;
-        }
-    }
-}
-
-__device__ __forceinline__ void precond(const float *m, const float r[3], float z[3], int use) {
-    if (!use) {
-        z[0] = r[0];
-        z[1] = r[1];
-        z[2] = r[2];
-        return;
-    }
-    z[0] = m[0] * r[0] + m[1] * r[1] + m[2] * r[2];
-    z[1] = m[3] * r[0] + m[4] * r[1] + m[5] * r[2];
-    z[2] = m[6] * r[0] + m[7] * r[1] + m[8] * r[2];
-}
-
-struct Common {
-    int row_lo, nrows, win_lo, nwin, blk_lo, nblk;
-};
-
-__device__ __forceinline__ Common setup_common(const PcgArgs &a) {
-    const int4 info = a.cta[blockIdx.x];
-    Common c;
-    c.row_lo = info.x;
-    c.nrows = info.y - info.x;
-    c.win_lo = info.z;
-    c.nwin = info.w - info.z;
-    c.blk_lo = a.row_ptr[c.row_lo];
-    c.nblk = a.row_ptr[info.y] - c.blk_lo;
-    return c;
-}
-
-__device__ __forceinline__ void load_matrix_slice(const PcgArgs &a, const Common &c, int *rowoff, float *sH,
-                                                  int *sCol, bool cache) {
-    for (int i = threadIdx.x; i <= c.nrows; i += blockDim.x) rowoff[i] = a.row_ptr[c.row_lo + i] - c.blk_lo;
-    if (cache) {
-        for (int k = threadIdx.x; k < 9 * c.nblk; k += blockDim.x) sH[k] = a.values[(size_t)9 * c.blk_lo + k];
-        for (int k = threadIdx.x; k < c.nblk; k += blockDim.x) sCol[k] = a.col_idx[c.blk_lo + k] - c.win_lo;
-    }
-}
-
-// Final bookkeeping: solution rows and stats.
-__device__ __forceinline__ void finish(const PcgArgs &a, const Common &cm, const float *sX, const Scalars &sc,
-                                       int it) {
-    for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) a.x[(size_t)3 * cm.row_lo + i] = sX[i];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        const float rel = sc.bb > 0.0f ? sqrtf(sc.rr / sc.bb) : sqrtf(sc.rr);
-        a.stats[a.slot] = SolveStats{it, sc.status, rel, 0.0f};
-    }
-}
-
-#define PCG_PROLOGUE                                                                        \
-    __shared__ float s_redf[4][32];                                                         \
-    __shared__ float s_val[4 * kMaxCtas];                                                   \
-    __shared__ float s_tot[4];                                                              \
-    __shared__ Scalars sc;                                                                  \
-    __shared__ int s_ok;                                                                    \
-    __shared__ unsigned long long s_base;                                                   \
-    __shared__ __align__(8) uint64_t s_mbar;                                                \
-    const Common cm = setup_common(a);                                                      \
-    if (threadIdx.x == 0) {                                                                 \
-        s_base = (ld_relaxed(a.counter) / gridDim.x) * (unsigned long long)gridDim.x;     \
-        s_ok = ld_volatile(a.error) == 0;                                                   \
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&s_mbar)) : "memory"); \
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");                  \
-    }                                                                                       \
-    __syncthreads();                                                                        \
-    unsigned long long target = s_base;                                                     \
-    unsigned bar = 0;                                                                       \
-    uint32_t parity = 0;                                                                    \
-    if (!s_ok) {                                                                            \
-        if (blockIdx.x == 0 && threadIdx.x == 0) a.stats[a.slot] = SolveStats{0, MFEM_TIMEOUT, 0.0f, 0.0f}; \
-        return;                                                                             \
-    }
 
 // ===========================================================================
 // single-reduction (Chronopoulos-Gear) PCG
@@ -1063,7 +772,7 @@ cudaError_t pcg_plan_layout(int device, PcgLayout &L, const int32_t *row_ptr, co
 
 cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const PcgLayout &L, int ctas,
                        int slot, float tol, int maxiter, int use_precond, cudaStream_t s) {
-    PcgArgs a;
+    PcgArgs a = {};
     a.n = bv.n;
     a.row_ptr = bv.row_ptr;
     a.col_idx = bv.col_idx;

@@ -1,0 +1,600 @@
+// The persistent PCG with a factor preconditioner: M = F^T F (FSAI,
+// use_precond 2) or M = F F^T (the learned factor, use_precond 3), F on H's
+// lower block pattern.  One cooperative launch per solve, one CTA per SM.
+//
+// It is the standard two-barrier iteration of the persistent PCG (pcg.cu),
+// with z = M r formed without a third and fourth grid barrier:
+//
+//   A: p = z + beta p over the CTA's column window, Ap = H p for its rows,
+//      publish Ap, (p, Ap)                                  -> grid barrier
+//   B: stage the published Ap over the row range R, r -= alpha Ap over R,
+//      y = F0 r over the row range Y, z = F1 y for its rows, publish z,
+//      (r, z), (r, r)                                       -> grid barrier
+//
+// F0 is the first pass's form (F for mode 2, F^T for mode 3) and F1 the
+// second's.  Y holds the columns F1 reaches from the CTA's rows, R the
+// columns F0 reaches from Y: two hops of H's pattern, about one column window
+// on either side.  Each CTA keeps r over R in shared memory for the whole
+// solve and updates it with the same instructions, from the same published
+// Ap and the same alpha, as the rows' owners, so every copy of a row's r
+// equals the owner's bit for bit; y over Y is recomputed by each CTA instead
+// of exchanged.  The factor's BF16 blocks and columns are read through the
+// read-only path (L2-resident, unchanged during a solve).
+//
+// A factor solve that breaks down (non-finite values or p.Ap <= 0) is solved
+// again from the same warm start with block-Jacobi inside the launch; every
+// CTA takes that decision from the same totals.  Every wait is bounded.
+#include <algorithm>
+
+#include "factor_apply.cuh"
+#include "pcg_common.cuh"
+
+namespace mfem {
+namespace {
+
+// Orders this thread's earlier generic-proxy accesses to shared memory
+// before later bulk copies (async proxy) into the same bytes.
+__device__ __forceinline__ void proxy_fence_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// A 3x3 block from its five words of BF16 pairs (the tenth value is padding).
+template <bool FCACHE>
+__device__ __forceinline__ void block_words(const uint32_t *w, float f[9]) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const uint32_t u = FCACHE ? w[i] : __ldg(w + i);
+        __nv_bfloat162 b;
+        memcpy(&b, &u, 4);
+        const float2 t = __bfloat1622float2(b);
+        f[2 * i] = t.x;
+        if (2 * i + 1 < 9) f[2 * i + 1] = t.y;
+    }
+}
+
+// The factor rows a CTA applies: its shared-memory copy (FCACHE; local row
+// indices, columns relative to the input vector's first row) or the global
+// forms.
+struct FactorRows {
+    const int *rp, *col;
+    const uint32_t *words;  // kFactorLd BF16 values (five words) per block
+    int row0;               // first row (global forms) or 0 (shared-memory copy)
+    int in_lo;              // subtracted from the columns (0 for the copy)
+};
+
+// One row of a factor form times a shared-memory vector `in`, kGroup lanes a
+// row, two blocks a lane and trip; the row's sum in every lane of the group.
+template <bool FCACHE>
+__device__ __forceinline__ void factor_row(const FactorRows &f, const float *in, int j, int g_lane, unsigned gmask,
+                                           float &a0, float &a1, float &a2) {
+    a0 = a1 = a2 = 0.0f;
+    const int row = f.row0 + j;
+    const int kb = FCACHE ? f.rp[row] : __ldg(f.rp + row);
+    const int ke = FCACHE ? f.rp[row + 1] : __ldg(f.rp + row + 1);
+    for (int k = kb + g_lane; k < ke; k += 2 * kGroup) {
+        const int k2 = k + kGroup;
+        const bool two = k2 < ke;
+        const int kk2 = two ? k2 : k;
+        const int c = (FCACHE ? f.col[k] : __ldg(f.col + k)) - f.in_lo;
+        const int c2 = (FCACHE ? f.col[kk2] : __ldg(f.col + kk2)) - f.in_lo;
+        const float v0 = in[3 * c], v1 = in[3 * c + 1], v2 = in[3 * c + 2];
+        float w0 = in[3 * c2], w1 = in[3 * c2 + 1], w2 = in[3 * c2 + 2];
+        if (!two) w0 = w1 = w2 = 0.0f;
+        float m[9], m2[9];
+        block_words<FCACHE>(f.words + (size_t)5 * k, m);
+        block_words<FCACHE>(f.words + (size_t)5 * kk2, m2);
+        a0 += m[0] * v0 + m[1] * v1 + m[2] * v2;
+        a1 += m[3] * v0 + m[4] * v1 + m[5] * v2;
+        a2 += m[6] * v0 + m[7] * v1 + m[8] * v2;
+        a0 += m2[0] * w0 + m2[1] * w1 + m2[2] * w2;
+        a1 += m2[3] * w0 + m2[4] * w1 + m2[5] * w2;
+        a2 += m2[6] * w0 + m2[7] * w1 + m2[8] * w2;
+    }
+#pragma unroll
+    for (int off = kGroup / 2; off > 0; off >>= 1) {
+        a0 += __shfl_xor_sync(gmask, a0, off);
+        a1 += __shfl_xor_sync(gmask, a1, off);
+        a2 += __shfl_xor_sync(gmask, a2, off);
+    }
+}
+
+// y[j] = (F0 r)_(y_lo + j) for j < ny, r over R in shared memory.
+template <bool FCACHE>
+__device__ __forceinline__ void first_pass(const FactorRows &f0, const float *sR, float *sY, int ny) {
+    const int g_lane = threadIdx.x & (kGroup - 1);
+    const unsigned gmask = ((1u << kGroup) - 1u) << (threadIdx.x & (32 - kGroup));
+    const int group = threadIdx.x / kGroup, ngroups = blockDim.x / kGroup;
+    for (int j = group; j < ny; j += ngroups) {
+        float a0, a1, a2;
+        factor_row<FCACHE>(f0, sR, j, g_lane, gmask, a0, a1, a2);
+        if (g_lane == 0) {
+            sY[3 * j] = a0;
+            sY[3 * j + 1] = a1;
+            sY[3 * j + 2] = a2;
+        }
+    }
+}
+
+// z = F1 y for the CTA's rows: published, and (r, z), (r, r) added to acc.
+template <bool FCACHE>
+__device__ __forceinline__ void second_pass(const FactorRows &f1, const float *sY, const float *sRown, int row_lo,
+                                            int nrows, float *pubZ, float (&acc)[2]) {
+    const int g_lane = threadIdx.x & (kGroup - 1);
+    const unsigned gmask = ((1u << kGroup) - 1u) << (threadIdx.x & (32 - kGroup));
+    const int group = threadIdx.x / kGroup, ngroups = blockDim.x / kGroup;
+    for (int i = group; i < nrows; i += ngroups) {
+        float z[3];
+        factor_row<FCACHE>(f1, sY, i, g_lane, gmask, z[0], z[1], z[2]);
+        if (g_lane == 0) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float r = sRown[3 * i + c];
+                pubZ[(size_t)3 * (row_lo + i) + c] = z[c];
+                acc[0] = __fmaf_rn(r, z[c], acc[0]);
+                acc[1] = __fmaf_rn(r, r, acc[1]);
+            }
+        }
+    }
+}
+
+// Copies rows [r0, r0 + nrows) of a global factor form into shared memory:
+// row offsets, columns minus col_lo, and the blocks' words.
+__device__ __forceinline__ void stage_factor_rows(const int *rp, const int *col, const __nv_bfloat16 *val, int r0,
+                                                  int nrows, int col_lo, int *s_rp, int *s_col, uint32_t *s_words) {
+    const int kb = rp[r0], nb = rp[r0 + nrows] - kb;
+    for (int j = threadIdx.x; j <= nrows; j += blockDim.x) s_rp[j] = rp[r0 + j] - kb;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) s_col[k] = col[kb + k] - col_lo;
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(val + (size_t)kFactorLd * kb);
+    for (int t = threadIdx.x; t < 5 * nb; t += blockDim.x) s_words[t] = w[t];
+}
+
+template <bool CACHE, bool FCACHE>
+__global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    PCG_PROLOGUE
+    const int rows_max = a.rows_max, win_max = a.win_max;
+    float *sX = reinterpret_cast<float *>(smem);
+    float *sAp = sX + 3 * rows_max;
+    float *winA = sAp + 3 * rows_max;
+    float *winB = winA + 3 * win_max;  // the p window in A, Ap over R in B
+    float *sR = winB + 3 * max(win_max, a.r_max);
+    float *sY = sR + 3 * a.r_max;
+    int *rowoff = reinterpret_cast<int *>(sY + 3 * a.y_max);
+    float *sH = reinterpret_cast<float *>(rowoff + rows_max + 4);
+    int *sCol = reinterpret_cast<int *>(sH + (CACHE ? 9 * a.blk_max : 0));
+    int *f_rp0 = sCol + (CACHE ? a.blk_max : 0);  // FCACHE: the CTA's factor rows
+    int *f_rp1 = f_rp0 + a.y_max + 4;
+    int *f_c0 = f_rp1 + rows_max + 4;
+    int *f_c1 = f_c0 + a.f0_max;
+    uint32_t *f_w0 = reinterpret_cast<uint32_t *>(f_c1 + a.f1_max);
+    uint32_t *f_w1 = f_w0 + 5 * a.f0_max;
+
+    const int4 fi = a.fcta[blockIdx.x];
+    const int y_lo = fi.x, y_hi = fi.y, r_lo = fi.z, nr = fi.w - fi.z;
+    const size_t vec = (size_t)3 * a.n_pad;
+    float *pubZ = a.pub;
+    float *pubP[2] = {a.pub + vec, a.pub + 2 * vec};
+    float *pubR = a.pub + 3 * vec;
+    float *pubAp = a.pub + 4 * vec;
+    const int own = cm.row_lo - cm.win_lo;  // the CTA's rows in the window
+    float *sRown = sR + 3 * (cm.row_lo - r_lo);  // the CTA's rows in R
+    const uint32_t wbytes = (uint32_t)cm.nwin * 12u, rbytes = (uint32_t)nr * 12u;
+
+    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE);
+    FactorRows f0, f1;
+    if (FCACHE) {
+        stage_factor_rows(a.rp0, a.c0, a.v0, y_lo, y_hi - y_lo, r_lo, f_rp0, f_c0, f_w0);
+        stage_factor_rows(a.rp1, a.c1, a.v1, cm.row_lo, cm.nrows, y_lo, f_rp1, f_c1, f_w1);
+        f0 = FactorRows{f_rp0, f_c0, f_w0, 0, 0};
+        f1 = FactorRows{f_rp1, f_c1, f_w1, 0, 0};
+    } else {
+        f0 = FactorRows{a.rp0, a.c0, reinterpret_cast<const uint32_t *>(a.v0), y_lo, r_lo};
+        f1 = FactorRows{a.rp1, a.c1, reinterpret_cast<const uint32_t *>(a.v1), cm.row_lo, y_lo};
+    }
+    int mode = a.use_precond;  // 2 or 3; 1 after a breakdown
+    int it = 0, it_done = 0;
+    bool pending = false;  // window copies in flight
+    for (;;) {  // one attempt
+        const bool factor = mode >= 2;
+        it = 0;
+        // ---- r = g - H x0 (x0: the warm start), z = M r
+        proxy_fence_smem();
+        __syncthreads();
+        bool ok = true;
+        if (threadIdx.x == 0 && cm.nwin > 0) {
+            tma_expect(&s_mbar, wbytes);
+            tma_copy(winA, a.x + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+        }
+        if (cm.nwin > 0) ok = tma_wait(&s_mbar, parity, a.error);
+        if (ok) {
+            for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = winA[3 * own + i];
+            window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp);
+            __syncthreads();
+            float acc[3] = {0.0f, 0.0f, 0.0f};
+            for (int i = threadIdx.x; i < cm.nrows; i += blockDim.x) {
+                const int row = cm.row_lo + i;
+                float r[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float bc = a.b[3 * row + c];
+                    r[c] = bc - sAp[3 * i + c];
+                    acc[2] = __fmaf_rn(bc, bc, acc[2]);
+                }
+                if (factor) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) pubR[3 * row + c] = r[c];
+                } else {
+                    float z[3];
+                    precond(a.Minv + (size_t)9 * row, r, z, 1);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        sRown[3 * i + c] = r[c];
+                        pubZ[3 * row + c] = z[c];
+                        acc[0] = __fmaf_rn(r[c], z[c], acc[0]);
+                        acc[1] = __fmaf_rn(r[c], r[c], acc[1]);
+                    }
+                }
+            }
+            if (factor) {
+                // every row's r is published; each CTA stages r over R
+                float bb[1] = {acc[2]};
+                ok = reduce_arrive<1>(bb, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok);
+                if (ok) {
+                    if (threadIdx.x == 0 && nr > 0) {
+                        tma_expect(&s_mbar, rbytes);
+                        tma_copy(sR, pubR + (size_t)3 * r_lo, rbytes, &s_mbar);
+                    }
+                    reduce_totals<1>(a.partials, bar, s_val, s_tot);
+                    if (threadIdx.x == 0) sc.bb = s_tot[0];
+                    if (nr > 0) ok = tma_wait(&s_mbar, parity, a.error);
+                }
+                ++bar;
+                if (ok) {
+                    first_pass<FCACHE>(f0, sR, sY, y_hi - y_lo);
+                    __syncthreads();
+                    float rz[2] = {0.0f, 0.0f};
+                    second_pass<FCACHE>(f1, sY, sRown, cm.row_lo, cm.nrows, pubZ, rz);
+                    proxy_fence_smem();
+                    ok = reduce_arrive<2>(rz, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok);
+                }
+            } else {
+                proxy_fence_smem();
+                ok = reduce_arrive<3>(acc, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok);
+            }
+        }
+        if (ok) {
+            if (threadIdx.x == 0 && cm.nwin > 0) {
+                tma_expect(&s_mbar, wbytes);
+                tma_copy(winA, pubZ + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+            }
+            if (factor) reduce_totals<2>(a.partials, bar, s_val, s_tot);
+            else reduce_totals<3>(a.partials, bar, s_val, s_tot);
+            if (threadIdx.x == 0) {
+                if (!factor) sc.bb = s_tot[2];
+                sc.gamma = s_tot[0];  // r.z
+                sc.rr = s_tot[1];
+                sc.thr2 = a.tol * a.tol * sc.bb;
+                sc.beta = 0.0f;
+                sc.status = (!isfinite(s_tot[0]) || !isfinite(s_tot[1]) || !isfinite(sc.bb)) ? MFEM_NONFINITE : MFEM_OK;
+                sc.done = sc.status != MFEM_OK || s_tot[1] <= sc.thr2;
+            }
+            pending = cm.nwin > 0;
+        } else if (threadIdx.x == 0) {
+            sc.status = MFEM_TIMEOUT;
+            sc.done = 1;
+            sc.rr = 0.0f;
+            sc.bb = 1.0f;
+        }
+        ++bar;
+        __syncthreads();
+        while (!sc.done) {
+            if (it >= a.maxiter) {
+                if (threadIdx.x == 0) sc.status = MFEM_MAXITER;
+                break;
+            }
+            // ---- phase A: p = z + beta p over the window, Ap = H p, p.Ap
+            float *p_new = pubP[it & 1];
+            if (pending && !tma_wait(&s_mbar, parity, a.error)) {
+                pending = false;
+                if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+                break;
+            }
+            pending = false;
+            const float fbeta = sc.beta;
+            if (it > 0) {
+                for (int j = threadIdx.x; j < 3 * cm.nwin; j += blockDim.x)
+                    winA[j] = __fmaf_rn(fbeta, winB[j], winA[j]);
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x)
+                p_new[(size_t)3 * cm.row_lo + i] = winA[3 * own + i];
+            window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp);
+            __syncthreads();
+            float pap[1] = {0.0f};
+            for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) {
+                pap[0] = __fmaf_rn(winA[3 * own + i], sAp[i], pap[0]);
+                if (factor) pubAp[(size_t)3 * cm.row_lo + i] = sAp[i];
+            }
+            proxy_fence_smem();
+            if (!reduce_arrive<1>(pap, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok)) {
+                if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+                break;
+            }
+            const bool ap_pending = factor && nr > 0;
+            if (ap_pending && threadIdx.x == 0) {
+                tma_expect(&s_mbar, rbytes);
+                tma_copy(winB, pubAp + (size_t)3 * r_lo, rbytes, &s_mbar);
+            }
+            reduce_totals<1>(a.partials, bar, s_val, s_tot);
+            ++bar;
+            if (threadIdx.x == 0) {
+                const float pAp = s_tot[0];
+                if (!isfinite(pAp)) {
+                    sc.status = MFEM_NONFINITE;
+                    sc.done = 1;
+                } else if (!(pAp > 0.0f)) {
+                    sc.status = MFEM_STAGNATION;
+                    sc.done = 1;
+                } else {
+                    sc.alpha = sc.gamma / pAp;
+                }
+            }
+            __syncthreads();
+            if (sc.done) {
+                if (ap_pending) tma_wait(&s_mbar, parity, a.error);
+                break;
+            }
+            const float alpha = sc.alpha;
+            if (ap_pending && !tma_wait(&s_mbar, parity, a.error)) {
+                if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+                break;
+            }
+            // ---- phase B: r -= alpha Ap (over R with a factor), x += alpha p, z = M r
+            if (factor) {
+                for (int j = threadIdx.x; j < 3 * nr; j += blockDim.x) sR[j] = __fmaf_rn(-alpha, winB[j], sR[j]);
+            } else {
+                for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x)
+                    sRown[i] = __fmaf_rn(-alpha, sAp[i], sRown[i]);
+            }
+            for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x)
+                sX[i] = __fmaf_rn(alpha, winA[3 * own + i], sX[i]);
+            __syncthreads();
+            float acc[2] = {0.0f, 0.0f};
+            if (factor) {
+                first_pass<FCACHE>(f0, sR, sY, y_hi - y_lo);
+                __syncthreads();
+                second_pass<FCACHE>(f1, sY, sRown, cm.row_lo, cm.nrows, pubZ, acc);
+            } else {
+                for (int i = threadIdx.x; i < cm.nrows; i += blockDim.x) {
+                    const int row = cm.row_lo + i;
+                    float r[3], z[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) r[c] = sRown[3 * i + c];
+                    precond(a.Minv + (size_t)9 * row, r, z, 1);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        pubZ[3 * row + c] = z[c];
+                        acc[0] = __fmaf_rn(r[c], z[c], acc[0]);
+                        acc[1] = __fmaf_rn(r[c], r[c], acc[1]);
+                    }
+                }
+            }
+            proxy_fence_smem();
+            if (!reduce_arrive<2>(acc, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok)) {
+                if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
+                break;
+            }
+            ++it;
+            if (threadIdx.x == 0 && cm.nwin > 0) {
+                tma_expect(&s_mbar, 2u * wbytes);
+                tma_copy(winA, pubZ + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+                tma_copy(winB, p_new + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+            }
+            pending = cm.nwin > 0;
+            reduce_totals<2>(a.partials, bar, s_val, s_tot);
+            ++bar;
+            if (threadIdx.x == 0) {
+                sc.rr = s_tot[1];
+                if (!isfinite(s_tot[0]) || !isfinite(s_tot[1])) {
+                    sc.status = MFEM_NONFINITE;
+                    sc.done = 1;
+                } else {
+                    sc.beta = s_tot[0] / sc.gamma;
+                    sc.gamma = s_tot[0];
+                    sc.done = s_tot[1] <= sc.thr2;
+                }
+            }
+            __syncthreads();
+        }
+        if (pending) tma_wait(&s_mbar, parity, a.error);
+        pending = false;
+        __syncthreads();
+        if (factor && (sc.status == MFEM_STAGNATION || sc.status == MFEM_NONFINITE)) {
+            it_done += it;
+            mode = 1;
+            continue;
+        }
+        break;
+    }
+    __syncthreads();
+    finish(a, cm, sX, sc, it_done + it);
+}
+
+size_t smem_factor(const PcgLayout &L, bool cache, bool fcache) {
+    const size_t floats = (size_t)L.rows_max * 6 + (size_t)L.win_max * 3 +
+                          (size_t)std::max(L.win_max, L.r_max) * 3 + (size_t)L.r_max * 3 + (size_t)L.y_max * 3;
+    size_t bytes = floats * 4 + (size_t)(L.rows_max + 4) * 4;
+    if (cache) bytes += (size_t)L.blk_max * 40;
+    if (fcache)
+        bytes += (size_t)(L.y_max + 4 + L.rows_max + 4 + L.f0_max + L.f1_max) * 4 +
+                 (size_t)(L.f0_max + L.f1_max) * 20;
+    return (bytes + 15) & ~(size_t)15;
+}
+
+typedef void (*FactorKernel)(PcgArgs);
+
+FactorKernel pick_factor_kernel(const PcgLayout &L) {
+    if (L.cache_matrix) return L.factor_cache ? pcg_factor_kernel<true, true> : pcg_factor_kernel<true, false>;
+    return L.factor_cache ? pcg_factor_kernel<false, true> : pcg_factor_kernel<false, false>;
+}
+
+}  // namespace
+
+cudaError_t pcg_factor_layout(int device, PcgLayout &L, const int32_t *row_ptr, const int32_t *col_idx, int n,
+                              int ctas, int mode, std::vector<int4> &cta_info, std::vector<int4> &factor_info,
+                              std::string &err) {
+    int optin = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (e != cudaSuccess) return e;
+    const size_t budget = (size_t)optin > kStaticSmem ? (size_t)optin - kStaticSmem : 0;
+    if (ctas < 1 || ctas > kMaxCtas || (mode != 2 && mode != 3)) {
+        err = "factor PCG layout: bad CTA count or mode";
+        return cudaErrorInvalidValue;
+    }
+    // per row the smallest and largest column (the diagonal is in every row)
+    std::vector<int> cmin(n), cmax(n);
+    for (int j = 0; j < n; ++j) {
+        int lo = j, hi = j;
+        for (int64_t k = row_ptr[j]; k < row_ptr[j + 1]; ++k) {
+            lo = std::min(lo, (int)col_idx[k]);
+            hi = std::max(hi, (int)col_idx[k]);
+        }
+        cmin[j] = lo;
+        cmax[j] = hi;
+    }
+    cta_info.assign(ctas, make_int4(0, 0, 0, 0));
+    factor_info.assign(ctas, make_int4(0, 0, 0, 0));
+    // blocks per row of the lower (columns <= row) and upper (>= row) forms
+    std::vector<int64_t> lower_ptr(n + 1, 0), upper_ptr(n + 1, 0);
+    for (int j = 0; j < n; ++j) {
+        int nl = 0, nu = 0;
+        for (int64_t k = row_ptr[j]; k < row_ptr[j + 1]; ++k) {
+            nl += col_idx[k] <= j;
+            nu += col_idx[k] >= j;
+        }
+        lower_ptr[j + 1] = lower_ptr[j] + nl;
+        upper_ptr[j + 1] = upper_ptr[j] + nu;
+    }
+    const std::vector<int64_t> &first = mode == 2 ? lower_ptr : upper_ptr;
+    const std::vector<int64_t> &second = mode == 2 ? upper_ptr : lower_ptr;
+    int rows_max = 0, win_max = 0, blk_max = 0, y_max = 0, r_max = 0;
+    int64_t f0_max = 0, f1_max = 0;
+    for (int c = 0; c < ctas; ++c) {
+        const int lo = (int)(((long long)n * c) / ctas);
+        const int hi = (int)(((long long)n * (c + 1)) / ctas);
+        int wlo = lo, whi = hi;
+        for (int i = lo; i < hi; ++i) {
+            wlo = std::min(wlo, cmin[i]);
+            whi = std::max(whi, cmax[i] + 1);
+        }
+        // Y: the second pass's columns from [lo, hi); R: the first pass's from Y
+        int ylo, yhi, rlo, rhi;
+        if (mode == 2) {  // F^T (upper) second, F (lower) first
+            ylo = lo;
+            yhi = whi;
+            rlo = ylo;
+            for (int j = ylo; j < yhi; ++j) rlo = std::min(rlo, cmin[j]);
+            rhi = yhi;
+        } else {  // F (lower) second, F^T (upper) first
+            ylo = wlo;
+            yhi = hi;
+            rlo = ylo;
+            rhi = yhi;
+            for (int j = ylo; j < yhi; ++j) rhi = std::max(rhi, cmax[j] + 1);
+        }
+        rlo = std::min(rlo, lo) & ~3;  // 48-byte aligned copies, whole groups of 4 rows
+        rhi = (std::max(rhi, hi) + 3) & ~3;
+        wlo &= ~3;
+        whi = (whi + 3) & ~3;
+        if (hi == lo) {
+            wlo = whi = rlo = rhi = lo & ~3;
+            ylo = yhi = lo;
+        }
+        cta_info[c] = make_int4(lo, hi, wlo, whi);
+        factor_info[c] = make_int4(ylo, yhi, rlo, rhi);
+        rows_max = std::max(rows_max, hi - lo);
+        win_max = std::max(win_max, whi - wlo);
+        blk_max = std::max(blk_max, (int)(row_ptr[hi] - row_ptr[lo]));
+        y_max = std::max(y_max, yhi - ylo);
+        r_max = std::max(r_max, rhi - rlo);
+        f0_max = std::max(f0_max, first[yhi] - first[ylo]);
+        f1_max = std::max(f1_max, second[hi] - second[lo]);
+    }
+    L.rows_max = (rows_max + 3) & ~3;
+    L.win_max = (win_max + 3) & ~3;
+    L.blk_max = (blk_max + 3) & ~3;
+    L.y_max = (y_max + 3) & ~3;
+    L.r_max = (r_max + 3) & ~3;
+    L.f0_max = (int)((f0_max + 3) & ~(int64_t)3);
+    L.f1_max = (int)((f1_max + 3) & ~(int64_t)3);
+    L.variant = PcgLayout::kFactor;
+    // shared-memory copies in order of worth: with few rows a CTA, the
+    // factor passes (several trips of dependent loads) gain more than H's
+    // product (one trip)
+    const bool opts[4][2] = {{true, true}, {false, true}, {true, false}, {false, false}};
+    for (const auto &o : opts) {
+        const size_t bytes = smem_factor(L, o[0], o[1]);
+        if (bytes <= budget) {
+            L.cache_matrix = o[0] ? 1 : 0;
+            L.factor_cache = o[1] ? 1 : 0;
+            L.smem = bytes;
+            return cudaFuncSetAttribute(pick_factor_kernel(L), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)L.smem);
+        }
+    }
+    err = "mesh too large for the persistent factor PCG (shared memory per CTA exceeded)";
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_pcg_factor(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const BatchViews &bw,
+                              const PcgLayout &L, int ctas, int slot, float tol, int maxiter, int mode,
+                              cudaStream_t s) {
+    if (mode != 2 && mode != 3) return cudaErrorInvalidValue;
+    PcgArgs a = {};
+    a.n = bv.n;
+    a.row_ptr = bv.row_ptr;
+    a.col_idx = bv.col_idx;
+    a.values = bv.values;
+    a.Minv = vv.Minv;
+    a.b = vv.rhs;
+    a.x = vv.dx;
+    a.pub = w.pub;
+    a.n_pad = w.n_pad;
+    a.cta = L.cta_info;
+    a.rows_max = L.rows_max;
+    a.blk_max = L.blk_max;
+    a.win_max = L.win_max;
+    a.partials = w.partials;
+    a.counter = w.counter;
+    a.error = w.error;
+    a.stats = bw.stats;  // the one-body records, [slot][1]
+    a.slot = slot;
+    a.tol = tol;
+    a.maxiter = maxiter;
+    a.use_precond = mode;
+    a.fcta = L.factor_info;
+    const bool lower_first = mode == 2;
+    a.rp0 = lower_first ? bw.lrow : bw.urow;
+    a.c0 = lower_first ? bw.lcol : bw.ucol;
+    a.v0 = lower_first ? bw.Lb : bw.Ub;
+    a.rp1 = lower_first ? bw.urow : bw.lrow;
+    a.c1 = lower_first ? bw.ucol : bw.lcol;
+    a.v1 = lower_first ? bw.Ub : bw.Lb;
+    a.y_max = L.y_max;
+    a.r_max = L.r_max;
+    a.f0_max = L.f0_max;
+    a.f1_max = L.f1_max;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(kPcgThreads);
+    cfg.dynamicSmemBytes = L.smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t err = cudaLaunchKernelEx(&cfg, pick_factor_kernel(L), a);
+    count_launches(1);
+    return err;
+}
+
+}  // namespace mfem

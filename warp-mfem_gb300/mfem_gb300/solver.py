@@ -96,8 +96,8 @@ class MixedFEMSolver:
             cfg.preconditioner = 1 if pc else 0
         cfg.use_cuda_graph = 1 if kwargs.get("use_cuda_graph", True) else 0
         cfg.pcg_ctas = int(kwargs.get("pcg_ctas", 0))
-        cfg.pcg_variant = {"auto": 0, "standard": 1, "single_reduction": 2,
-                           "gather": 3}[kwargs.get("pcg_variant", "auto")]
+        cfg.pcg_variant = {"auto": 0, "standard": 1, "single_reduction": 2, "gather": 3, "factor": 4,
+                           "global_memory": 5}[kwargs.get("pcg_variant", "auto")]
         self.line_search = bool(kwargs.get("line_search", True))
         cfg.line_search = 1 if self.line_search else 0
         cfg.line_search_max_iterations = int(kwargs.get("line_search_max_iterations", 20))
@@ -227,7 +227,7 @@ class MixedFEMSolver:
         smem = ctypes.c_int64()
         _lib.check(self._lib.mfem_plan_pcg_layout(self._plan, ctypes.byref(v), ctypes.byref(c), ctypes.byref(m),
                                                   ctypes.byref(smem)), self._plan)
-        name = {0: "global_memory", 1: "standard", 2: "single_reduction", 3: "gather"}[v.value]
+        name = {0: "global_memory", 1: "standard", 2: "single_reduction", 3: "gather", 4: "factor"}[v.value]
         return dict(variant=name, ctas=c.value, cache_matrix=bool(m.value), smem_bytes=smem.value)
 
     # ------------------------------------------------------------------
