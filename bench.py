@@ -164,10 +164,10 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback 6.8 TB/s"
 
 
-def ncu_traffic_per_launch():
+def ncu_traffic_per_launch(summary="pcg_kernel_nh_beam.md"):
     """DRAM bytes (read + write) of one PCG launch from the committed ncu
-    summary of this workload (profiles/pcg_kernel_nh_beam.md)."""
-    path = os.path.join(ROOT, "profiles", "pcg_kernel_nh_beam.md")
+    summary of this workload (profiles/<summary>)."""
+    path = os.path.join(ROOT, "profiles", summary)
     try:
         text = open(path).read()
     except OSError:
@@ -707,7 +707,9 @@ def run_gb300(args, rank, world, local_rank):
         b_it = 64 * nnzb + 208 * mesh.n
         roofline.update({
             "achieved": b_it * (prof_iters + prof_solves) / (stage_ms["pcg"] / 1000.0) / 1e9,
-            "traffic": None, "traffic_note": None,
+            "traffic": ncu_traffic_per_launch("pcg_factor_kernel_nh_beam.md") if args.workload == "nh_beam" else None,
+            "traffic_note": ("DRAM bytes of one captured FSAI launch (about 160 iterations), "
+                             "profiles/pcg_factor_kernel_nh_beam.md" if args.workload == "nh_beam" else None),
             "kernel": f"pcg_factor_kernel (persistent cooperative {args.preconditioner} PCG)",
             "algorithmic_bytes_per_launch": b_it * per_launch_iters, "bytes_per_pcg_iteration": b_it,
             "bytes_per_pcg_iteration_formula": "64 nnzb + 208 n"})
