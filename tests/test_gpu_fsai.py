@@ -166,6 +166,26 @@ def test_persistent_and_global_memory_pcg_agree(pc, name, cells):
     assert np.abs(da - db).max() <= 1e-4 * np.abs(db).max()
 
 
+@pytest.mark.parametrize("pc", ["fsai", "learned"])
+def test_persistent_factor_pcg_with_global_factor_rows(pc):
+    """nh_beam on 40 CTAs: 470 rows a CTA leave room in shared memory for the
+    factor's row pointers only (columns and blocks through L2); the solve
+    agrees with the global-memory PCG's."""
+    out = {}
+    for variant in ("factor", "global_memory"):
+        mesh, _, solver = make("nh_beam", None, preconditioner=pc, pcg_variant=variant, pcg_ctas=40)
+        lay = solver.pcg_layout()
+        assert lay["variant"] == variant
+        if variant == "factor":
+            assert not lay["cache_matrix"] and lay["smem_bytes"] < 160 * 1024, lay
+        st = one_solve(mesh, solver)
+        assert st["status"] == _lib.MFEM_OK and st["iterations"] > 0, (variant, st)
+        out[variant] = (st, solver.read_buffer("dx").cpu().numpy().astype(np.float64))
+    (sa, da), (sb, db) = out["factor"], out["global_memory"]
+    assert abs(sa["iterations"] - sb["iterations"]) <= max(2, sb["iterations"] // 50), (sa, sb)
+    assert np.abs(da - db).max() <= 1e-4 * np.abs(db).max()
+
+
 def test_mesh_too_large_for_the_persistent_factor_pcg():
     """One CTA cannot hold nh_beam's rows: auto falls back to the
     global-memory PCG, an explicit "factor" is refused."""

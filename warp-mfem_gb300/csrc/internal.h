@@ -278,7 +278,8 @@ struct PcgLayout {
     int rows_max = 0, blk_max = 0, win_max = 0;
     int y_max = 0, r_max = 0;  // kFactor: longest row ranges Y and R of a CTA
     int f0_max = 0, f1_max = 0;  // kFactor: most first- / second-pass factor blocks of a CTA
-    int factor_cache = 0;      // kFactor: 1: each CTA keeps its factor rows in shared memory
+    int factor_cache = 0;      // kFactor: factor rows a CTA keeps in shared memory (0 none, 1 row
+                               // pointers, 2 row pointers, columns and blocks)
     int cache_matrix = 0;      // 1: each CTA keeps its slice of H in shared memory
     size_t smem = 0;           // dynamic shared memory per CTA
 };

@@ -36,12 +36,16 @@ namespace {
 // before later bulk copies (async proxy) into the same bytes.
 __device__ __forceinline__ void proxy_fence_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// How much of its factor rows a CTA keeps in shared memory: nothing, the row
+// pointers (absolute block indices), or row pointers, columns and blocks.
+constexpr int kFactorNone = 0, kFactorRows = 1, kFactorAll = 2;
+
 // A 3x3 block from its five words of BF16 pairs (the tenth value is padding).
-template <bool FCACHE>
+template <bool SHARED>
 __device__ __forceinline__ void block_words(const uint32_t *w, float f[9]) {
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
-        const uint32_t u = FCACHE ? w[i] : __ldg(w + i);
+        const uint32_t u = SHARED ? w[i] : __ldg(w + i);
         __nv_bfloat162 b;
         memcpy(&b, &u, 4);
         const float2 t = __bfloat1622float2(b);
@@ -50,37 +54,38 @@ __device__ __forceinline__ void block_words(const uint32_t *w, float f[9]) {
     }
 }
 
-// The factor rows a CTA applies: its shared-memory copy (FCACHE; local row
-// indices, columns relative to the input vector's first row) or the global
-// forms.
+// The factor rows a CTA applies (FC: kFactorNone, kFactorRows or
+// kFactorAll in shared memory).  With kFactorAll the columns are relative to
+// the input vector's first row and the row pointers to the first block.
 struct FactorRows {
     const int *rp, *col;
     const uint32_t *words;  // kFactorLd BF16 values (five words) per block
-    int row0;               // first row (global forms) or 0 (shared-memory copy)
-    int in_lo;              // subtracted from the columns (0 for the copy)
+    int row0;               // first row (global row pointers) or 0 (shared)
+    int in_lo;              // subtracted from the columns (0 for kFactorAll)
 };
 
 // One row of a factor form times a shared-memory vector `in`, kGroup lanes a
 // row, two blocks a lane and trip; the row's sum in every lane of the group.
-template <bool FCACHE>
+template <int FC>
 __device__ __forceinline__ void factor_row(const FactorRows &f, const float *in, int j, int g_lane, unsigned gmask,
-                                           float &a0, float &a1, float &a2) {
-    a0 = a1 = a2 = 0.0f;
+                                           float (&y)[3]) {
+    constexpr bool SH = FC == kFactorAll;
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
     const int row = f.row0 + j;
-    const int kb = FCACHE ? f.rp[row] : __ldg(f.rp + row);
-    const int ke = FCACHE ? f.rp[row + 1] : __ldg(f.rp + row + 1);
+    const int kb = FC != kFactorNone ? f.rp[row] : __ldg(f.rp + row);
+    const int ke = FC != kFactorNone ? f.rp[row + 1] : __ldg(f.rp + row + 1);
     for (int k = kb + g_lane; k < ke; k += 2 * kGroup) {
         const int k2 = k + kGroup;
         const bool two = k2 < ke;
         const int kk2 = two ? k2 : k;
-        const int c = (FCACHE ? f.col[k] : __ldg(f.col + k)) - f.in_lo;
-        const int c2 = (FCACHE ? f.col[kk2] : __ldg(f.col + kk2)) - f.in_lo;
+        const int c = (SH ? f.col[k] : __ldg(f.col + k)) - f.in_lo;
+        const int c2 = (SH ? f.col[kk2] : __ldg(f.col + kk2)) - f.in_lo;
         const float v0 = in[3 * c], v1 = in[3 * c + 1], v2 = in[3 * c + 2];
         float w0 = in[3 * c2], w1 = in[3 * c2 + 1], w2 = in[3 * c2 + 2];
         if (!two) w0 = w1 = w2 = 0.0f;
         float m[9], m2[9];
-        block_words<FCACHE>(f.words + (size_t)5 * k, m);
-        block_words<FCACHE>(f.words + (size_t)5 * kk2, m2);
+        block_words<SH>(f.words + (size_t)5 * k, m);
+        block_words<SH>(f.words + (size_t)5 * kk2, m2);
         a0 += m[0] * v0 + m[1] * v1 + m[2] * v2;
         a1 += m[3] * v0 + m[4] * v1 + m[5] * v2;
         a2 += m[6] * v0 + m[7] * v1 + m[8] * v2;
@@ -94,42 +99,139 @@ __device__ __forceinline__ void factor_row(const FactorRows &f, const float *in,
         a1 += __shfl_xor_sync(gmask, a1, off);
         a2 += __shfl_xor_sync(gmask, a2, off);
     }
+    y[0] = a0;
+    y[1] = a1;
+    y[2] = a2;
+}
+
+// Rows ja and jb (if has_b) of a factor form times a shared-memory vector
+// `in`, kGroup lanes a row pair: per lane and trip two blocks of each row,
+// the four blocks' loads in flight at once; the rows' sums in every lane of
+// the group.  For factor rows read through L2 (half the dependent-load
+// trips); with the rows in shared memory the single-row form issues fewer
+// instructions and runs faster.
+template <int FC>
+__device__ __forceinline__ void factor_row_pair(const FactorRows &f, const float *in, int ja, int jb, bool has_b,
+                                                int g_lane, unsigned gmask, float (&ya)[3], float (&yb)[3]) {
+    constexpr bool SH = FC == kFactorAll;
+    const int ra = f.row0 + ja, rb = f.row0 + (has_b ? jb : ja);
+    const int kba = FC != kFactorNone ? f.rp[ra] : __ldg(f.rp + ra);
+    const int kea = FC != kFactorNone ? f.rp[ra + 1] : __ldg(f.rp + ra + 1);
+    int kbb = FC != kFactorNone ? f.rp[rb] : __ldg(f.rp + rb);
+    int keb = FC != kFactorNone ? f.rp[rb + 1] : __ldg(f.rp + rb + 1);
+    if (!has_b) keb = kbb;
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, b0 = 0.0f, b1 = 0.0f, b2 = 0.0f;
+    for (int t = g_lane; kba + t < kea || kbb + t < keb; t += 2 * kGroup) {
+        const int k[4] = {kba + t, kba + t + kGroup, kbb + t, kbb + t + kGroup};
+        const bool ok[4] = {k[0] < kea, k[1] < kea, k[2] < keb, k[3] < keb};
+        int c[4];
+        float m[4][9];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int kk = ok[u] ? k[u] : kba;  // every row holds its diagonal block
+            c[u] = (SH ? f.col[kk] : __ldg(f.col + kk)) - f.in_lo;
+            block_words<SH>(f.words + (size_t)5 * kk, m[u]);
+        }
+        float v[4][3];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) v[u][q] = ok[u] ? in[3 * c[u] + q] : 0.0f;
+        a0 += m[0][0] * v[0][0] + m[0][1] * v[0][1] + m[0][2] * v[0][2];
+        a1 += m[0][3] * v[0][0] + m[0][4] * v[0][1] + m[0][5] * v[0][2];
+        a2 += m[0][6] * v[0][0] + m[0][7] * v[0][1] + m[0][8] * v[0][2];
+        a0 += m[1][0] * v[1][0] + m[1][1] * v[1][1] + m[1][2] * v[1][2];
+        a1 += m[1][3] * v[1][0] + m[1][4] * v[1][1] + m[1][5] * v[1][2];
+        a2 += m[1][6] * v[1][0] + m[1][7] * v[1][1] + m[1][8] * v[1][2];
+        b0 += m[2][0] * v[2][0] + m[2][1] * v[2][1] + m[2][2] * v[2][2];
+        b1 += m[2][3] * v[2][0] + m[2][4] * v[2][1] + m[2][5] * v[2][2];
+        b2 += m[2][6] * v[2][0] + m[2][7] * v[2][1] + m[2][8] * v[2][2];
+        b0 += m[3][0] * v[3][0] + m[3][1] * v[3][1] + m[3][2] * v[3][2];
+        b1 += m[3][3] * v[3][0] + m[3][4] * v[3][1] + m[3][5] * v[3][2];
+        b2 += m[3][6] * v[3][0] + m[3][7] * v[3][1] + m[3][8] * v[3][2];
+    }
+#pragma unroll
+    for (int off = kGroup / 2; off > 0; off >>= 1) {
+        a0 += __shfl_xor_sync(gmask, a0, off);
+        a1 += __shfl_xor_sync(gmask, a1, off);
+        a2 += __shfl_xor_sync(gmask, a2, off);
+        b0 += __shfl_xor_sync(gmask, b0, off);
+        b1 += __shfl_xor_sync(gmask, b1, off);
+        b2 += __shfl_xor_sync(gmask, b2, off);
+    }
+    ya[0] = a0;
+    ya[1] = a1;
+    ya[2] = a2;
+    yb[0] = b0;
+    yb[1] = b1;
+    yb[2] = b2;
 }
 
 // y[j] = (F0 r)_(y_lo + j) for j < ny, r over R in shared memory.
-template <bool FCACHE>
+template <int FC>
 __device__ __forceinline__ void first_pass(const FactorRows &f0, const float *sR, float *sY, int ny) {
     const int g_lane = threadIdx.x & (kGroup - 1);
     const unsigned gmask = ((1u << kGroup) - 1u) << (threadIdx.x & (32 - kGroup));
     const int group = threadIdx.x / kGroup, ngroups = blockDim.x / kGroup;
-    for (int j = group; j < ny; j += ngroups) {
-        float a0, a1, a2;
-        factor_row<FCACHE>(f0, sR, j, g_lane, gmask, a0, a1, a2);
-        if (g_lane == 0) {
-            sY[3 * j] = a0;
-            sY[3 * j + 1] = a1;
-            sY[3 * j + 2] = a2;
+    if constexpr (FC == kFactorAll) {
+        for (int j = group; j < ny; j += ngroups) {
+            float y[3];
+            factor_row<FC>(f0, sR, j, g_lane, gmask, y);
+            if (g_lane == 0)
+#pragma unroll
+                for (int q = 0; q < 3; ++q) sY[3 * j + q] = y[q];
+        }
+    } else {
+        for (int j = group; j < ny; j += 2 * ngroups) {  // rows j and j + ngroups together
+            const int jb = j + ngroups;
+            const bool has_b = jb < ny;
+            float ya[3], yb[3];
+            factor_row_pair<FC>(f0, sR, j, jb, has_b, g_lane, gmask, ya, yb);
+            if (g_lane == 0) {
+#pragma unroll
+                for (int q = 0; q < 3; ++q) sY[3 * j + q] = ya[q];
+                if (has_b)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) sY[3 * jb + q] = yb[q];
+            }
         }
     }
 }
 
+// Row i's z: published, and (r, z), (r, r) added to acc.
+__device__ __forceinline__ void emit_z(const float z[3], const float *sRown, int i, int row_lo, float *pubZ,
+                                       float (&acc)[2]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float r = sRown[3 * i + c];
+        pubZ[(size_t)3 * (row_lo + i) + c] = z[c];
+        acc[0] = __fmaf_rn(r, z[c], acc[0]);
+        acc[1] = __fmaf_rn(r, r, acc[1]);
+    }
+}
+
 // z = F1 y for the CTA's rows: published, and (r, z), (r, r) added to acc.
-template <bool FCACHE>
+template <int FC>
 __device__ __forceinline__ void second_pass(const FactorRows &f1, const float *sY, const float *sRown, int row_lo,
                                             int nrows, float *pubZ, float (&acc)[2]) {
     const int g_lane = threadIdx.x & (kGroup - 1);
     const unsigned gmask = ((1u << kGroup) - 1u) << (threadIdx.x & (32 - kGroup));
     const int group = threadIdx.x / kGroup, ngroups = blockDim.x / kGroup;
-    for (int i = group; i < nrows; i += ngroups) {
-        float z[3];
-        factor_row<FCACHE>(f1, sY, i, g_lane, gmask, z[0], z[1], z[2]);
-        if (g_lane == 0) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float r = sRown[3 * i + c];
-                pubZ[(size_t)3 * (row_lo + i) + c] = z[c];
-                acc[0] = __fmaf_rn(r, z[c], acc[0]);
-                acc[1] = __fmaf_rn(r, r, acc[1]);
+    if constexpr (FC == kFactorAll) {
+        for (int i = group; i < nrows; i += ngroups) {
+            float z[3];
+            factor_row<FC>(f1, sY, i, g_lane, gmask, z);
+            if (g_lane == 0) emit_z(z, sRown, i, row_lo, pubZ, acc);
+        }
+    } else {
+        for (int i = group; i < nrows; i += 2 * ngroups) {  // rows i and i + ngroups together
+            const int ib = i + ngroups;
+            const bool has_b = ib < nrows;
+            float za[3], zb[3];
+            factor_row_pair<FC>(f1, sY, i, ib, has_b, g_lane, gmask, za, zb);
+            if (g_lane == 0) {
+                emit_z(za, sRown, i, row_lo, pubZ, acc);
+                if (has_b) emit_z(zb, sRown, ib, row_lo, pubZ, acc);
             }
         }
     }
@@ -146,7 +248,7 @@ __device__ __forceinline__ void stage_factor_rows(const int *rp, const int *col,
     for (int t = threadIdx.x; t < 5 * nb; t += blockDim.x) s_words[t] = w[t];
 }
 
-template <bool CACHE, bool FCACHE>
+template <bool CACHE, int FC>
 __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     PCG_PROLOGUE
@@ -160,7 +262,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
     int *rowoff = reinterpret_cast<int *>(sY + 3 * a.y_max);
     float *sH = reinterpret_cast<float *>(rowoff + rows_max + 4);
     int *sCol = reinterpret_cast<int *>(sH + (CACHE ? 9 * a.blk_max : 0));
-    int *f_rp0 = sCol + (CACHE ? a.blk_max : 0);  // FCACHE: the CTA's factor rows
+    int *f_rp0 = sCol + (CACHE ? a.blk_max : 0);  // the CTA's factor rows (FC)
     int *f_rp1 = f_rp0 + a.y_max + 4;
     int *f_c0 = f_rp1 + rows_max + 4;
     int *f_c1 = f_c0 + a.f0_max;
@@ -180,11 +282,16 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
 
     load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE);
     FactorRows f0, f1;
-    if (FCACHE) {
+    if (FC == kFactorAll) {
         stage_factor_rows(a.rp0, a.c0, a.v0, y_lo, y_hi - y_lo, r_lo, f_rp0, f_c0, f_w0);
         stage_factor_rows(a.rp1, a.c1, a.v1, cm.row_lo, cm.nrows, y_lo, f_rp1, f_c1, f_w1);
         f0 = FactorRows{f_rp0, f_c0, f_w0, 0, 0};
         f1 = FactorRows{f_rp1, f_c1, f_w1, 0, 0};
+    } else if (FC == kFactorRows) {
+        for (int j = threadIdx.x; j <= y_hi - y_lo; j += blockDim.x) f_rp0[j] = a.rp0[y_lo + j];
+        for (int j = threadIdx.x; j <= cm.nrows; j += blockDim.x) f_rp1[j] = a.rp1[cm.row_lo + j];
+        f0 = FactorRows{f_rp0, a.c0, reinterpret_cast<const uint32_t *>(a.v0), 0, r_lo};
+        f1 = FactorRows{f_rp1, a.c1, reinterpret_cast<const uint32_t *>(a.v1), 0, y_lo};
     } else {
         f0 = FactorRows{a.rp0, a.c0, reinterpret_cast<const uint32_t *>(a.v0), y_lo, r_lo};
         f1 = FactorRows{a.rp1, a.c1, reinterpret_cast<const uint32_t *>(a.v1), cm.row_lo, y_lo};
@@ -248,10 +355,10 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
                 }
                 ++bar;
                 if (ok) {
-                    first_pass<FCACHE>(f0, sR, sY, y_hi - y_lo);
+                    first_pass<FC>(f0, sR, sY, y_hi - y_lo);
                     __syncthreads();
                     float rz[2] = {0.0f, 0.0f};
-                    second_pass<FCACHE>(f1, sY, sRown, cm.row_lo, cm.nrows, pubZ, rz);
+                    second_pass<FC>(f1, sY, sRown, cm.row_lo, cm.nrows, pubZ, rz);
                     proxy_fence_smem();
                     ok = reduce_arrive<2>(rz, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok);
                 }
@@ -359,9 +466,9 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
             __syncthreads();
             float acc[2] = {0.0f, 0.0f};
             if (factor) {
-                first_pass<FCACHE>(f0, sR, sY, y_hi - y_lo);
+                first_pass<FC>(f0, sR, sY, y_hi - y_lo);
                 __syncthreads();
-                second_pass<FCACHE>(f1, sY, sRown, cm.row_lo, cm.nrows, pubZ, acc);
+                second_pass<FC>(f1, sY, sRown, cm.row_lo, cm.nrows, pubZ, acc);
             } else {
                 for (int i = threadIdx.x; i < cm.nrows; i += blockDim.x) {
                     const int row = cm.row_lo + i;
@@ -418,22 +525,25 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
     finish(a, cm, sX, sc, it_done + it);
 }
 
-size_t smem_factor(const PcgLayout &L, bool cache, bool fcache) {
+size_t smem_factor(const PcgLayout &L, bool cache, int fc) {
     const size_t floats = (size_t)L.rows_max * 6 + (size_t)L.win_max * 3 +
                           (size_t)std::max(L.win_max, L.r_max) * 3 + (size_t)L.r_max * 3 + (size_t)L.y_max * 3;
     size_t bytes = floats * 4 + (size_t)(L.rows_max + 4) * 4;
     if (cache) bytes += (size_t)L.blk_max * 40;
-    if (fcache)
-        bytes += (size_t)(L.y_max + 4 + L.rows_max + 4 + L.f0_max + L.f1_max) * 4 +
-                 (size_t)(L.f0_max + L.f1_max) * 20;
+    if (fc != kFactorNone) bytes += (size_t)(L.y_max + 4 + L.rows_max + 4) * 4;
+    if (fc == kFactorAll) bytes += (size_t)(L.f0_max + L.f1_max) * 24;
     return (bytes + 15) & ~(size_t)15;
 }
 
 typedef void (*FactorKernel)(PcgArgs);
 
 FactorKernel pick_factor_kernel(const PcgLayout &L) {
-    if (L.cache_matrix) return L.factor_cache ? pcg_factor_kernel<true, true> : pcg_factor_kernel<true, false>;
-    return L.factor_cache ? pcg_factor_kernel<false, true> : pcg_factor_kernel<false, false>;
+    if (L.cache_matrix)
+        return L.factor_cache == kFactorAll ? pcg_factor_kernel<true, kFactorAll>
+                                            : pcg_factor_kernel<true, kFactorRows>;
+    if (L.factor_cache == kFactorAll) return pcg_factor_kernel<false, kFactorAll>;
+    return L.factor_cache == kFactorRows ? pcg_factor_kernel<false, kFactorRows>
+                                         : pcg_factor_kernel<false, kFactorNone>;
 }
 
 }  // namespace
@@ -528,13 +638,14 @@ cudaError_t pcg_factor_layout(int device, PcgLayout &L, const int32_t *row_ptr, 
     L.variant = PcgLayout::kFactor;
     // shared-memory copies in order of worth: with few rows a CTA, the
     // factor passes (several trips of dependent loads) gain more than H's
-    // product (one trip)
-    const bool opts[4][2] = {{true, true}, {false, true}, {true, false}, {false, false}};
+    // product (one trip); the factor's row pointers (a few KB) take one
+    // dependent load off every trip
+    const int opts[5][2] = {{1, kFactorAll}, {0, kFactorAll}, {1, kFactorRows}, {0, kFactorRows}, {0, kFactorNone}};
     for (const auto &o : opts) {
-        const size_t bytes = smem_factor(L, o[0], o[1]);
+        const size_t bytes = smem_factor(L, o[0] != 0, o[1]);
         if (bytes <= budget) {
-            L.cache_matrix = o[0] ? 1 : 0;
-            L.factor_cache = o[1] ? 1 : 0;
+            L.cache_matrix = o[0];
+            L.factor_cache = o[1];
             L.smem = bytes;
             return cudaFuncSetAttribute(pick_factor_kernel(L), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)L.smem);
