@@ -18,8 +18,10 @@
 // solve and updates it with the same instructions, from the same published
 // Ap and the same alpha, as the rows' owners, so every copy of a row's r
 // equals the owner's bit for bit; y over Y is recomputed by each CTA instead
-// of exchanged.  The factor's BF16 blocks and columns are read through the
-// read-only path (L2-resident, unchanged during a solve).
+// of exchanged.  The factor does not change during a solve: where shared
+// memory allows, each CTA copies its rows of both forms (row pointers,
+// columns, BF16 blocks) there once per launch, else only their row pointers,
+// and reads the rest through the read-only path (L2).
 //
 // A factor solve that breaks down (non-finite values or p.Ap <= 0) is solved
 // again from the same warm start with block-Jacobi inside the launch; every
