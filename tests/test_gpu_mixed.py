@@ -142,21 +142,26 @@ def test_set_solver_rejects_bad_config():
         MixedFEMSolver(model, iterations=1, solver_precision="fp8")
 
 
+@pytest.mark.parametrize("variant", ["factor", "global_memory"])
 @pytest.mark.parametrize("pc", ["fsai", "learned"])
-def test_mixed_with_factor_preconditioner(pc):
-    """16-bit blocks with a factor preconditioner in the inner PCG: the fp64
-    tolerance is reached with fewer inner iterations than block-Jacobi, and a
-    trajectory stays within 1e-5 of the float64 oracle."""
+def test_mixed_with_factor_preconditioner(pc, variant):
+    """16-bit blocks with a factor preconditioner in the inner PCG (the
+    persistent factor PCG on an fp32 copy of the 16-bit blocks, or the
+    global-memory inner PCG): the fp64 tolerance is reached with fewer inner
+    iterations than block-Jacobi, and a trajectory stays within 1e-5 of the
+    float64 oracle."""
     inner = {}
     for p in ("block_jacobi", pc):
-        mesh, _, solver = make("nh_beam", (16, 4, 4), "fp16", preconditioner=p)
+        kw = {} if p == "block_jacobi" else {"pcg_variant": variant}
+        mesh, _, solver = make("nh_beam", (16, 4, 4), "fp16", preconditioner=p, **kw)
         H, g, dx64, _ = one_solve(mesh, solver)
         rel = np.linalg.norm(g - H @ dx64) / np.linalg.norm(g)
         st = solver.mixed_stats()[0]
         assert st["status"] == _lib.MFEM_OK and rel <= 1e-8, (p, st, rel)
         inner[p] = st["inner_iterations"]
     assert 0 < inner[pc] < inner["block_jacobi"], inner
-    mesh, model, solver = make("nh_beam", (16, 4, 4), "fp16", preconditioner=pc, factor_refresh=8)
+    mesh, model, solver = make("nh_beam", (16, 4, 4), "fp16", preconditioner=pc, factor_refresh=8,
+                               pcg_variant=variant)
     ref = O.OracleSolver(mesh, dtype=np.float64)
     A, B = model.state(), model.state()
     A.particle_q.copy_(torch.as_tensor(mesh.q0, device=DEV))
@@ -169,12 +174,14 @@ def test_mixed_with_factor_preconditioner(pc):
         close(A.particle_q.cpu().numpy(), q, 1e-5)
 
 
-@pytest.mark.parametrize("pc", ["block_jacobi", "fsai"])
-def test_tiny_residual_does_not_underflow(pc):
+@pytest.mark.parametrize("pc,variant", [("block_jacobi", "auto"), ("fsai", "global_memory"), ("fsai", "factor")])
+def test_tiny_residual_does_not_underflow(pc, variant):
     """A right-hand side of 1e-25 scale (late, nearly converged Newton
-    iterations): the inner PCG's sums of products would underflow in fp32;
-    they are fp64, so the solve still reaches the fp64 tolerance."""
-    mesh, _, solver = make("nh_beam", (16, 4, 4), "fp16", preconditioner=pc)
+    iterations): fp32 sums of products of its entries would underflow. The
+    global-memory inner PCG sums in fp64; the persistent factor PCG solves
+    for the residual scaled to unit norm. Either way the solve still reaches
+    the fp64 tolerance."""
+    mesh, _, solver = make("nh_beam", (16, 4, 4), "fp16", preconditioner=pc, pcg_variant=variant)
     q = torch.as_tensor(mesh.q0, device=DEV)
     x = q.clone()
     solver.predict(q, torch.zeros_like(q), mesh.spec.dt)

@@ -205,9 +205,8 @@ bool net_ready(const mfem_plan *p) { return p->cfg.preconditioner != 3 || p->fv.
 // The reference's float32 PCG, or the mixed-precision iterative refinement.
 cudaError_t global_solve(mfem_plan *p, int slot, cudaStream_t s) {
     if (p->ir.mode != 0)
-        return launch_mixed_solve(p->bv, p->vv, p->ir, p->pw, p->bw, slot, p->cfg.cg_max_iterations,
-                                  p->cfg.preconditioner,
-                                  s);
+        return launch_mixed_solve(p->bv, p->vv, p->ir, p->pw, p->bw, p->pl, p->pcg_ctas, slot,
+                                  p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
     if (p->pl.variant == PcgLayout::kFactor)
         return launch_pcg_factor(p->bv, p->vv, p->pw, p->bw, p->pl, p->pcg_ctas, slot, p->cfg.cg_tolerance,
                                  p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
@@ -1119,6 +1118,10 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
     alloc(&w.dx_init, n3 * sizeof(float));
     alloc(&w.best, sizeof(double));
     alloc(&w.stats, (size_t)p->max_stats * sizeof(IrStats));
+    alloc(&w.scale, 2 * sizeof(float));
+    // a plan on the persistent factor PCG runs its inner solves there, on an
+    // fp32 copy of the 16-bit blocks (the same rounding)
+    if (p->pl.variant == PcgLayout::kFactor) alloc(&w.hq, nz * 9 * sizeof(float));
     int max_ctas = 1;
     if (e == cudaSuccess) e = ir_max_ctas(p->device, &max_ctas);
     if (e == cudaSuccess) e = cudaMemset(w.counter, 0, sizeof(unsigned long long));

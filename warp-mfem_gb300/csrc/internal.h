@@ -264,6 +264,9 @@ struct IrWork {
     float *dx_init;            // [n][3] the warm start, for a restart
     double *best;              // [1] smallest fp64 relative residual of the solve so far
     IrStats *stats;            // [max solves per step]
+    // inner solves in the persistent factor PCG (a plan with pcg_variant 4):
+    float *hq;                 // [nnzb][9] the 16-bit blocks times their row scale, as fp32 (else null)
+    float *scale;              // [2] 1 / ||r|| and ||r|| of the latest fp64 residual
 };
 
 // Row partition and shared-memory plan of the persistent PCG.
@@ -349,7 +352,13 @@ cudaError_t launch_batched_pcg(const BsrViews &bv, const VertexViews &vv, const 
                                float tol, int maxiter, int use_precond, cudaStream_t s);
 int ir_residual_blocks(int n);
 cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const IrWork &w, const PcgWork &pw,
-                               const BatchViews &fb, int slot, int maxiter, int use_precond, cudaStream_t s);
+                               const BatchViews &fb, const PcgLayout &pl, int pcg_ctas, int slot, int maxiter,
+                               int use_precond, cudaStream_t s);
+// The inner solve of the mixed refinement, Hq e = r to inner_tol from e = 0,
+// in the persistent factor PCG.
+cudaError_t launch_pcg_factor_inner(const BsrViews &bv, const VertexViews &vv, const IrWork &w, const PcgWork &pw,
+                                    const BatchViews &bw, const PcgLayout &L, int ctas, int slot, int maxiter,
+                                    int mode, cudaStream_t s);
 
 // Number of kernels launched by the launchers above (process-wide).
 void count_launches(uint64_t k);

@@ -44,6 +44,11 @@ struct PcgArgs {
     const __nv_bfloat16 *v0, *v1;
     int y_max, r_max;
     int f0_max, f1_max;  // most first- / second-pass blocks of a CTA (factor kept in shared memory)
+    // the inner solve of the mixed-precision refinement (pcg_factor.cu): its
+    // state words, the right-hand side's scale, H's blocks rounded to 16 bits
+    int *ir_state;
+    const float *ir_scale;
+    const float *values_q;
 };
 
 __device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *p) {
@@ -196,10 +201,12 @@ __device__ bool tma_wait(uint64_t *mbar, uint32_t &parity, int *error) {
     return ok;
 }
 
-// out[i] = sum_k H[k] win[col_k] over the CTA's rows, kGroup lanes per row.
+// out[i] = sum_k H[k] win[col_k] over the CTA's rows, kGroup lanes per row;
+// H's blocks from the shared-memory slice (CACHE) or from `values`.
 template <bool CACHE>
 __device__ __forceinline__ void window_product(const PcgArgs &a, const int *rowoff, const float *sH, const int *sCol,
-                                               int blk_lo, int win_lo, int nrows, const float *win, float *out) {
+                                               int blk_lo, int win_lo, int nrows, const float *win, float *out,
+                                               const float *values) {
     const int g_lane = threadIdx.x & (kGroup - 1);
     const int group = threadIdx.x / kGroup;
     const int ngroups = blockDim.x / kGroup;
@@ -215,7 +222,7 @@ __device__ __forceinline__ void window_product(const PcgArgs &a, const int *rowo
                 h = sH + (size_t)k * 9;
                 c = sCol[k];
             } else {
-                h = a.values + (size_t)(blk_lo + k) * 9;
+                h = values + (size_t)(blk_lo + k) * 9;
                 c = __ldg(a.col_idx + blk_lo + k) - win_lo;
             }
             const float v0 = win[3 * c + 0], v1 = win[3 * c + 1], v2 = win[3 * c + 2];
@@ -266,10 +273,10 @@ __device__ __forceinline__ Common setup_common(const PcgArgs &a) {
 }
 
 __device__ __forceinline__ void load_matrix_slice(const PcgArgs &a, const Common &c, int *rowoff, float *sH,
-                                                  int *sCol, bool cache) {
+                                                  int *sCol, bool cache, const float *values) {
     for (int i = threadIdx.x; i <= c.nrows; i += blockDim.x) rowoff[i] = a.row_ptr[c.row_lo + i] - c.blk_lo;
     if (cache) {
-        for (int k = threadIdx.x; k < 9 * c.nblk; k += blockDim.x) sH[k] = a.values[(size_t)9 * c.blk_lo + k];
+        for (int k = threadIdx.x; k < 9 * c.nblk; k += blockDim.x) sH[k] = values[(size_t)9 * c.blk_lo + k];
         for (int k = threadIdx.x; k < c.nblk; k += blockDim.x) sCol[k] = a.col_idx[c.blk_lo + k] - c.win_lo;
     }
 }

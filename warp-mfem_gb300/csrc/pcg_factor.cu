@@ -253,7 +253,27 @@ __device__ __forceinline__ void stage_factor_rows(const int *rp, const int *col,
 template <bool CACHE, int FC>
 __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
+    // As the refinement's inner solve: nothing to do once it has finished or
+    // when it restarts from the warm start (its state words, as every CTA
+    // reads them: the previous launch wrote them)
+    const bool inner = a.ir_state != nullptr;
+    if (inner) {
+        if (ld_volatile(a.ir_state) != 0 || ld_volatile(a.ir_state + 7) != 0) return;
+        if (ld_volatile(a.error) != 0) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                a.ir_state[5] = MFEM_TIMEOUT;
+                a.ir_state[0] = 1;
+            }
+            return;
+        }
+    }
     PCG_PROLOGUE
+    // the inner solve runs on the 16-bit blocks (as fp32) unless the
+    // refinement switched to the fp32 H; its right-hand side is scaled to
+    // unit norm and its solution scaled back
+    const bool full = !inner || ld_volatile(a.ir_state + 6) != 0;
+    const float *vals = full ? a.values : a.values_q;
+    const float bscale = inner ? a.ir_scale[0] : 1.0f;
     const int rows_max = a.rows_max, win_max = a.win_max;
     float *sX = reinterpret_cast<float *>(smem);
     float *sAp = sX + 3 * rows_max;
@@ -282,7 +302,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
     float *sRown = sR + 3 * (cm.row_lo - r_lo);  // the CTA's rows in R
     const uint32_t wbytes = (uint32_t)cm.nwin * 12u, rbytes = (uint32_t)nr * 12u;
 
-    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE);
+    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE, vals);
     FactorRows f0, f1;
     if (FC == kFactorAll) {
         stage_factor_rows(a.rp0, a.c0, a.v0, y_lo, y_hi - y_lo, r_lo, f_rp0, f_c0, f_w0);
@@ -308,14 +328,20 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
         proxy_fence_smem();
         __syncthreads();
         bool ok = true;
-        if (threadIdx.x == 0 && cm.nwin > 0) {
-            tma_expect(&s_mbar, wbytes);
-            tma_copy(winA, a.x + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+        if (!inner) {
+            if (threadIdx.x == 0 && cm.nwin > 0) {
+                tma_expect(&s_mbar, wbytes);
+                tma_copy(winA, a.x + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+            }
+            if (cm.nwin > 0) ok = tma_wait(&s_mbar, parity, a.error);
         }
-        if (cm.nwin > 0) ok = tma_wait(&s_mbar, parity, a.error);
         if (ok) {
-            for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = winA[3 * own + i];
-            window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp);
+            if (inner) {  // x0 = 0: r = b
+                for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = sAp[i] = 0.0f;
+            } else {
+                for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = winA[3 * own + i];
+                window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp, vals);
+            }
             __syncthreads();
             float acc[3] = {0.0f, 0.0f, 0.0f};
             for (int i = threadIdx.x; i < cm.nrows; i += blockDim.x) {
@@ -323,7 +349,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
                 float r[3];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    const float bc = a.b[3 * row + c];
+                    const float bc = a.b[3 * row + c] * bscale;
                     r[c] = bc - sAp[3 * i + c];
                     acc[2] = __fmaf_rn(bc, bc, acc[2]);
                 }
@@ -415,7 +441,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
             __syncthreads();
             for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x)
                 p_new[(size_t)3 * cm.row_lo + i] = winA[3 * own + i];
-            window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp);
+            window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp, vals);
             __syncthreads();
             float pap[1] = {0.0f};
             for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) {
@@ -524,7 +550,28 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
         break;
     }
     __syncthreads();
-    finish(a, cm, sX, sc, it_done + it);
+    if (!inner) {
+        finish(a, cm, sX, sc, it_done + it);
+        return;
+    }
+    // the correction for the refinement, and its state: the outer loop adds
+    // the correction at its next residual; a broken inner solve still hands
+    // over its iterate, as the reference's CG does
+    const float es = a.ir_scale[1];
+    for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) a.x[(size_t)3 * cm.row_lo + i] = sX[i] * es;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.ir_state[2] += it_done + it;
+        a.ir_state[3] = 1;
+        if (sc.status == MFEM_NONFINITE && !full) {
+            // the 16-bit H broke the inner solve: restart on the fp32 H
+            a.ir_state[3] = 0;
+            a.ir_state[6] = 1;
+            a.ir_state[7] = 1;
+        } else if (sc.status == MFEM_TIMEOUT || sc.status == MFEM_NONFINITE) {
+            a.ir_state[5] = sc.status;
+            a.ir_state[0] = 1;
+        }
+    }
 }
 
 size_t smem_factor(const PcgLayout &L, bool cache, int fc) {
@@ -657,9 +704,11 @@ cudaError_t pcg_factor_layout(int device, PcgLayout &L, const int32_t *row_ptr, 
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_pcg_factor(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const BatchViews &bw,
-                              const PcgLayout &L, int ctas, int slot, float tol, int maxiter, int mode,
-                              cudaStream_t s) {
+namespace {
+
+cudaError_t launch_factor_args(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const BatchViews &bw,
+                               const PcgLayout &L, int ctas, int slot, float tol, int maxiter, int mode,
+                               const float *b, float *x, const IrWork *ir, cudaStream_t s) {
     if (mode != 2 && mode != 3) return cudaErrorInvalidValue;
     PcgArgs a = {};
     a.n = bv.n;
@@ -667,8 +716,8 @@ cudaError_t launch_pcg_factor(const BsrViews &bv, const VertexViews &vv, const P
     a.col_idx = bv.col_idx;
     a.values = bv.values;
     a.Minv = vv.Minv;
-    a.b = vv.rhs;
-    a.x = vv.dx;
+    a.b = b;
+    a.x = x;
     a.pub = w.pub;
     a.n_pad = w.n_pad;
     a.cta = L.cta_info;
@@ -678,7 +727,9 @@ cudaError_t launch_pcg_factor(const BsrViews &bv, const VertexViews &vv, const P
     a.partials = w.partials;
     a.counter = w.counter;
     a.error = w.error;
-    a.stats = bw.stats;  // the one-body records, [slot][1]
+    // the one-body records, [slot][1]; an inner solve's record is the
+    // refinement's, which its residual pass writes
+    a.stats = ir ? w.stats : bw.stats;
     a.slot = slot;
     a.tol = tol;
     a.maxiter = maxiter;
@@ -695,6 +746,11 @@ cudaError_t launch_pcg_factor(const BsrViews &bv, const VertexViews &vv, const P
     a.r_max = L.r_max;
     a.f0_max = L.f0_max;
     a.f1_max = L.f1_max;
+    if (ir) {
+        a.ir_state = ir->state;
+        a.ir_scale = ir->scale;
+        a.values_q = ir->hq;
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(ctas);
     cfg.blockDim = dim3(kPcgThreads);
@@ -708,6 +764,20 @@ cudaError_t launch_pcg_factor(const BsrViews &bv, const VertexViews &vv, const P
     cudaError_t err = cudaLaunchKernelEx(&cfg, pick_factor_kernel(L), a);
     count_launches(1);
     return err;
+}
+
+}  // namespace
+
+cudaError_t launch_pcg_factor(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const BatchViews &bw,
+                              const PcgLayout &L, int ctas, int slot, float tol, int maxiter, int mode,
+                              cudaStream_t s) {
+    return launch_factor_args(bv, vv, w, bw, L, ctas, slot, tol, maxiter, mode, vv.rhs, vv.dx, nullptr, s);
+}
+
+cudaError_t launch_pcg_factor_inner(const BsrViews &bv, const VertexViews &vv, const IrWork &ir, const PcgWork &pw,
+                                    const BatchViews &bw, const PcgLayout &L, int ctas, int slot, int maxiter,
+                                    int mode, cudaStream_t s) {
+    return launch_factor_args(bv, vv, pw, bw, L, ctas, slot, ir.inner_tol, maxiter, mode, ir.res, ir.e, &ir, s);
 }
 
 }  // namespace mfem

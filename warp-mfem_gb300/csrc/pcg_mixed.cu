@@ -26,6 +26,12 @@
 //                       to finish adds the partials in a fixed order and
 //                       decides (converged / outer cap)
 //   ir_pcg_kernel<T>    persistent cooperative PCG on Hq e = r, e0 = 0
+//
+// A plan on the persistent factor PCG (pcg_factor.cu) runs the inner solves
+// there instead: ir_convert_kernel also writes Hq back as fp32 (each 16-bit
+// value times its row scale, the values ir_pcg_kernel multiplies with), and
+// the residual kernel hands over r / ||r|| (so the fp32 sums of products
+// cannot underflow) with ||r|| to scale the correction back.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -74,7 +80,11 @@ __global__ void ir_convert_kernel(BsrViews bv, IrWork w) {
     T *q = reinterpret_cast<T *>(w.lowp);
     for (int k = kb + lane; k < ke; k += 32)
 #pragma unroll
-        for (int i = 0; i < 9; ++i) q[(size_t)9 * k + i] = to_lowp<T>(bv.values[(size_t)9 * k + i] * inv);
+        for (int i = 0; i < 9; ++i) {
+            const T v = to_lowp<T>(bv.values[(size_t)9 * k + i] * inv);
+            q[(size_t)9 * k + i] = v;
+            if (w.hq) w.hq[(size_t)9 * k + i] = from_lowp(v) * s;  // what the 16-bit product computes
+        }
 }
 
 __global__ void ir_begin_kernel(VertexViews vv, IrWork w) {
@@ -178,6 +188,13 @@ __global__ void __launch_bounds__(kResThreads)
             tgg += __ldcg(w.res_partials + 2 * b + 1);
         }
         const double rel = tgg > 0.0 ? sqrt(trr / tgg) : sqrt(trr);
+        // the scale of the next inner right-hand side (unit norm: fp32 sums
+        // of products of a tiny residual's entries would underflow)
+        const double rn = sqrt(trr);
+        const float inv = (float)(1.0 / rn);
+        const bool scaled = rn > 0.0 && isfinite(rn) && isfinite(inv);
+        w.scale[0] = scaled ? inv : 1.0f;
+        w.scale[1] = scaled ? (float)rn : 1.0f;
         const int outer = w.state[1];
         int status = MFEM_OK;
         int done = 0;
@@ -636,7 +653,8 @@ cudaError_t ir_max_ctas(int device, int *ctas) {
 int ir_residual_blocks(int n) { return std::max(1, blocks_for(n * kIrGroup, kResThreads)); }
 
 cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const IrWork &w, const PcgWork &pw,
-                               const BatchViews &fb, int slot, int maxiter, int use_precond, cudaStream_t s) {
+                               const BatchViews &fb, const PcgLayout &pl, int pcg_ctas, int slot, int maxiter,
+                               int use_precond, cudaStream_t s) {
     if (bv.n == 0) return cudaSuccess;
     const bool bf16 = w.mode == kIrBf16;
     cudaError_t e;
@@ -651,7 +669,9 @@ cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const 
         ir_residual_kernel<<<rb, kResThreads, 0, s>>>(bv, vv, w, pw, slot);
         count_launches(1);
         e = cudaGetLastError();
-        if (e == cudaSuccess)
+        if (e == cudaSuccess && w.hq)
+            e = launch_pcg_factor_inner(bv, vv, w, pw, fb, pl, pcg_ctas, slot, maxiter, use_precond, s);
+        else if (e == cudaSuccess)
             e = bf16 ? launch_ir_pcg<__nv_bfloat16>(bv, vv, w, fb, pw.error, maxiter, use_precond, s)
                      : launch_ir_pcg<__half>(bv, vv, w, fb, pw.error, maxiter, use_precond, s);
     }
