@@ -689,11 +689,17 @@ def run_gb300(args, rank, world, local_rank):
     achieved = pcg_bytes / (stage_ms["pcg"] / 1000.0) / 1e9
     peak, peak_src = hbm_peak()
     per_launch_iters = (prof_iters + prof_solves) / prof_solves
-    traffic = ncu_traffic_per_launch()
+    # DRAM bytes of one captured launch of this workload's PCG (committed ncu summaries)
+    summary, note = {
+        "nh_beam": ("pcg_kernel_nh_beam.md", "about 378 iterations"),
+        "stiff_beam": ("pcg_standard_kernel_stiff_beam.md",
+                       "about 950 iterations; H stays in the 129 MB L2 across iterations"),
+    }.get(args.workload, (None, None))
+    traffic = ncu_traffic_per_launch(summary) if summary else None
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
         "traffic": traffic,
-        "traffic_note": "DRAM bytes of one captured launch (about 378 iterations), profiles/pcg_kernel_nh_beam.md",
+        "traffic_note": f"DRAM bytes of one captured launch ({note}), profiles/{summary}" if summary else None,
         "kernel": "pcg_kernel (persistent cooperative block-Jacobi PCG)",
         "algorithmic_bytes_per_launch": b_it * per_launch_iters,
         "bytes_per_pcg_iteration": b_it, "pcg_iterations_per_launch": per_launch_iters - 1,

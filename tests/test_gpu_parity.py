@@ -308,3 +308,31 @@ def test_pcg_variants_agree(name, cells, steps):
             s0, s1 = s1, s0
         outs[variant] = s0.particle_q.cpu().numpy()
     close(outs["single_reduction"], outs["standard"], 1e-5)
+
+
+@pytest.mark.parametrize("variant", ["standard", "single_reduction"])
+def test_uncached_matrix_product_agrees(variant):
+    """nh_beam on 16 CTAs: a CTA's slice of H (about 16k blocks) does not fit
+    in shared memory, so the product reads H's blocks from global memory;
+    one solve agrees with the default plan's (H in shared memory)."""
+    mesh = beams.build_beam("nh_beam")
+    out = {}
+    for key, kw in (("uncached", dict(pcg_variant=variant, pcg_ctas=16)), ("default", {})):
+        model = Model.from_beam(mesh, device=DEV)
+        solver = MixedFEMSolver(model, iterations=1, energy=mesh.spec.energy, line_search=False, **kw)
+        lay = solver.pcg_layout()
+        if key == "uncached":
+            assert lay["variant"] == variant and not lay["cache_matrix"], lay
+        q = t(mesh.q0)
+        x = q.clone()
+        solver.predict(q, torch.zeros_like(q), mesh.spec.dt)
+        solver.update_system(x)
+        solver.assemble(x, mesh.spec.dt)
+        solver.global_solve(0)
+        torch.cuda.synchronize()
+        st = solver.solve_stats()[0]
+        assert st["status"] == 0 and st["iterations"] > 0, (key, st)
+        out[key] = (st["iterations"], solver.read_buffer("dx").cpu().numpy().astype(np.float64))
+    (ia, da), (ib, db) = out["uncached"], out["default"]
+    assert abs(ia - ib) <= max(2, ib // 50), (ia, ib)
+    close(da, db, 1e-4)

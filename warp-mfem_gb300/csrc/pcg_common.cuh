@@ -201,6 +201,26 @@ __device__ bool tma_wait(uint64_t *mbar, uint32_t &parity, int *error) {
     return ok;
 }
 
+// Block k of H (nine floats; blocks are 36 bytes, so an even k starts on an
+// 8-byte boundary and an odd k 4 bytes past one) in four 8-byte loads and
+// one 4-byte load instead of nine.
+__device__ __forceinline__ void load_block9(const float *values, long long k, float m[9]) {
+    const bool odd = (k & 1) != 0;
+    const float *h = values + 9 * k;
+    const float2 *b2 = reinterpret_cast<const float2 *>(h + (odd ? 1 : 0));
+    const float2 p0 = __ldg(b2), p1 = __ldg(b2 + 1), p2 = __ldg(b2 + 2), p3 = __ldg(b2 + 3);
+    const float t = __ldg(odd ? h : h + 8);
+    m[0] = odd ? t : p0.x;
+    m[1] = odd ? p0.x : p0.y;
+    m[2] = odd ? p0.y : p1.x;
+    m[3] = odd ? p1.x : p1.y;
+    m[4] = odd ? p1.y : p2.x;
+    m[5] = odd ? p2.x : p2.y;
+    m[6] = odd ? p2.y : p3.x;
+    m[7] = odd ? p3.x : p3.y;
+    m[8] = odd ? p3.y : t;
+}
+
 // out[i] = sum_k H[k] win[col_k] over the CTA's rows, kGroup lanes per row;
 // H's blocks from the shared-memory slice (CACHE) or from `values`.
 template <bool CACHE>
@@ -216,19 +236,22 @@ __device__ __forceinline__ void window_product(const PcgArgs &a, const int *rowo
         float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
 #pragma unroll 4
         for (int k = kb + g_lane; k < ke; k += kGroup) {
-            const float *h;
-            int c;
-            if (CACHE) {
-                h = sH + (size_t)k * 9;
-                c = sCol[k];
+            if constexpr (CACHE) {
+                const float *h = sH + (size_t)k * 9;
+                const int c = sCol[k];
+                const float v0 = win[3 * c + 0], v1 = win[3 * c + 1], v2 = win[3 * c + 2];
+                a0 += h[0] * v0 + h[1] * v1 + h[2] * v2;
+                a1 += h[3] * v0 + h[4] * v1 + h[5] * v2;
+                a2 += h[6] * v0 + h[7] * v1 + h[8] * v2;
             } else {
-                h = values + (size_t)(blk_lo + k) * 9;
-                c = __ldg(a.col_idx + blk_lo + k) - win_lo;
+                float h[9];
+                load_block9(values, (long long)blk_lo + k, h);
+                const int c = __ldg(a.col_idx + blk_lo + k) - win_lo;
+                const float v0 = win[3 * c + 0], v1 = win[3 * c + 1], v2 = win[3 * c + 2];
+                a0 += h[0] * v0 + h[1] * v1 + h[2] * v2;
+                a1 += h[3] * v0 + h[4] * v1 + h[5] * v2;
+                a2 += h[6] * v0 + h[7] * v1 + h[8] * v2;
             }
-            const float v0 = win[3 * c + 0], v1 = win[3 * c + 1], v2 = win[3 * c + 2];
-            a0 += h[0] * v0 + h[1] * v1 + h[2] * v2;
-            a1 += h[3] * v0 + h[4] * v1 + h[5] * v2;
-            a2 += h[6] * v0 + h[7] * v1 + h[8] * v2;
         }
 #pragma unroll
         for (int off = kGroup / 2; off > 0; off >>= 1) {

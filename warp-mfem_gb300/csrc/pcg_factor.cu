@@ -43,16 +43,33 @@ __device__ __forceinline__ void proxy_fence_smem() { asm volatile("fence.proxy.a
 constexpr int kFactorNone = 0, kFactorRows = 1, kFactorAll = 2;
 
 // A 3x3 block from its five words of BF16 pairs (the tenth value is padding).
+// Through L2 in three loads: blocks are 20 bytes, so block k starts on an
+// 8-byte boundary for even k and 4 bytes past one for odd k.
 template <bool SHARED>
-__device__ __forceinline__ void block_words(const uint32_t *w, float f[9]) {
+__device__ __forceinline__ void block_words(const uint32_t *words, long long k, float f[9]) {
+    const uint32_t *w = words + 5 * k;
+    uint32_t u[5];
+    if (SHARED) {
+#pragma unroll
+        for (int i = 0; i < 5; ++i) u[i] = w[i];
+    } else {
+        const bool odd = (k & 1) != 0;
+        const uint2 *b2 = reinterpret_cast<const uint2 *>(w + (odd ? 1 : 0));
+        const uint2 q0 = __ldg(b2), q1 = __ldg(b2 + 1);
+        const uint32_t t = __ldg(odd ? w : w + 4);
+        u[0] = odd ? t : q0.x;
+        u[1] = odd ? q0.x : q0.y;
+        u[2] = odd ? q0.y : q1.x;
+        u[3] = odd ? q1.x : q1.y;
+        u[4] = odd ? q1.y : t;
+    }
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
-        const uint32_t u = SHARED ? w[i] : __ldg(w + i);
         __nv_bfloat162 b;
-        memcpy(&b, &u, 4);
-        const float2 t = __bfloat1622float2(b);
-        f[2 * i] = t.x;
-        if (2 * i + 1 < 9) f[2 * i + 1] = t.y;
+        memcpy(&b, &u[i], 4);
+        const float2 t2 = __bfloat1622float2(b);
+        f[2 * i] = t2.x;
+        if (2 * i + 1 < 9) f[2 * i + 1] = t2.y;
     }
 }
 
@@ -86,8 +103,8 @@ __device__ __forceinline__ void factor_row(const FactorRows &f, const float *in,
         float w0 = in[3 * c2], w1 = in[3 * c2 + 1], w2 = in[3 * c2 + 2];
         if (!two) w0 = w1 = w2 = 0.0f;
         float m[9], m2[9];
-        block_words<SH>(f.words + (size_t)5 * k, m);
-        block_words<SH>(f.words + (size_t)5 * kk2, m2);
+        block_words<SH>(f.words, k, m);
+        block_words<SH>(f.words, kk2, m2);
         a0 += m[0] * v0 + m[1] * v1 + m[2] * v2;
         a1 += m[3] * v0 + m[4] * v1 + m[5] * v2;
         a2 += m[6] * v0 + m[7] * v1 + m[8] * v2;
@@ -132,7 +149,7 @@ __device__ __forceinline__ void factor_row_pair(const FactorRows &f, const float
         for (int u = 0; u < 4; ++u) {
             const int kk = ok[u] ? k[u] : kba;  // every row holds its diagonal block
             c[u] = (SH ? f.col[kk] : __ldg(f.col + kk)) - f.in_lo;
-            block_words<SH>(f.words + (size_t)5 * kk, m[u]);
+            block_words<SH>(f.words, kk, m[u]);
         }
         float v[4][3];
 #pragma unroll
