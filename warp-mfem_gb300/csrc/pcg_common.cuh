@@ -231,38 +231,80 @@ __device__ __forceinline__ void window_product(const PcgArgs &a, const int *rowo
     const int group = threadIdx.x / kGroup;
     const int ngroups = blockDim.x / kGroup;
     const unsigned gmask = ((1u << kGroup) - 1u) << (threadIdx.x & (32 - kGroup));
-    for (int i = group; i < nrows; i += ngroups) {
-        const int kb = rowoff[i], ke = rowoff[i + 1];
-        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+    if constexpr (!CACHE) {
+        // H through L2: a group takes rows i and i + ngroups together, so
+        // each lane has both rows' loads in flight; each row's sum runs in
+        // the single-row order
+        for (int i = group; i < nrows; i += 2 * ngroups) {
+            const int ib = i + ngroups;
+            const bool has_b = ib < nrows;
+            const int kba = rowoff[i], kea = rowoff[i + 1];
+            const int kbb = has_b ? rowoff[ib] : kba, keb = has_b ? rowoff[ib + 1] : kba;
+            float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, b0 = 0.0f, b1 = 0.0f, b2 = 0.0f;
+#pragma unroll 2
+            for (int t = g_lane; kba + t < kea || kbb + t < keb; t += kGroup) {
+                const bool oka = kba + t < kea, okb = kbb + t < keb;
+                const int ka = oka ? kba + t : kba, kq = okb ? kbb + t : kba;  // in-range stand-ins
+                float ha[9], hb[9];
+                load_block9(values, (long long)blk_lo + ka, ha);
+                load_block9(values, (long long)blk_lo + kq, hb);
+                const int ca = __ldg(a.col_idx + blk_lo + ka) - win_lo;
+                const int cb = __ldg(a.col_idx + blk_lo + kq) - win_lo;
+                const float u0 = oka ? win[3 * ca] : 0.0f, u1 = oka ? win[3 * ca + 1] : 0.0f,
+                            u2 = oka ? win[3 * ca + 2] : 0.0f;
+                const float w0 = okb ? win[3 * cb] : 0.0f, w1 = okb ? win[3 * cb + 1] : 0.0f,
+                            w2 = okb ? win[3 * cb + 2] : 0.0f;
+                a0 += ha[0] * u0 + ha[1] * u1 + ha[2] * u2;
+                a1 += ha[3] * u0 + ha[4] * u1 + ha[5] * u2;
+                a2 += ha[6] * u0 + ha[7] * u1 + ha[8] * u2;
+                b0 += hb[0] * w0 + hb[1] * w1 + hb[2] * w2;
+                b1 += hb[3] * w0 + hb[4] * w1 + hb[5] * w2;
+                b2 += hb[6] * w0 + hb[7] * w1 + hb[8] * w2;
+            }
+#pragma unroll
+            for (int off = kGroup / 2; off > 0; off >>= 1) {
+                a0 += __shfl_xor_sync(gmask, a0, off);
+                a1 += __shfl_xor_sync(gmask, a1, off);
+                a2 += __shfl_xor_sync(gmask, a2, off);
+                b0 += __shfl_xor_sync(gmask, b0, off);
+                b1 += __shfl_xor_sync(gmask, b1, off);
+                b2 += __shfl_xor_sync(gmask, b2, off);
+            }
+            if (g_lane == 0) {
+                out[3 * i + 0] = a0;
+                out[3 * i + 1] = a1;
+                out[3 * i + 2] = a2;
+                if (has_b) {
+                    out[3 * ib + 0] = b0;
+                    out[3 * ib + 1] = b1;
+                    out[3 * ib + 2] = b2;
+                }
+            }
+        }
+    } else {
+        for (int i = group; i < nrows; i += ngroups) {
+            const int kb = rowoff[i], ke = rowoff[i + 1];
+            float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
 #pragma unroll 4
-        for (int k = kb + g_lane; k < ke; k += kGroup) {
-            if constexpr (CACHE) {
+            for (int k = kb + g_lane; k < ke; k += kGroup) {
                 const float *h = sH + (size_t)k * 9;
                 const int c = sCol[k];
                 const float v0 = win[3 * c + 0], v1 = win[3 * c + 1], v2 = win[3 * c + 2];
                 a0 += h[0] * v0 + h[1] * v1 + h[2] * v2;
                 a1 += h[3] * v0 + h[4] * v1 + h[5] * v2;
                 a2 += h[6] * v0 + h[7] * v1 + h[8] * v2;
-            } else {
-                float h[9];
-                load_block9(values, (long long)blk_lo + k, h);
-                const int c = __ldg(a.col_idx + blk_lo + k) - win_lo;
-                const float v0 = win[3 * c + 0], v1 = win[3 * c + 1], v2 = win[3 * c + 2];
-                a0 += h[0] * v0 + h[1] * v1 + h[2] * v2;
-                a1 += h[3] * v0 + h[4] * v1 + h[5] * v2;
-                a2 += h[6] * v0 + h[7] * v1 + h[8] * v2;
             }
-        }
 #pragma unroll
-        for (int off = kGroup / 2; off > 0; off >>= 1) {
-            a0 += __shfl_xor_sync(gmask, a0, off);
-            a1 += __shfl_xor_sync(gmask, a1, off);
-            a2 += __shfl_xor_sync(gmask, a2, off);
-        }
-        if (g_lane == 0) {
-            out[3 * i + 0] = a0;
-            out[3 * i + 1] = a1;
-            out[3 * i + 2] = a2;
+            for (int off = kGroup / 2; off > 0; off >>= 1) {
+                a0 += __shfl_xor_sync(gmask, a0, off);
+                a1 += __shfl_xor_sync(gmask, a1, off);
+                a2 += __shfl_xor_sync(gmask, a2, off);
+            }
+            if (g_lane == 0) {
+                out[3 * i + 0] = a0;
+                out[3 * i + 1] = a1;
+                out[3 * i + 2] = a2;
+            }
         }
     }
 }
