@@ -8,22 +8,16 @@
 
 #include <cstring>
 
+#include "block_loads.cuh"
 #include "internal.h"
 
 namespace mfem {
 
 // the 3x3 block k of a BF16 factor form (kFactorLd values per block)
 __device__ __forceinline__ void factor_block(const __nv_bfloat16 *val, int k, float f[9]) {
-    const uint32_t *w = reinterpret_cast<const uint32_t *>(val + (size_t)kFactorLd * k);
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-        const uint32_t u = __ldg(w + i);
-        __nv_bfloat162 b;
-        memcpy(&b, &u, 4);
-        const float2 t = __bfloat1622float2(b);
-        f[2 * i] = t.x;
-        if (2 * i + 1 < 9) f[2 * i + 1] = t.y;
-    }
+    uint32_t u[5];
+    load_bf16_words(reinterpret_cast<const uint32_t *>(val), k, u);
+    bf16_words_to_block(u, f);
 }
 
 template <bool LOCAL, int GROUP>

@@ -20,6 +20,7 @@
 // a given schedule.  Every wait is bounded.
 #include <algorithm>
 
+#include "block_loads.cuh"
 #include "factor_apply.cuh"
 #include "internal.h"
 
@@ -155,14 +156,15 @@ __device__ __forceinline__ void bt_row_product(const BsrViews &bv, int row, cons
             v2[q] = p_old ? __fmaf_rn(beta, bt_ld<SHARED>(p_old + 3 * c2 + q), zc2) : zc2;
         }
         if (!two) v2[0] = v2[1] = v2[2] = 0.0f;
-        const float *h = bv.values + (size_t)9 * k;
-        const float *h2 = bv.values + (size_t)9 * (two ? k2 : k);
-        a0 += __ldg(h + 0) * v[0] + __ldg(h + 1) * v[1] + __ldg(h + 2) * v[2];
-        a1 += __ldg(h + 3) * v[0] + __ldg(h + 4) * v[1] + __ldg(h + 5) * v[2];
-        a2 += __ldg(h + 6) * v[0] + __ldg(h + 7) * v[1] + __ldg(h + 8) * v[2];
-        a0 += __ldg(h2 + 0) * v2[0] + __ldg(h2 + 1) * v2[1] + __ldg(h2 + 2) * v2[2];
-        a1 += __ldg(h2 + 3) * v2[0] + __ldg(h2 + 4) * v2[1] + __ldg(h2 + 5) * v2[2];
-        a2 += __ldg(h2 + 6) * v2[0] + __ldg(h2 + 7) * v2[1] + __ldg(h2 + 8) * v2[2];
+        float h[9], h2[9];
+        load_block9(bv.values, k, h);
+        load_block9(bv.values, two ? k2 : k, h2);
+        a0 += h[0] * v[0] + h[1] * v[1] + h[2] * v[2];
+        a1 += h[3] * v[0] + h[4] * v[1] + h[5] * v[2];
+        a2 += h[6] * v[0] + h[7] * v[1] + h[8] * v[2];
+        a0 += h2[0] * v2[0] + h2[1] * v2[1] + h2[2] * v2[2];
+        a1 += h2[3] * v2[0] + h2[4] * v2[1] + h2[5] * v2[2];
+        a2 += h2[6] * v2[0] + h2[7] * v2[1] + h2[8] * v2[2];
     }
 #pragma unroll
     for (int off = kBtGroup / 2; off > 0; off >>= 1) {

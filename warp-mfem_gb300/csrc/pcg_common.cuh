@@ -5,6 +5,7 @@
 // instantiates its own copy.
 #pragma once
 
+#include "block_loads.cuh"
 #include "internal.h"
 
 namespace mfem {
@@ -199,26 +200,6 @@ __device__ bool tma_wait(uint64_t *mbar, uint32_t &parity, int *error) {
     if (!ok && threadIdx.x == 0) atomicExch(error, 1);
     parity ^= 1u;
     return ok;
-}
-
-// Block k of H (nine floats; blocks are 36 bytes, so an even k starts on an
-// 8-byte boundary and an odd k 4 bytes past one) in four 8-byte loads and
-// one 4-byte load instead of nine.
-__device__ __forceinline__ void load_block9(const float *values, long long k, float m[9]) {
-    const bool odd = (k & 1) != 0;
-    const float *h = values + 9 * k;
-    const float2 *b2 = reinterpret_cast<const float2 *>(h + (odd ? 1 : 0));
-    const float2 p0 = __ldg(b2), p1 = __ldg(b2 + 1), p2 = __ldg(b2 + 2), p3 = __ldg(b2 + 3);
-    const float t = __ldg(odd ? h : h + 8);
-    m[0] = odd ? t : p0.x;
-    m[1] = odd ? p0.x : p0.y;
-    m[2] = odd ? p0.y : p1.x;
-    m[3] = odd ? p1.x : p1.y;
-    m[4] = odd ? p1.y : p2.x;
-    m[5] = odd ? p2.x : p2.y;
-    m[6] = odd ? p2.y : p3.x;
-    m[7] = odd ? p3.x : p3.y;
-    m[8] = odd ? p3.y : t;
 }
 
 // out[i] = sum_k H[k] win[col_k] over the CTA's rows, kGroup lanes per row;

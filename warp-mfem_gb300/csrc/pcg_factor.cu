@@ -42,35 +42,18 @@ __device__ __forceinline__ void proxy_fence_smem() { asm volatile("fence.proxy.a
 // pointers (absolute block indices), or row pointers, columns and blocks.
 constexpr int kFactorNone = 0, kFactorRows = 1, kFactorAll = 2;
 
-// A 3x3 block from its five words of BF16 pairs (the tenth value is padding).
-// Through L2 in three loads: blocks are 20 bytes, so block k starts on an
-// 8-byte boundary for even k and 4 bytes past one for odd k.
+// A 3x3 block from its five words of BF16 pairs (the tenth value is padding):
+// from the shared-memory copy, or through L2 in three loads.
 template <bool SHARED>
 __device__ __forceinline__ void block_words(const uint32_t *words, long long k, float f[9]) {
-    const uint32_t *w = words + 5 * k;
     uint32_t u[5];
     if (SHARED) {
 #pragma unroll
-        for (int i = 0; i < 5; ++i) u[i] = w[i];
+        for (int i = 0; i < 5; ++i) u[i] = words[5 * k + i];
     } else {
-        const bool odd = (k & 1) != 0;
-        const uint2 *b2 = reinterpret_cast<const uint2 *>(w + (odd ? 1 : 0));
-        const uint2 q0 = __ldg(b2), q1 = __ldg(b2 + 1);
-        const uint32_t t = __ldg(odd ? w : w + 4);
-        u[0] = odd ? t : q0.x;
-        u[1] = odd ? q0.x : q0.y;
-        u[2] = odd ? q0.y : q1.x;
-        u[3] = odd ? q1.x : q1.y;
-        u[4] = odd ? q1.y : t;
+        load_bf16_words(words, k, u);
     }
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-        __nv_bfloat162 b;
-        memcpy(&b, &u[i], 4);
-        const float2 t2 = __bfloat1622float2(b);
-        f[2 * i] = t2.x;
-        if (2 * i + 1 < 9) f[2 * i + 1] = t2.y;
-    }
+    bf16_words_to_block(u, f);
 }
 
 // The factor rows a CTA applies (FC: kFactorNone, kFactorRows or
