@@ -60,9 +60,13 @@ def one_solve(mesh, solver):
     return H, g, dx64, dx32
 
 
+@pytest.mark.parametrize("variant", ["auto", "global_memory"])
 @pytest.mark.parametrize("precision", ["fp16", "bf16"])
-def test_mixed_solve_reaches_fp64_tolerance(precision):
-    mesh, _, solver = make("nh_beam", (16, 4, 4), precision)
+def test_mixed_solve_reaches_fp64_tolerance(precision, variant):
+    """Block-Jacobi inner solves in the persistent factor PCG (the default
+    plan keeps a block-Jacobi layout of it for them) or in the global-memory
+    inner PCG."""
+    mesh, _, solver = make("nh_beam", (16, 4, 4), precision, pcg_variant=variant)
     H, g, dx64, dx32 = one_solve(mesh, solver)
     rel = np.linalg.norm(g - H @ dx64) / np.linalg.norm(g)
     st = solver.mixed_stats()[0]
@@ -174,7 +178,8 @@ def test_mixed_with_factor_preconditioner(pc, variant):
         close(A.particle_q.cpu().numpy(), q, 1e-5)
 
 
-@pytest.mark.parametrize("pc,variant", [("block_jacobi", "auto"), ("fsai", "global_memory"), ("fsai", "factor")])
+@pytest.mark.parametrize("pc,variant", [("block_jacobi", "auto"), ("block_jacobi", "global_memory"),
+                                        ("fsai", "global_memory"), ("fsai", "factor")])
 def test_tiny_residual_does_not_underflow(pc, variant):
     """A right-hand side of 1e-25 scale (late, nearly converged Newton
     iterations): fp32 sums of products of its entries would underflow. The

@@ -46,6 +46,9 @@ struct mfem_plan {
     BsrViews bv{};
     PcgWork pw{};
     PcgLayout pl{};
+    // block-Jacobi plans: the persistent factor PCG's layout (block-Jacobi
+    // only) for the inner solves of the mixed refinement, when it fits
+    PcgLayout ir_pl{};
     LineSearchWork ls{};
     float stage_dt = 0.0f;     // dt of the last mfem_assemble (the line search's 1/dt^2)
     int stage_slot = 0;        // slot of the last mfem_global_solve
@@ -205,7 +208,8 @@ bool net_ready(const mfem_plan *p) { return p->cfg.preconditioner != 3 || p->fv.
 // The reference's float32 PCG, or the mixed-precision iterative refinement.
 cudaError_t global_solve(mfem_plan *p, int slot, cudaStream_t s) {
     if (p->ir.mode != 0)
-        return launch_mixed_solve(p->bv, p->vv, p->ir, p->pw, p->bw, p->pl, p->pcg_ctas, slot,
+        return launch_mixed_solve(p->bv, p->vv, p->ir, p->pw, p->bw,
+                                  p->pl.variant == PcgLayout::kFactor ? p->pl : p->ir_pl, p->pcg_ctas, slot,
                                   p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
     if (p->pl.variant == PcgLayout::kFactor)
         return launch_pcg_factor(p->bv, p->vv, p->pw, p->bw, p->pl, p->pcg_ctas, slot, p->cfg.cg_tolerance,
@@ -593,6 +597,19 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
             cta_info.assign(1, make_int4(0, 0, 0, 0));
         }
     }
+    std::vector<int4> ir_cta, ir_fcta;
+    if (e == cudaSuccess && !p->global_memory_pcg && cfg.preconditioner == 1) {
+        std::string lerr;
+        PcgLayout il{};
+        if (pcg_factor_layout(device, il, sym.row_ptr.data(), sym.col_idx.data(), n, p->pcg_ctas, 2, ir_cta, ir_fcta,
+                              lerr, false) == cudaSuccess) {
+            p->ir_pl = il;
+        } else {
+            cudaGetLastError();
+            ir_cta.clear();
+            ir_fcta.clear();
+        }
+    }
     int4 *d_cta = nullptr;
     if (e == cudaSuccess) e = dev_alloc(p, &d_cta, cta_info.size());
     if (e == cudaSuccess) e = upload(d_cta, cta_info.data(), cta_info.size());
@@ -602,6 +619,15 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
         e = dev_alloc(p, &d_fcta, factor_info.size());
         if (e == cudaSuccess) e = upload(d_fcta, factor_info.data(), factor_info.size());
         p->pl.factor_info = d_fcta;
+    }
+    if (e == cudaSuccess && p->ir_pl.variant == PcgLayout::kFactor) {
+        int4 *d_icta = nullptr, *d_ifcta = nullptr;
+        e = dev_alloc(p, &d_icta, ir_cta.size());
+        if (e == cudaSuccess) e = upload(d_icta, ir_cta.data(), ir_cta.size());
+        if (e == cudaSuccess) e = dev_alloc(p, &d_ifcta, ir_fcta.size());
+        if (e == cudaSuccess) e = upload(d_ifcta, ir_fcta.data(), ir_fcta.size());
+        p->ir_pl.cta_info = d_icta;
+        p->ir_pl.factor_info = d_ifcta;
     }
     if (e == cudaSuccess) e = upload(tets, reinterpret_cast<const int4 *>(h_tets), nT);
     if (e == cudaSuccess) e = upload(dminv, h_poses, nT * 9);
@@ -1121,7 +1147,9 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
     alloc(&w.scale, 2 * sizeof(float));
     // a plan on the persistent factor PCG runs its inner solves there, on an
     // fp32 copy of the 16-bit blocks (the same rounding)
-    if (p->pl.variant == PcgLayout::kFactor) alloc(&w.hq, nz * 9 * sizeof(float));
+    if ((p->pl.variant == PcgLayout::kFactor || p->ir_pl.variant == PcgLayout::kFactor) &&
+        p->cfg.preconditioner >= 1)
+        alloc(&w.hq, nz * 9 * sizeof(float));
     int max_ctas = 1;
     if (e == cudaSuccess) e = ir_max_ctas(p->device, &max_ctas);
     if (e == cudaSuccess) e = cudaMemset(w.counter, 0, sizeof(unsigned long long));

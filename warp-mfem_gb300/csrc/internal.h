@@ -335,10 +335,12 @@ cudaError_t pcg_plan_layout(int device, PcgLayout &L, const int32_t *row_ptr, co
                             int ctas, int variant, std::vector<int4> &cta_info, std::string &err);
 // The persistent PCG with a factor preconditioner (mode 2: M = F^T F, 3: M =
 // F F^T; the factor in bw's lower / upper CSR).  The layout fails (err set)
-// when a CTA's rows and ranges do not fit in shared memory.
+// when a CTA's rows and ranges do not fit in shared memory.  factor = false
+// plans it for block-Jacobi inner solves of the mixed refinement only (no
+// factor rows in shared memory; mode 2's ranges).
 cudaError_t pcg_factor_layout(int device, PcgLayout &L, const int32_t *row_ptr, const int32_t *col_idx, int n,
                               int ctas, int mode, std::vector<int4> &cta_info, std::vector<int4> &factor_info,
-                              std::string &err);
+                              std::string &err, bool factor = true);
 cudaError_t launch_pcg_factor(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const BatchViews &bw,
                               const PcgLayout &L, int ctas, int slot, float tol, int maxiter, int mode,
                               cudaStream_t s);

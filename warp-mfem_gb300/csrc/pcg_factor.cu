@@ -587,19 +587,21 @@ size_t smem_factor(const PcgLayout &L, bool cache, int fc) {
 typedef void (*FactorKernel)(PcgArgs);
 
 FactorKernel pick_factor_kernel(const PcgLayout &L) {
-    if (L.cache_matrix)
-        return L.factor_cache == kFactorAll ? pcg_factor_kernel<true, kFactorAll>
-                                            : pcg_factor_kernel<true, kFactorRows>;
+    if (L.cache_matrix) {
+        if (L.factor_cache == kFactorAll) return pcg_factor_kernel<true, kFactorAll>;
+        if (L.factor_cache == kFactorRows) return pcg_factor_kernel<true, kFactorRows>;
+        return pcg_factor_kernel<true, kFactorNone>;
+    }
     if (L.factor_cache == kFactorAll) return pcg_factor_kernel<false, kFactorAll>;
-    return L.factor_cache == kFactorRows ? pcg_factor_kernel<false, kFactorRows>
-                                         : pcg_factor_kernel<false, kFactorNone>;
+    if (L.factor_cache == kFactorRows) return pcg_factor_kernel<false, kFactorRows>;
+    return pcg_factor_kernel<false, kFactorNone>;
 }
 
 }  // namespace
 
 cudaError_t pcg_factor_layout(int device, PcgLayout &L, const int32_t *row_ptr, const int32_t *col_idx, int n,
                               int ctas, int mode, std::vector<int4> &cta_info, std::vector<int4> &factor_info,
-                              std::string &err) {
+                              std::string &err, bool factor) {
     int optin = 0;
     cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     if (e != cudaSuccess) return e;
@@ -690,7 +692,9 @@ cudaError_t pcg_factor_layout(int device, PcgLayout &L, const int32_t *row_ptr, 
     // product (one trip); the factor's row pointers (a few KB) take one
     // dependent load off every trip
     const int opts[5][2] = {{1, kFactorAll}, {0, kFactorAll}, {1, kFactorRows}, {0, kFactorRows}, {0, kFactorNone}};
+    const int plain[2][2] = {{1, kFactorNone}, {0, kFactorNone}};  // block-Jacobi only: no factor rows
     for (const auto &o : opts) {
+        if (!factor) break;
         const size_t bytes = smem_factor(L, o[0] != 0, o[1]);
         if (bytes <= budget) {
             L.cache_matrix = o[0];
@@ -699,6 +703,14 @@ cudaError_t pcg_factor_layout(int device, PcgLayout &L, const int32_t *row_ptr, 
             return cudaFuncSetAttribute(pick_factor_kernel(L), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)L.smem);
         }
+    }
+    for (const auto &o : plain) {
+        const size_t bytes = smem_factor(L, o[0] != 0, o[1]);
+        if (factor || bytes > budget) continue;
+        L.cache_matrix = o[0];
+        L.factor_cache = o[1];
+        L.smem = bytes;
+        return cudaFuncSetAttribute(pick_factor_kernel(L), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
     }
     err = "mesh too large for the persistent factor PCG (shared memory per CTA exceeded)";
     return cudaErrorInvalidValue;
@@ -709,7 +721,8 @@ namespace {
 cudaError_t launch_factor_args(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const BatchViews &bw,
                                const PcgLayout &L, int ctas, int slot, float tol, int maxiter, int mode,
                                const float *b, float *x, const IrWork *ir, cudaStream_t s) {
-    if (mode != 2 && mode != 3) return cudaErrorInvalidValue;
+    // 1 (block-Jacobi) only as an inner solve of a plan without a factor
+    if (mode != 2 && mode != 3 && !(ir && mode == 1)) return cudaErrorInvalidValue;
     PcgArgs a = {};
     a.n = bv.n;
     a.row_ptr = bv.row_ptr;

@@ -669,7 +669,7 @@ cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const 
         ir_residual_kernel<<<rb, kResThreads, 0, s>>>(bv, vv, w, pw, slot);
         count_launches(1);
         e = cudaGetLastError();
-        if (e == cudaSuccess && w.hq)
+        if (e == cudaSuccess && w.hq && pl.variant == PcgLayout::kFactor)
             e = launch_pcg_factor_inner(bv, vv, w, pw, fb, pl, pcg_ctas, slot, maxiter, use_precond, s);
         else if (e == cudaSuccess)
             e = bf16 ? launch_ir_pcg<__nv_bfloat16>(bv, vv, w, fb, pw.error, maxiter, use_precond, s)
