@@ -301,14 +301,17 @@ int mfem_set_body_poses(mfem_plan *plan, const float *body_q, int32_t n_bodies, 
 
 void mfem_solver_config_default(mfem_solver_config *cfg);
 
-/* Selects the global solve: the reference's float32 block-Jacobi PCG
- * (precision FP32, the default) or the mixed-precision iterative refinement
- * (BF16 / FP16 blocks, fp32 inner PCG to inner_tolerance with the fp32
- * block-Jacobi inverse, fp64 residual; stops at outer_tolerance or after
- * outer_max_iterations corrections, starting from the reference's warm
- * start).  It has no reference counterpart: it is the mixed-precision variant
- * of src/mfem/refinement/solver.py:581-609.  Synchronises the device and
- * drops the plan's captured graphs. */
+/* Selects the global solve: the reference's float32 PCG (precision FP32,
+ * the default) or the mixed-precision iterative refinement (BF16 / FP16
+ * blocks, fp32 inner PCG to inner_tolerance with the plan's preconditioner,
+ * fp64 residual; stops at outer_tolerance or after outer_max_iterations
+ * corrections, starting from the reference's warm start).  Where the plan
+ * has a persistent factor PCG layout (pcg_variant 4, or the block-Jacobi one
+ * a one-mesh plan keeps when it fits) the inner solves run there, on an fp32
+ * copy of the 16-bit blocks, for the residual scaled to unit norm; else in
+ * the global-memory inner PCG.  It has no reference counterpart: it is the
+ * mixed-precision variant of src/mfem/refinement/solver.py:581-609.
+ * Synchronises the device and drops the plan's captured graphs. */
 int mfem_plan_set_solver(mfem_plan *plan, const mfem_solver_config *cfg);
 
 /* Outcomes of the mixed-precision solves of the last step (synchronises the
