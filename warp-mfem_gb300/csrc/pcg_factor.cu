@@ -26,6 +26,13 @@
 // A factor solve that breaks down (non-finite values or p.Ap <= 0) is solved
 // again from the same warm start with block-Jacobi inside the launch; every
 // CTA takes that decision from the same totals.  Every wait is bounded.
+//
+// It also serves as the inner solve of the mixed-precision refinement
+// (pcg_mixed.cu): from e = 0 it solves Hq e = r / ||r||, on an fp32 copy of
+// the 16-bit blocks (or on H once the refinement has switched to it), reads
+// and writes the refinement's state words, and returns e ||r||.  A
+// block-Jacobi plan keeps a layout of this kernel, without factor rows, for
+// that use only.
 #include <algorithm>
 
 #include "factor_apply.cuh"
