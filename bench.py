@@ -57,6 +57,10 @@ def parse_args():
                     help="global solve: fp32 PCG (the workload's) or mixed-precision iterative refinement")
     ap.add_argument("--outer-tolerance", type=float, default=1.0e-6,
                     help="fp64 relative residual of the mixed-precision solve")
+    ap.add_argument("--inner-tolerance", type=float, default=1.0e-3,
+                    help="relative residual of the mixed-precision solve's inner PCG")
+    ap.add_argument("--outer-max-iterations", type=int, default=10,
+                    help="corrections of the mixed-precision solve before it reports MAXITER")
     ap.add_argument("--preconditioner", default="block_jacobi", choices=["block_jacobi", "fsai", "learned"],
                     help="PCG preconditioner: the workload's block-Jacobi, or the FSAI / learned factor "
                          "(global-memory PCG)")
@@ -72,7 +76,7 @@ def parse_args():
 
 
 def workload_config(mesh, extra=None, precision="fp32", outer_tolerance=1e-6, preconditioner="block_jacobi",
-                    factor_refresh=1, pcg_variant="global_memory"):
+                    factor_refresh=1, pcg_variant="global_memory", inner_tolerance=1e-3):
     spec = mesh.spec
     if precision == "fp32" and preconditioner == "block_jacobi":
         pcg = "plain fp32 block-Jacobi, the reference's (persistent PCG)"
@@ -81,8 +85,8 @@ def workload_config(mesh, extra=None, precision="fp32", outer_tolerance=1e-6, pr
         pcg = (f"fp32 PCG with the {preconditioner} factor preconditioner ({kind}), factor recomputed "
                f"every {factor_refresh} Newton iteration(s)")
     else:
-        pcg = (f"{precision} blocks with per-row scales, fp32 {preconditioner} inner PCG to 1e-3, fp64 iterative "
-               f"refinement to {outer_tolerance:g}")
+        pcg = (f"{precision} blocks with per-row scales, fp32 {preconditioner} inner PCG to {inner_tolerance:g}, "
+               f"fp64 iterative refinement to {outer_tolerance:g}")
     cfg = {
         "workload": (f"{spec.name}: {spec.cells[0]}x{spec.cells[1]}x{spec.cells[2]} hex cells x 6 tets "
                      f"({mesh.T} tets, {mesh.n} vertices, {3 * mesh.n} DoF), {spec.energy}, "
@@ -553,7 +557,8 @@ def run_gb300(args, rank, world, local_rank):
                             # the workload is the plain local/global step unless asked
                             line_search=args.line_search, preconditioner=args.preconditioner,
                             factor_refresh=args.factor_refresh,
-                            solver_precision=args.precision, outer_tolerance=args.outer_tolerance)
+                            solver_precision=args.precision, outer_tolerance=args.outer_tolerance,
+                            inner_tolerance=args.inner_tolerance, outer_max_iterations=args.outer_max_iterations)
     s_init = solver.tet_stretch.clone().reshape(-1)
     lam0 = torch.zeros_like(s_init)
     q0 = torch.as_tensor(mesh.q0, device=dev)
@@ -751,7 +756,8 @@ def run_gb300(args, rank, world, local_rank):
                                          "global_memory_autotune_ms": tune_ms},
                                   precision=args.precision, outer_tolerance=args.outer_tolerance,
                                   preconditioner=args.preconditioner, factor_refresh=args.factor_refresh,
-                                  pcg_variant=solver.pcg_layout()["variant"]),
+                                  pcg_variant=solver.pcg_layout()["variant"],
+                                  inner_tolerance=args.inner_tolerance),
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes, "matches_resident_run": e2e_match},
         "gpu_launches": int(launches),
