@@ -27,7 +27,6 @@
 namespace mfem {
 namespace {
 
-constexpr int kBtMaxThreads = 512;
 constexpr int kBtGroup = 4;  // lanes per block row in the product
 constexpr long long kBtWaitCycles = 8000000000ll;
 
@@ -216,7 +215,8 @@ struct BtScalars {
 // or 3, with the block-Jacobi retry); the other one, for use_precond 0 or 1,
 // carries none of that code.  Register caps (no spills at either): 48 lets
 // 10 CTAs of 128 threads share an SM, 56 lets 9 (the kernel waits on gather
-// latency, so resident warps matter); up to kBtMaxThreads threads a CTA.
+// latency, so resident warps matter); up to 512 threads a CTA (the host's
+// schedules use 128 to 512).
 template <bool FACTOR>
 __global__ void __maxnreg__(FACTOR ? 56 : 48)
     batched_pcg_kernel(BsrViews bv, VertexViews vv, BatchViews bw, int *error, int slot, float tol, int maxiter,
