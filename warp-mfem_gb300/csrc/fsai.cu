@@ -203,7 +203,6 @@ __global__ void __launch_bounds__(kFsaiThreads) fsai_setup_kernel(BsrViews bv, B
     float *A = s_A[wid];
     float *X = s_X[wid];
     const int lb = bw.lrow[row], m = bw.lrow[row + 1] - lb;
-    const int *cols = bw.lcol + lb;
     float *G = bw.Lval + (size_t)9 * lb;
     const int N = 3 * m;
     const int S = N | 1;  // odd row stride: the rows lanes own fall in distinct banks
