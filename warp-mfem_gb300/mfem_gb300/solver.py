@@ -52,9 +52,16 @@ class MixedFEMSolver:
     lower block-triangular on H's block pattern, recomputed after every
     assembly, or "learned": M = L L^T with L written by the factor net
     (``factor_net``; parameters ``factor_net_params`` or the shipped
-    weights).  Both factor forms run the global-memory PCG (fp32 solve
-    only); ``factor_refresh`` k recomputes the factor at every k-th Newton
+    weights).  Both factor forms run the persistent factor PCG where its
+    per-CTA ranges fit in shared memory, else the global-memory PCG
+    (``pcg_variant`` "factor" or "global_memory" forces one); with a 16-bit
+    ``solver_precision`` they precondition the inner PCG.
+    ``factor_refresh`` k recomputes the factor at every k-th Newton
     iteration of a step (default 1: every assembly).
+
+    ``pcg_variant``: "auto" (default), "standard", "single_reduction",
+    "gather" (block-Jacobi / no preconditioner), "factor" (the persistent
+    factor PCG) or "global_memory" (the batched kernel's PCG on one body).
     """
 
     def __init__(self, model: Model, iterations: int, max_tets: Optional[int] = None,
@@ -209,8 +216,8 @@ class MixedFEMSolver:
                                                  _stream_handle(self.device)), self._plan)
 
     def autotune(self, q: torch.Tensor, dt: float) -> float:
-        """For a plan on the global-memory PCG (a factor preconditioner, or a
-        mesh too large for the persistent PCG): picks the fastest schedule
+        """For a plan on the global-memory PCG (a mesh too large for the
+        persistent PCGs, or pcg_variant="global_memory"): picks the fastest schedule
         on the system at q (at rest); returns that solve's time in ms."""
         if self.pcg_layout()["variant"] != "global_memory":
             raise ValueError("autotune serves plans on the global-memory PCG")
