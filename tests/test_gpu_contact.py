@@ -213,6 +213,24 @@ def test_contact_trajectory_with_factor_preconditioner(pc):
         close(A.particle_q.cpu().numpy(), q, 1e-5)
 
 
+@pytest.mark.parametrize("pc", ["block_jacobi", "fsai"])
+def test_contact_trajectory_with_mixed_precision(pc):
+    """fp16 blocks with contact: the contact blocks enter H before its 16-bit
+    copy is made, and the refined solve keeps the trajectory on the oracle."""
+    mesh, model, solver, co = scene(preconditioner=pc, solver_precision="fp16")
+    ref = O.OracleSolver(mesh, dtype=np.float64, contact=co)
+    A, B = model.state(), model.state()
+    q, qd = mesh.q0.astype(np.float64), mesh.qd0.astype(np.float64)
+    for k in range(12):
+        B.body_q.copy_(torch.as_tensor(tool_pose(k), device=DEV))
+        solver.step(A, B, None, None, mesh.spec.dt)
+        ref.body_q = tool_pose(k).astype(np.float64)
+        q, qd = ref.step(q, qd, mesh.spec.dt)
+        A, B = B, A
+        assert all(st["status"] == 0 for st in solver.mixed_stats())
+        close(A.particle_q.cpu().numpy(), q, 1e-5)
+
+
 def test_graph_and_eager_agree_bitwise_with_contact():
     runs = []
     for graph in (True, False):

@@ -206,3 +206,25 @@ def test_tiny_residual_does_not_underflow(pc, variant):
     gg = g.cpu().numpy().astype(np.float64)
     dx = solver.read_buffer("mixed_dx").cpu().numpy()
     assert np.linalg.norm(gg - H @ dx) <= 1e-8 * np.linalg.norm(gg)
+
+
+@pytest.mark.parametrize("pc", ["block_jacobi", "learned"])
+def test_mixed_with_line_search_matches_oracle(pc):
+    """fp16 blocks under the reference's default update, the line search:
+    a trajectory stays within 1e-5 of the float64 oracle with line search."""
+    mesh = beams.build_beam("nh_beam", cells=(16, 4, 4))
+    model = Model.from_beam(mesh, device=DEV)
+    solver = MixedFEMSolver(model, iterations=8, energy=mesh.spec.energy, solver_precision="fp16",
+                            preconditioner=pc, factor_refresh=8)
+    assert solver.line_search
+    ref = O.OracleSolver(mesh, dtype=np.float64, line_search=True)
+    A, B = model.state(), model.state()
+    A.particle_q.copy_(torch.as_tensor(mesh.q0, device=DEV))
+    q, qd = mesh.q0, mesh.qd0
+    for _ in range(3):
+        solver.step(A, B, None, None, mesh.spec.dt)
+        A, B = B, A
+        q, qd = ref.step(q, qd, mesh.spec.dt)
+        assert all(s["status"] == _lib.MFEM_OK for s in solver.mixed_stats())
+        assert all(e["status"] == 0 for e in solver.line_search_stats())
+        close(A.particle_q.cpu().numpy(), q, 1e-5)
