@@ -438,10 +438,16 @@ def block_jacobi_inverse(diag_blocks, singular_threshold):
 
 def pcg(apply_A, b, x0, Minv_blocks, tol, maxiter):
     """Block-Jacobi PCG on [n, 3] vectors; stops when ||r|| <= tol ||b||."""
+    import scipy.sparse as sp
     dt = b.dtype
+    n = Minv_blocks.shape[0]
+    M = sp.bsr_matrix((Minv_blocks, np.arange(n), np.arange(n + 1)), shape=(3 * n, 3 * n))
+
+    def precond(v):
+        return (M @ v.reshape(-1)).reshape(n, 3)
     x = x0.copy()
     r = b - apply_A(x)
-    z = np.einsum("nij,nj->ni", Minv_blocks, r)
+    z = precond(r)
     p = z.copy()
     rz = np.sum(r * z, dtype=dt)
     b_norm = math.sqrt(float(np.sum(b * b, dtype=dt)))
@@ -454,7 +460,7 @@ def pcg(apply_A, b, x0, Minv_blocks, tol, maxiter):
         alpha = rz / pAp
         x = x + alpha * p
         r = r - alpha * Ap
-        z = np.einsum("nij,nj->ni", Minv_blocks, r)
+        z = precond(r)
         rz_new = np.sum(r * z, dtype=dt)
         beta = rz_new / rz
         rz = rz_new
@@ -630,16 +636,14 @@ class OracleSolver:
         return blocks.astype(dtp), g.astype(dtp), Hs
 
     def bsr_apply(self, blocks):
+        """v -> H v for H's 3x3 blocks in slot order (warp.sparse.bsr_mv), as
+        scipy's block-sparse product in the blocks' dtype."""
+        import scipy.sparse as sp
         n = self.n
-        rp, ci = self.row_ptr, self.col_idx
-        br = np.repeat(np.arange(n), np.diff(rp))
-        dtp = self.dtype
+        H = sp.bsr_matrix((blocks, self.col_idx, self.row_ptr), shape=(3 * n, 3 * n))
 
         def apply(v):
-            prod = np.einsum("kij,kj->ki", blocks, v[ci])
-            out = np.zeros((n, 3), dtype=dtp)
-            np.add.at(out, br, prod)
-            return out
+            return (H @ np.ascontiguousarray(v).reshape(-1)).reshape(n, 3)
         return apply
 
     def diag_blocks(self, blocks):
