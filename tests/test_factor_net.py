@@ -93,3 +93,28 @@ def test_reference_factor_structure(built_lib):
     # emulating BF16 changes the factor only at BF16 resolution
     L32 = F.reference_factor(net, rp, ci, vals, vs, emulate_bf16=False)
     assert np.abs(L - L32).max() <= 3e-2 * np.abs(L32).max()
+
+
+def test_smooth_field_loss_term(built_lib):
+    """The opt-in smooth-field term: off by default (the residual form
+    alone, bit for bit), finite, larger and differentiable when on."""
+    mesh, rp, ci, vals = _system()
+    G = F.Graph(rp, ci)
+    v = torch.as_tensor(vals, dtype=torch.float32)
+    vs = torch.as_tensor(F.static_features(mesh.rest_q, mesh.tet_indices, mesh.tet_materials))
+    rhs = torch.ones(mesh.n, 3)
+    sm = torch.as_tensor(F.smooth_fields(mesh.rest_q, 4, np.random.default_rng(0)))
+    assert sm.shape == (mesh.n, 3, 4) and torch.isfinite(sm).all() and sm.abs().max() > 0
+    torch.manual_seed(4)
+    net = F.FactorNet()
+    g0 = torch.Generator().manual_seed(0)
+    base = F.loss(net, G, v, vs, rhs, 8, g0)
+    g1 = torch.Generator().manual_seed(0)
+    off = F.loss(net, G, v, vs, rhs, 8, g1, sm, 0.0)
+    assert torch.equal(base, off)
+    g2 = torch.Generator().manual_seed(0)
+    on = F.loss(net, G, v, vs, rhs, 8, g2, sm, 2.0)
+    assert torch.isfinite(on) and on > base
+    on.backward()
+    assert all(p.grad is None or torch.isfinite(p.grad).all() for p in net.parameters())
+    assert any(p.grad is not None and p.grad.abs().sum() > 0 for p in net.parameters())

@@ -240,14 +240,42 @@ def apply_blocks(G: Graph, Ks, v):
     return torch.zeros_like(v).index_add_(0, G.rows, torch.einsum("kij,kjm->kim", Ks, v[G.cols]))
 
 
-def loss(net: FactorNet, G: Graph, values, vstatic, rhs, k: int = 8, generator=None):
+def smooth_fields(rest_q: np.ndarray, k: int, rng, kmax: float = 1.5) -> np.ndarray:
+    """k random low-frequency vector fields [n, 3, k] over the rest positions
+    (sums of sinusoids with wave vectors ~ N(0, kmax) on the unit-scaled
+    body): the smooth modes that set CG's iteration count."""
+    X = np.asarray(rest_q, dtype=np.float64)
+    X = (X - X.min(0)) / max(float(np.ptp(X, axis=0).max()), 1e-30)
+    out = np.zeros((X.shape[0], 3, k))
+    for j in range(k):
+        for c in range(3):
+            for _ in range(3):
+                kv = rng.normal(0.0, kmax, 3)
+                out[:, c, j] += rng.normal() * np.sin(2.0 * np.pi * (X @ kv) + rng.uniform(0.0, 2.0 * np.pi))
+    return out.astype(np.float32)
+
+
+def loss(net: FactorNet, G: Graph, values, vstatic, rhs, k: int = 8, generator=None, smooth=None,
+         smooth_weight: float = 0.0):
+    """||r - K M r||^2 / ||r||^2 over k vectors r (the scaled rhs and normal
+    noise), plus, with ``smooth`` fields [n, 3, k'] and smooth_weight > 0,
+    that weight times ||z - M K z||^2 / ||z||^2 over the fields z (in the
+    scaled system's variables): the residual form with white noise weights
+    every eigenmode alike, the smooth term the low-frequency ones."""
     s, Ld, Lo = forward(net, G, values, vstatic)
     _, _, Ks = scaled_system(G, values)
     r = torch.randn(G.n, 3, k, device=values.device, generator=generator)
     r[:, :, 0] = rhs * s[:, None]
     r = r / torch.linalg.vector_norm(r.reshape(-1, k), dim=0).clamp_min(1e-30)
     res = r - apply_blocks(G, Ks, apply_scaled_M(G, Ld, Lo, r))
-    return (torch.linalg.vector_norm(res.reshape(-1, k), dim=0) ** 2).mean()
+    out = (torch.linalg.vector_norm(res.reshape(-1, k), dim=0) ** 2).mean()
+    if smooth is None or smooth_weight <= 0.0:
+        return out
+    z = smooth / s[:, None, None]  # fields of x; the scaled system's variables are S^-1 x
+    kz = z.shape[2]
+    z = z / torch.linalg.vector_norm(z.reshape(-1, kz), dim=0).clamp_min(1e-30)
+    e = z - apply_scaled_M(G, Ld, Lo, apply_blocks(G, Ks, z))
+    return out + smooth_weight * (torch.linalg.vector_norm(e.reshape(-1, kz), dim=0) ** 2).mean()
 
 
 # -- training data from this library's solver --------------------------------
@@ -291,9 +319,10 @@ def solver_systems(mesh, n_steps: int, seed: int, device: str = "cuda:0", veloci
 
 
 def train(meshes, pairs: int = 2000, r_per_system: int = 8, epochs: int = 12, seed: int = 5,
-          device: str = "cuda:0", log=print) -> FactorNet:
+          device: str = "cuda:0", log=print, smooth_weight: float = 0.0) -> FactorNet:
     """Trains on about ``pairs`` (K, r) pairs: pairs / r_per_system systems
-    drawn along trajectories of ``meshes``."""
+    drawn along trajectories of ``meshes``; smooth_weight > 0 adds the
+    smooth-field term of ``loss`` (8 fields a system)."""
     torch.manual_seed(seed)
     systems = []
     per_mesh = max(1, pairs // r_per_system // len(meshes))
@@ -303,8 +332,11 @@ def train(meshes, pairs: int = 2000, r_per_system: int = 8, epochs: int = 12, se
         rp, ci, sysl, vs = solver_systems(mesh, steps, seed + 17 * m_i, device)
         G = Graph(rp, ci, device)
         vst = torch.as_tensor(vs, device=device)
+        frng = np.random.default_rng(seed + 31 * m_i)
         for vals, rhs in sysl[:per_mesh]:
-            systems.append((G, vals, vst, rhs))
+            sm = (torch.as_tensor(smooth_fields(mesh.rest_q, 8, frng), device=device)
+                  if smooth_weight > 0 else None)
+            systems.append((G, vals, vst, rhs, sm))
         log(f"mesh {mesh.spec.name} {mesh.spec.cells}: {min(per_mesh, len(sysl))} systems")
     net = FactorNet().to(device)
     opt = torch.optim.Adam(net.parameters(), lr=2e-3)
@@ -315,9 +347,9 @@ def train(meshes, pairs: int = 2000, r_per_system: int = 8, epochs: int = 12, se
         perm = np.random.default_rng(seed + ep).permutation(len(systems))
         tot = 0.0
         for i in perm:
-            G, vals, vst, rhs = systems[i]
+            G, vals, vst, rhs, sm = systems[i]
             opt.zero_grad()
-            lv = loss(net, G, vals, vst, rhs, r_per_system, gen)
+            lv = loss(net, G, vals, vst, rhs, r_per_system, gen, sm, smooth_weight)
             lv.backward()
             opt.step()
             tot += float(lv.detach())
@@ -334,9 +366,11 @@ def main(argv=None):
     ap.add_argument("--pairs", type=int, default=2000)
     ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--device", default="cuda:0")
+    ap.add_argument("--smooth-weight", type=float, default=0.0,
+                    help="weight of the smooth-field term of the loss (0: the residual form only)")
     args = ap.parse_args(argv)
     meshes = [beams.build_beam("nh_beam"), beams.build_beam("stiff_beam")]
-    net = train(meshes, pairs=args.pairs, epochs=args.epochs, device=args.device)
+    net = train(meshes, pairs=args.pairs, epochs=args.epochs, device=args.device, smooth_weight=args.smooth_weight)
     np.savez(args.out, params=net.pack())
     print(f"wrote {args.out} ({N_PARAMS} parameters)")
 
