@@ -155,3 +155,23 @@ def test_initial_stretch_is_identity_at_rest():
     m = beams.build_beam("nh_beam", cells=(4, 2, 2))
     s = O.precompute_tet_stretch(m.rest_q.astype(np.float64), m.tet_indices, m.tet_poses.astype(np.float64))
     np.testing.assert_allclose(s, np.tile([1, 1, 1, 0, 0, 0], (m.T, 1)), atol=1e-6)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_bsr_apply_equals_dense_product(dtype):
+    """The oracle's block-sparse product (warp.sparse.bsr_mv) against the
+    dense matrix of the same blocks."""
+    mesh = beams.build_beam("cantilever")
+    S = O.OracleSolver(mesh, dtype=dtype)
+    n, rp, ci = S.n, S.row_ptr, S.col_idx
+    rng = np.random.default_rng(5)
+    blocks = rng.standard_normal((ci.shape[0], 3, 3)).astype(dtype)
+    v = rng.standard_normal((n, 3)).astype(dtype)
+    D = np.zeros((3 * n, 3 * n))
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    for k in range(ci.shape[0]):
+        D[3 * rows[k]:3 * rows[k] + 3, 3 * ci[k]:3 * ci[k] + 3] = blocks[k]
+    got = S.bsr_apply(blocks)(v)
+    assert got.dtype == dtype and got.shape == (n, 3)
+    tol = 1e-12 if dtype == np.float64 else 1e-5
+    np.testing.assert_allclose(got.ravel(), D @ v.astype(np.float64).ravel(), rtol=tol, atol=tol * np.abs(D).max())
