@@ -8,11 +8,21 @@ known_answers.npz -- the inputs of the reference's own known-answer tests for
 cantilever_fp64.npz -- the float64 oracle's 100-step trajectory of the
     10x2x2 ARAP cantilever (positions after every step, final s and lambda,
     PCG iterations per Newton iteration).
+nh_beam_fp64.npz -- the float64 oracle's 50-step run of the full Neo-Hookean
+    beam (64x16x16 cells, 98,304 tets): displacements from rest (float32)
+    after step 1 and every 5th step, PCG iterations per Newton iteration.
+    About half an hour on one core.
 reference_fixture_digests.json -- sha256 digests and shapes of the arrays of
     the reference's fem_beam.npz (written only where the reference tree is
-    present), so the 5-tet grid generator is pinned to it without copying it.
+    given and holds it), so the 5-tet grid generator is pinned to it without
+    copying it.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:
+    python tests/golden/make_golden.py [--reference-tree DIR] [fixture ...]
+with fixture among known_answers, cantilever, nh_beam, digests (default:
+all).  The reference tree comes from --reference-tree or the environment
+variable MFEM_REFERENCE_TREE; without either the digests are left as they
+are.
 """
 from __future__ import annotations
 
@@ -115,7 +125,24 @@ def cantilever_trajectory():
                 pcg_iterations=np.array(iters, dtype=np.int32))
 
 
-REFERENCE_TREE = "/root/reference"
+def nh_beam_trajectory(stride: int = 5):
+    """The full nh_beam workload (64x16x16 cells, 50 steps) by the float64
+    oracle: displacements q - q_rest after steps 1, stride, 2 stride, ...
+    stored as float32 (1e-8 m resolution, far below the 1e-5 relative
+    tolerance the GPU test applies to positions of up to 2 m)."""
+    mesh = beams.build_beam("nh_beam")
+    solver = O.OracleSolver(mesh, dtype=np.float64)
+    q, qd = mesh.q0, mesh.qd0
+    keep, disp, iters = [], [], []
+    for k in range(1, mesh.spec.steps + 1):
+        q, qd = solver.step(q, qd, mesh.spec.dt)
+        iters.append([r.iterations for r in solver.last_pcg])
+        if k == 1 or k % stride == 0:
+            keep.append(k)
+            disp.append((q - mesh.rest_q).astype(np.float32))
+        print(f"nh_beam oracle step {k}: PCG iterations {iters[-1]}", flush=True)
+    return dict(steps=np.array(keep, dtype=np.int32), displacement=np.stack(disp),
+                pcg_iterations=np.array(iters, dtype=np.int32))
 
 
 def array_digest(a: np.ndarray) -> dict:
@@ -124,24 +151,46 @@ def array_digest(a: np.ndarray) -> dict:
     return {"dtype": str(a.dtype), "shape": list(a.shape), "sha256": hashlib.sha256(a.tobytes()).hexdigest()}
 
 
-def reference_fixture_digests():
-    path = os.path.join(REFERENCE_TREE, "fem_beam.npz")
-    if not os.path.exists(path):
+def reference_fixture_digests(reference_tree):
+    if not reference_tree:
         return None
+    path = os.path.join(reference_tree, "fem_beam.npz")
+    if not os.path.exists(path):
+        raise SystemExit(f"{path} not found: --reference-tree must name the reference's checkout")
     d = np.load(path)
     return {"fem_beam.npz": {k: array_digest(d[k]) for k in ("particles", "tet_indices", "tet_materials")}
             | {"parameters": d["parameters"].tolist()}}
 
 
-def main():
+FIXTURES = ("known_answers", "cantilever", "nh_beam", "digests")
+
+
+def main(argv=None):
+    import argparse
     import json
-    digests = reference_fixture_digests()
-    if digests is not None:
-        with open(os.path.join(HERE, "reference_fixture_digests.json"), "w") as f:
-            json.dump(digests, f, indent=1)
-    np.savez_compressed(os.path.join(HERE, "known_answers.npz"), **known_answers())
-    np.savez_compressed(os.path.join(HERE, "cantilever_fp64.npz"), **cantilever_trajectory())
-    print("wrote", os.listdir(HERE))
+    ap = argparse.ArgumentParser(description="Regenerates the golden fixtures of tests/golden/.")
+    ap.add_argument("--reference-tree", default=os.environ.get("MFEM_REFERENCE_TREE"),
+                    help="checkout of the reference (default: $MFEM_REFERENCE_TREE)")
+    ap.add_argument("fixtures", nargs="*", help=f"any of {', '.join(FIXTURES)} (default: all)")
+    args = ap.parse_args(argv)
+    unknown = set(args.fixtures) - set(FIXTURES)
+    if unknown:
+        ap.error(f"unknown fixture(s) {sorted(unknown)}; choose from {FIXTURES}")
+    which = set(args.fixtures or FIXTURES)
+    if "digests" in which:
+        digests = reference_fixture_digests(args.reference_tree)
+        if digests is not None:
+            with open(os.path.join(HERE, "reference_fixture_digests.json"), "w") as f:
+                json.dump(digests, f, indent=1)
+        else:
+            print("no reference tree given: reference_fixture_digests.json left as it is")
+    if "known_answers" in which:
+        np.savez_compressed(os.path.join(HERE, "known_answers.npz"), **known_answers())
+    if "cantilever" in which:
+        np.savez_compressed(os.path.join(HERE, "cantilever_fp64.npz"), **cantilever_trajectory())
+    if "nh_beam" in which:
+        np.savez_compressed(os.path.join(HERE, "nh_beam_fp64.npz"), **nh_beam_trajectory())
+    print("wrote", sorted(os.listdir(HERE)))
 
 
 if __name__ == "__main__":
