@@ -16,9 +16,10 @@ step; the timed run is the workload's 50 steps from its initial state.
 --workload batched512 steps the batch of 512 uneven beams (per-body PCGs in
 one persistent launch): value = batch steps/s (every body advanced one step).
 
---impl reference times the CPU oracle (the restatement of the reference's
-step, float32) on the host instead.  With --gpus N under torchrun every rank
-runs an independent replica (the step does not shard across GPUs).
+--impl reference times the OpenMP C++ restatement of the step
+(oracle/cpu_step.cpp) on all host cores instead: the reference's own Warp
+path cannot run here.  With --gpus N under torchrun every rank runs an
+independent replica (the step does not shard across GPUs).
 """
 from __future__ import annotations
 
@@ -53,8 +54,9 @@ def parse_args():
     ap.add_argument("--pcg-ctas", type=int, default=0, help="persistent PCG CTAs (0: one per SM)")
     ap.add_argument("--pcg-variant", default="auto",
                     choices=["auto", "standard", "single_reduction", "gather", "factor", "global_memory"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16", "fp16"],
-                    help="global solve: fp32 PCG (the workload's) or mixed-precision iterative refinement")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16", "fp16", "fp32_refined"],
+                    help="global solve: fp32 PCG (the workload's) or fp64 iterative refinement around an "
+                         "inner PCG on 16-bit (bf16, fp16) or fp32 (fp32_refined) blocks")
     ap.add_argument("--outer-tolerance", type=float, default=1.0e-6,
                     help="fp64 relative residual of the mixed-precision solve")
     ap.add_argument("--inner-tolerance", type=float, default=1.0e-3,
@@ -71,7 +73,11 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the solve variants (learned / FSAI factors, fp16) of the default line")
+    ap.add_argument("--no-extra-workloads", action="store_true",
+                    help="skip the stiff_beam and batched512 entries of the default line")
     ap.add_argument("--cpu-budget-s", type=float, default=30.0, help="CPU time budget of the oracle leg")
+    ap.add_argument("--variant-inner-tolerance", type=float, default=1.0e-2,
+                    help="inner PCG tolerance of the refined solve variants of the default line")
     return ap.parse_args()
 
 
@@ -204,23 +210,54 @@ def pcg_bytes_per_iteration(nnzb: int, n: int) -> int:
     return 40 * nnzb + 172 * n
 
 
-def cpu_oracle_rate(mesh, budget_s: float):
-    """Steps/s of the float32 oracle on this host (at least one full step,
-    more while within budget)."""
-    import numpy as np
-    from oracle import mfem_oracle
+def host_cpu() -> dict:
+    """This host's core count and CPU model (lscpu, else /proc/cpuinfo)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        m = re.search(r"^Model name:\s*(.+)$", out, re.M)
+        model = m.group(1).strip() if m else None
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if model is None:
+        try:
+            m = re.search(r"^model name\s*:\s*(.+)$", open("/proc/cpuinfo").read(), re.M)
+            model = m.group(1).strip() if m else None
+        except OSError:
+            pass
+    return {"nproc": os.cpu_count(), "model": model}
 
-    ref = mfem_oracle.OracleSolver(mesh, dtype=np.float32)
+
+def cpu_step_rate(mesh, budget_s: float, max_steps: int):
+    """Steps/s of the OpenMP C++ restatement of the step (oracle/cpu_step.cpp)
+    on all host cores, from the workload's initial state: at least one step,
+    more while within budget, at most max_steps.  Returns (rate, steps,
+    seconds, threads)."""
+    from oracle import cpu_step
+    cs = cpu_step.CpuStep(mesh)
     q, qd = mesh.q0, mesh.qd0
     t0 = time.perf_counter()
     steps = 0
     while True:
-        q, qd = ref.step(q, qd, mesh.spec.dt)
+        q, qd = cs.step(q, qd, mesh.spec.dt)
         steps += 1
         el = time.perf_counter() - t0
-        if el * (steps + 1) / steps > budget_s or steps >= mesh.spec.steps:
+        if el * (steps + 1) / steps > budget_s or steps >= max_steps:
             break
-    return steps / el, steps, el
+    threads = cs.threads
+    cs.close()
+    return steps / el, steps, el, threads
+
+
+def cpu_baseline_line(mesh, budget_s: float, max_steps: int, workload: str) -> dict:
+    rate, steps, el, threads = cpu_step_rate(mesh, budget_s, max_steps)
+    cpu = host_cpu()
+    return {"value": rate, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": (f"{steps} step(s) of {workload} ({mesh.T} tets, {mesh.spec.iterations} local/global "
+                       f"iterations each) from its initial state by the OpenMP C++ restatement of the step "
+                       f"(oracle/cpu_step.cpp, float32, block-Jacobi PCG to 1e-6; restatement, not the "
+                       f"reference) on {threads} threads in {el:.1f} s"),
+            "host": cpu}
 
 
 # ---------------------------------------------------------------------------
@@ -233,17 +270,20 @@ def run_reference(args, rank, world):
     if args.workload.startswith("batched"):
         return run_reference_batched(args)
     mesh = beams.build_beam(args.workload)
-    budget = max(10.0, min(150.0, args.cpu_budget_s * max(1, args.steps) / 10.0))
-    rate, steps, el = cpu_oracle_rate(mesh, budget)
-    sample = (f"{steps} step(s) of {args.workload} ({mesh.T} tets, {mesh.spec.iterations} local/global iterations "
-              f"each, scipy/numpy float32 oracle restating the reference step) in {el:.1f} s")
+    # one untimed step pages the code and data in; the timed run is the
+    # workload's first --steps steps from its initial state, like the GPU
+    # arm's, within a budget of a few minutes
+    cpu_step_rate(mesh, 0.0, 1)
+    cpu = cpu_baseline_line(mesh, 180.0, max(1, args.steps), args.workload)
+    rate, steps = cpu["value"], int(re.match(r"(\d+)", cpu["sample"]).group(1))
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": args.gpus,
-        "steps": steps, "warmup": 0, "ms_per_step": 1000.0 / rate, "higher_is_better": True,
+        "steps": steps, "warmup": 1, "ms_per_step": 1000.0 / rate, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(mesh, {"reference": "CPU oracle port (the reference's Warp path cannot run: "
-                                                      "warp-lang / newton absent, Python >= 3.13 required)"}),
-        "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": 1, "kind": "port", "sample": sample},
+        "config": workload_config(mesh, {"reference": "OpenMP C++ restatement of the step on all host cores "
+                                                      "(the reference's Warp path cannot run: warp-lang / newton "
+                                                      "absent, Python >= 3.13 required)"}),
+        "cpu_baseline": cpu,
         "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -398,20 +438,7 @@ def run_batched(args, rank, world, local_rank):
         return 0
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
-        # the float32 oracle stepping bodies one after another, within budget
-        from oracle import mfem_oracle
-        t0 = time.perf_counter()
-        done = 0
-        for m in batch.bodies:
-            ref = mfem_oracle.OracleSolver(m, dtype=np.float32)
-            ref.step(m.q0, m.qd0, m.spec.dt)
-            done += 1
-            if time.perf_counter() - t0 > args.cpu_budget_s:
-                break
-        el = time.perf_counter() - t0
-        cpu = {"value": done / el / B, "unit": "steps/s", "cores": 1, "kind": "port",
-               "sample": f"one step of the first {done} of {B} bodies by the float32 oracle in {el:.1f} s "
-                         "(batch steps/s = body steps/s / bodies)"}
+        cpu = batched_cpu_line(batch, args.cpu_budget_s)
     it_all = np.stack(its)
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
@@ -442,32 +469,46 @@ def run_batched(args, rank, world, local_rank):
     return 0
 
 
+def batched_cpu_line(batch, budget_s: float) -> dict:
+    """The OpenMP C++ restatement stepping the bodies one after another from
+    their initial states, within budget; batch steps/s = body steps/s /
+    bodies."""
+    from oracle import cpu_step
+    B = batch.n_bodies
+    t0 = time.perf_counter()
+    done, threads = 0, 1
+    for m in batch.bodies:
+        cs = cpu_step.CpuStep(m)
+        cs.step(m.q0, m.qd0, m.spec.dt)
+        threads = cs.threads
+        cs.close()
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return {"value": done / el / B, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": (f"one step of the first {done} of {B} bodies by the OpenMP C++ restatement of the step "
+                       f"(oracle/cpu_step.cpp; restatement, not the reference) on {threads} threads in {el:.1f} s "
+                       "(batch steps/s = body steps/s / bodies)"),
+            "host": host_cpu()}
+
+
 def run_reference_batched(args):
-    """The float32 oracle steps the bodies one after another (a bounded
+    """The C++ restatement steps the bodies one after another (a bounded
     sample); batch steps/s = body steps/s / bodies."""
-    import numpy as np
     from mfem_gb300 import beams
-    from oracle import mfem_oracle
     B = batched_count(args.workload)
     batch = beams.batched_bodies(B, seed=4)
     budget = max(10.0, min(150.0, args.cpu_budget_s * max(1, args.steps) / 10.0))
-    t0 = time.perf_counter()
-    done = 0
-    for m in batch.bodies:
-        mfem_oracle.OracleSolver(m, dtype=np.float32).step(m.q0, m.qd0, m.spec.dt)
-        done += 1
-        if time.perf_counter() - t0 > budget:
-            break
-    el = time.perf_counter() - t0
-    rate = done / el / B
-    sample = f"one step of the first {done} of {B} bodies by the float32 oracle in {el:.1f} s"
+    cpu = batched_cpu_line(batch, budget)
+    rate = cpu["value"]
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": args.gpus,
         "steps": 1, "warmup": 0, "ms_per_step": 1000.0 / rate, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{B} uneven beams (seed 4)", "bodies": B,
-                   "reference": "CPU oracle port (the reference's Warp path cannot run here)"},
-        "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": 1, "kind": "port", "sample": sample},
+                   "reference": "OpenMP C++ restatement of the step (the reference's Warp path cannot run here)"},
+        "cpu_baseline": cpu,
         "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -477,67 +518,288 @@ def run_reference_batched(args):
 # ---------------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------------
-def solve_variants(mesh, dev, steps=20, warmup=2):
-    """steps/s over the workload's first `steps` steps with the other solves
-    -- learned (or FSAI) factor preconditioners, fp16 mixed precision,
-    every solve to the workload's 1e-6 -- beside the plain fp32 block-Jacobi
-    PCG over the same steps (graph replays, L2 flushed between steps)."""
+SOLVE_VARIANTS = (("fp32", "block_jacobi"), ("fp32", "fsai"), ("fp32", "learned"),
+                  ("fp32_refined", "block_jacobi"), ("fp32_refined", "fsai"),
+                  ("fp16", "block_jacobi"), ("fp16", "fsai"), ("fp16", "learned"))
+
+
+def checked_summary(residuals, tol):
+    """Counts of the solves whose float64 residual meets `tol`, and the
+    worst and median residuals."""
+    r = sorted(residuals)
+    return {"solves": len(r), "meet_tolerance": sum(1 for v in r if v <= tol),
+            "worst": r[-1] if r else None, "median": statistics.median(r) if r else None}
+
+
+def run_checked(solver, model, q0, s_init, dt, steps):
+    """The first `steps` steps from the initial state with the fp64 check of
+    every global solve on (graph replays, untimed).  Returns the float64
+    residuals of the float32 dx of each solve, the mixed solves' own
+    residuals (of their float64 dx; empty for the fp32 PCG) and the final
+    positions."""
+    import torch
+    st = [model.state(), model.state()]
+    st[0].particle_q.copy_(q0)
+    st[0].particle_qd.zero_()
+    solver.write_buffer("tet_stretch", s_init)
+    solver.write_buffer("tet_lambda", torch.zeros_like(s_init))
+    solver.set_residual_check(True)
+    res32, res_own = [], []
+    for _ in range(steps):
+        solver.step(st[0], st[1], None, None, dt)
+        res32 += solver.step_true_residuals()
+        res_own += [r["rel_residual"] for r in solver.mixed_stats()]
+        st.reverse()
+    q = st[0].particle_q.cpu().numpy()
+    solver.set_residual_check(False)
+    return res32, res_own, q
+
+
+def measure_variant(mesh, dev, precision, pc, steps, warmup, inner_tolerance, outer_tolerance=None,
+                    outer_max_iterations=20, factor_refresh=8, profile=False):
+    """One solve variant on `mesh`: steps/s over the workload's first `steps`
+    steps (graph replays, L2 flushed between steps, after `warmup` steps),
+    the float64 check of every one of their solves (a separate untimed run
+    with the check on, bit-identical positions), and with `profile` the
+    persistent PCG's roofline from one eager step timed stage by stage."""
+    import numpy as np
     import torch
     from mfem_gb300 import Model, MixedFEMSolver
     spec = mesh.spec
+    tol = spec.cg_tolerance
     q0 = torch.as_tensor(mesh.q0, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
-    out = {"steps": steps, "tolerance": spec.cg_tolerance, "factor_refresh": 8}
-    for precision, pc in (("fp32", "block_jacobi"), ("fp32", "fsai"), ("fp32", "learned"), ("fp16", "block_jacobi"),
-                          ("fp16", "fsai"), ("fp16", "learned")):
-        model = Model.from_beam(mesh, device=dev)
-        kw = dict(iterations=spec.iterations, energy=spec.energy, cg_tolerance=spec.cg_tolerance,
-                  cg_max_iterations=spec.cg_max_iterations, line_search=False, preconditioner=pc,
-                  solver_precision=precision, outer_tolerance=spec.cg_tolerance)
-        if pc != "block_jacobi":
-            kw["factor_refresh"] = 8
-        solver = MixedFEMSolver(model, **kw)
-        if solver.pcg_layout()["variant"] == "global_memory":
-            solver.autotune(q0, spec.dt)
-        s_init = solver.tet_stretch.clone().reshape(-1)
-        st = [model.state(), model.state()]
+    model = Model.from_beam(mesh, device=dev)
+    kw = dict(iterations=spec.iterations, energy=spec.energy, cg_tolerance=tol,
+              cg_max_iterations=spec.cg_max_iterations, line_search=False, preconditioner=pc,
+              solver_precision=precision, outer_tolerance=tol if outer_tolerance is None else outer_tolerance,
+              inner_tolerance=inner_tolerance, outer_max_iterations=outer_max_iterations)
+    if pc != "block_jacobi":
+        kw["factor_refresh"] = factor_refresh
+    solver = MixedFEMSolver(model, **kw)
+    if solver.pcg_layout()["variant"] == "global_memory":
+        solver.autotune(q0, spec.dt)
+    s_init = solver.tet_stretch.clone().reshape(-1)
+    st = [model.state(), model.state()]
 
-        def reset():
-            st[0].particle_q.copy_(q0)
-            st[0].particle_qd.zero_()
-            solver.write_buffer("tet_stretch", s_init)
-            solver.write_buffer("tet_lambda", torch.zeros_like(s_init))
+    def reset():
+        st[0].particle_q.copy_(q0)
+        st[0].particle_qd.zero_()
+        solver.write_buffer("tet_stretch", s_init)
+        solver.write_buffer("tet_lambda", torch.zeros_like(s_init))
 
+    res32, res_own, q_checked = run_checked(solver, model, q0, s_init, spec.dt, steps)
+    reset()
+    for _ in range(max(2, warmup)):  # both state orientations captured before timing
+        solver.step(st[0], st[1], None, None, spec.dt)
+        st.reverse()
+    reset()
+    total_ms, its, codes = 0.0, 0, []
+    for _ in range(steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        solver.step(st[0], st[1], None, None, spec.dt)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        if precision == "fp32":
+            rec = solver.solve_stats()
+            its += sum(r["iterations"] for r in rec)
+        else:
+            rec = solver.mixed_stats()
+            its += sum(r["inner_iterations"] for r in rec)
+        codes += [int(r["status"]) for r in rec]
+        st.reverse()
+    q_timed = st[0].particle_q.cpu().numpy()
+    own = res_own if precision != "fp32" else res32
+    out = {
+        "steps_per_s": 1000.0 * steps / total_ms, "pcg_iterations_per_step": its / steps,
+        "status_codes": sorted(set(codes)),
+        "converged_fraction": sum(1 for c in codes if c == 0) / max(1, len(codes)),
+        "pcg": ("fp64 iterative refinement" if precision != "fp32" else solver.pcg_layout()["variant"]),
+        "fp64_check": {"solution": checked_summary(own, tol), "fp32_dx": checked_summary(res32, tol)},
+        "checked_run_matches_timed": bool(np.array_equal(q_checked, q_timed)),
+    }
+    if profile and precision == "fp32":
+        # one eager step, the global solves timed on the launch stream
         reset()
-        for _ in range(warmup):
-            solver.step(st[0], st[1], None, None, spec.dt)
-            st.reverse()
-        reset()
-        total_ms, its, codes = 0.0, 0, set()
-        for _ in range(steps):
-            flush.zero_()
+        x = st[1].particle_q
+        solver.predict(st[0].particle_q, st[0].particle_qd, spec.dt)
+        x.copy_(st[0].particle_q)
+        pcg_ms = 0.0
+        for it in range(spec.iterations):
+            solver.update_system(x)
+            solver.assemble(x, spec.dt)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            solver.step(st[0], st[1], None, None, spec.dt)
+            solver.global_solve(it)
             e1.record(stream)
+            solver.local_solve(x)
             e1.synchronize()
-            total_ms += e0.elapsed_time(e1)
-            if precision == "fp32":
-                rec = solver.solve_stats()
-                its += sum(r["iterations"] for r in rec)
-            else:
-                rec = solver.mixed_stats()
-                its += sum(r["inner_iterations"] for r in rec)
-            codes.update(int(r["status"]) for r in rec)
-            st.reverse()
-        out[f"{precision}+{pc}"] = {"steps_per_s": 1000.0 * steps / total_ms, "pcg_iterations_per_step": its / steps,
-                                    "status_codes": sorted(codes),
-                                    "pcg": ("mixed-precision refinement" if precision != "fp32"
-                                            else solver.pcg_layout()["variant"])}
-        solver.close()
+            pcg_ms += e0.elapsed_time(e1)
+        its1 = sum(r["iterations"] for r in solver.solve_stats())
+        factor = pc != "block_jacobi"
+        b_it = (64 * solver.nnzb + 208 * mesh.n) if factor else pcg_bytes_per_iteration(solver.nnzb, mesh.n)
+        peak, _ = hbm_peak()
+        achieved = b_it * (its1 + spec.iterations) / (pcg_ms / 1000.0) / 1e9
+        out["pcg_roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                               "frac": achieved / peak, "bytes_per_iteration": b_it,
+                               "formula": "64 nnzb + 208 n" if factor else "40 nnzb + 172 n",
+                               "us_per_iteration": 1000.0 * pcg_ms / (its1 + spec.iterations)}
+    solver.close()
     return out
+
+
+def solve_variants(mesh, dev, steps=20, warmup=2, inner_tolerance=1e-2):
+    """steps/s over the workload's first `steps` steps for each solve
+    variant -- the plain fp32 block-Jacobi PCG (the reference's), the FSAI
+    and learned factor preconditioners, the fp32 and fp16 blocks inside the
+    fp64 iterative refinement -- beside the float64 check of every one of
+    their solves: how many meet the 1e-6 tolerance in the float64 residual
+    ||g - H dx|| / ||g||, and the worst.  Timed runs are graph replays with the
+    L2 flushed between steps; the checked run (check on, untimed) follows the
+    same trajectory, which `checked_run_matches_timed` confirms bit for bit."""
+    tol = mesh.spec.cg_tolerance
+    out = {"steps": steps, "tolerance": tol, "factor_refresh": 8, "inner_tolerance": inner_tolerance,
+           "fp64_check": ("float64 ||g - H dx|| / ||g|| of every solve, with the assembled float32 H and g: "
+                          "'solution' is the solve's own output (float32 dx for the fp32 PCG, the refinement's "
+                          "float64 dx for the refined solves), 'fp32_dx' the float32 dx the local solve reads")}
+    for precision, pc in SOLVE_VARIANTS:
+        out[f"{precision}+{pc}"] = measure_variant(mesh, dev, precision, pc, steps, warmup, inner_tolerance)
+
+    def rate(k):
+        return out[k]["steps_per_s"]
+
+    def all_checked(k):
+        c = out[k]["fp64_check"]["solution"]
+        return c["meet_tolerance"] == c["solves"]
+
+    plain, plain_checked = rate("fp32+block_jacobi"), rate("fp32_refined+block_jacobi")
+    out["ratios"] = {
+        "learned_mixed_over_plain": rate("fp16+learned") / plain,
+        "learned_mixed_over_plain_fp64_checked": rate("fp16+learned") / plain_checked,
+        "fsai_mixed_over_plain_fp64_checked": rate("fp16+fsai") / plain_checked,
+        "fsai_refined_fp32_over_plain_fp64_checked": rate("fp32_refined+fsai") / plain_checked,
+        "plain_meets_fp64_checked_tolerance": all_checked("fp32+block_jacobi"),
+        "note": ("plain = the reference's fp32 block-Jacobi PCG, which stops on its float32 recurrence "
+                 "residual; plain_fp64_checked = the same PCG inside the fp64 refinement (fp32_refined), "
+                 "whose every solve meets 1e-6 in the float64 residual"),
+    }
+    checked = [k for k in out if isinstance(out[k], dict) and "fp64_check" in out[k] and all_checked(k)]
+    if checked:
+        best = max(checked, key=rate)
+        out["ratios"]["fastest_fp64_checked"] = {"variant": best, "steps_per_s": rate(best),
+                                                 "over_plain_fp64_checked": rate(best) / plain_checked,
+                                                 "over_plain": rate(best) / plain}
+    return out
+
+
+def extra_workloads(dev, steps=3):
+    """The other configs' step rates on the default line: the stiff beam
+    (128x32x32 cells, 786,432 tets, E log-uniform [1e4, 1e7]) with the plain
+    fp32 PCG, FSAI, and the fp16 / bf16 blocks in the fp64 refinement at the
+    config's tolerances (inner 1e-3, outer 1e-8); and the 512 uneven bodies
+    in one launch with block-Jacobi and FSAI."""
+    from mfem_gb300 import beams
+    out = {}
+    mesh = beams.build_beam("stiff_beam")
+    sb = {"steps": steps, "workload": f"stiff_beam 128x32x32 cells ({mesh.T} tets, {mesh.n} vertices)"}
+    sb["fp32+block_jacobi"] = measure_variant(mesh, dev, "fp32", "block_jacobi", steps, 1, 1e-3, profile=True)
+    sb["fp32+fsai"] = measure_variant(mesh, dev, "fp32", "fsai", steps, 1, 1e-3, profile=True)
+    sb["fp16+block_jacobi (inner 1e-3, outer 1e-8)"] = measure_variant(mesh, dev, "fp16", "block_jacobi", steps, 1,
+                                                                       1e-3, outer_tolerance=1e-8,
+                                                                       outer_max_iterations=10)
+    sb["fp16+fsai (inner 1e-3, outer 1e-8)"] = measure_variant(mesh, dev, "fp16", "fsai", steps, 1, 1e-3,
+                                                               outer_tolerance=1e-8, outer_max_iterations=10)
+    out["stiff_beam"] = sb
+    del mesh
+    out["batched512"] = {pc: measure_batched(dev, pc, steps) for pc in ("block_jacobi", "fsai")}
+    return out
+
+
+def measure_batched(dev, pc, steps, B=512):
+    """Batch steps/s of the B uneven bodies (seed 4) in one plan after the
+    autotuner, and the batched PCG's roofline from one eager step."""
+    import numpy as np
+    import torch
+    from mfem_gb300 import beams
+    from mfem_gb300.batched import BatchedSolver
+    batch = beams.batched_bodies(B, seed=4)
+    kw = {"preconditioner": pc}
+    if pc != "block_jacobi":
+        kw["factor_refresh"] = 8
+    bs = BatchedSolver(batch, device=dev, **kw)
+    bs.autotune()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    A, Bst = bs.state(), bs.model.state()
+    q0 = A.particle_q.clone()
+    s_init = bs.solver.tet_stretch.clone().reshape(-1)
+
+    def reset():
+        A.particle_q.copy_(q0)
+        A.particle_qd.zero_()
+        bs.solver.write_buffer("tet_stretch", s_init)
+        bs.solver.write_buffer("tet_lambda", torch.zeros_like(s_init))
+
+    for _ in range(2):  # both state orientations captured before timing
+        bs.step(A, Bst)
+        A, Bst = Bst, A
+    reset()
+    total_ms, codes, its = 0.0, set(), []
+    for _ in range(steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        bs.step(A, Bst)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        st = bs.body_stats()
+        codes.update(int(c) for c in np.unique(st["status"]))
+        its.append(st["iterations"].sum(0))
+        A, Bst = Bst, A
+    # roofline: one eager step's global solves
+    solver = bs.solver
+    row_ptr = solver.read_buffer("row_ptr").cpu().numpy()
+    voff = batch.vertex_offsets
+    nnzb_b = (row_ptr[voff[1:]] - row_ptr[voff[:-1]]).astype(np.float64)
+    n_b = np.diff(voff).astype(np.float64)
+    factor = pc != "block_jacobi"
+    per_it_b = (64.0 * nnzb_b + 208.0 * n_b) if factor else (40.0 * nnzb_b + 172.0 * n_b)
+    reset()
+    x = Bst.particle_q
+    solver.predict(A.particle_q, A.particle_qd, batch.dt)
+    x.copy_(A.particle_q)
+    pcg_ms = 0.0
+    for it in range(solver.iterations):
+        solver.update_system(x)
+        solver.assemble(x, batch.dt)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        solver.global_solve(it)
+        e1.record(stream)
+        solver.local_solve(x)
+        e1.synchronize()
+        pcg_ms += e0.elapsed_time(e1)
+    st = bs.body_stats()
+    bytes_pcg = float(((st["iterations"].astype(np.float64) + 1.0) * per_it_b[None, :]).sum())
+    peak, _ = hbm_peak()
+    achieved = bytes_pcg / (pcg_ms / 1000.0) / 1e9
+    it_all = np.stack(its)
+    return {"batch_steps_per_s": 1000.0 * steps / total_ms, "body_steps_per_s": B * 1000.0 * steps / total_ms,
+            "steps": steps, "status_codes": sorted(codes), "schedule": bs.layout(),
+            "pcg_iterations_per_body_step": {"mean": float(it_all.mean()), "max": int(it_all.max())},
+            "pcg_roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak,
+                             "formula": ("64 nnzb_b + 208 n_b" if factor else "40 nnzb_b + 172 n_b") +
+                                        " per body iteration, summed over bodies x (iterations_b + 1)"}}
 
 
 def run_gb300(args, rank, world, local_rank):
@@ -579,6 +841,10 @@ def run_gb300(args, rank, world, local_rank):
             dist.barrier()
         torch.cuda.synchronize(dev)
 
+    # ---- the fp64 check of every solve of the timed trajectory (untimed,
+    # graph replays with the check on; the check only reads)
+    res32, res_own, q_checked = run_checked(solver, model, q0, s_init, spec.dt, args.steps)
+
     # ---- warm-up (captures the step graphs)
     reset()
     for _ in range(args.warmup):
@@ -595,6 +861,7 @@ def run_gb300(args, rank, world, local_rank):
     total_ms = 0.0
     pcg_iters = []
     statuses = set()
+    codes = []
     for _ in range(args.steps):
         flush.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -607,6 +874,7 @@ def run_gb300(args, rank, world, local_rank):
         st = solver.solve_stats()
         pcg_iters.append(sum(s["iterations"] for s in st))
         statuses.update(s["status"] for s in st)
+        codes += [s["status"] for s in st]
         A, B = B, A
     launches = _lib.kernel_launch_count() - launches0
     barrier()
@@ -738,13 +1006,14 @@ def run_gb300(args, rank, world, local_rank):
     variants = None
     if (world == 1 and not args.no_variants and args.precision == "fp32" and args.preconditioner == "block_jacobi"
             and not args.line_search):
-        variants = solve_variants(mesh, dev)
+        variants = solve_variants(mesh, dev, inner_tolerance=args.variant_inner_tolerance)
+    extra = None
+    if (world == 1 and not args.no_extra_workloads and args.workload == "nh_beam" and args.precision == "fp32"
+            and args.preconditioner == "block_jacobi" and not args.line_search):
+        extra = extra_workloads(dev)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
-        rate, steps, el = cpu_oracle_rate(mesh, args.cpu_budget_s)
-        cpu = {"value": rate, "unit": "steps/s", "cores": 1, "kind": "port",
-               "sample": f"{steps} step(s) of {args.workload} ({mesh.T} tets, {spec.iterations} local/global "
-                         f"iterations each) by the float32 numpy/scipy oracle in {el:.1f} s"}
+        cpu = cpu_baseline_line(mesh, args.cpu_budget_s, spec.steps, args.workload)
     avg_iters = statistics.mean(pcg_iters)
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
@@ -767,9 +1036,18 @@ def run_gb300(args, rank, world, local_rank):
         "pcg_iterations_per_step": avg_iters,
         "dof_iterations_per_s": world * 3 * mesh.n * sum(pcg_iters) / t_max,
         "pcg_status_codes": sorted(statuses),
+        "converged_fraction": sum(1 for c in codes if c == 0) / max(1, len(codes)),
+        "fp64_check": {
+            "what": ("float64 ||g - H dx|| / ||g|| of every solve of the timed trajectory (a separate untimed run "
+                     "with the check on, bit-identical positions); 'solution' is the solve's own output"),
+            "solution": checked_summary(res_own if args.precision != "fp32" else res32, spec.cg_tolerance),
+            "fp32_dx": checked_summary(res32, spec.cg_tolerance),
+            "checked_run_matches_timed": bool(np.array_equal(q_checked, q_final)),
+        },
         "stage_share": shares,
         "stage_ms_per_step": {k: v / prof_steps for k, v in stage_ms.items()},
         "solve_variants": variants,
+        "extra_workloads": extra,
     }
     print(json.dumps(line), flush=True)
     return 0

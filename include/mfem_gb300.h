@@ -91,8 +91,9 @@ typedef enum mfem_buffer {
     MFEM_BUF_GRAD_CONSTRAINT = 3, /* f32 [72][T] G, entry (i, 3k+a) at (i*12 + 3k+a)*T+t  */
     MFEM_BUF_GRAD_S = 4,        /* f32 [6][T]  g_s                                         */
     MFEM_BUF_H_LAMBDA = 5,      /* f32 [21][T] H_lambda, packed upper triangle row-major  */
-    MFEM_BUF_HESS_S_INV = 6,    /* f32 [21][T] H_s^-1, packed upper triangle row-major    */
-    MFEM_BUF_G_LAMBDA = 7,      /* f32 [6][T]  g_lambda                                    */
+    MFEM_BUF_HESS_S_INV = 6,    /* f32 [21][T] H_s^-1, packed upper triangle row-major
+                                   (written only with mfem_plan_set_diagnostics on)        */
+    MFEM_BUF_G_LAMBDA = 7,      /* f32 [6][T]  g_lambda (diagnostics on only)             */
     MFEM_BUF_ELEMENT_HESSIAN = 8, /* f32 [T][10][3][3] upper blocks (k<=l) of G^T H_l G   */
     MFEM_BUF_ELEMENT_RHS = 9,   /* f32 [T][12] (H_l G)^T g_lambda                          */
     MFEM_BUF_ROW_PTR = 10,      /* i32 [n+1]   BSR row offsets                             */
@@ -157,7 +158,10 @@ typedef struct mfem_solve_stats {
 typedef enum mfem_precision {
     MFEM_PRECISION_FP32 = 0,
     MFEM_PRECISION_BF16 = 1,
-    MFEM_PRECISION_FP16 = 2
+    MFEM_PRECISION_FP16 = 2,
+    /* the fp32 blocks in the inner PCG, inside the same fp64 refinement: the
+     * plain fp32 PCG brought to an fp64-checked residual */
+    MFEM_PRECISION_FP32_REFINED = 3
 } mfem_precision;
 
 typedef struct mfem_solver_config {
@@ -344,6 +348,34 @@ int mfem_step_mixed_stats(mfem_plan *plan, mfem_mixed_solve_stats *h_stats, int3
 int mfem_plan_set_factor_net(mfem_plan *plan, const float *h_params, int64_t n_params,
                              const float *h_vertex_static);
 
+/* ---- training the factor net (no plan) ---------------------------------- */
+
+/* C = op(A) op(B), or C += op(A) op(B) with accumulate != 0, on the tensor
+ * cores: device float32 operands rounded to BF16 as they are staged, FP32
+ * accumulation.  op(A) is A (stored [M][K], row stride lda) or, with a_trans,
+ * A^T (A stored [K][M]); op(B) is B (stored [K][N]) or, with b_trans, B^T
+ * (B stored [N][K]); C is [M][N] with row stride ldc.  The three products of
+ * a linear layer y = x W^T are forward (A = x, B = W, b_trans), the input
+ * gradient (A = dy, B = W) and the weight gradient (A = dy, a_trans, B = x).
+ * A long K with a small C is split over CTAs into partial tiles in the
+ * optional device workspace (workspace_floats floats; NULL: no split), added
+ * in a fixed order.  Asynchronous on `stream`; errors through
+ * mfem_train_last_error().  No reference counterpart: the factor net and its
+ * training are this library's (mfem_plan_set_factor_net). */
+int mfem_train_gemm(int32_t M, int32_t N, int32_t K, const float *d_A, int32_t lda, int32_t a_trans,
+                    const float *d_B, int32_t ldb, int32_t b_trans, float *d_C, int32_t ldc, int32_t accumulate,
+                    float *d_workspace, int64_t workspace_floats, mfem_stream stream);
+
+/* One Adam step (Kingma & Ba 2015) over n float32 parameters on the device:
+ * m = beta1 m + (1 - beta1) g, v = beta2 v + (1 - beta2) g^2,
+ * p -= lr m^ / (sqrt(v^) + eps) with the bias corrections of step >= 1.
+ * No reference counterpart. */
+int mfem_train_adam(float *d_params, const float *d_grads, float *d_m, float *d_v, int64_t n, float lr, float beta1,
+                    float beta2, float eps, int32_t step, mfem_stream stream);
+
+/* Message of the last failed mfem_train_* call on this host thread. */
+const char *mfem_train_last_error(void);
+
 /* ---- independent bodies in one plan ------------------------------------ */
 
 /* Declares the plan's mesh to be n_bodies independent bodies: the vertices
@@ -443,6 +475,29 @@ int mfem_local_solve(mfem_plan *plan, float *d_x, mfem_stream stream);
  * true-residual check of the float32 recurrence. */
 int mfem_true_residual(mfem_plan *plan, double *h_rel_residual, mfem_stream stream);
 
+/* Turns on (on != 0) or off the element stage's diagnostic outputs H_s^-1
+ * (MFEM_BUF_HESS_S_INV) and g_lambda (MFEM_BUF_G_LAMBDA): the reference's
+ * intermediates (src/mfem/refinement/kernels.py:189-217), which the step
+ * does not read -- its local solve and rhs use the cancellation-free form
+ * lambda = -(H_l u + INV_SYM g_s), ds = INV_SYM u, u = c - G dx.  Off by
+ * default (those buffers then keep stale contents).  Synchronises the device
+ * and drops captured graphs when the setting changes. */
+int mfem_plan_set_diagnostics(mfem_plan *plan, int32_t on);
+
+/* Turns on (on != 0) or off the fp64 check of every global solve inside
+ * mfem_step: after each Newton iteration's solve the step also forms
+ * ||g - H dx|| / ||g|| in float64 for the float32 dx the local solve reads
+ * (mfem_true_residual's sum, one entry per Newton iteration).  It reads
+ * only, so the trajectory is unchanged.  The reference has no counterpart:
+ * it checks the float32 CG's recurrence residual only.  Synchronises the
+ * device and drops captured graphs when the setting changes. */
+int mfem_plan_set_residual_check(mfem_plan *plan, int32_t on);
+
+/* The check's results for the last step, one per Newton iteration
+ * (synchronises the stream; MFEM_BAD_ARG while the check is off). */
+int mfem_step_true_residuals(mfem_plan *plan, double *h_rel_residual, int32_t max_entries, int32_t *count,
+                             mfem_stream stream);
+
 /* ---- allocation-free solve ---------------------------------------------- */
 
 /* Block-Jacobi PCG on a caller-provided 3x3-block BSR system that allocates
@@ -452,14 +507,17 @@ int mfem_true_residual(mfem_plan *plan, double *h_rel_residual, mfem_stream stre
  * Device arrays, all caller-owned: row_ptr [n+1], col_idx [nnzb], values
  * [nnzb][3][3], precond [n][3][3] block inverse (NULL: unpreconditioned),
  * b [n][3]; x [n][3] holds the warm start and receives the solution;
+ * the caller keeps the BSR well formed (row_ptr[0] = 0, non-decreasing,
+ * row_ptr[n] = nnzb; 0 <= col_idx < n), which the device does not check;
  * stats (device pointer, may be NULL) receives the outcome.  Stops when
  * ||r|| <= tol ||b|| or after maxiter iterations.
  * Its scratch is a fixed array of about 2 MB inside the library (every GPU
  * that loads the library holds it until exit) serving at most 32768 block
  * rows; larger systems return MFEM_BAD_ARG.  All calls share that array:
- * calls whose kernels overlap on the GPU race and must be serialised.  The
- * first call on a device looks up the array's address with that device
- * current; make it before any stream capture.  Asynchronous on `stream`;
+ * calls whose kernels overlap on the GPU race and must be serialised.  Each
+ * call looks up the array's address with the caller's device current; the
+ * first lookup on a device loads the module, so make the first call before
+ * any stream capture.  Asynchronous on `stream`;
  * errors are reported by mfem_plan_last_error(NULL). */
 int mfem_pcg_solve_noalloc(int32_t n, const int32_t *d_row_ptr, const int32_t *d_col_idx,
                            const float *d_values, const float *d_precond, const float *d_b, float *d_x,

@@ -102,6 +102,7 @@ def test_initial_stretch_matches_oracle():
 def test_element_stage_matches_oracle(energy):
     mesh, _, solver = make("cantilever", energy=energy)
     x, s = deformed_inputs(mesh)
+    solver.set_diagnostics(True)  # H_s^-1 and g_lambda are written on request only
     solver.write_buffer("tet_stretch", torch.as_tensor(s).reshape(-1))
     solver.update_system(t(x))
     torch.cuda.synchronize()

@@ -84,6 +84,36 @@ def test_noalloc_solve_matches_plan_solve_on_two_calls():
     _close(a, systems[0]["x_ref"], 1e-4)
 
 
+def test_noalloc_call_leaves_free_device_memory_unchanged():
+    """The property the entry point exists for: after a warm-up call, a call
+    changes the device's free memory (cudaMemGetInfo) by nothing, so it
+    allocated nothing.  Every tensor the call touches exists before the
+    first reading."""
+    lib = _lib.load()
+    sysd = _assembled("nh_beam", (16, 4, 4), 5)
+    x = sysd["x0"].clone()
+    stats = torch.zeros(4, dtype=torch.int32, device=DEV)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def call():
+        x.copy_(sysd["x0"])
+        rc = lib.mfem_pcg_solve_noalloc(sysd["n"], P(sysd["row_ptr"]), P(sysd["col_idx"]), P(sysd["values"]),
+                                        P(sysd["precond"]), P(sysd["rhs"]), P(x), 1e-6, 1000, P(stats), stream)
+        assert rc == _lib.MFEM_OK, lib.mfem_plan_last_error(None).decode()
+        torch.cuda.synchronize()
+
+    call()  # warm-up: the module and its scratch array are loaded by now
+    free0, _ = torch.cuda.mem_get_info()
+    reserved0 = torch.cuda.memory_reserved()
+    for _ in range(3):
+        call()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes"
+    assert torch.cuda.memory_reserved() == reserved0
+    _close(x, sysd["x_ref"], 1e-4)
+
+
 def test_noalloc_rejects_oversized_and_invalid_arguments():
     lib = _lib.load()
     dummy = torch.zeros(16, dtype=torch.float32, device=DEV)

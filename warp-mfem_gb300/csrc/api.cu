@@ -79,6 +79,10 @@ struct mfem_plan {
     bool global_memory_pcg = false;  // the mesh is solved as a one-body batch
     int32_t *tet_slots = nullptr;
     double *resid = nullptr;
+    // per-solve fp64 check of the step's global solves (mfem_plan_set_residual_check)
+    double *check_resid = nullptr;  // [max_stats][2]: ||g - H dx||^2, ||g||^2
+    bool check_on = false;
+    bool diagnostics = false;  // the element stage also writes H_s^-1 and g_lambda
     cudaStream_t capture_stream = nullptr;
     // captured steps, keyed by (q_in, qd_in, q_out, qd_out, dt); a simulation
     // loop that swaps two states alternates between two entries
@@ -252,9 +256,11 @@ cudaError_t run_step(mfem_plan *p, const float *q_in, const float *qd_in, float 
     // lagged friction anchor at the start-of-step positions (solver.py:515-520)
     if (err == cudaSuccess) err = launch_contact_begin(p->cv, p->vv, s);
     for (int it = 0; err == cudaSuccess && it < p->cfg.iterations; ++it) {
-        err = launch_element(q_out, p->cfg.energy, p->tv, s);
+        err = launch_element(q_out, p->cfg.energy, p->tv, p->diagnostics, s);
         if (err == cudaSuccess) err = contact_and_assemble(p, q_out, dt, s, it % p->factor_refresh == 0);
         if (err == cudaSuccess) err = global_solve(p, it, s);
+        if (err == cudaSuccess && p->check_on)
+            err = launch_true_residual(p->bv, p->vv, p->check_resid + 2 * it, s);
         if (err == cudaSuccess) err = local_update(p, q_out, dt, it, s);
     }
     if (err == cudaSuccess) err = launch_velocity(q_out, qd_out, dt, p->vv, s);
@@ -493,6 +499,8 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
     ALLOC(p->tv.g_l, nT * 6);
     ALLOC(p->tv.Ke, nT * kKeFloats);
     ALLOC(p->tv.fe, nT * kFeFloats);
+    ALLOC(p->tv.degenerate, nT);
+    ALLOC(p->tv.n_degenerate, 1);
     ALLOC(p->tet_slots, nT * 16);
     ALLOC(mass, nn);
     ALLOC(hd, nn);
@@ -688,7 +696,8 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
     p->cv.tri_code_base = INT32_MAX;
 
     // s = S(F) at rest, lambda = 0 (additional_state.py:146-189)
-    e = launch_initial_stretch(rest, p->tv, 0);
+    e = prepare_element_kernels();
+    if (e == cudaSuccess) e = launch_initial_stretch(rest, p->tv, 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -1085,7 +1094,7 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
     if (cfg_in) cfg = *cfg_in;
     else mfem_solver_config_default(&cfg);
     if (cfg.precision != MFEM_PRECISION_FP32 && cfg.precision != MFEM_PRECISION_BF16 &&
-        cfg.precision != MFEM_PRECISION_FP16)
+        cfg.precision != MFEM_PRECISION_FP16 && cfg.precision != MFEM_PRECISION_FP32_REFINED)
         return fail(p, MFEM_BAD_ARG, "unknown precision");
     if (!(cfg.inner_tolerance > 0.0f) || !(cfg.inner_tolerance < 1.0f))
         return fail(p, MFEM_BAD_ARG, "inner_tolerance must be in (0, 1)");
@@ -1121,11 +1130,12 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
         }
     };
     IrWork w{};
-    w.mode = cfg.precision == MFEM_PRECISION_BF16 ? kIrBf16 : kIrFp16;
+    const bool refined32 = cfg.precision == MFEM_PRECISION_FP32_REFINED;
+    w.mode = refined32 ? kIrFp32 : (cfg.precision == MFEM_PRECISION_BF16 ? kIrBf16 : kIrFp16);
     w.outer_max = cfg.outer_max_iterations;
     w.inner_tol = cfg.inner_tolerance;
     w.outer_tol = cfg.outer_tolerance;
-    alloc(&w.lowp, nz * 9 * 2);
+    alloc(&w.lowp, refined32 ? 16 : nz * 9 * 2);
     alloc(&w.row_scale, (size_t)p->n * sizeof(float));
     alloc(&w.dx64, 2 * n3 * sizeof(double));
     alloc(&w.dx_out, n3 * sizeof(double));
@@ -1147,7 +1157,7 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
     alloc(&w.scale, 2 * sizeof(float));
     // a plan on the persistent factor PCG runs its inner solves there, on an
     // fp32 copy of the 16-bit blocks (the same rounding)
-    if ((p->pl.variant == PcgLayout::kFactor || p->ir_pl.variant == PcgLayout::kFactor) &&
+    if (!refined32 && (p->pl.variant == PcgLayout::kFactor || p->ir_pl.variant == PcgLayout::kFactor) &&
         p->cfg.preconditioner >= 1)
         alloc(&w.hq, nz * 9 * sizeof(float));
     int max_ctas = 1;
@@ -1184,6 +1194,63 @@ int mfem_step_mixed_stats(mfem_plan *p, mfem_mixed_solve_stats *h_stats, int32_t
     if (e != cudaSuccess) return cuda_fail(p, e, "stats readback");
     for (int i = 0; i < k; ++i) std::memcpy(&h_stats[i], &tmp[i], sizeof(IrStats));
     if (count) *count = k;
+    return MFEM_OK;
+}
+
+int mfem_plan_set_diagnostics(mfem_plan *p, int32_t on) {
+    if (!p) return MFEM_BAD_ARG;
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(p, e, "cudaDeviceSynchronize");
+    if ((on != 0) != p->diagnostics) {
+        for (auto &ge : p->graphs) {
+            if (ge.exec) cudaGraphExecDestroy(ge.exec);
+            ge = mfem_plan::GraphEntry{};
+        }
+    }
+    p->diagnostics = on != 0;
+    return MFEM_OK;
+}
+
+int mfem_plan_set_residual_check(mfem_plan *p, int32_t on) {
+    if (!p) return MFEM_BAD_ARG;
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaDeviceSynchronize();  // no step of this plan may still run the old graphs
+    if (e != cudaSuccess) return cuda_fail(p, e, "cudaDeviceSynchronize");
+    if (on && !p->check_resid) {
+        void *raw = nullptr;
+        e = cudaMalloc(&raw, (size_t)2 * p->max_stats * sizeof(double));
+        if (e != cudaSuccess) return cuda_fail(p, e, "residual check buffer");
+        p->allocs.push_back(raw);
+        p->check_resid = static_cast<double *>(raw);
+        e = cudaMemset(raw, 0, (size_t)2 * p->max_stats * sizeof(double));
+        if (e != cudaSuccess) return cuda_fail(p, e, "residual check buffer");
+    }
+    if ((on != 0) != p->check_on) {
+        for (auto &ge : p->graphs) {
+            if (ge.exec) cudaGraphExecDestroy(ge.exec);
+            ge = mfem_plan::GraphEntry{};
+        }
+    }
+    p->check_on = on != 0;
+    return MFEM_OK;
+}
+
+int mfem_step_true_residuals(mfem_plan *p, double *h_rel, int32_t max_entries, int32_t *count, mfem_stream stream) {
+    if (!p || (max_entries > 0 && !h_rel)) return MFEM_BAD_ARG;
+    if (!p->check_on || !p->check_resid) return fail(p, MFEM_BAD_ARG, "the residual check is off");
+    DeviceGuard g(p->device);
+    const int m = std::min<int>(std::max(0, max_entries), std::min(p->max_stats, p->cfg.iterations));
+    std::vector<double> buf((size_t)2 * std::max(1, m));
+    cudaError_t e = cudaSuccess;
+    if (m > 0)
+        e = cudaMemcpyAsync(buf.data(), p->check_resid, (size_t)2 * m * sizeof(double), cudaMemcpyDeviceToHost,
+                            (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(p, e, "step true residuals");
+    for (int i = 0; i < m; ++i)
+        h_rel[i] = buf[2 * i + 1] > 0.0 ? std::sqrt(buf[2 * i] / buf[2 * i + 1]) : std::sqrt(buf[2 * i]);
+    if (count) *count = m;
     return MFEM_OK;
 }
 
@@ -1609,7 +1676,7 @@ int mfem_plan_autotune_batch(mfem_plan *p, const float *d_q, float dt, double *h
     if (e == cudaSuccess) e = cudaMalloc(&dx0, bytes);
     if (e == cudaSuccess) e = cudaMemsetAsync(dx0, 0, bytes, s);
     if (e == cudaSuccess) e = launch_predict(d_q, dx0, x, p->gravity, dt, p->vv, s);
-    if (e == cudaSuccess) e = launch_element(x, p->cfg.energy, p->tv, s);
+    if (e == cudaSuccess) e = launch_element(x, p->cfg.energy, p->tv, p->diagnostics, s);
     if (e == cudaSuccess) e = contact_and_assemble(p, x, dt, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dx0, p->vv.dx, bytes, cudaMemcpyDeviceToDevice, s);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1759,7 +1826,7 @@ int mfem_update_system(mfem_plan *p, const float *x, mfem_stream stream) {
     if (!p) return MFEM_BAD_ARG;
     if (!x) return fail(p, MFEM_BAD_ARG, "x is NULL");
     DeviceGuard g(p->device);
-    cudaError_t e = launch_element(x, p->cfg.energy, p->tv, (cudaStream_t)stream);
+    cudaError_t e = launch_element(x, p->cfg.energy, p->tv, p->diagnostics, (cudaStream_t)stream);
     return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "update_system");
 }
 

@@ -27,11 +27,54 @@ __device__ __forceinline__ void load_vec3(const float *__restrict__ p, int i, fl
     v[2] = p[3 * i + 2];
 }
 
-__global__ void __launch_bounds__(kElementThreads)
-    element_kernel(const float *__restrict__ x, int energy, TetViews tv) {
+// Element outputs staged per warp in shared memory, so that the tet-major
+// element blocks and rhs (which the assembly gathers per tet) leave in
+// 16-byte stores of consecutive tets instead of 90 scalar stores 360 bytes
+// apart.  Odd row strides keep the lanes' scalar writes free of bank
+// conflicts.
+constexpr int kElementWarps = kElementThreads / 32;
+constexpr int kKeStride = kKeFloats + 1;
+constexpr int kFeStride = kFeFloats + 1;
+constexpr int kElementSmem = kElementWarps * 32 * (kKeStride + kFeStride) * (int)sizeof(float);
+// grid of the fp64 pass: it loops over however many tets were listed
+constexpr int kElementFp64Blocks = 304;
+
+// Copies `count` floats of the warp's staged rows (row r = tet t0 + r, `per`
+// floats a row, stride `stride` in shared memory) to dst = the first tet's
+// output, 16 bytes a store where the destination allows.
+template <int per, int stride>
+__device__ __forceinline__ void warp_copy_out(const float *__restrict__ src, float *__restrict__ dst, int count,
+                                              int lane) {
+    const int n4 = count >> 2;
+    float4 *d4 = reinterpret_cast<float4 *>(dst);
+    for (int q = lane; q < n4; q += 32) {
+        float v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int j = 4 * q + u;
+            const int r = j / per;
+            v[u] = src[r * stride + (j - r * per)];
+        }
+        d4[q] = make_float4(v[0], v[1], v[2], v[3]);
+    }
+    for (int j = 4 * n4 + lane; j < count; j += 32) {
+        const int r = j / per;
+        dst[j] = src[r * stride + (j - r * per)];
+    }
+}
+
+// Everything one Newton iteration needs from tet t: the per-tet terms
+// (component-major, straight to global memory) and the element blocks and
+// rhs, written to ke [90] and fe [12] (shared-memory staging rows in the
+// element kernel, the tet's global rows in the fp64 pass).  FP64 takes the
+// polar decomposition and dS/dF in float64.  DIAG also writes H_s^-1 and
+// g_lambda, which the step does not read (the local solve and the rhs use
+// the cancellation-free form) but the stage diagnostics expose.  Returns
+// det F in float32.
+template <bool FP64, bool DIAG>
+__device__ __forceinline__ float element_tet(const float *__restrict__ x, int energy, const TetViews &tv, int t,
+                                             float *ke, float *fe) {
     const int T = tv.n_tets;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= T) return;
     const int4 tt = tv.tets[t];
     float xv[4][3];
     load_vec3(x, tt.x, xv[0]);
@@ -51,32 +94,37 @@ __global__ void __launch_bounds__(kElementThreads)
     // rest volume 1/(6 det DmInv) (elastic_energy.py:143-145)
     const float vol = 1.0f / (6.0f * em::det3(Dm));
 
-    float g_s[6], H_l[21], H_si[21];
-    em::energy_terms(tv.energy_code ? (int)tv.energy_code[t] : energy, s, mu, lam, vol, g_s, H_l, H_si);
-    float hsg[6];  // H_s^-1 g_s
+    float g_s[6], H_l[21];
+    {
+        float H_si[21];
+        em::energy_terms(tv.energy_code ? (int)tv.energy_code[t] : energy, s, mu, lam, vol, g_s, H_l, H_si);
+        if (DIAG) {
 #pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        float acc = 0.0f;
+            for (int k = 0; k < 21; ++k) tv.H_si[(size_t)k * T + t] = H_si[k];
+            // g_l = c + SYM H_s^-1 g_s (kernels.py:189-205): the second term
+            // now, c added below
 #pragma unroll
-        for (int j = 0; j < 6; ++j) acc += H_si[em::p21(i, j)] * g_s[j];
-        hsg[i] = acc;
+            for (int i = 0; i < 6; ++i) {
+                float acc = 0.0f;
+#pragma unroll
+                for (int j = 0; j < 6; ++j) acc += H_si[em::p21(i, j)] * g_s[j];
+                tv.g_l[(size_t)i * T + t] = em::sym_w(i) * acc;
+            }
+        }
     }
 #pragma unroll
     for (int i = 0; i < 6; ++i) tv.g_s[(size_t)i * T + t] = g_s[i];
 #pragma unroll
-    for (int k = 0; k < 21; ++k) {
-        tv.H_l[(size_t)k * T + t] = H_l[k];
-        tv.H_si[(size_t)k * T + t] = H_si[k];
-    }
+    for (int k = 0; k < 21; ++k) tv.H_l[(size_t)k * T + t] = H_l[k];
 
+    const float detF = em::deformation_det(xv, Dm);
     float c[6], G[6][12];
-    em::element_geometry(xv, Dm, s, c, G);
-    float g_l[6];  // c + SYM H_s^-1 g_s (kernels.py:189-205)
+    if (FP64) em::element_geometry_t<double>(xv, Dm, s, c, G);
+    else em::element_geometry_t<float>(xv, Dm, s, c, G);
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
-        g_l[i] = c[i] + em::sym_w(i) * hsg[i];
         tv.c[(size_t)i * T + t] = c[i];
-        tv.g_l[(size_t)i * T + t] = g_l[i];
+        if (DIAG) tv.g_l[(size_t)i * T + t] += c[i];
     }
 #pragma unroll
     for (int r = 0; r < 6; ++r)
@@ -94,8 +142,6 @@ __global__ void __launch_bounds__(kElementThreads)
         for (int j = 0; j < 6; ++j) acc += H_l[em::p21(i, j)] * c[j];
         w[i] = acc;
     }
-    float *Ke = tv.Ke + (size_t)t * kKeFloats;
-    float *fe = tv.fe + (size_t)t * kFeFloats;
 #pragma unroll
     for (int l = 0; l < 4; ++l) {
         float P[6][3];  // H_l G_l
@@ -117,7 +163,7 @@ __global__ void __launch_bounds__(kElementThreads)
         }
 #pragma unroll
         for (int k = 0; k <= l; ++k) {
-            float *blk = Ke + ke_block(k, l) * 9;
+            float *blk = ke + ke_block(k, l) * 9;
 #pragma unroll
             for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -128,6 +174,43 @@ __global__ void __launch_bounds__(kElementThreads)
                     blk[a * 3 + b] = acc;
                 }
         }
+    }
+    return detF;
+}
+
+// One thread per tet, in float32; tets with det F < 1e-3 are listed for
+// element_fp64_kernel, which redoes them with the float64 polar path.
+template <bool DIAG>
+__global__ void __launch_bounds__(kElementThreads, 3)
+    element_kernel(const float *__restrict__ x, int energy, TetViews tv) {
+    extern __shared__ __align__(16) float s_stage[];
+    const int T = tv.n_tets;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int t0 = blockIdx.x * blockDim.x + warp * 32;  // the warp's first tet
+    if (t0 >= T) return;                                 // warp-uniform
+    const int t = t0 + lane;
+    float *const w_ke = s_stage + warp * 32 * kKeStride;                                   // [32][kKeStride]
+    float *const w_fe = s_stage + kElementWarps * 32 * kKeStride + warp * 32 * kFeStride;  // [32][kFeStride]
+    if (t < T) {
+        const float detF = element_tet<false, DIAG>(x, energy, tv, t, w_ke + lane * kKeStride, w_fe + lane * kFeStride);
+        if (!(detF >= em::kPolarFp64Det)) tv.degenerate[atomicAdd(tv.n_degenerate, 1u)] = t;
+    }
+    __syncwarp();
+    const int nv = min(32, T - t0);
+    warp_copy_out<kKeFloats, kKeStride>(w_ke, tv.Ke + (size_t)t0 * kKeFloats, nv * kKeFloats, lane);
+    warp_copy_out<kFeFloats, kFeStride>(w_fe, tv.fe + (size_t)t0 * kFeFloats, nv * kFeFloats, lane);
+}
+
+// The listed near-degenerate or inverted tets again, with the polar
+// decomposition and dS/dF in float64; overwrites the element kernel's
+// float32 results of those tets.
+template <bool DIAG>
+__global__ void __launch_bounds__(kElementThreads)
+    element_fp64_kernel(const float *__restrict__ x, int energy, TetViews tv) {
+    const unsigned count = *tv.n_degenerate;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const int t = tv.degenerate[i];
+        element_tet<true, DIAG>(x, energy, tv, t, tv.Ke + (size_t)t * kKeFloats, tv.fe + (size_t)t * kFeFloats);
     }
 }
 
@@ -358,10 +441,28 @@ cudaError_t launch_predict(const float *q_in, const float *qd_in, float *q_out, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_element(const float *x, int energy, const TetViews &tv, cudaStream_t s) {
+cudaError_t prepare_element_kernels() {
+    cudaError_t e = cudaFuncSetAttribute(element_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kElementSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(element_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kElementSmem);
+    return e;
+}
+
+cudaError_t launch_element(const float *x, int energy, const TetViews &tv, bool diagnostics, cudaStream_t s) {
     if (tv.n_tets == 0) return cudaSuccess;
-    element_kernel<<<blocks_for(tv.n_tets, kElementThreads), kElementThreads, 0, s>>>(x, energy, tv);
-    count_launches(1);
+    const int blocks = blocks_for(tv.n_tets, kElementThreads);
+    cudaError_t e = cudaMemsetAsync(tv.n_degenerate, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    const int fix_blocks = std::min(blocks, kElementFp64Blocks);
+    if (diagnostics) {
+        element_kernel<true><<<blocks, kElementThreads, kElementSmem, s>>>(x, energy, tv);
+        element_fp64_kernel<true><<<fix_blocks, kElementThreads, 0, s>>>(x, energy, tv);
+    } else {
+        element_kernel<false><<<blocks, kElementThreads, kElementSmem, s>>>(x, energy, tv);
+        element_fp64_kernel<false><<<fix_blocks, kElementThreads, 0, s>>>(x, energy, tv);
+    }
+    count_launches(2);
     return cudaGetLastError();
 }
 

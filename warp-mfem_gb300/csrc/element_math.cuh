@@ -25,7 +25,32 @@ MFEM_HD constexpr int p21(int i, int j) {
     return (i <= j) ? (i * 6 - (i * (i - 1)) / 2 + (j - i)) : (j * 6 - (j * (j - 1)) / 2 + (i - j));
 }
 
-MFEM_HD float det3(const float a[3][3]) {
+// Scalar helpers that pick the float or double function, so the polar
+// decomposition below serves both precisions from one source.
+MFEM_HD float sqrt_r(float v) { return sqrtf(v); }
+MFEM_HD double sqrt_r(double v) { return sqrt(v); }
+MFEM_HD float abs_r(float v) { return fabsf(v); }
+MFEM_HD double abs_r(double v) { return fabs(v); }
+MFEM_HD float max_r(float a, float b) { return fmaxf(a, b); }
+MFEM_HD double max_r(double a, double b) { return fmax(a, b); }
+MFEM_HD float sign_r(float v) { return copysignf(1.0f, v); }
+MFEM_HD double sign_r(double v) { return copysign(1.0, v); }
+
+// Below this ratio of the second to the first column norm the QR step of the
+// SVD takes any unit vector orthogonal to u0 (a tet collapsed onto a line).
+template <class Real>
+struct QrTiny;
+template <>
+struct QrTiny<float> {
+    static constexpr float value = 1.0e-7f;
+};
+template <>
+struct QrTiny<double> {
+    static constexpr double value = 1.0e-14;
+};
+
+template <class Real>
+MFEM_HD Real det3(const Real a[3][3]) {
     return a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) -
            a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
            a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
@@ -34,44 +59,44 @@ MFEM_HD float det3(const float a[3][3]) {
 // One Jacobi rotation zeroing A[p][q] of a symmetric 3x3 (Golub & Van Loan,
 // "Matrix Computations", sec. 8.5.2: the symmetric Schur decomposition),
 // accumulated into V.
-template <int p, int q>
-MFEM_HD void jacobi_rotate(float A[3][3], float V[3][3]) {
+template <int p, int q, class Real>
+MFEM_HD void jacobi_rotate(Real A[3][3], Real V[3][3]) {
     constexpr int r = 3 - p - q;
-    const float apq = A[p][q];
-    if (apq == 0.0f) return;
-    const float theta = (A[q][q] - A[p][p]) / (2.0f * apq);
-    float t;
-    if (fabsf(theta) > 1.0e18f) {
-        t = 0.5f / theta;
+    const Real apq = A[p][q];
+    if (apq == Real(0)) return;
+    const Real theta = (A[q][q] - A[p][p]) / (Real(2) * apq);
+    Real t;
+    if (abs_r(theta) > Real(1.0e18)) {
+        t = Real(0.5) / theta;
     } else {
-        t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+        t = sign_r(theta) / (abs_r(theta) + sqrt_r(theta * theta + Real(1)));
     }
-    const float c = 1.0f / sqrtf(t * t + 1.0f);
-    const float s = t * c;
+    const Real c = Real(1) / sqrt_r(t * t + Real(1));
+    const Real s = t * c;
     A[p][p] -= t * apq;
     A[q][q] += t * apq;
-    A[p][q] = 0.0f;
-    A[q][p] = 0.0f;
-    const float arp = A[r][p], arq = A[r][q];
+    A[p][q] = Real(0);
+    A[q][p] = Real(0);
+    const Real arp = A[r][p], arq = A[r][q];
     A[r][p] = A[p][r] = c * arp - s * arq;
     A[r][q] = A[q][r] = s * arp + c * arq;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const float vkp = V[k][p], vkq = V[k][q];
+        const Real vkp = V[k][p], vkq = V[k][q];
         V[k][p] = c * vkp - s * vkq;
         V[k][q] = s * vkp + c * vkq;
     }
 }
 
-template <int i, int j>
-MFEM_HD void sort_pair(float d[3], float V[3][3]) {
+template <int i, int j, class Real>
+MFEM_HD void sort_pair(Real d[3], Real V[3][3]) {
     if (d[i] < d[j]) {
-        float t = d[i];
+        Real t = d[i];
         d[i] = d[j];
         d[j] = t;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            float v = V[k][i];
+            Real v = V[k][i];
             V[k][i] = V[k][j];
             V[k][j] = v;
         }
@@ -85,8 +110,9 @@ MFEM_HD void sort_pair(float d[3], float V[3][3]) {
 // 3x3 matrices with minimal branching and elementary floating point
 // operations"): Jacobi eigen-analysis of F^T F gives V; a QR factorisation of
 // F V that keeps U a rotation gives U and the signed singular values.
-MFEM_HD void polar_svd(const float F[3][3], float U[3][3], float sig[3], float V[3][3]) {
-    float A[3][3];
+template <class Real>
+MFEM_HD void polar_svd(const Real F[3][3], Real U[3][3], Real sig[3], Real V[3][3]) {
+    Real A[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -95,69 +121,69 @@ MFEM_HD void polar_svd(const float F[3][3], float U[3][3], float sig[3], float V
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) V[i][j] = (i == j) ? 1.0f : 0.0f;
+        for (int j = 0; j < 3; ++j) V[i][j] = (i == j) ? Real(1) : Real(0);
 #pragma unroll
     for (int sweep = 0; sweep < 5; ++sweep) {
-        jacobi_rotate<0, 1>(A, V);
-        jacobi_rotate<0, 2>(A, V);
-        jacobi_rotate<1, 2>(A, V);
+        jacobi_rotate<0, 1, Real>(A, V);
+        jacobi_rotate<0, 2, Real>(A, V);
+        jacobi_rotate<1, 2, Real>(A, V);
     }
-    float d[3] = {A[0][0], A[1][1], A[2][2]};
-    sort_pair<0, 1>(d, V);
-    sort_pair<0, 2>(d, V);
-    sort_pair<1, 2>(d, V);
+    Real d[3] = {A[0][0], A[1][1], A[2][2]};
+    sort_pair<0, 1, Real>(d, V);
+    sort_pair<0, 2, Real>(d, V);
+    sort_pair<1, 2, Real>(d, V);
     // make V a rotation (flip the column of the smallest eigenvalue)
-    float vdet = det3(V);
-    if (vdet < 0.0f) {
+    Real vdet = det3(V);
+    if (vdet < Real(0)) {
         V[0][2] = -V[0][2];
         V[1][2] = -V[1][2];
         V[2][2] = -V[2][2];
     }
     // B = F V
-    float B[3][3];
+    Real B[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) B[i][j] = F[i][0] * V[0][j] + F[i][1] * V[1][j] + F[i][2] * V[2][j];
     // u0 = b0 / |b0|
-    float n0 = sqrtf(B[0][0] * B[0][0] + B[1][0] * B[1][0] + B[2][0] * B[2][0]);
-    float u0[3];
-    if (n0 > 1.0e-30f) {
-        float inv = 1.0f / n0;
+    Real n0 = sqrt_r(B[0][0] * B[0][0] + B[1][0] * B[1][0] + B[2][0] * B[2][0]);
+    Real u0[3];
+    if (n0 > Real(1.0e-30)) {
+        Real inv = Real(1) / n0;
         u0[0] = B[0][0] * inv;
         u0[1] = B[1][0] * inv;
         u0[2] = B[2][0] * inv;
     } else {
-        u0[0] = 1.0f;
-        u0[1] = 0.0f;
-        u0[2] = 0.0f;
+        u0[0] = Real(1);
+        u0[1] = Real(0);
+        u0[2] = Real(0);
     }
     // u1 = normalise(b1 - (u0.b1) u0), or any unit vector orthogonal to u0
-    float proj = u0[0] * B[0][1] + u0[1] * B[1][1] + u0[2] * B[2][1];
-    float w[3] = {B[0][1] - proj * u0[0], B[1][1] - proj * u0[1], B[2][1] - proj * u0[2]};
-    float n1 = sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-    float u1[3];
-    if (n1 > 1.0e-30f && n1 > 1.0e-7f * n0) {
-        float inv = 1.0f / n1;
+    Real proj = u0[0] * B[0][1] + u0[1] * B[1][1] + u0[2] * B[2][1];
+    Real w[3] = {B[0][1] - proj * u0[0], B[1][1] - proj * u0[1], B[2][1] - proj * u0[2]};
+    Real n1 = sqrt_r(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    Real u1[3];
+    if (n1 > Real(1.0e-30) && n1 > QrTiny<Real>::value * n0) {
+        Real inv = Real(1) / n1;
         u1[0] = w[0] * inv;
         u1[1] = w[1] * inv;
         u1[2] = w[2] * inv;
     } else {
         // cross u0 with the axis it is least aligned with
-        float ax = fabsf(u0[0]), ay = fabsf(u0[1]), az = fabsf(u0[2]);
-        float e[3] = {0.0f, 0.0f, 0.0f};
-        if (ax <= ay && ax <= az) e[0] = 1.0f;
-        else if (ay <= az) e[1] = 1.0f;
-        else e[2] = 1.0f;
-        float cx = u0[1] * e[2] - u0[2] * e[1];
-        float cy = u0[2] * e[0] - u0[0] * e[2];
-        float cz = u0[0] * e[1] - u0[1] * e[0];
-        float inv = 1.0f / sqrtf(cx * cx + cy * cy + cz * cz);
+        Real ax = abs_r(u0[0]), ay = abs_r(u0[1]), az = abs_r(u0[2]);
+        Real e[3] = {Real(0), Real(0), Real(0)};
+        if (ax <= ay && ax <= az) e[0] = Real(1);
+        else if (ay <= az) e[1] = Real(1);
+        else e[2] = Real(1);
+        Real cx = u0[1] * e[2] - u0[2] * e[1];
+        Real cy = u0[2] * e[0] - u0[0] * e[2];
+        Real cz = u0[0] * e[1] - u0[1] * e[0];
+        Real inv = Real(1) / sqrt_r(cx * cx + cy * cy + cz * cz);
         u1[0] = cx * inv;
         u1[1] = cy * inv;
         u1[2] = cz * inv;
     }
-    float u2[3] = {u0[1] * u1[2] - u0[2] * u1[1], u0[2] * u1[0] - u0[0] * u1[2], u0[0] * u1[1] - u0[1] * u1[0]};
+    Real u2[3] = {u0[1] * u1[2] - u0[2] * u1[1], u0[2] * u1[0] - u0[0] * u1[2], u0[0] * u1[1] - u0[1] * u1[0]};
     sig[0] = u0[0] * B[0][0] + u0[1] * B[1][0] + u0[2] * B[2][0];
     sig[1] = u1[0] * B[0][1] + u1[1] * B[1][1] + u1[2] * B[2][1];
     sig[2] = u2[0] * B[0][2] + u2[1] * B[1][2] + u2[2] * B[2][2];
@@ -170,8 +196,9 @@ MFEM_HD void polar_svd(const float F[3][3], float U[3][3], float sig[3], float V
 }
 
 // sym6 of the polar stretch S = V diag(sig) V^T (src/mfem/refinement/utils.py:70-72).
-MFEM_HD void stretch_sym6(const float sig[3], const float V[3][3], float sF[6]) {
-    float VS[3][3];
+template <class Real>
+MFEM_HD void stretch_sym6(const Real sig[3], const Real V[3][3], Real sF[6]) {
+    Real VS[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -192,28 +219,29 @@ MFEM_HD void stretch_sym6(const float sig[3], const float V[3][3], float sF[6]) 
 // Omega_ij = (E^_ij - E^_ji) / max(sig_i + sig_j, 1e-8) (the reference's
 // dR/dF, same clamp), and dS = dR^T F + R^T dF = V (E^ - Omega diag(sig)) V^T.
 // The reference stores sym6 of dS^T, i.e. the lower triangle of dS.
-MFEM_HD void stretch_gradient_row(int a, const float U[3][3], const float sig[3], const float V[3][3],
-                                  float Jc[3][6]) {
-    const float s01 = fmaxf(sig[0] + sig[1], 1.0e-8f);
-    const float s12 = fmaxf(sig[1] + sig[2], 1.0e-8f);
-    const float s02 = fmaxf(sig[0] + sig[2], 1.0e-8f);
+template <class Real>
+MFEM_HD void stretch_gradient_row(int a, const Real U[3][3], const Real sig[3], const Real V[3][3],
+                                  Real Jc[3][6]) {
+    const Real s01 = max_r(sig[0] + sig[1], Real(1.0e-8));
+    const Real s12 = max_r(sig[1] + sig[2], Real(1.0e-8));
+    const Real s02 = max_r(sig[0] + sig[2], Real(1.0e-8));
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-        float N[3][3];
+        Real N[3][3];
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = 0; j < 3; ++j) N[i][j] = U[a][i] * V[b][j];
-        const float o01 = (N[0][1] - N[1][0]) / s01;
-        const float o12 = (N[1][2] - N[2][1]) / s12;
-        const float o02 = (N[0][2] - N[2][0]) / s02;
+        const Real o01 = (N[0][1] - N[1][0]) / s01;
+        const Real o12 = (N[1][2] - N[2][1]) / s12;
+        const Real o02 = (N[0][2] - N[2][0]) / s02;
         N[0][1] -= o01 * sig[1];
         N[1][0] += o01 * sig[0];
         N[1][2] -= o12 * sig[2];
         N[2][1] += o12 * sig[1];
         N[0][2] -= o02 * sig[2];
         N[2][0] += o02 * sig[0];
-        float W[3][3];  // V N
+        Real W[3][3];  // V N
 #pragma unroll
         for (int p = 0; p < 3; ++p)
 #pragma unroll
@@ -406,64 +434,78 @@ MFEM_HD float elastic_energy(int energy, const float s[6], float mu, float lam, 
     return vol * (mu * (0.5f * fro - m2 - dE) + 0.5f * lam * jm1 * jm1);
 }
 
-// F = [x1-x0, x2-x0, x3-x0] DmInv (src/mfem/refinement/kernels.py:145-156).
-MFEM_HD void deformation_gradient(const float x[4][3], const float Dm[3][3], float F[3][3]) {
-    float e[3][3];  // e[c] = x_{c+1} - x0
+// F = [x1-x0, x2-x0, x3-x0] DmInv (src/mfem/refinement/kernels.py:145-156),
+// evaluated in Real from the float32 positions and DmInv.
+template <class Real>
+MFEM_HD void deformation_gradient(const float x[4][3], const float Dm[3][3], Real F[3][3]) {
+    Real e[3][3];  // e[c] = x_{c+1} - x0
 #pragma unroll
     for (int c = 0; c < 3; ++c)
 #pragma unroll
-        for (int i = 0; i < 3; ++i) e[c][i] = x[c + 1][i] - x[0][i];
+        for (int i = 0; i < 3; ++i) e[c][i] = Real(x[c + 1][i]) - Real(x[0][i]);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) F[i][j] = e[0][i] * Dm[0][j] + e[1][i] * Dm[1][j] + e[2][i] * Dm[2][j];
+        for (int j = 0; j < 3; ++j)
+            F[i][j] = e[0][i] * Real(Dm[0][j]) + e[1][i] * Real(Dm[1][j]) + e[2][i] * Real(Dm[2][j]);
 }
 
-// Everything one Newton iteration needs from one tet.  Outputs:
-//   c[6], G[6][12] (the reference's four mat63 blocks side by side),
-//   g_s[6], H_l[21], H_si[21], g_l[6], Ke[10][9] (upper blocks of G^T H_l G),
-//   fe[12] = (H_l G)^T g_l.
-struct ElementOut {
-    float c[6];
-    float G[6][12];
-    float g_s[6];
-    float H_l[21];
-    float H_si[21];
-    float g_l[6];
-};
+// Tets with det F below this take the polar decomposition and its
+// derivative in float64 (near-degenerate, flattened or inverted tets, where
+// dS/dF carries 1 / (sig_i + sig_j) and float32 loses the small singular
+// values of F^T F).
+constexpr float kPolarFp64Det = 1.0e-3f;
 
-MFEM_HD void element_geometry(const float x[4][3], const float Dm[3][3], const float s[6], float c[6],
-                              float G[6][12]) {
-    float F[3][3];
-    deformation_gradient(x, Dm, F);
-    float U[3][3], sig[3], V[3][3];
-    polar_svd(F, U, sig, V);
-    float sF[6];
-    stretch_sym6(sig, V, sF);
+// Constraint c = SYM (sym6(S(F)) - s) and its Jacobian G = -SYM dS/dF dF/dx
+// (the reference's compute_constraints, src/mfem/refinement/kernels.py:
+// 131-169), the polar decomposition and dS/dF evaluated in Real, c and G
+// rounded to float.
+template <class Real>
+MFEM_HD void element_geometry_t(const float x[4][3], const float Dm[3][3], const float s[6], float c[6],
+                                float G[6][12]) {
+    Real F[3][3];
+    deformation_gradient<Real>(x, Dm, F);
+    Real U[3][3], sig[3], V[3][3];
+    polar_svd<Real>(F, U, sig, V);
+    Real sF[6];
+    stretch_sym6<Real>(sig, V, sF);
 #pragma unroll
-    for (int i = 0; i < 6; ++i) c[i] = sym_w(i) * (sF[i] - s[i]);
+    for (int i = 0; i < 6; ++i) c[i] = (float)(Real(sym_w(i)) * (sF[i] - Real(s[i])));
     // dF/dx rows: B[0] = -(sum of DmInv rows), B[k] = DmInv[k-1] (utils.py:123-177)
-    float B[4][3];
+    Real B[4][3];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-        B[0][j] = -Dm[0][j] - Dm[1][j] - Dm[2][j];
-        B[1][j] = Dm[0][j];
-        B[2][j] = Dm[1][j];
-        B[3][j] = Dm[2][j];
+        B[0][j] = -Real(Dm[0][j]) - Real(Dm[1][j]) - Real(Dm[2][j]);
+        B[1][j] = Real(Dm[0][j]);
+        B[2][j] = Real(Dm[1][j]);
+        B[3][j] = Real(Dm[2][j]);
     }
     // G[:, 3k+a] = -(SYM sum_b J[:, a*3+b] B[k][b])  (kernels.py:161-169)
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        float Jc[3][6];
-        stretch_gradient_row(a, U, sig, V, Jc);
+        Real Jc[3][6];
+        stretch_gradient_row<Real>(a, U, sig, V, Jc);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
 #pragma unroll
             for (int r = 0; r < 6; ++r) {
-                const float sr = sym_w(r);
-                G[r][3 * k + a] = -((sr * Jc[0][r]) * B[k][0] + (sr * Jc[1][r]) * B[k][1] + (sr * Jc[2][r]) * B[k][2]);
+                const Real sr = Real(sym_w(r));
+                G[r][3 * k + a] =
+                    (float)(-((sr * Jc[0][r]) * B[k][0] + (sr * Jc[1][r]) * B[k][1] + (sr * Jc[2][r]) * B[k][2]));
             }
     }
+}
+
+// det F in float32: the test that sends a tet to the float64 polar path.
+MFEM_HD float deformation_det(const float x[4][3], const float Dm[3][3]) {
+    float F[3][3];
+    deformation_gradient<float>(x, Dm, F);
+    return det3(F);
+}
+
+MFEM_HD void element_geometry(const float x[4][3], const float Dm[3][3], const float s[6], float c[6],
+                              float G[6][12]) {
+    element_geometry_t<float>(x, Dm, s, c, G);
 }
 
 }  // namespace em

@@ -56,6 +56,9 @@ struct TetViews {
     float *Ke;                 // [T][90]
     float *fe;                 // [T][12]
     const unsigned char *energy_code;  // [T] per-tet energy (batched bodies), or null: the plan's
+    // tets with det F < 1e-3, listed by the element kernel for its float64 pass
+    int *degenerate;           // [T]
+    unsigned *n_degenerate;    // [1]
 };
 
 struct VertexViews {
@@ -234,6 +237,7 @@ struct ContactViews {
 // fp64 residual around a PCG on 16-bit blocks with per-row scales.
 constexpr int kIrBf16 = 1;
 constexpr int kIrFp16 = 2;
+constexpr int kIrFp32 = 3;  // the fp32 H in the inner PCG from the start: no 16-bit copy
 
 struct IrStats {               // same layout as mfem_mixed_solve_stats
     int32_t outer_iterations;
@@ -244,7 +248,7 @@ struct IrStats {               // same layout as mfem_mixed_solve_stats
 };
 
 struct IrWork {
-    int mode;                  // kIrBf16 or kIrFp16
+    int mode;                  // kIrBf16, kIrFp16 or kIrFp32
     int ctas;                  // inner PCG CTAs
     int outer_max;
     float inner_tol;
@@ -309,7 +313,11 @@ bool build_contributions(int n, int T, const int32_t *tets, const int32_t *row_p
 cudaError_t launch_initial_stretch(const float *rest_q, const TetViews &tv, cudaStream_t s);
 cudaError_t launch_predict(const float *q_in, const float *qd_in, float *q_out, const float *gravity_dev,
                            float dt, const VertexViews &vv, cudaStream_t s);
-cudaError_t launch_element(const float *x, int energy, const TetViews &tv, cudaStream_t s);
+// Sets the element kernels' shared-memory limit (once per device, before the
+// first launch).  With diagnostics the element stage also writes H_s^-1 and
+// g_lambda, which the step itself does not read.
+cudaError_t prepare_element_kernels();
+cudaError_t launch_element(const float *x, int energy, const TetViews &tv, bool diagnostics, cudaStream_t s);
 cudaError_t launch_assemble(const float *x, float dt, float singular_threshold, int use_precond,
                             const TetViews &tv, const VertexViews &vv, const BsrViews &bv, const ContactViews &cv,
                             cudaStream_t s);

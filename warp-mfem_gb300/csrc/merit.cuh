@@ -34,6 +34,10 @@ __device__ __forceinline__ double tet_merit(const TetViews &tv, const float *x, 
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) Dm[i][j] = tv.dminv[(size_t)t * 9 + i * 3 + j];
+    // The merit needs S(F) only, which the float32 polar decomposition gives
+    // to about eps |F| even for near-degenerate tets (the QR step recovers
+    // the small singular value from F v); the float64 path of the element
+    // stage is for dS/dF, whose 1 / (sig_i + sig_j) float32 cannot carry.
     float F[3][3], U[3][3], sig[3], V[3][3], sF[6];
     em::deformation_gradient(xv, Dm, F);
     em::polar_svd(F, U, sig, V);

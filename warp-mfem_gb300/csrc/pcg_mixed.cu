@@ -27,6 +27,10 @@
 //                       decides (converged / outer cap)
 //   ir_pcg_kernel<T>    persistent cooperative PCG on Hq e = r, e0 = 0
 //
+// Precision FP32 (kIrFp32) keeps the fp32 H in the inner PCG from the start
+// and converts nothing: the plain fp32 PCG inside the same fp64 refinement,
+// for a solution whose fp64 residual reaches the outer tolerance.
+//
 // A plan on the persistent factor PCG (pcg_factor.cu) runs the inner solves
 // there instead: ir_convert_kernel also writes Hq back as fp32 (each 16-bit
 // value times its row scale, the values ir_pcg_kernel multiplies with), and
@@ -94,7 +98,7 @@ __global__ void ir_begin_kernel(VertexViews vv, IrWork w) {
         w.dx_init[i] = vv.dx[i];
     }
     if (i == 0) {
-        w.state[6] = 0;  // inner PCG on the fp32 H
+        w.state[6] = w.mode == kIrFp32 ? 1 : 0;  // inner PCG on the fp32 H
         w.state[7] = 0;  // restart from the warm start at the next residual
         *w.best = __longlong_as_double(0x7ff0000000000000ll);  // +inf
         w.state[0] = 0;  // done
@@ -657,19 +661,20 @@ cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const 
                                int use_precond, cudaStream_t s) {
     if (bv.n == 0) return cudaSuccess;
     const bool bf16 = w.mode == kIrBf16;
+    const bool fp32 = w.mode == kIrFp32;  // the inner PCG reads the fp32 H itself
     cudaError_t e;
     const int rows_per_block = 256 / 32;
     if (bf16) ir_convert_kernel<__nv_bfloat16><<<blocks_for(bv.n, rows_per_block), 256, 0, s>>>(bv, w);
-    else ir_convert_kernel<__half><<<blocks_for(bv.n, rows_per_block), 256, 0, s>>>(bv, w);
+    else if (!fp32) ir_convert_kernel<__half><<<blocks_for(bv.n, rows_per_block), 256, 0, s>>>(bv, w);
     ir_begin_kernel<<<blocks_for(3 * vv.n, 256), 256, 0, s>>>(vv, w);
-    count_launches(2);
+    count_launches(fp32 ? 1 : 2);
     e = cudaGetLastError();
     const int rb = ir_residual_blocks(vv.n);
     for (int k = 0; e == cudaSuccess && k < w.outer_max; ++k) {
         ir_residual_kernel<<<rb, kResThreads, 0, s>>>(bv, vv, w, pw, slot);
         count_launches(1);
         e = cudaGetLastError();
-        if (e == cudaSuccess && w.hq && pl.variant == PcgLayout::kFactor)
+        if (e == cudaSuccess && (w.hq || fp32) && pl.variant == PcgLayout::kFactor)
             e = launch_pcg_factor_inner(bv, vv, w, pw, fb, pl, pcg_ctas, slot, maxiter, use_precond, s);
         else if (e == cudaSuccess)
             e = bf16 ? launch_ir_pcg<__nv_bfloat16>(bv, vv, w, fb, pw.error, maxiter, use_precond, s)

@@ -18,9 +18,13 @@
 //    and the error flag) on its stream before its kernel runs.  Calls whose
 //    kernels overlap on the GPU (two streams, or two host threads) race on
 //    the array and produce wrong results; serialise them.
-//  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture begins.
+//  * every call looks up the array's device address (cudaGetSymbolAddress)
+//    with the caller's device current; the first lookup on a device loads
+//    the module, so make that first call before any stream capture begins;
+//  * the caller keeps the system well formed: row_ptr[0] = 0, row_ptr
+//    non-decreasing with row_ptr[n] = nnzb, and 0 <= col_idx < n.  Indices
+//    outside that range are not checked on the device and read the wrong
+//    memory.
 //
 // The solve is the standard two-phase PCG (p = z + beta p, Ap, alpha; x, r
 // updates, z = M r, beta), one persistent cooperative kernel with a grid
@@ -28,7 +32,6 @@
 // vectors of other rows from global memory (no shared-memory windows, so the
 // caller's arrays need no padding).
 #include <algorithm>
-#include <mutex>
 #include <string>
 
 #include "internal.h"
@@ -343,11 +346,6 @@ __global__ void __launch_bounds__(kNaThreads, 1) pcg_noalloc_kernel(NaArgs a) {
     }
 }
 
-// Device address of the scratch array, looked up once per device.
-constexpr int kNaMaxDevices = 64;
-std::mutex g_na_mutex;
-void *g_na_scratch[kNaMaxDevices] = {};
-
 }  // namespace
 }  // namespace mfem
 
@@ -366,21 +364,18 @@ extern "C" int mfem_pcg_solve_noalloc(int32_t n, const int32_t *d_row_ptr, const
         return set_create_error(MFEM_BAD_ARG, "mfem_pcg_solve_noalloc: tol must be >= 0 and maxiter >= 0");
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= kNaMaxDevices)
+    if (e != cudaSuccess || dev < 0)
         return set_create_error(MFEM_CUDA_ERROR, "mfem_pcg_solve_noalloc: no usable current device");
+    // The scratch array's device address, looked up on every call with the
+    // caller's device current: after a cudaDeviceReset or in a new primary
+    // context the module may load at another address, so no address is
+    // cached.  Only the first lookup on a device loads the module (the reason
+    // that call must come before any stream capture); later ones are cheap.
     void *base = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_na_mutex);
-        if (!g_na_scratch[dev]) {
-            void *ptr = nullptr;
-            e = cudaGetSymbolAddress(&ptr, g_pcg_noalloc_scratch);
-            if (e != cudaSuccess)
-                return set_create_error(MFEM_CUDA_ERROR, std::string("mfem_pcg_solve_noalloc: cudaGetSymbolAddress: ") +
-                                                             cudaGetErrorString(e));
-            g_na_scratch[dev] = ptr;
-        }
-        base = g_na_scratch[dev];
-    }
+    e = cudaGetSymbolAddress(&base, g_pcg_noalloc_scratch);
+    if (e != cudaSuccess)
+        return set_create_error(MFEM_CUDA_ERROR,
+                                std::string("mfem_pcg_solve_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return set_create_error(MFEM_CUDA_ERROR, "mfem_pcg_solve_noalloc: device query failed");

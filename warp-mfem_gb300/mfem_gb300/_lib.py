@@ -113,7 +113,7 @@ class MfemMixedSolveStats(ctypes.Structure):
     ]
 
 
-PRECISION = {"fp32": 0, "bf16": 1, "fp16": 2}
+PRECISION = {"fp32": 0, "bf16": 1, "fp16": 2, "fp32_refined": 3}
 
 
 class MfemError(RuntimeError):
@@ -166,7 +166,15 @@ _SIGNATURES = {
     "mfem_global_solve": (ctypes.c_int, [_P, _I32, _P]),
     "mfem_local_solve": (ctypes.c_int, [_P, _P, _P]),
     "mfem_true_residual": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _P]),
+    "mfem_plan_set_residual_check": (ctypes.c_int, [_P, _I32]),
+    "mfem_plan_set_diagnostics": (ctypes.c_int, [_P, _I32]),
+    "mfem_step_true_residuals": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _I32, ctypes.POINTER(_I32),
+                                                _P]),
     "mfem_pcg_solve_noalloc": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _P, _F32, _I32, _P, _P]),
+    "mfem_train_gemm": (ctypes.c_int, [_I32, _I32, _I32, _P, _I32, _I32, _P, _I32, _I32, _P, _I32, _I32, _P, _I64,
+                                       _P]),
+    "mfem_train_adam": (ctypes.c_int, [_P, _P, _P, _P, _I64, _F32, _F32, _F32, _F32, _I32, _P]),
+    "mfem_train_last_error": (ctypes.c_char_p, []),
 }
 
 _lib = None

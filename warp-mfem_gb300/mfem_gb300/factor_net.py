@@ -255,18 +255,28 @@ def smooth_fields(rest_q: np.ndarray, k: int, rng, kmax: float = 1.5) -> np.ndar
     return out.astype(np.float32)
 
 
+def probe_vectors(G: Graph, s, rhs, k: int, generator=None):
+    """k unit vectors [n, 3, k] of the scaled system: the scaled rhs S g and
+    k - 1 normal ones."""
+    r = torch.randn(G.n, 3, k, device=rhs.device, generator=generator)
+    r[:, :, 0] = rhs * s[:, None]
+    return r / torch.linalg.vector_norm(r.reshape(-1, k), dim=0).clamp_min(1e-30)
+
+
 def loss(net: FactorNet, G: Graph, values, vstatic, rhs, k: int = 8, generator=None, smooth=None,
-         smooth_weight: float = 0.0):
+         smooth_weight: float = 0.0, r=None):
     """||r - K M r||^2 / ||r||^2 over k vectors r (the scaled rhs and normal
-    noise), plus, with ``smooth`` fields [n, 3, k'] and smooth_weight > 0,
-    that weight times ||z - M K z||^2 / ||z||^2 over the fields z (in the
-    scaled system's variables): the residual form with white noise weights
-    every eigenmode alike, the smooth term the low-frequency ones."""
+    noise, or the given r), plus, with ``smooth`` fields [n, 3, k'] and
+    smooth_weight > 0, that weight times ||z - M K z||^2 / ||z||^2 over the
+    fields z (in the scaled system's variables): the residual form with white
+    noise weights every eigenmode alike, the smooth term the low-frequency
+    ones.  A torch autograd expression: the float32 reference that the
+    hand-written training gradients (``HandGrad``) are checked against."""
     s, Ld, Lo = forward(net, G, values, vstatic)
     _, _, Ks = scaled_system(G, values)
-    r = torch.randn(G.n, 3, k, device=values.device, generator=generator)
-    r[:, :, 0] = rhs * s[:, None]
-    r = r / torch.linalg.vector_norm(r.reshape(-1, k), dim=0).clamp_min(1e-30)
+    if r is None:
+        r = probe_vectors(G, s, rhs, k, generator)
+    k = r.shape[2]
     res = r - apply_blocks(G, Ks, apply_scaled_M(G, Ld, Lo, r))
     out = (torch.linalg.vector_norm(res.reshape(-1, k), dim=0) ** 2).mean()
     if smooth is None or smooth_weight <= 0.0:
@@ -318,11 +328,220 @@ def solver_systems(mesh, n_steps: int, seed: int, device: str = "cuda:0", veloci
     return rp, ci, out, vs
 
 
+# -- hand-written training: BF16 tensor-core GEMMs, manual backward, Adam --
+def param_views(flat: torch.Tensor) -> dict:
+    """Views of a packed [N_PARAMS] tensor by LAYOUT name."""
+    out, o = {}, 0
+    for k, shape in LAYOUT:
+        m = int(np.prod(shape))
+        out[k] = flat[o:o + m].view(shape)
+        o += m
+    return out
+
+
+class TrainKernels:
+    """The library's training kernels through its C ABI: mfem_train_gemm
+    (BF16 operands, FP32 accumulation, tensor cores) and mfem_train_adam."""
+
+    def __init__(self, device):
+        from . import _lib
+        self._libmod = _lib
+        self.lib = _lib.load()
+        self.device = torch.device(device)
+        self.ws = torch.empty(1 << 22, dtype=torch.float32, device=self.device)  # split-K partials
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(f"training kernel failed ({rc}): {self.lib.mfem_train_last_error().decode()}")
+
+    def gemm(self, A, B, a_trans=False, b_trans=False, out=None, accumulate=False):
+        """op(A) op(B): op(A) = A [M, K] or A^T (A [K, M]); op(B) = B [K, N]
+        or B^T (B [N, K])."""
+        import ctypes
+        A = A.contiguous()
+        B = B.contiguous()
+        M, K = (A.shape[1], A.shape[0]) if a_trans else (A.shape[0], A.shape[1])
+        N = B.shape[0] if b_trans else B.shape[1]
+        if (B.shape[1] if b_trans else B.shape[0]) != K:
+            raise ValueError(f"inner dimensions differ: {tuple(A.shape)} {tuple(B.shape)}")
+        if out is None:
+            out = torch.empty(M, N, dtype=torch.float32, device=self.device)
+        P = lambda t: ctypes.c_void_p(t.data_ptr())
+        stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        self._check(self.lib.mfem_train_gemm(M, N, K, P(A), A.shape[1], int(a_trans), P(B), B.shape[1],
+                                             int(b_trans), P(out), out.shape[1], int(accumulate), P(self.ws),
+                                             self.ws.numel(), stream))
+        return out
+
+    def linear(self, x, W, b=None):
+        y = self.gemm(x, W, b_trans=True)
+        return y + b if b is not None else y
+
+    def adam(self, params, grads, m, v, lr, step, beta1=0.9, beta2=0.999, eps=1e-8):
+        import ctypes
+        P = lambda t: ctypes.c_void_p(t.data_ptr())
+        stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        self._check(self.lib.mfem_train_adam(P(params), P(grads), P(m), P(v), params.numel(), float(lr), beta1,
+                                             beta2, eps, int(step), stream))
+
+
+def net_inputs(G: Graph, Ks, d, vstatic):
+    """The 16 per-vertex inputs of the net (as ``forward``)."""
+    n = G.n
+    Kd = Ks[G.diag]
+    ld = torch.log10(torch.where(d > 0, d, torch.ones_like(d)))
+    offr, offc = G.rows[G.off], G.cols[G.off]
+    cnt = torch.zeros(n, device=Ks.device).index_add_(0, offr, torch.ones_like(offr, dtype=torch.float32))
+    ldn = torch.zeros(n, device=Ks.device).index_add_(0, offr, ld[offc]) / cnt.clamp_min(1.0)
+    x = torch.zeros(n, N_IN, device=Ks.device)
+    x[:, 0] = Kd[:, 0, 0] - 1.0
+    x[:, 1] = Kd[:, 1, 1] - 1.0
+    x[:, 2] = Kd[:, 2, 2] - 1.0
+    x[:, 3] = Kd[:, 0, 1]
+    x[:, 4] = Kd[:, 0, 2]
+    x[:, 5] = Kd[:, 1, 2]
+    x[:, 6] = torch.where(cnt > 0, ld - ldn, torch.zeros_like(ld))
+    x[:, 7:11] = vstatic
+    x[:, 11] = G.deg / 15.0
+    return x
+
+
+def _apply_LT(G: Graph, Ld, Lo, r):
+    """L~^T r for r [n, 3, k]."""
+    li, lj = G.rows[G.lo], G.cols[G.lo]
+    t = torch.einsum("nji,njk->nik", Ld, r)
+    return t.index_add(0, lj, torch.einsum("eji,ejk->eik", Lo, r[li]))
+
+
+def _apply_L(G: Graph, Ld, Lo, t):
+    """L~ t for t [n, 3, k]."""
+    li, lj = G.rows[G.lo], G.cols[G.lo]
+    y = torch.einsum("nij,njk->nik", Ld, t)
+    return y.index_add(0, li, torch.einsum("eij,ejk->eik", Lo, t[lj]))
+
+
+class HandGrad:
+    """Loss and gradient of the factor net written out by hand: the forward
+    pass keeps what the backward pass needs, every dense product (forward,
+    input gradient, weight gradient) runs on the library's BF16 tensor-core
+    GEMM, and the graph operations (gathers, scatter-adds, block products of
+    the loss) are explicit adjoints.  No autograd is involved."""
+
+    def __init__(self, kernels: TrainKernels):
+        self.tk = kernels
+
+    def forward(self, P: dict, G: Graph, values, vstatic):
+        tk = self.tk
+        s, d, Ks = scaled_system(G, values)
+        x = net_inputs(G, Ks, d, vstatic)
+        offr, offc = G.rows[G.off], G.cols[G.off]
+        w = torch.linalg.vector_norm(Ks[G.off].reshape(-1, 9), dim=1)
+        wsum = torch.zeros(G.n, device=values.device).index_add_(0, offr, w)
+        winv = torch.where(wsum > 0, 1.0 / wsum.clamp_min(1e-30), torch.zeros_like(wsum))
+        u = tk.linear(x, P["inp.weight"], P["inp.bias"])
+        h = torch.relu(u)
+        c = dict(x=x, m_in=u > 0, w=w, winv=winv, cats=[], masks=[])
+        for layer in range(3):
+            a = torch.zeros_like(h).index_add_(0, offr, w[:, None] * h[offc]) * winv[:, None]
+            cat = torch.cat([h, a], 1)
+            u = tk.linear(cat, P[f"mp.{layer}.weight"], P[f"mp.{layer}.bias"])
+            h = h + torch.relu(u)
+            c["cats"].append(cat)
+            c["masks"].append(u > 0)
+        o = tk.linear(h, P["diag.weight"], P["diag.bias"])
+        sp = nn.functional.softplus
+        z0 = torch.zeros(G.n, device=values.device)
+        Ld = torch.stack([torch.stack([sp(o[:, 0]), z0, z0], 1),
+                          torch.stack([o[:, 3], sp(o[:, 1]), z0], 1),
+                          torch.stack([o[:, 4], o[:, 5], sp(o[:, 2])], 1)], 1)
+        li, lj = G.rows[G.lo], G.cols[G.lo]
+        e = Ks[G.lo].reshape(-1, 9)
+        v = (tk.linear(h, P["P.weight"], P["P.bias"])[li] + tk.linear(h, P["Q.weight"])[lj] +
+             tk.linear(e, P["R.weight"]))
+        z = torch.relu(v)
+        Lo = tk.linear(z, P["out.weight"], P["out.bias"]).reshape(-1, 3, 3)
+        c.update(h=h, o=o, e=e, z=z, m_z=v > 0)
+        return s, Ks, Ld, Lo, c
+
+    def loss_and_grad(self, flat, grad, G: Graph, values, vstatic, r, smooth=None, smooth_weight: float = 0.0):
+        """The loss of ``loss`` (same r, same smooth fields) and its gradient
+        by the packed parameters, written into ``grad`` [N_PARAMS]."""
+        tk = self.tk
+        P, dP = param_views(flat), param_views(grad)
+        s, Ks, Ld, Lo, c = self.forward(P, G, values, vstatic)
+        li, lj = G.rows[G.lo], G.cols[G.lo]
+        dLd = torch.zeros_like(Ld)
+        dLo = torch.zeros_like(Lo)
+
+        # residual form: res = r - K L~ L~^T r
+        k = r.shape[2]
+        t = _apply_LT(G, Ld, Lo, r)
+        y = _apply_L(G, Ld, Lo, t)
+        res = r - apply_blocks(G, Ks, y)
+        total = (torch.linalg.vector_norm(res.reshape(-1, k), dim=0) ** 2).mean()
+        dy = -apply_blocks(G, Ks, (2.0 / k) * res)  # K is symmetric
+        pairs = [(dy, t, r)]
+        if smooth is not None and smooth_weight > 0.0:
+            zf = smooth / s[:, None, None]
+            kz = zf.shape[2]
+            zf = zf / torch.linalg.vector_norm(zf.reshape(-1, kz), dim=0).clamp_min(1e-30)
+            q = apply_blocks(G, Ks, zf)
+            t2 = _apply_LT(G, Ld, Lo, q)
+            err = zf - _apply_L(G, Ld, Lo, t2)
+            total = total + smooth_weight * (torch.linalg.vector_norm(err.reshape(-1, kz), dim=0) ** 2).mean()
+            pairs.append((-(2.0 * smooth_weight / kz) * err, t2, q))
+        # y = L~ t with t = L~^T q: dL~ = dy t^T + q (L~^T dy)^T on the pattern
+        for dyy, tt, qq in pairs:
+            dt = _apply_LT(G, Ld, Lo, dyy)
+            dLd += torch.einsum("nik,njk->nij", dyy, tt) + torch.einsum("nik,njk->nij", qq, dt)
+            dLo += torch.einsum("eik,ejk->eij", dyy[li], tt[lj]) + torch.einsum("eik,ejk->eij", qq[li], dt[lj])
+        # diagonal blocks from o (softplus on the diagonal)
+        o = c["o"]
+        do = torch.stack([dLd[:, 0, 0] * torch.sigmoid(o[:, 0]), dLd[:, 1, 1] * torch.sigmoid(o[:, 1]),
+                          dLd[:, 2, 2] * torch.sigmoid(o[:, 2]), dLd[:, 1, 0], dLd[:, 2, 0], dLd[:, 2, 1]], 1)
+        h = c["h"]
+        # off-diagonal blocks: Lo = W_o z + b_o, z = relu(P h_i + b_p + Q h_j + R e)
+        dLo9 = dLo.reshape(-1, 9)
+        dP["out.bias"].copy_(dLo9.sum(0))
+        tk.gemm(dLo9, c["z"], a_trans=True, out=dP["out.weight"])
+        dv = tk.gemm(dLo9, P["out.weight"]) * c["m_z"]
+        dPh = torch.zeros(G.n, WIDTH, device=h.device).index_add_(0, li, dv)
+        dQh = torch.zeros(G.n, WIDTH, device=h.device).index_add_(0, lj, dv)
+        tk.gemm(dv, c["e"], a_trans=True, out=dP["R.weight"])
+        dP["P.bias"].copy_(dPh.sum(0))
+        tk.gemm(dPh, h, a_trans=True, out=dP["P.weight"])
+        tk.gemm(dQh, h, a_trans=True, out=dP["Q.weight"])
+        dP["diag.bias"].copy_(do.sum(0))
+        tk.gemm(do, h, a_trans=True, out=dP["diag.weight"])
+        dh = tk.gemm(dPh, P["P.weight"])
+        tk.gemm(dQh, P["Q.weight"], out=dh, accumulate=True)
+        tk.gemm(do, P["diag.weight"], out=dh, accumulate=True)
+        # message-passing layers, last first: h' = h + relu(W [h, a] + b), a = A h
+        offr, offc = G.rows[G.off], G.cols[G.off]
+        w, winv = c["w"], c["winv"]
+        for layer in reversed(range(3)):
+            du = dh * c["masks"][layer]
+            dP[f"mp.{layer}.bias"].copy_(du.sum(0))
+            tk.gemm(du, c["cats"][layer], a_trans=True, out=dP[f"mp.{layer}.weight"])
+            dcat = tk.gemm(du, P[f"mp.{layer}.weight"])
+            da = dcat[:, WIDTH:] * winv[:, None]
+            dh = dh + dcat[:, :WIDTH]
+            dh = dh.index_add(0, offc, w[:, None] * da[offr])
+        du = dh * c["m_in"]
+        dP["inp.bias"].copy_(du.sum(0))
+        tk.gemm(du, c["x"], a_trans=True, out=dP["inp.weight"])
+        return float(total)
+
+
 def train(meshes, pairs: int = 2000, r_per_system: int = 8, epochs: int = 12, seed: int = 5,
-          device: str = "cuda:0", log=print, smooth_weight: float = 0.0) -> FactorNet:
+          device: str = "cuda:0", log=print, smooth_weight: float = 0.0, lr: float = 2e-3,
+          init: Optional[np.ndarray] = None) -> FactorNet:
     """Trains on about ``pairs`` (K, r) pairs: pairs / r_per_system systems
     drawn along trajectories of ``meshes``; smooth_weight > 0 adds the
-    smooth-field term of ``loss`` (8 fields a system)."""
+    smooth-field term of ``loss`` (8 fields a system).  The gradient is
+    ``HandGrad``'s and the update the library's Adam kernel, with a cosine
+    learning-rate schedule over the epochs; ``init`` starts from packed
+    parameters (default: FactorNet's block-Jacobi-like start)."""
     torch.manual_seed(seed)
     systems = []
     per_mesh = max(1, pairs // r_per_system // len(meshes))
@@ -338,24 +557,29 @@ def train(meshes, pairs: int = 2000, r_per_system: int = 8, epochs: int = 12, se
                   if smooth_weight > 0 else None)
             systems.append((G, vals, vst, rhs, sm))
         log(f"mesh {mesh.spec.name} {mesh.spec.cells}: {min(per_mesh, len(sysl))} systems")
-    net = FactorNet().to(device)
-    opt = torch.optim.Adam(net.parameters(), lr=2e-3)
-    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, epochs)
+    start = FactorNet().pack() if init is None else np.asarray(init, dtype=np.float32)
+    flat = torch.as_tensor(start, device=device).clone()
+    grad = torch.zeros_like(flat)
+    m1 = torch.zeros_like(flat)
+    m2 = torch.zeros_like(flat)
+    hg = HandGrad(TrainKernels(device))
     gen = torch.Generator(device=device)
     gen.manual_seed(seed)
-    for ep in range(epochs):
-        perm = np.random.default_rng(seed + ep).permutation(len(systems))
-        tot = 0.0
-        for i in perm:
-            G, vals, vst, rhs, sm = systems[i]
-            opt.zero_grad()
-            lv = loss(net, G, vals, vst, rhs, r_per_system, gen, sm, smooth_weight)
-            lv.backward()
-            opt.step()
-            tot += float(lv.detach())
-        sched.step()
-        log(f"epoch {ep}: loss {tot / len(systems):.4f}")
-    return net.cpu()
+    step = 0
+    with torch.no_grad():
+        for ep in range(epochs):
+            lr_ep = 0.5 * lr * (1.0 + math.cos(math.pi * ep / epochs))
+            perm = np.random.default_rng(seed + ep).permutation(len(systems))
+            tot = 0.0
+            for i in perm:
+                G, vals, vst, rhs, sm = systems[i]
+                s, _, _ = scaled_system(G, vals)
+                r = probe_vectors(G, s, rhs, r_per_system, gen)
+                tot += hg.loss_and_grad(flat, grad, G, vals, vst, r, sm, smooth_weight)
+                step += 1
+                hg.tk.adam(flat, grad, m1, m2, lr_ep, step)
+            log(f"epoch {ep}: loss {tot / len(systems):.4f}")
+    return FactorNet().unpack(flat.cpu().numpy())
 
 
 def main(argv=None):

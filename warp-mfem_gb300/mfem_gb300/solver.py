@@ -45,7 +45,9 @@ class MixedFEMSolver:
     16-bit BSR blocks with per-row scales in an inner PCG to
     ``inner_tolerance`` (1e-3) inside an fp64-residual iterative refinement
     to ``outer_tolerance`` (1e-8), at most ``outer_max_iterations`` (10)
-    corrections.
+    corrections.  "fp32_refined" runs the same refinement with the fp32
+    blocks in the inner PCG: the plain fp32 PCG brought to an fp64-checked
+    residual.
 
     ``preconditioner`` is the reference's flag (True: block-Jacobi, False:
     none), "fsai": a factorized sparse approximate inverse M = G^T G with G
@@ -331,6 +333,27 @@ class MixedFEMSolver:
         _lib.check(self._lib.mfem_true_residual(self._plan, ctypes.byref(out), _stream_handle(self.device)),
                    self._plan)
         return out.value
+
+    def set_diagnostics(self, on: bool) -> None:
+        """Turns on or off the element stage's diagnostic outputs (H_s^-1 and
+        g_lambda buffers, the reference's intermediates that the step does not
+        read)."""
+        _lib.check(self._lib.mfem_plan_set_diagnostics(self._plan, int(bool(on))), self._plan)
+
+    def set_residual_check(self, on: bool) -> None:
+        """Turns on or off the fp64 check of every global solve inside step()
+        (read back with step_true_residuals); the trajectory is unchanged."""
+        _lib.check(self._lib.mfem_plan_set_residual_check(self._plan, int(bool(on))), self._plan)
+
+    def step_true_residuals(self) -> list[float]:
+        """||g - H dx|| / ||g|| in float64 of each global solve of the last
+        step, for the float32 dx the local solve read (synchronises)."""
+        buf = (ctypes.c_double * max(1, self.iterations))()
+        count = ctypes.c_int32()
+        rc = self._lib.mfem_step_true_residuals(self._plan, buf, max(1, self.iterations), ctypes.byref(count),
+                                                _stream_handle(self.device))
+        _lib.check(rc, self._plan)
+        return [buf[i] for i in range(count.value)]
 
     # -- buffers ---------------------------------------------------------------
     _BUF_DTYPE = {"row_ptr": torch.int32, "col_idx": torch.int32, "tet_slots": torch.int32,
