@@ -592,9 +592,18 @@ def main(argv=None):
     ap.add_argument("--device", default="cuda:0")
     ap.add_argument("--smooth-weight", type=float, default=0.0,
                     help="weight of the smooth-field term of the loss (0: the residual form only)")
+    ap.add_argument("--lr", type=float, default=2e-3, help="peak Adam learning rate (cosine schedule)")
+    ap.add_argument("--init", default=None,
+                    help="start from these packed weights (.npz, 'shipped' for the package's) instead of "
+                         "the block-Jacobi-like start")
+    ap.add_argument("--seed", type=int, default=5)
     args = ap.parse_args(argv)
     meshes = [beams.build_beam("nh_beam"), beams.build_beam("stiff_beam")]
-    net = train(meshes, pairs=args.pairs, epochs=args.epochs, device=args.device, smooth_weight=args.smooth_weight)
+    init = None
+    if args.init:
+        init = load_weights(None if args.init == "shipped" else Path(args.init))
+    net = train(meshes, pairs=args.pairs, epochs=args.epochs, device=args.device, smooth_weight=args.smooth_weight,
+                lr=args.lr, init=init, seed=args.seed)
     np.savez(args.out, params=net.pack())
     print(f"wrote {args.out} ({N_PARAMS} parameters)")
 
