@@ -119,8 +119,8 @@ __device__ __forceinline__ float element_tet(const float *__restrict__ x, int en
 
     const float detF = em::deformation_det(xv, Dm);
     float c[6], G[6][12];
-    if (FP64) em::element_geometry_t<double>(xv, Dm, s, c, G);
-    else em::element_geometry_t<float>(xv, Dm, s, c, G);
+    if (FP64) em::element_geometry_t<double, true>(xv, Dm, s, c, G);
+    else em::element_geometry_t<float, true>(xv, Dm, s, c, G);
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
         tv.c[(size_t)i * T + t] = c[i];

@@ -110,7 +110,11 @@ MFEM_HD void sort_pair(Real d[3], Real V[3][3]) {
 // 3x3 matrices with minimal branching and elementary floating point
 // operations"): Jacobi eigen-analysis of F^T F gives V; a QR factorisation of
 // F V that keeps U a rotation gives U and the signed singular values.
-template <class Real>
+// ROLLED keeps the five sweeps as a loop (same operations in the same
+// order): the element kernel, whose fully unrolled body overflows the
+// instruction cache, takes it; the line-search trial, which unrolled needs
+// fewer registers, does not.
+template <class Real, bool ROLLED = false>
 MFEM_HD void polar_svd(const Real F[3][3], Real U[3][3], Real sig[3], Real V[3][3]) {
     Real A[3][3];
 #pragma unroll
@@ -122,11 +126,20 @@ MFEM_HD void polar_svd(const Real F[3][3], Real U[3][3], Real sig[3], Real V[3][
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) V[i][j] = (i == j) ? Real(1) : Real(0);
+    if (ROLLED) {
+#pragma unroll 1
+        for (int sweep = 0; sweep < 5; ++sweep) {
+            jacobi_rotate<0, 1, Real>(A, V);
+            jacobi_rotate<0, 2, Real>(A, V);
+            jacobi_rotate<1, 2, Real>(A, V);
+        }
+    } else {
 #pragma unroll
-    for (int sweep = 0; sweep < 5; ++sweep) {
-        jacobi_rotate<0, 1, Real>(A, V);
-        jacobi_rotate<0, 2, Real>(A, V);
-        jacobi_rotate<1, 2, Real>(A, V);
+        for (int sweep = 0; sweep < 5; ++sweep) {
+            jacobi_rotate<0, 1, Real>(A, V);
+            jacobi_rotate<0, 2, Real>(A, V);
+            jacobi_rotate<1, 2, Real>(A, V);
+        }
     }
     Real d[3] = {A[0][0], A[1][1], A[2][2]};
     sort_pair<0, 1, Real>(d, V);
@@ -460,13 +473,13 @@ constexpr float kPolarFp64Det = 1.0e-3f;
 // (the reference's compute_constraints, src/mfem/refinement/kernels.py:
 // 131-169), the polar decomposition and dS/dF evaluated in Real, c and G
 // rounded to float.
-template <class Real>
+template <class Real, bool ROLLED = false>
 MFEM_HD void element_geometry_t(const float x[4][3], const float Dm[3][3], const float s[6], float c[6],
                                 float G[6][12]) {
     Real F[3][3];
     deformation_gradient<Real>(x, Dm, F);
     Real U[3][3], sig[3], V[3][3];
-    polar_svd<Real>(F, U, sig, V);
+    polar_svd<Real, ROLLED>(F, U, sig, V);
     Real sF[6];
     stretch_sym6<Real>(sig, V, sF);
 #pragma unroll
