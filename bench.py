@@ -718,7 +718,79 @@ def extra_workloads(dev, steps=3):
     out["stiff_beam"] = sb
     del mesh
     out["batched512"] = {pc: measure_batched(dev, pc, steps) for pc in ("block_jacobi", "fsai")}
+    out["refinement"] = measure_refinement(dev)
     return out
+
+
+def measure_refinement(dev, strain_steps=5, repeats=5):
+    """One adaptive-refinement pass on the Neo-Hookean beam after a few
+    steps of strain: the device time of mfem_refine (legacy scores, tet
+    weight 1, threshold 0, so every strained edge competes and the selection
+    splits a maximal conflict-free set), then the host rebuild of the plan on
+    the refined mesh and the step rate there."""
+    import ctypes
+
+    import torch
+    from mfem_gb300 import MixedFEMSolver, Model, beams
+    mesh = beams.build_beam("nh_beam")
+    # a tet holds at most one split edge, so 2 T tets always suffice
+    model = Model.from_beam(mesh, device=dev).pad_particles(4 * mesh.n)
+    solver = MixedFEMSolver(model, iterations=mesh.spec.iterations, energy=mesh.spec.energy, line_search=False,
+                            max_tets=2 * mesh.T, enable_refinement=True, refine_every_n_steps=10 ** 9,
+                            refine_tet_score_weight=1.0, min_refine_score=0.0,
+                            refine_density=float(mesh.spec.density))
+    solver._refine_pass = 1  # no pass during the strain steps
+    s0, s1 = model.state(), model.state()
+    dt = mesh.spec.dt
+    for _ in range(strain_steps):
+        solver.step(s0, s1, None, None, dt)
+        s0, s1 = s1, s0
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    q = s0.particle_q.clone()
+    qd = s0.particle_qd.clone()
+    call = lambda: solver._lib.mfem_refine(solver._plan, ctypes.byref(solver.refine_config), None,
+                                           ctypes.c_void_p(q.data_ptr()), ctypes.c_void_p(qd.data_ptr()), None,
+                                           ctypes.byref(solver._rmesh_struct), ctypes.c_void_p(stream.cuda_stream))
+    assert call() == 0  # builds the edge lists
+    times = []
+    for _ in range(repeats):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        assert call() == 0
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    counts = solver._rmesh["counts"].cpu().tolist()
+    T0, n0 = solver.active_tet_count, solver.active_particle_count
+    s1.assign(s0)
+    solver._refine_pass = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    solver._refine(s0, s1)
+    torch.cuda.synchronize()
+    rebuild_s = time.perf_counter() - t0
+    s0.assign(s1)
+    solver._refine_pass = 1
+    for _ in range(2):
+        solver.step(s0, s1, None, None, dt)
+        s0, s1 = s1, s0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(strain_steps):
+        solver.step(s0, s1, None, None, dt)
+        s0, s1 = s1, s0
+    torch.cuda.synchronize()
+    rate = strain_steps / (time.perf_counter() - t0)
+    finite = bool(torch.isfinite(s0.particle_q[:solver.active_particle_count]).all().item())
+    return {"workload": f"nh_beam after {strain_steps} steps, legacy scores (tet weight 1, threshold 0), "
+                        "5 selection sweeps",
+            "pass_ms": statistics.median(times), "pass_ms_all": times, "split_edges": int(counts[3]),
+            "tets": [T0, int(counts[1])], "vertices": [n0, int(counts[0])],
+            "rebuild_ms": 1000.0 * rebuild_s,
+            "rebuild": "host: copy the refined mesh back, build a new plan (sparsity, slot maps, PCG layout), "
+                       "carry s and lambda over",
+            "refined_steps_per_s": rate, "refined_state_finite": finite}
 
 
 def measure_batched(dev, pc, steps, B=512):

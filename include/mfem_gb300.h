@@ -498,6 +498,100 @@ int mfem_plan_set_residual_check(mfem_plan *plan, int32_t on);
 int mfem_step_true_residuals(mfem_plan *plan, double *h_rel_residual, int32_t max_entries, int32_t *count,
                              mfem_stream stream);
 
+/* ---- adaptive refinement ------------------------------------------------- */
+
+typedef enum mfem_refine_scoring {
+    MFEM_REFINE_LEGACY = 0,     /* refinement.py:74-121: sum over an edge's tets of
+                                   (E_t w_t + min(vs_a, vs_b) w_v) L; an edge whose
+                                   midpoint is inside a shape scores penetrating_edge_score */
+    MFEM_REFINE_GEOMETRIC = 1   /* refinement.py:157-316: max over an edge's tets and
+                                   surface tris of (L/h)(L/L_max)(w_e s_elastic + w_c s_contact) */
+} mfem_refine_scoring;
+
+/* refine()'s settings (src/mfem/refinement/refinement.py:914-940) with
+ * RefinementSolver's refine_* kwargs (src/mfem/refinement/solver.py:56-87). */
+typedef struct mfem_refine_config {
+    int32_t scoring;                /* mfem_refine_scoring                                     */
+    float threshold;                /* an edge is a candidate when its score exceeds it:
+                                       min_refine_score (10.1) for legacy scores,
+                                       refine_geometric_threshold (1.0) for geometric ones      */
+    float tet_score_weight;         /* legacy: refine_tet_score_weight, default 0             */
+    float vertex_score_weight;      /* legacy: refine_vertex_score_weight, default 0.1        */
+    float penetrating_edge_score;   /* legacy: default 1e6                                     */
+    float min_edge_length;          /* geometric h: edges shorter than 2h are never split      */
+    float contact_d1;               /* geometric: the contact barrier range                    */
+    float elastic_weight;           /* geometric: refine_elastic_weight, default 1             */
+    float vertex_contact_weight;    /* geometric: refine_contact_weight, default 1             */
+    float tri_contact_weight;       /* geometric: refine_tri_contact_weight, default 1         */
+    float split_position;           /* new vertex at q_lo + (q_hi - q_lo) t, default 0.5       */
+    float density;                  /* lumped masses of a refined mesh: density * volume / 4   */
+    int32_t conflict_iterations;    /* selection sweeps, default 5                             */
+    int32_t refine_every;           /* with a pass counter: split only on passes whose counter
+                                       is a multiple (refine_every_n_steps, default 10)       */
+    int32_t reserved[4];
+} mfem_refine_config;
+
+/* Optional per-element inputs of the scores, device arrays over the plan's
+ * current mesh (refine()'s tet_scores / vertex_scores / particle_distance /
+ * particle_shape_id / tri_distance / tri_bary).  NULL: the library computes
+ * them at the positions given to mfem_refine, from the plan's s (elastic
+ * energy per tet) and its contact shapes (barrier energy per vertex plus the
+ * tris' weighted barrier energies; nearest-shape distance and shape; tri
+ * distance and closest-point weights). */
+typedef struct mfem_refine_inputs {
+    const float *tet_scores;          /* [T]                                           */
+    const float *vertex_scores;       /* [n] legacy                                    */
+    const float *particle_distance;   /* [n] geometric                                 */
+    const int32_t *particle_shape_id; /* [n] geometric, index into the plan's shapes   */
+    const float *tri_distance;        /* [m] geometric                                 */
+    const float *tri_bary;            /* [m][3] geometric                              */
+} mfem_refine_inputs;
+
+/* The refined mesh: caller-owned device arrays of capacity max_* rows that
+ * receive the mesh after the pass (a copy of the plan's mesh when the pass
+ * splits nothing).  tris receives the plan's contact tris and may be NULL
+ * when the plan has none.  counts (device, 8 int32) receives: particles,
+ * tets, tris of the result, edges split, 1 if the pass was dropped for
+ * capacity, 1 if the pass was a refining one, 0, 0. */
+typedef struct mfem_refine_mesh {
+    int32_t max_particles, max_tets, max_tris;
+    int32_t reserved;
+    int32_t *tet_indices;     /* [max_tets][4]                                          */
+    float *tet_poses;         /* [max_tets][3][3] DmInv                                 */
+    float *tet_materials;     /* [max_tets][3]                                          */
+    float *tet_stretch;       /* [max_tets][6] s, the parent's for both children        */
+    float *tet_lambda;        /* [max_tets][6] lambda, likewise                         */
+    float *rest_q;            /* [max_particles][3]                                     */
+    float *particle_mass;     /* [max_particles]                                        */
+    float *particle_inv_mass; /* [max_particles]                                        */
+    int32_t *tri_indices;     /* [max_tris][3] or NULL                                  */
+    int32_t *counts;          /* [8]                                                    */
+} mfem_refine_mesh;
+
+void mfem_refine_config_default(mfem_refine_config *cfg);
+
+/* One refine() pass (src/mfem/refinement/refinement.py:914-1322) over the
+ * plan's mesh at positions d_q, velocities d_qd ([max_particles][3]; rows
+ * [0, n) are read, and the new vertices' rows [n, n + new) are written there,
+ * at split_position along their edges).  Edges are scored, each tet picks its
+ * best edge above the threshold, conflicts are resolved over
+ * conflict_iterations sweeps so that no tet holds two, and every tet and
+ * contact tri around a selected edge splits in two.  The selection is
+ * deterministic (ranked by score, ties by the smaller vertex pair) where the
+ * reference's depends on thread order; new vertices are numbered in
+ * ascending (lower vertex, higher vertex) order; a splitting pass rebuilds
+ * the lumped masses from density (vertices with inv_mass 0 stay kinematic).
+ * A pass that would exceed a capacity is dropped whole, as the reference's.
+ * With d_pass_counter (device int32, may be NULL) only passes whose counter
+ * is a multiple of refine_every split, and the counter advances by one
+ * (refinement.py:560-575).  The plan itself is unchanged: create a plan
+ * from the refined mesh to step it.  The first call on a plan builds its edge
+ * lists (synchronises and allocates); later calls are asynchronous on
+ * `stream` and allocate only when max_tets grows.  Plans with bodies
+ * (mfem_plan_set_bodies) are not refined. */
+int mfem_refine(mfem_plan *plan, const mfem_refine_config *cfg, const mfem_refine_inputs *inputs, float *d_q,
+                float *d_qd, int32_t *d_pass_counter, const mfem_refine_mesh *out, mfem_stream stream);
+
 /* ---- allocation-free solve ---------------------------------------------- */
 
 /* Block-Jacobi PCG on a caller-provided 3x3-block BSR system that allocates

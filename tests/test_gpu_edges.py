@@ -107,8 +107,11 @@ def test_bad_arguments_raise():
         solver.step(s0, type(s0)(bad, s0.particle_qd), None, None, 0.01)
     with pytest.raises(_lib.MfemError):
         solver.step(s0, model.state(), None, None, -1.0)
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(ValueError, match="max_tets"):
         MixedFEMSolver(model, iterations=2, enable_refinement=True)
+    with pytest.raises(ValueError, match="refine_scoring"):
+        MixedFEMSolver(model, iterations=2, enable_refinement=True, max_tets=model.tet_count,
+                       refine_scoring="nearest")
     with pytest.raises(_lib.MfemError):
         MixedFEMSolver(model, iterations=2, line_search_max_iterations=-1)
     with pytest.raises(ValueError):

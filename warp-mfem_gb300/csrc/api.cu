@@ -78,6 +78,16 @@ struct mfem_plan {
     std::vector<int32_t> h_body_row, h_body_nnzb, h_body_its;
     bool global_memory_pcg = false;  // the mesh is solved as a one-body batch
     int32_t *tet_slots = nullptr;
+    float *rest_q = nullptr;    // [n][3] rest positions
+    float *inv_mass = nullptr;  // [n] particle_inv_mass as given
+    float *mass = nullptr;      // [n] particle_mass as given
+    std::vector<int32_t> h_tris;  // the contact tris, host copy
+    // adaptive refinement (mfem_refine): edge lists built on the first call
+    RefineViews rv{};
+    bool refine_ready = false;
+    int64_t refine_tmass_cap = 0;
+    int64_t refine_scan_cap = 0;
+    std::vector<void *> refine_allocs;
     double *resid = nullptr;
     // per-solve fp64 check of the step's global solves (mfem_plan_set_residual_check)
     double *check_resid = nullptr;  // [max_stats][2]: ||g - H dx||^2, ||g||^2
@@ -420,6 +430,7 @@ void mfem_plan_destroy(mfem_plan *p) {
         for (void *a : p->batch_allocs) cudaFree(a);
         for (void *a : p->layout_allocs) cudaFree(a);
         for (void *a : p->net_allocs) cudaFree(a);
+        for (void *a : p->refine_allocs) cudaFree(a);
     }
     delete p;
 }
@@ -507,6 +518,7 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
     ALLOC(pk, nn);
     ALLOC(pt, nn * 3);
     ALLOC(rest, nn * 3);
+    ALLOC(p->inv_mass, nn);
     ALLOC(p->vv.x_tilde, nn * 3);
     ALLOC(p->vv.x_start, nn * 3);
     ALLOC(p->vv.rhs, nn * 3);
@@ -646,6 +658,7 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
     if (e == cudaSuccess) e = upload(pk, pin_k.data(), nn);
     if (e == cudaSuccess) e = upload(pt, h_rest_q, nn * 3);
     if (e == cudaSuccess) e = upload(rest, h_rest_q, nn * 3);
+    if (e == cudaSuccess) e = upload(p->inv_mass, h_inv_mass, nn);
     if (e == cudaSuccess) e = upload(row_ptr, sym.row_ptr.data(), nn + 1);
     if (e == cudaSuccess) e = upload(col_idx, sym.col_idx.data(), nz);
     if (e == cudaSuccess) e = upload(chunk_ptr, sym.chunk_ptr.data(), (size_t)n_chunks + 1);
@@ -672,6 +685,8 @@ int mfem_plan_create(const mfem_config *cfg_in, int32_t n, int32_t T, const int3
     p->tv.tets = tets;
     p->tv.dminv = dminv;
     p->tv.materials = materials;
+    p->rest_q = rest;
+    p->mass = mass;
     p->vv.n = n;
     p->vv.mass = mass;
     p->vv.hess_diag = hd;
@@ -948,6 +963,8 @@ int mfem_plan_set_contact(mfem_plan *p, const mfem_contact_config *cfg_in, int32
     p->bv.n_chunks = p->base_chunks;
     p->n_bodies = 0;
     p->n_tris = 0;
+    p->h_tris.clear();
+    p->refine_ready = false;
     if (n_shapes == 0) return MFEM_OK;  // contact off
 
     const size_t n = p->n;
@@ -1064,6 +1081,8 @@ int mfem_plan_set_contact(mfem_plan *p, const mfem_contact_config *cfg_in, int32
     }
     p->n_bodies = n_bodies;
     p->n_tris = m;
+    p->h_tris.assign(h_tris, h_tris + (size_t)m * 3);
+    p->refine_ready = false;  // the refinement's tri edge lists follow the tris
     return MFEM_OK;
 }
 
@@ -1870,6 +1889,274 @@ int mfem_true_residual(mfem_plan *p, double *h_rel, mfem_stream stream) {
     if (e != cudaSuccess) return cuda_fail(p, e, "true_residual");
     *h_rel = out[1] > 0.0 ? std::sqrt(out[0] / out[1]) : std::sqrt(out[0]);
     return MFEM_OK;
+}
+
+}  // extern "C"
+
+// ---- adaptive refinement -------------------------------------------------
+
+namespace {
+
+// Per-edge and per-vertex tet lists of the plan's mesh in ascending tet
+// order, each tet's and tri's edge slots, and the work arrays of a pass.
+int refine_prepare(mfem_plan *p) {
+    if (p->refine_ready) return MFEM_OK;
+    for (void *a : p->refine_allocs) cudaFree(a);
+    p->refine_allocs.clear();
+    p->refine_tmass_cap = 0;
+    const int n = p->n, T = p->T, m = p->n_tris;
+    const int64_t nnzb = p->nnzb;
+    std::vector<int32_t> slot_row(nnzb), tet_edge((size_t)T * 6), tri_edge((size_t)m * 3);
+    for (int r = 0; r < n; ++r)
+        for (int k = p->h_row_ptr[r]; k < p->h_row_ptr[r + 1]; ++k) slot_row[k] = r;
+    static const int pi[6] = {1, 2, 2, 3, 3, 3}, pj[6] = {0, 0, 1, 0, 1, 2};
+    for (int t = 0; t < T; ++t) {
+        const int32_t *v = p->h_tets.data() + 4 * (size_t)t;
+        const int32_t *sl = p->h_tet_slots.data() + 16 * (size_t)t;
+        for (int q = 0; q < 6; ++q) {
+            const int i = pi[q], j = pj[q];
+            tet_edge[6 * (size_t)t + q] = v[i] < v[j] ? sl[4 * i + j] : sl[4 * j + i];
+        }
+    }
+    auto slot_of = [&](int a, int b) -> int32_t {
+        if (a > b) std::swap(a, b);
+        const int32_t *lo = p->h_col_idx.data() + p->h_row_ptr[a], *hi = p->h_col_idx.data() + p->h_row_ptr[a + 1];
+        const int32_t *it = std::lower_bound(lo, hi, b);
+        return (it != hi && *it == b) ? (int32_t)(it - p->h_col_idx.data()) : -1;
+    };
+    for (int t = 0; t < m; ++t) {
+        const int32_t *v = p->h_tris.data() + 3 * (size_t)t;
+        for (int q = 0; q < 3; ++q) {
+            const int32_t s = slot_of(v[pi[q]], v[pj[q]]);
+            if (s < 0) return fail(p, MFEM_BAD_ARG, "a contact tri joins vertices that share no tet");
+            tri_edge[3 * (size_t)t + q] = s;
+        }
+    }
+    // counting sorts keep ascending tet order within each edge and vertex
+    std::vector<int32_t> edge_start(nnzb + 1, 0), edge_tet((size_t)T * 6);
+    for (size_t i = 0; i < tet_edge.size(); ++i) edge_start[tet_edge[i] + 1]++;
+    for (int64_t s = 0; s < nnzb; ++s) edge_start[s + 1] += edge_start[s];
+    {
+        std::vector<int32_t> fill(edge_start.begin(), edge_start.end() - 1);
+        for (int t = 0; t < T; ++t)
+            for (int q = 0; q < 6; ++q) edge_tet[fill[tet_edge[6 * (size_t)t + q]]++] = t;
+    }
+    std::vector<int32_t> vert_start(n + 1, 0), vert_code((size_t)T * 4);
+    for (size_t i = 0; i < (size_t)T * 4; ++i) vert_start[p->h_tets[i] + 1]++;
+    for (int v = 0; v < n; ++v) vert_start[v + 1] += vert_start[v];
+    {
+        std::vector<int32_t> fill(vert_start.begin(), vert_start.end() - 1);
+        for (int t = 0; t < T; ++t)
+            for (int k = 0; k < 4; ++k) vert_code[fill[p->h_tets[4 * (size_t)t + k]]++] = 4 * t + k;
+    }
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](auto **ptr, size_t count) {
+        if (e != cudaSuccess) return;
+        void *raw = nullptr;
+        e = cudaMalloc(&raw, std::max<size_t>(count, 1) * sizeof(**ptr));
+        if (e == cudaSuccess) {
+            p->refine_allocs.push_back(raw);
+            *ptr = static_cast<std::remove_reference_t<decltype(*ptr)>>(raw);
+        }
+    };
+    RefineViews rv{};
+    int32_t *d_slot_row = nullptr, *d_tet_edge = nullptr, *d_tri_edge = nullptr, *d_es = nullptr, *d_et = nullptr,
+            *d_vs = nullptr, *d_vc = nullptr;
+    alloc(&d_slot_row, nnzb);
+    alloc(&d_tet_edge, (size_t)T * 6);
+    alloc(&d_tri_edge, (size_t)m * 3);
+    alloc(&d_es, nnzb + 1);
+    alloc(&d_et, (size_t)T * 6);
+    alloc(&d_vs, n + 1);
+    alloc(&d_vc, (size_t)T * 4);
+    alloc(&rv.e_tet, T);
+    alloc(&rv.dens, T);
+    alloc(&rv.lmax, T);
+    alloc(&rv.vscore, n);
+    alloc(&rv.vdist, n);
+    alloc(&rv.vsid, n);
+    alloc(&rv.tdist, m);
+    alloc(&rv.tbary, (size_t)m * 3);
+    alloc(&rv.tenergy, m);
+    const int stat_blocks = std::max(1, (T + 255) / 256);
+    alloc(&rv.partials, stat_blocks);
+    alloc(&rv.mean_density, 1);
+    alloc(&rv.score, nnzb);
+    alloc(&rv.state, nnzb);
+    alloc(&rv.blocked, nnzb);
+    alloc(&rv.cand, T);
+    alloc(&rv.split_slot, T);
+    alloc(&rv.split_pair, T);
+    alloc(&rv.tet_cnt, (size_t)T + 1);
+    alloc(&rv.edge_cnt, nnzb + 1);
+    alloc(&rv.tri_slot, m);
+    alloc(&rv.tri_cnt, (size_t)m + 1);
+    const int64_t longest = std::max<int64_t>({(int64_t)T, nnzb, (int64_t)m});
+    rv.scan_tmp_len = (longest + 1023) / 1024 + 2;
+    alloc(&rv.scan_tmp, rv.scan_tmp_len);
+    alloc(&rv.ctrl, kRefineCtrl);
+    if (e == cudaSuccess) e = upload(d_slot_row, slot_row.data(), nnzb);
+    if (e == cudaSuccess) e = upload(d_tet_edge, tet_edge.data(), tet_edge.size());
+    if (e == cudaSuccess) e = upload(d_tri_edge, tri_edge.data(), tri_edge.size());
+    if (e == cudaSuccess) e = upload(d_es, edge_start.data(), edge_start.size());
+    if (e == cudaSuccess) e = upload(d_et, edge_tet.data(), edge_tet.size());
+    if (e == cudaSuccess) e = upload(d_vs, vert_start.data(), vert_start.size());
+    if (e == cudaSuccess) e = upload(d_vc, vert_code.data(), vert_code.size());
+    if (e == cudaSuccess) e = cudaMemset(rv.split_pair, 0, std::max<size_t>(T, 1) * sizeof(int));
+    if (e != cudaSuccess) {
+        for (void *a : p->refine_allocs) cudaFree(a);
+        p->refine_allocs.clear();
+        return cuda_fail(p, e, "refinement buffers");
+    }
+    rv.n = n;
+    rv.T = T;
+    rv.m = m;
+    rv.nnzb = nnzb;
+    rv.energy = p->cfg.energy;
+    rv.tets = p->tv.tets;
+    rv.dminv = p->tv.dminv;
+    rv.materials = p->tv.materials;
+    rv.stretch = p->tv.stretch;
+    rv.lambda = p->tv.lambda;
+    rv.rest = p->rest_q;
+    rv.mass = p->mass;
+    rv.inv_mass = p->inv_mass;
+    rv.tris = p->cv.tris;
+    rv.col_idx = p->bv.col_idx;
+    rv.slot_row = d_slot_row;
+    rv.tet_edge = d_tet_edge;
+    rv.tri_edge = d_tri_edge;
+    rv.edge_start = d_es;
+    rv.edge_tet = d_et;
+    rv.vert_start = d_vs;
+    rv.vert_code = d_vc;
+    p->rv = rv;
+    p->refine_ready = true;
+    return MFEM_OK;
+}
+
+bool finite_all(std::initializer_list<float> v) {
+    for (float x : v)
+        if (!std::isfinite(x)) return false;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+void mfem_refine_config_default(mfem_refine_config *cfg) {
+    if (!cfg) return;
+    *cfg = mfem_refine_config{};
+    cfg->scoring = MFEM_REFINE_LEGACY;
+    cfg->threshold = 10.1f;
+    cfg->tet_score_weight = 0.0f;
+    cfg->vertex_score_weight = 0.1f;
+    cfg->penetrating_edge_score = 1.0e6f;
+    cfg->min_edge_length = 0.1f;
+    cfg->contact_d1 = 0.1f;
+    cfg->elastic_weight = 1.0f;
+    cfg->vertex_contact_weight = 1.0f;
+    cfg->tri_contact_weight = 1.0f;
+    cfg->split_position = 0.5f;
+    cfg->density = 1.0f;
+    cfg->conflict_iterations = 5;
+    cfg->refine_every = 10;
+}
+
+int mfem_refine(mfem_plan *p, const mfem_refine_config *cfg_in, const mfem_refine_inputs *inputs, float *d_q,
+                float *d_qd, int32_t *d_pass_counter, const mfem_refine_mesh *out, mfem_stream stream) {
+    if (!p) return MFEM_BAD_ARG;
+    mfem_refine_config cfg;
+    if (cfg_in) cfg = *cfg_in;
+    else mfem_refine_config_default(&cfg);
+    if (!d_q || !d_qd || !out) return fail(p, MFEM_BAD_ARG, "mfem_refine: q, qd and out are required");
+    if (cfg.scoring != MFEM_REFINE_LEGACY && cfg.scoring != MFEM_REFINE_GEOMETRIC)
+        return fail(p, MFEM_BAD_ARG, "mfem_refine: unknown scoring");
+    if (!finite_all({cfg.threshold, cfg.tet_score_weight, cfg.vertex_score_weight, cfg.penetrating_edge_score,
+                     cfg.min_edge_length, cfg.contact_d1, cfg.elastic_weight, cfg.vertex_contact_weight,
+                     cfg.tri_contact_weight, cfg.split_position, cfg.density}))
+        return fail(p, MFEM_BAD_ARG, "mfem_refine: non-finite setting");
+    if (cfg.scoring == MFEM_REFINE_GEOMETRIC && !(cfg.min_edge_length > 0.0f && cfg.contact_d1 > 0.0f))
+        return fail(p, MFEM_BAD_ARG, "mfem_refine: geometric scoring needs min_edge_length > 0 and contact_d1 > 0");
+    if (!(cfg.density > 0.0f)) return fail(p, MFEM_BAD_ARG, "mfem_refine: density must be > 0");
+    if (cfg.conflict_iterations < 0 || cfg.conflict_iterations > 1000 || cfg.refine_every < 0)
+        return fail(p, MFEM_BAD_ARG, "mfem_refine: conflict_iterations in [0, 1000], refine_every >= 0");
+    if (p->bw.n_bodies > 1) return fail(p, MFEM_BAD_ARG, "mfem_refine: plans with several bodies are not refined");
+    if (out->max_particles < p->n || out->max_tets < p->T || out->max_tris < p->n_tris)
+        return fail(p, MFEM_BAD_ARG, "mfem_refine: the output capacities are below the plan's mesh");
+    if (!out->tet_indices || !out->tet_poses || !out->tet_materials || !out->tet_stretch || !out->tet_lambda ||
+        !out->rest_q || !out->particle_mass || !out->particle_inv_mass || !out->counts ||
+        (p->n_tris > 0 && !out->tri_indices))
+        return fail(p, MFEM_BAD_ARG, "mfem_refine: NULL output array");
+    int rc = refine_prepare(p);
+    if (rc != MFEM_OK) return rc;
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaSuccess;
+    if (out->max_tets > p->refine_tmass_cap) {
+        float *tm = nullptr;
+        e = cudaMalloc(&tm, (size_t)std::max(out->max_tets, 1) * sizeof(float));
+        if (e != cudaSuccess) return cuda_fail(p, e, "mfem_refine: cudaMalloc");
+        if (p->rv.tmass) {
+            // a pass still in flight may read the old array
+            cudaError_t se = cudaStreamSynchronize((cudaStream_t)stream);
+            if (se != cudaSuccess) {
+                cudaFree(tm);
+                return cuda_fail(p, se, "mfem_refine: cudaStreamSynchronize");
+            }
+            auto it = std::find(p->refine_allocs.begin(), p->refine_allocs.end(), (void *)p->rv.tmass);
+            if (it != p->refine_allocs.end()) p->refine_allocs.erase(it);
+            cudaFree(p->rv.tmass);
+        }
+        p->refine_allocs.push_back(tm);
+        p->rv.tmass = tm;
+        p->refine_tmass_cap = out->max_tets;
+    }
+    RefineViews rv = p->rv;
+    if (inputs) {
+        rv.tet_scores = inputs->tet_scores;
+        rv.vertex_scores = inputs->vertex_scores;
+        rv.particle_distance = inputs->particle_distance;
+        rv.particle_shape_id = inputs->particle_shape_id;
+        rv.tri_distance = inputs->tri_distance;
+        rv.tri_bary = inputs->tri_bary;
+    }
+    if (cfg.scoring == MFEM_REFINE_GEOMETRIC && (!rv.tri_distance) != (!rv.tri_bary))
+        return fail(p, MFEM_BAD_ARG, "mfem_refine: give both tri_distance and tri_bary, or neither");
+    RefineParams rp{};
+    rp.scoring = cfg.scoring;
+    rp.threshold = cfg.threshold;
+    rp.tet_w = cfg.tet_score_weight;
+    rp.vert_w = cfg.vertex_score_weight;
+    rp.pen_score = cfg.penetrating_edge_score;
+    rp.min_edge = cfg.min_edge_length;
+    rp.d1 = cfg.contact_d1;
+    rp.el_w = cfg.elastic_weight;
+    rp.vc_w = cfg.vertex_contact_weight;
+    rp.tri_w = cfg.tri_contact_weight;
+    rp.split_t = cfg.split_position;
+    rp.density = cfg.density;
+    rp.sweeps = cfg.conflict_iterations;
+    rp.refine_every = cfg.refine_every;
+    rp.max_particles = out->max_particles;
+    rp.max_tets = out->max_tets;
+    rp.max_tris = out->max_tris;
+    RefineOut ro{};
+    ro.tets = out->tet_indices;
+    ro.poses = out->tet_poses;
+    ro.materials = out->tet_materials;
+    ro.stretch = out->tet_stretch;
+    ro.lambda = out->tet_lambda;
+    ro.rest = out->rest_q;
+    ro.mass = out->particle_mass;
+    ro.inv_mass = out->particle_inv_mass;
+    ro.tris = out->tri_indices;
+    ro.counts = out->counts;
+    ro.q = d_q;
+    ro.qd = d_qd;
+    e = launch_refine(rv, p->cv, rp, d_pass_counter, ro, (cudaStream_t)stream);
+    return e == cudaSuccess ? MFEM_OK : cuda_fail(p, e, "mfem_refine");
 }
 
 }  // extern "C"

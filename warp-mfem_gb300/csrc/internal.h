@@ -291,6 +291,69 @@ struct PcgLayout {
     size_t smem = 0;           // dynamic shared memory per CTA
 };
 
+// One edge-bisection pass of adaptive refinement (refine.cu) over a plan's
+// mesh.  Edges are the upper off-diagonal slots of H's sparsity (row < col),
+// so a slot index doubles as the edge's id and ascending slots are ascending
+// (min vertex, max vertex) keys.
+constexpr int kRefineCtrl = 4;  // device control words: refining pass, pass applied
+struct RefineViews {
+    // the plan's mesh
+    int n, T, m;
+    int64_t nnzb;
+    int energy;
+    const int4 *tets;
+    const float *dminv, *materials, *stretch, *lambda;
+    const float *rest, *mass, *inv_mass;  // [n][3], [n], [n]
+    const int *tris;                      // [m][3] (the plan's contact tris)
+    const int *col_idx;                   // [nnzb]
+    const int *slot_row;                  // [nnzb] row of each slot
+    const int *tet_edge;                  // [T][6] edge of local pair (1,0) (2,0) (2,1) (3,0) (3,1) (3,2)
+    const int *tri_edge;                  // [m][3] edge of local pair (1,0) (2,0) (2,1)
+    const int *edge_start;                // [nnzb + 1] tets of each edge, ascending, in edge_tet
+    const int *edge_tet;                  // [6 T]
+    const int *vert_start;                // [n + 1] tets of each vertex, ascending, in vert_code
+    const int *vert_code;                 // [4 T] tet * 4 + corner
+    // optional inputs (null: computed from the plan's state and contact)
+    const float *tet_scores, *vertex_scores, *particle_distance, *tri_distance, *tri_bary;
+    const int *particle_shape_id;
+    // work
+    float *e_tet, *dens, *lmax;          // [T]
+    float *vscore, *vdist;               // [n]
+    int *vsid;                           // [n]
+    float *tdist, *tbary, *tenergy;      // [m], [m][3], [m]
+    double *partials;                    // [stat blocks]
+    float *mean_density;                 // [1]
+    float *score;                        // [nnzb]
+    unsigned char *state, *blocked;      // [nnzb]
+    int *cand, *split_slot, *split_pair; // [T]
+    int *tet_cnt;                        // [T + 1] 1 + split, then its exclusive scan
+    int *edge_cnt;                       // [nnzb + 1] selected, then its exclusive scan
+    int *tri_slot;                       // [m]
+    int *tri_cnt;                        // [m + 1]
+    int *scan_tmp;                       // block sums of the scans
+    int64_t scan_tmp_len;
+    float *tmass;                        // [max_tets] lumped mass of each new tet
+    int *ctrl;                           // [kRefineCtrl]
+};
+
+struct RefineParams {
+    int scoring;  // 0 legacy, 1 geometric
+    float threshold, tet_w, vert_w, pen_score, min_edge, d1, el_w, vc_w, tri_w, split_t, density;
+    int sweeps, refine_every;
+    int max_particles, max_tets, max_tris;
+};
+
+struct RefineOut {
+    int *tets;
+    float *poses, *materials, *stretch, *lambda, *rest, *mass, *inv_mass;
+    int *tris;
+    int *counts;
+    float *q, *qd;  // the caller's positions and velocities, rows [n, n + new) written
+};
+
+cudaError_t launch_refine(const RefineViews &rv, const ContactViews &cv, const RefineParams &rp, int *pass_counter,
+                          const RefineOut &out, cudaStream_t s);
+
 // Host-side symbolic analysis (symbolic.cpp).
 struct Symbolic {
     std::vector<int32_t> row_ptr, col_idx, tet_slots;

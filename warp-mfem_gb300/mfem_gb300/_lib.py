@@ -115,6 +115,58 @@ class MfemMixedSolveStats(ctypes.Structure):
 
 PRECISION = {"fp32": 0, "bf16": 1, "fp16": 2, "fp32_refined": 3}
 
+REFINE_SCORING = {"legacy": 0, "geometric": 1}
+
+
+class MfemRefineConfig(ctypes.Structure):
+    _fields_ = [
+        ("scoring", ctypes.c_int32),
+        ("threshold", ctypes.c_float),
+        ("tet_score_weight", ctypes.c_float),
+        ("vertex_score_weight", ctypes.c_float),
+        ("penetrating_edge_score", ctypes.c_float),
+        ("min_edge_length", ctypes.c_float),
+        ("contact_d1", ctypes.c_float),
+        ("elastic_weight", ctypes.c_float),
+        ("vertex_contact_weight", ctypes.c_float),
+        ("tri_contact_weight", ctypes.c_float),
+        ("split_position", ctypes.c_float),
+        ("density", ctypes.c_float),
+        ("conflict_iterations", ctypes.c_int32),
+        ("refine_every", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 4),
+    ]
+
+
+class MfemRefineInputs(ctypes.Structure):
+    _fields_ = [
+        ("tet_scores", ctypes.c_void_p),
+        ("vertex_scores", ctypes.c_void_p),
+        ("particle_distance", ctypes.c_void_p),
+        ("particle_shape_id", ctypes.c_void_p),
+        ("tri_distance", ctypes.c_void_p),
+        ("tri_bary", ctypes.c_void_p),
+    ]
+
+
+class MfemRefineMesh(ctypes.Structure):
+    _fields_ = [
+        ("max_particles", ctypes.c_int32),
+        ("max_tets", ctypes.c_int32),
+        ("max_tris", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("tet_indices", ctypes.c_void_p),
+        ("tet_poses", ctypes.c_void_p),
+        ("tet_materials", ctypes.c_void_p),
+        ("tet_stretch", ctypes.c_void_p),
+        ("tet_lambda", ctypes.c_void_p),
+        ("rest_q", ctypes.c_void_p),
+        ("particle_mass", ctypes.c_void_p),
+        ("particle_inv_mass", ctypes.c_void_p),
+        ("tri_indices", ctypes.c_void_p),
+        ("counts", ctypes.c_void_p),
+    ]
+
 
 class MfemError(RuntimeError):
     def __init__(self, code: int, message: str):
@@ -170,6 +222,9 @@ _SIGNATURES = {
     "mfem_plan_set_diagnostics": (ctypes.c_int, [_P, _I32]),
     "mfem_step_true_residuals": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _I32, ctypes.POINTER(_I32),
                                                 _P]),
+    "mfem_refine_config_default": (None, [ctypes.POINTER(MfemRefineConfig)]),
+    "mfem_refine": (ctypes.c_int, [_P, ctypes.POINTER(MfemRefineConfig), ctypes.POINTER(MfemRefineInputs), _P, _P,
+                                   _P, ctypes.POINTER(MfemRefineMesh), _P]),
     "mfem_pcg_solve_noalloc": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _P, _F32, _I32, _P, _P]),
     "mfem_train_gemm": (ctypes.c_int, [_I32, _I32, _I32, _P, _I32, _I32, _P, _I32, _I32, _P, _I32, _I32, _P, _I64,
                                        _P]),

@@ -111,6 +111,27 @@ class Model:
     def set_tri_indices(self, tris) -> None:
         self.tri_indices = torch.as_tensor(np.asarray(tris, dtype=np.int32), device=self.device).reshape(-1, 3)
 
+    def pad_particles(self, max_particles: int) -> "Model":
+        """The same model with its particle arrays padded to `max_particles`
+        rows (zero position, velocity and mass, inverse mass 0): the headroom
+        an adaptive refinement grows into, as the reference's
+        ``load_sim_model(..., max_particles=...)`` pads Newton's particle
+        buffer (src/mfem/refinement/models/refinement_model.py:104-143)."""
+        n = self.particle_count
+        if max_particles < n:
+            raise ValueError(f"max_particles={max_particles} is below particle_count={n}")
+        pad = max_particles - n
+
+        def grow(t):
+            return torch.cat([t, torch.zeros((pad,) + tuple(t.shape[1:]), dtype=t.dtype, device=t.device)])
+
+        out = Model(grow(self.particle_q), grow(self.particle_qd), grow(self.particle_mass),
+                    grow(self.particle_inv_mass), self.tet_indices, self.tet_poses, self.tet_materials, self.gravity,
+                    device=self.device)
+        for name in ("shape_transform", "shape_type", "shape_scale", "shape_body", "body_q", "tri_indices"):
+            setattr(out, name, getattr(self, name).clone())
+        return out
+
     def state(self) -> State:
         return State(self.particle_q.clone(), self.particle_qd.clone(),
                      self.body_q.clone() if self.body_count > 0 else None)

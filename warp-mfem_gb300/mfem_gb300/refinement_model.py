@@ -111,8 +111,7 @@ class MFEMRefinementModel:
 
     def sim_arrays(self, mu: float, rotate: bool = True):
         """Host arrays of the simulation model the reference builds with
-        ``load_sim_model`` (refinement_model.py:104-143; no padding: this
-        solver does not refine): rest positions, DmInv, materials with `mu`,
+        ``load_sim_model`` (refinement_model.py:104-143; unpadded): rest positions, DmInv, materials with `mu`,
         lumped masses and inverse masses."""
         x = np.asarray(self.particles, dtype=np.float64)
         if rotate:
@@ -132,8 +131,13 @@ class MFEMRefinementModel:
         return (x.astype(np.float32), tets.astype(np.int32), np.linalg.inv(Dm).astype(np.float32),
                 materials.astype(np.float32), mass.astype(np.float32), inv_mass.astype(np.float32))
 
-    def load_sim_model(self, mu: float, gravity=(0.0, -9.81, 0.0), device="cuda:0", rotate: bool = True):
+    def load_sim_model(self, mu: float, gravity=(0.0, -9.81, 0.0), device="cuda:0", rotate: bool = True,
+                       max_particles: int | None = None):
+        """``max_particles`` pads the particle arrays for refinement
+        (refinement_model.py:104-143); None (the default here) leaves them
+        unpadded, which is what a solver without refinement wants."""
         from .model import Model
         x, tets, dminv, materials, mass, inv_mass = self.sim_arrays(mu, rotate)
-        return Model(x, np.zeros_like(x), mass, inv_mass, tets, dminv, materials,
-                     np.asarray(gravity, dtype=np.float32), device=device)
+        model = Model(x, np.zeros_like(x), mass, inv_mass, tets, dminv, materials,
+                      np.asarray(gravity, dtype=np.float32), device=device)
+        return model.pad_particles(max_particles) if max_particles is not None else model

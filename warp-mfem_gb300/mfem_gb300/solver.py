@@ -16,9 +16,7 @@ import torch
 from . import _lib
 from .model import Model, State
 
-_OUT_OF_SCOPE_TRUE = {
-    "enable_refinement": "adaptive refinement",
-}
+_REFINE_COUNTS = 8  # mfem_refine_mesh.counts
 
 
 def _stream_handle(device: torch.device) -> int:
@@ -61,6 +59,27 @@ class MixedFEMSolver:
     ``factor_refresh`` k recomputes the factor at every k-th Newton
     iteration of a step (default 1: every assembly).
 
+    ``enable_refinement=True`` (default False here; the reference defaults to
+    True but, with its default weights and no contact, never splits) runs an
+    edge-bisection refinement pass on the GPU (``mfem_refine``) at the start
+    of every ``refine_every_n_steps``-th step, counted from the first, with
+    the reference's ``refine_*`` kwargs (solver.py:56-87): ``refine_scoring``
+    "legacy" (threshold ``min_refine_score``) or "geometric" (threshold
+    ``refine_geometric_threshold``), ``refine_tet_score_weight``,
+    ``refine_vertex_score_weight``, ``penetrating_edge_score``,
+    ``refine_min_edge_length`` (default ``contact_d1``),
+    ``refine_elastic_weight``, ``refine_contact_weight``,
+    ``refine_tri_contact_weight``, ``refine_conflict_iterations``,
+    ``refine_split_position`` and ``refine_density`` (the lumped masses of a
+    refined mesh; default 1.0 as the reference's).  As in the reference the
+    model's particle arrays are padded to ``max_particles`` rows and the
+    mesh's vertices are those its tets reference; states carry all
+    ``max_particles`` rows and ``max_tets`` bounds the tets.  A pass that
+    splits edges writes the new vertices into state_out and state_in (the
+    reference copies them into state_in too, solver.py:500) and rebuilds the
+    plan on the refined mesh, carrying s and lambda over; the host reads the
+    pass's counts back, so a refining step synchronises.
+
     ``pcg_variant``: "auto" (default), "standard", "single_reduction",
     "gather" (block-Jacobi / no preconditioner), "factor" (the persistent
     factor PCG) or "global_memory" (the batched kernel's PCG on one body).
@@ -69,9 +88,6 @@ class MixedFEMSolver:
     def __init__(self, model: Model, iterations: int, max_tets: Optional[int] = None,
                  max_particles: Optional[int] = None, max_tris: Optional[int] = None,
                  refine_every_n_steps: int = 10, min_refine_score: float = 10.1, **kwargs):
-        for key, what in _OUT_OF_SCOPE_TRUE.items():
-            if kwargs.get(key, False):
-                raise NotImplementedError(f"{key}=True: {what} is not part of this solver")
         if kwargs.get("shell_mu", 0.0) != 0.0:
             raise NotImplementedError("shell_mu > 0: the membrane shell is not part of this solver")
         if max_particles is not None and max_particles != model.particle_count:
@@ -79,6 +95,9 @@ class MixedFEMSolver:
                 f"max_particles={max_particles} does not match model.particle_count={model.particle_count}")
         if max_tets is not None and max_tets < model.tet_count:
             raise ValueError(f"max_tets={max_tets} is below model.tet_count={model.tet_count}")
+        self.refine_enabled = bool(kwargs.get("enable_refinement", False))
+        if self.refine_enabled and max_tets is None:
+            raise ValueError("enable_refinement=True needs max_tets")
         energy = kwargs.get("energy", "arap")
         if energy not in _lib.ENERGY:
             raise ValueError(f"Unknown energy type: {energy}")
@@ -116,17 +135,44 @@ class MixedFEMSolver:
         cfg.line_search_threshold = float(kwargs.get("line_search_threshold", 1.0e-8))
         self.config = cfg
 
+        self.solver_precision = kwargs.get("solver_precision", "fp32")
+        if self.solver_precision not in _lib.PRECISION:
+            raise ValueError(f"Unknown solver_precision {self.solver_precision!r}")
+        self._kwargs = dict(kwargs)
+        self._residual_check = False
+        self._diagnostics = False
+        self._plan = None
+
         host = lambda t, dt: np.ascontiguousarray(t.detach().to("cpu").numpy(), dtype=dt)
-        self._host = dict(
+        h = dict(
             tets=host(model.tet_indices, np.int32), poses=host(model.tet_poses, np.float32),
             materials=host(model.tet_materials, np.float32), rest=host(model.particle_q, np.float32),
             mass=host(model.particle_mass, np.float32), inv_mass=host(model.particle_inv_mass, np.float32),
             gravity=host(model.gravity.reshape(-1)[:3], np.float32))
+        tris = getattr(model, "tri_indices", None)
+        h["tris"] = host(tris, np.int32).reshape(-1, 3) if tris is not None else np.zeros((0, 3), np.int32)
+        self.max_particles = model.particle_count
+        if self.refine_enabled:
+            # the mesh's vertices are those its tets reference (get_active_particles,
+            # additional_state.py:7-15); the rest of the particle arrays is headroom
+            n_active = int(h["tets"].max()) + 1 if h["tets"].size else model.particle_count
+            for key in ("rest", "mass", "inv_mass"):
+                h[key] = np.ascontiguousarray(h[key][:n_active])
+        self._host = h
+        self._create_plan(model)
+        if self.refine_enabled:
+            self._init_refinement(model, max_tets, max_tris, refine_every_n_steps, min_refine_score, kwargs)
+
+    def _create_plan(self, model) -> None:
+        """Plan of the mesh in self._host, with the contact, factor net and
+        solver settings of the constructor's arguments."""
         h = self._host
+        kwargs = self._kwargs
         plan = ctypes.c_void_p()
         P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        n_rows = h["rest"].shape[0]
         rc = self._lib.mfem_plan_create(
-            ctypes.byref(cfg), model.particle_count, model.tet_count, P(h["tets"]), P(h["poses"]),
+            ctypes.byref(self.config), n_rows, h["tets"].shape[0], P(h["tets"]), P(h["poses"]),
             P(h["materials"]), P(h["rest"]), P(h["mass"]), P(h["inv_mass"]), P(h["gravity"]),
             self.device.index if self.device.index is not None else torch.cuda.current_device(), ctypes.byref(plan))
         if rc != _lib.MFEM_OK:
@@ -141,12 +187,9 @@ class MixedFEMSolver:
         self.n_bodies = 0
         self.n_contact_tris = 0
         if getattr(model, "shape_count", 0) > 0:
-            self._set_contact(model, kwargs)
-        if cfg.preconditioner == _lib.PRECONDITIONER["learned"]:
+            self._set_contact(model, kwargs, h["tris"])
+        if self.config.preconditioner == _lib.PRECONDITIONER["learned"]:
             self.set_factor_net(kwargs.get("factor_net_params"))
-        self.solver_precision = kwargs.get("solver_precision", "fp32")
-        if self.solver_precision not in _lib.PRECISION:
-            raise ValueError(f"Unknown solver_precision {self.solver_precision!r}")
         if self.solver_precision != "fp32" or "factor_refresh" in kwargs:
             scfg = _lib.MfemSolverConfig()
             self._lib.mfem_solver_config_default(ctypes.byref(scfg))
@@ -156,6 +199,116 @@ class MixedFEMSolver:
             scfg.outer_tolerance = float(kwargs.get("outer_tolerance", 1.0e-8))
             scfg.outer_max_iterations = int(kwargs.get("outer_max_iterations", 10))
             _lib.check(self._lib.mfem_plan_set_solver(self._plan, ctypes.byref(scfg)), self._plan)
+        if self._residual_check:
+            self.set_residual_check(True)
+        if self._diagnostics:
+            self.set_diagnostics(True)
+
+    # -- adaptive refinement -----------------------------------------------------
+    def _init_refinement(self, model, max_tets, max_tris, refine_every_n_steps, min_refine_score, kwargs) -> None:
+        """Capacity buffers and settings of the refinement passes
+        (RefinementSolver.__init__, src/mfem/refinement/solver.py:56-87, 139-170)."""
+        self._model = model
+        self.max_tets = int(max_tets)
+        headroom = max(1, -(-self.max_tets // max(1, model.tet_count)))
+        self.max_tris = int(max_tris) if max_tris else int(self._host["tris"].shape[0]) * headroom
+        self.refine_every_n_steps = int(refine_every_n_steps)
+        scoring = kwargs.get("refine_scoring", "legacy")
+        if scoring not in _lib.REFINE_SCORING:
+            raise ValueError(f"Unknown refine_scoring {scoring!r} (expected 'legacy' or 'geometric')")
+        rc = _lib.MfemRefineConfig()
+        self._lib.mfem_refine_config_default(ctypes.byref(rc))
+        rc.scoring = _lib.REFINE_SCORING[scoring]
+        rc.threshold = float(kwargs.get("refine_geometric_threshold", 1.0) if scoring == "geometric"
+                             else min_refine_score)
+        rc.tet_score_weight = float(kwargs.get("refine_tet_score_weight", 0.0))
+        rc.vertex_score_weight = float(kwargs.get("refine_vertex_score_weight", 0.1))
+        rc.penetrating_edge_score = float(kwargs.get("penetrating_edge_score", 1.0e6))
+        d1 = float(kwargs.get("contact_d1", 1.0e-1))
+        min_edge = kwargs.get("refine_min_edge_length", None)
+        rc.min_edge_length = float(min_edge) if min_edge is not None else d1
+        rc.contact_d1 = d1
+        rc.elastic_weight = float(kwargs.get("refine_elastic_weight", 1.0))
+        rc.vertex_contact_weight = float(kwargs.get("refine_contact_weight", 1.0))
+        rc.tri_contact_weight = float(kwargs.get("refine_tri_contact_weight", 1.0))
+        rc.split_position = float(kwargs.get("refine_split_position", 0.5))
+        rc.density = float(kwargs.get("refine_density", 1.0))
+        rc.conflict_iterations = int(kwargs.get("refine_conflict_iterations", 5))
+        rc.refine_every = max(self.refine_every_n_steps, 1)
+        self.refine_config = rc
+        self._refine_pass = 0
+        self.refine_history: list[dict] = []
+        dev = self.device
+        z = lambda shape, dt: torch.zeros(shape, dtype=dt, device=dev)
+        self._rmesh = dict(tets=z((self.max_tets, 4), torch.int32), poses=z((self.max_tets, 9), torch.float32),
+                           materials=z((self.max_tets, 3), torch.float32),
+                           stretch=z((self.max_tets, 6), torch.float32), lam=z((self.max_tets, 6), torch.float32),
+                           rest=z((self.max_particles, 3), torch.float32), mass=z((self.max_particles,), torch.float32),
+                           inv_mass=z((self.max_particles,), torch.float32),
+                           tris=z((max(self.max_tris, 1), 3), torch.int32), counts=z((_REFINE_COUNTS,), torch.int32))
+        r = self._rmesh
+        m = _lib.MfemRefineMesh()
+        m.max_particles, m.max_tets, m.max_tris = self.max_particles, self.max_tets, self.max_tris
+        for field, key in (("tet_indices", "tets"), ("tet_poses", "poses"), ("tet_materials", "materials"),
+                           ("tet_stretch", "stretch"), ("tet_lambda", "lam"), ("rest_q", "rest"),
+                           ("particle_mass", "mass"), ("particle_inv_mass", "inv_mass"), ("tri_indices", "tris"),
+                           ("counts", "counts")):
+            setattr(m, field, r[key].data_ptr())
+        self._rmesh_struct = m
+
+    @property
+    def active_particle_count(self) -> int:
+        return self.n
+
+    @property
+    def active_tet_count(self) -> int:
+        return self.T
+
+    def _refine(self, state_in: State, state_out: State) -> None:
+        """One refinement pass at state_out (= state_in) and, when it splits
+        edges, the plan rebuilt on the refined mesh."""
+        every = max(self.refine_every_n_steps, 1)
+        refining = self._refine_pass % every == 0
+        self._refine_pass += 1
+        if not refining:
+            return
+        stream = _stream_handle(self.device)
+        rc = self._lib.mfem_refine(self._plan, ctypes.byref(self.refine_config), None,
+                                   ctypes.c_void_p(state_out.particle_q.data_ptr()),
+                                   ctypes.c_void_p(state_out.particle_qd.data_ptr()), None,
+                                   ctypes.byref(self._rmesh_struct), stream)
+        _lib.check(rc, self._plan)
+        counts = self._rmesh["counts"].cpu().tolist()
+        n_new, T_new, m_new, split, overflow = counts[:5]
+        self.refine_history.append(dict(pass_index=self._refine_pass - 1, split_edges=split, overflow=bool(overflow),
+                                        particles=n_new, tets=T_new, tris=m_new))
+        if split == 0:
+            return
+        n_old = self.n
+        r = self._rmesh
+        host = lambda t: np.ascontiguousarray(t.cpu().numpy())
+        self._host = dict(tets=host(r["tets"][:T_new]), poses=host(r["poses"][:T_new]),
+                          materials=host(r["materials"][:T_new]), rest=host(r["rest"][:n_new]),
+                          mass=host(r["mass"][:n_new]), inv_mass=host(r["inv_mass"][:n_new]),
+                          gravity=self._host["gravity"],
+                          tris=host(r["tris"][:m_new]) if self.n_contact_tris > 0 else self._host["tris"])
+        stretch = r["stretch"][:T_new].clone()
+        lam = r["lam"][:T_new].clone()
+        torch.cuda.current_stream(self.device).synchronize()
+        self.close()
+        self._create_plan(self._model)
+        self.write_buffer("tet_stretch", stretch.reshape(-1))
+        self.write_buffer("tet_lambda", lam.reshape(-1))
+        state_in.particle_q[n_old:n_new].copy_(state_out.particle_q[n_old:n_new])
+        state_in.particle_qd[n_old:n_new].copy_(state_out.particle_qd[n_old:n_new])
+
+    def refined_mesh(self) -> dict:
+        """The current mesh as host arrays (tets, DmInv, materials, rest
+        positions, masses, inverse masses, contact tris) and s, lambda."""
+        out = {k: v.copy() for k, v in self._host.items() if k != "gravity"}
+        out["tet_stretch"] = self.tet_stretch.cpu().numpy()
+        out["tet_lambda"] = self.tet_lambda.cpu().numpy()
+        return out
 
     def set_factor_net(self, params=None, vertex_offsets=None) -> None:
         """Loads the learned preconditioner's parameters (packed float32,
@@ -174,7 +327,7 @@ class MixedFEMSolver:
                                                       params.size, vs.ctypes.data_as(ctypes.c_void_p)),
                    self._plan)
 
-    def _set_contact(self, model, kwargs) -> None:
+    def _set_contact(self, model, kwargs, tris) -> None:
         """Contact against the model's shapes (Contact.__init__,
         src/mfem/refinement/contact.py:778-862)."""
         ccfg = _lib.MfemContactConfig()
@@ -191,8 +344,7 @@ class MixedFEMSolver:
         elif mu.shape[0] != S:
             raise ValueError(f"friction_mu has {mu.shape[0]} entries but the model has {S} shapes")
         host = lambda t, dt: np.ascontiguousarray(t.detach().to("cpu").numpy(), dtype=dt)
-        tris = getattr(model, "tri_indices", None)
-        tris = host(tris, np.int32).reshape(-1, 3) if tris is not None else np.zeros((0, 3), np.int32)
+        tris = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
         self._contact_host = dict(type=host(model.shape_type, np.int32), pose=host(model.shape_transform, np.float32),
                                   scale=host(model.shape_scale, np.float32), body=host(model.shape_body, np.int32),
                                   mu=np.ascontiguousarray(mu), tris=np.ascontiguousarray(tris))
@@ -252,8 +404,9 @@ class MixedFEMSolver:
             pass
 
     def _check_state(self, t: torch.Tensor, name: str) -> int:
-        if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and tuple(t.shape) == (self.n, 3)):
-            raise ValueError(f"{name} must be a contiguous float32 CUDA tensor of shape ({self.n}, 3)")
+        rows = self.max_particles if self.refine_enabled else self.n
+        if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and tuple(t.shape) == (rows, 3)):
+            raise ValueError(f"{name} must be a contiguous float32 CUDA tensor of shape ({rows}, 3)")
         if t.device != self.device:
             raise ValueError(f"{name} lives on {t.device}, the solver on {self.device}")
         return t.data_ptr()
@@ -266,6 +419,13 @@ class MixedFEMSolver:
         qd_in = self._check_state(state_in.particle_qd, "state_in.particle_qd")
         q_out = self._check_state(state_out.particle_q, "state_out.particle_q")
         qd_out = self._check_state(state_out.particle_qd, "state_out.particle_qd")
+        if self.refine_enabled:
+            # refinement writes the new vertices into state_out first
+            # (solver.py:443-500)
+            state_out.assign(state_in)
+            if self.n_bodies > 0 and getattr(state_out, "body_q", None) is not None:
+                self.set_body_poses(state_out.body_q)
+            self._refine(state_in, state_out)
         if self.n_bodies > 0 and getattr(state_out, "body_q", None) is not None:
             # the reference reads the rigid bodies' poses from state_out
             self.set_body_poses(state_out.body_q)
@@ -339,11 +499,13 @@ class MixedFEMSolver:
         g_lambda buffers, the reference's intermediates that the step does not
         read)."""
         _lib.check(self._lib.mfem_plan_set_diagnostics(self._plan, int(bool(on))), self._plan)
+        self._diagnostics = bool(on)
 
     def set_residual_check(self, on: bool) -> None:
         """Turns on or off the fp64 check of every global solve inside step()
         (read back with step_true_residuals); the trajectory is unchanged."""
         _lib.check(self._lib.mfem_plan_set_residual_check(self._plan, int(bool(on))), self._plan)
+        self._residual_check = bool(on)
 
     def step_true_residuals(self) -> list[float]:
         """||g - H dx|| / ||g|| in float64 of each global solve of the last
