@@ -1174,11 +1174,11 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
     alloc(&w.best, sizeof(double));
     alloc(&w.stats, (size_t)p->max_stats * sizeof(IrStats));
     alloc(&w.scale, 2 * sizeof(float));
-    // a plan on the persistent factor PCG runs its inner solves there, on an
-    // fp32 copy of the 16-bit blocks (the same rounding)
+    // a plan on the persistent factor PCG runs its inner solves there, on a
+    // copy of the 16-bit blocks padded to 20 bytes (4-byte aligned loads)
     if (!refined32 && (p->pl.variant == PcgLayout::kFactor || p->ir_pl.variant == PcgLayout::kFactor) &&
         p->cfg.preconditioner >= 1)
-        alloc(&w.hq, nz * 9 * sizeof(float));
+        alloc(&w.hq_words, nz * 5 * sizeof(uint32_t));
     int max_ctas = 1;
     if (e == cudaSuccess) e = ir_max_ctas(p->device, &max_ctas);
     if (e == cudaSuccess) e = cudaMemset(w.counter, 0, sizeof(unsigned long long));

@@ -269,7 +269,8 @@ struct IrWork {
     double *best;              // [1] smallest fp64 relative residual of the solve so far
     IrStats *stats;            // [max solves per step]
     // inner solves in the persistent factor PCG (a plan with pcg_variant 4):
-    float *hq;                 // [nnzb][9] the 16-bit blocks times their row scale, as fp32 (else null)
+    uint32_t *hq_words;        // [nnzb][5] the 16-bit blocks as pairs in words, nine values and a zero
+                               // (20 bytes, 4-byte aligned), for the persistent factor PCG (else null)
     float *scale;              // [2] 1 / ||r|| and ||r|| of the latest fp64 residual
 };
 

@@ -62,6 +62,7 @@ template <bool CACHE>
 __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     PCG_PROLOGUE
+    const HBlocks hf32{a.values, nullptr, nullptr, 0};
     const int rows_max = a.rows_max, win_max = a.win_max;
     // own rows
     float *sX = reinterpret_cast<float *>(smem);
@@ -84,7 +85,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
     const int own = cm.row_lo - cm.win_lo;  // offset of the own rows inside the window
     const uint32_t wbytes = (uint32_t)cm.nwin * 12u;
 
-    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE, a.values);
+    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE, HBlocks{a.values, nullptr, nullptr, 0});
     // window of M^-1 blocks (kept for the whole solve) and of the warm start
     bool ok = true;
     if (threadIdx.x == 0 && cm.nwin > 0) {
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
     // ---- r0 = g - H x0, published
     if (ok) {
         for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = wR[3 * own + i];
-        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wR, sW, a.values);
+        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wR, sW, hf32, cm.row_lo);
         __syncthreads();
         float acc[1] = {0.0f};
         for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) {
@@ -133,7 +134,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
             wW[3 * j + 2] = u[2];
         }
         __syncthreads();
-        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wW, sW, a.values);
+        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wW, sW, hf32, cm.row_lo);
         __syncthreads();
         float acc[3] = {0.0f, 0.0f, 0.0f};
         for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) {
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
             ps[(size_t)3 * cm.row_lo + i] = wS[3 * own + i];
         }
         // w' = H u'
-        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wW, sW, a.values);
+        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wW, sW, hf32, cm.row_lo);
         __syncthreads();
         float *pw = pubW[(it + 1) & 1];
         float acc[3] = {0.0f, 0.0f, 0.0f};
@@ -278,6 +279,7 @@ template <bool CACHE>
 __global__ void __launch_bounds__(kPcgThreads, 1) pcg_standard_kernel(PcgArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     PCG_PROLOGUE
+    const HBlocks hf32{a.values, nullptr, nullptr, 0};
     const int rows_max = a.rows_max, win_max = a.win_max;
     float *sX = reinterpret_cast<float *>(smem);
     float *sR = sX + 3 * rows_max;
@@ -295,7 +297,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_standard_kernel(PcgArgs a)
     const int own = cm.row_lo - cm.win_lo;
     const uint32_t wbytes = (uint32_t)cm.nwin * 12u;
 
-    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE, a.values);
+    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE, HBlocks{a.values, nullptr, nullptr, 0});
     for (int i = threadIdx.x; i < 9 * cm.nrows; i += blockDim.x) sM[i] = a.Minv[(size_t)9 * cm.row_lo + i];
     bool ok = true;
     if (threadIdx.x == 0 && cm.nwin > 0) {
@@ -307,7 +309,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_standard_kernel(PcgArgs a)
     int it = 0;
     if (ok) {
         for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = winA[3 * own + i];
-        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp, a.values);
+        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp, hf32, cm.row_lo);
         __syncthreads();
         float acc[3] = {0.0f, 0.0f, 0.0f};
         for (int i = threadIdx.x; i < cm.nrows; i += blockDim.x) {
@@ -375,7 +377,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_standard_kernel(PcgArgs a)
         __syncthreads();
         for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x)
             p_new[(size_t)3 * cm.row_lo + i] = winA[3 * own + i];
-        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp, a.values);
+        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp, hf32, cm.row_lo);
         __syncthreads();
         float pap[1] = {0.0f};
         for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x)

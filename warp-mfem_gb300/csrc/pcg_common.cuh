@@ -49,8 +49,52 @@ struct PcgArgs {
     // state words, the right-hand side's scale, H's blocks rounded to 16 bits
     int *ir_state;
     const float *ir_scale;
-    const float *values_q;
+    // H's blocks rounded to 16 bits (kind 1 BF16, 2 FP16), nine values and a
+    // zero in five words a block, with per-row scales: the inner solve's
+    // matrix until the refinement switches to the fp32 H
+    const uint32_t *values_w;
+    const float *row_scale;
+    int lowp_kind;
 };
+
+// The matrix a product reads: fp32 blocks, or 16-bit blocks (five words of
+// pairs a block) times their row's scale.
+struct HBlocks {
+    const float *f32;
+    const uint32_t *w16;  // null: fp32
+    const float *scale;   // [n] row scales of the 16-bit blocks
+    int kind;             // 1 BF16, 2 FP16
+};
+
+// One 16-bit block as nine floats, each the widened value times the row
+// scale s: the numbers an fp32 copy of the scaled 16-bit blocks would hold.
+__device__ __forceinline__ void load_block16(const HBlocks &h, long long k, float s, float m[9]) {
+    uint32_t u[5];
+    load_bf16_words(h.w16, k, u);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        float2 t;
+        if (h.kind == 1) {
+            __nv_bfloat162 b;
+            memcpy(&b, &u[i], 4);
+            t = __bfloat1622float2(b);
+        } else {
+            __half2 b;
+            memcpy(&b, &u[i], 4);
+            t = __half22float2(b);
+        }
+        m[2 * i] = t.x * s;
+        if (2 * i + 1 < 9) m[2 * i + 1] = t.y * s;
+    }
+}
+
+// Value j (0..8) of 16-bit block k times s.
+__device__ __forceinline__ float block16_value(const HBlocks &h, long long k, int j, float s) {
+    const uint32_t w = __ldg(h.w16 + 5 * k + (j >> 1));
+    const unsigned short bits = (unsigned short)((j & 1) ? (w >> 16) : (w & 0xffffu));
+    const float v = h.kind == 1 ? __uint_as_float((uint32_t)bits << 16) : __half2float(__ushort_as_half(bits));
+    return v * s;
+}
 
 __device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *p) {
     unsigned long long v;
@@ -207,7 +251,7 @@ __device__ bool tma_wait(uint64_t *mbar, uint32_t &parity, int *error) {
 template <bool CACHE>
 __device__ __forceinline__ void window_product(const PcgArgs &a, const int *rowoff, const float *sH, const int *sCol,
                                                int blk_lo, int win_lo, int nrows, const float *win, float *out,
-                                               const float *values) {
+                                               const HBlocks &hm, int row_lo) {
     const int g_lane = threadIdx.x & (kGroup - 1);
     const int group = threadIdx.x / kGroup;
     const int ngroups = blockDim.x / kGroup;
@@ -222,13 +266,21 @@ __device__ __forceinline__ void window_product(const PcgArgs &a, const int *rowo
             const int kba = rowoff[i], kea = rowoff[i + 1];
             const int kbb = has_b ? rowoff[ib] : kba, keb = has_b ? rowoff[ib + 1] : kba;
             float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, b0 = 0.0f, b1 = 0.0f, b2 = 0.0f;
+            const bool q16 = hm.w16 != nullptr;
+            const float sa = q16 ? __ldg(hm.scale + row_lo + i) : 1.0f;
+            const float sb = q16 ? __ldg(hm.scale + row_lo + (has_b ? ib : i)) : 1.0f;
 #pragma unroll 2
             for (int t = g_lane; kba + t < kea || kbb + t < keb; t += kGroup) {
                 const bool oka = kba + t < kea, okb = kbb + t < keb;
                 const int ka = oka ? kba + t : kba, kq = okb ? kbb + t : kba;  // in-range stand-ins
                 float ha[9], hb[9];
-                load_block9(values, (long long)blk_lo + ka, ha);
-                load_block9(values, (long long)blk_lo + kq, hb);
+                if (q16) {
+                    load_block16(hm, (long long)blk_lo + ka, sa, ha);
+                    load_block16(hm, (long long)blk_lo + kq, sb, hb);
+                } else {
+                    load_block9(hm.f32, (long long)blk_lo + ka, ha);
+                    load_block9(hm.f32, (long long)blk_lo + kq, hb);
+                }
                 const int ca = __ldg(a.col_idx + blk_lo + ka) - win_lo;
                 const int cb = __ldg(a.col_idx + blk_lo + kq) - win_lo;
                 const float u0 = oka ? win[3 * ca] : 0.0f, u1 = oka ? win[3 * ca + 1] : 0.0f,
@@ -319,10 +371,24 @@ __device__ __forceinline__ Common setup_common(const PcgArgs &a) {
 }
 
 __device__ __forceinline__ void load_matrix_slice(const PcgArgs &a, const Common &c, int *rowoff, float *sH,
-                                                  int *sCol, bool cache, const float *values) {
+                                                  int *sCol, bool cache, const HBlocks &hm) {
     for (int i = threadIdx.x; i <= c.nrows; i += blockDim.x) rowoff[i] = a.row_ptr[c.row_lo + i] - c.blk_lo;
     if (cache) {
-        for (int k = threadIdx.x; k < 9 * c.nblk; k += blockDim.x) sH[k] = values[(size_t)9 * c.blk_lo + k];
+        if (hm.w16 == nullptr) {
+            for (int k = threadIdx.x; k < 9 * c.nblk; k += blockDim.x) sH[k] = hm.f32[(size_t)9 * c.blk_lo + k];
+        } else {
+            // a warp per row: its blocks' values times the row's scale
+            __syncthreads();  // rowoff
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+            for (int i = warp; i < c.nrows; i += nwarps) {
+                const float s = __ldg(hm.scale + c.row_lo + i);
+                const int k0 = rowoff[i], nv = 9 * (rowoff[i + 1] - k0);
+                for (int e = lane; e < nv; e += 32) {
+                    const int k = k0 + e / 9, j = e - 9 * (e / 9);
+                    sH[(size_t)9 * k + j] = block16_value(hm, (long long)c.blk_lo + k, j, s);
+                }
+            }
+        }
         for (int k = threadIdx.x; k < c.nblk; k += blockDim.x) sCol[k] = a.col_idx[c.blk_lo + k] - c.win_lo;
     }
 }

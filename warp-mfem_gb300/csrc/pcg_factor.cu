@@ -28,8 +28,9 @@
 // CTA takes that decision from the same totals.  Every wait is bounded.
 //
 // It also serves as the inner solve of the mixed-precision refinement
-// (pcg_mixed.cu): from e = 0 it solves Hq e = r / ||r||, on an fp32 copy of
-// the 16-bit blocks (or on H once the refinement has switched to it), reads
+// (pcg_mixed.cu): from e = 0 it solves Hq e = r / ||r||, reading the 16-bit
+// blocks (20 bytes a block, widened and scaled by their row's scale as they
+// are loaded) or H once the refinement has switched to it, reads
 // and writes the refinement's state words, and returns e ||r||.  A
 // block-Jacobi plan keeps a layout of this kernel, without factor rows, for
 // that use only.
@@ -275,11 +276,12 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
         }
     }
     PCG_PROLOGUE
-    // the inner solve runs on the 16-bit blocks (as fp32) unless the
-    // refinement switched to the fp32 H; its right-hand side is scaled to
+    // the inner solve runs on the 16-bit blocks unless the refinement
+    // switched to the fp32 H; its right-hand side is scaled to
     // unit norm and its solution scaled back
     const bool full = !inner || ld_volatile(a.ir_state + 6) != 0;
-    const float *vals = full ? a.values : a.values_q;
+    const HBlocks hm = full ? HBlocks{a.values, nullptr, nullptr, 0}
+                            : HBlocks{a.values, a.values_w, a.row_scale, a.lowp_kind};
     const float bscale = inner ? a.ir_scale[0] : 1.0f;
     const int rows_max = a.rows_max, win_max = a.win_max;
     float *sX = reinterpret_cast<float *>(smem);
@@ -309,7 +311,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
     float *sRown = sR + 3 * (cm.row_lo - r_lo);  // the CTA's rows in R
     const uint32_t wbytes = (uint32_t)cm.nwin * 12u, rbytes = (uint32_t)nr * 12u;
 
-    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE, vals);
+    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE, hm);
     FactorRows f0, f1;
     if (FC == kFactorAll) {
         stage_factor_rows(a.rp0, a.c0, a.v0, y_lo, y_hi - y_lo, r_lo, f_rp0, f_c0, f_w0);
@@ -347,7 +349,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
                 for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = sAp[i] = 0.0f;
             } else {
                 for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = winA[3 * own + i];
-                window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp, vals);
+                window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp, hm, cm.row_lo);
             }
             __syncthreads();
             float acc[3] = {0.0f, 0.0f, 0.0f};
@@ -448,7 +450,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
             __syncthreads();
             for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x)
                 p_new[(size_t)3 * cm.row_lo + i] = winA[3 * own + i];
-            window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp, vals);
+            window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp, hm, cm.row_lo);
             __syncthreads();
             float pap[1] = {0.0f};
             for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) {
@@ -769,7 +771,9 @@ cudaError_t launch_factor_args(const BsrViews &bv, const VertexViews &vv, const 
     if (ir) {
         a.ir_state = ir->state;
         a.ir_scale = ir->scale;
-        a.values_q = ir->hq;
+        a.values_w = ir->hq_words;
+        a.row_scale = ir->row_scale;
+        a.lowp_kind = ir->mode == kIrBf16 ? 1 : 2;
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(ctas);

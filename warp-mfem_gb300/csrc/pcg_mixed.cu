@@ -82,13 +82,20 @@ __global__ void ir_convert_kernel(BsrViews bv, IrWork w) {
     if (lane == 0) w.row_scale[row] = s;
     const float inv = 1.0f / s;
     T *q = reinterpret_cast<T *>(w.lowp);
-    for (int k = kb + lane; k < ke; k += 32)
+    for (int k = kb + lane; k < ke; k += 32) {
+        unsigned short bits[10];
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
             const T v = to_lowp<T>(bv.values[(size_t)9 * k + i] * inv);
             q[(size_t)9 * k + i] = v;
-            if (w.hq) w.hq[(size_t)9 * k + i] = from_lowp(v) * s;  // what the 16-bit product computes
+            memcpy(&bits[i], &v, 2);
         }
+        bits[9] = 0;
+        if (w.hq_words)  // the persistent factor PCG's copy: five words a block
+#pragma unroll
+            for (int i = 0; i < 5; ++i)
+                w.hq_words[(size_t)5 * k + i] = (uint32_t)bits[2 * i] | ((uint32_t)bits[2 * i + 1] << 16);
+    }
 }
 
 __global__ void ir_begin_kernel(VertexViews vv, IrWork w) {
@@ -674,7 +681,7 @@ cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const 
         ir_residual_kernel<<<rb, kResThreads, 0, s>>>(bv, vv, w, pw, slot);
         count_launches(1);
         e = cudaGetLastError();
-        if (e == cudaSuccess && (w.hq || fp32) && pl.variant == PcgLayout::kFactor)
+        if (e == cudaSuccess && (w.hq_words || fp32) && pl.variant == PcgLayout::kFactor)
             e = launch_pcg_factor_inner(bv, vv, w, pw, fb, pl, pcg_ctas, slot, maxiter, use_precond, s);
         else if (e == cudaSuccess)
             e = bf16 ? launch_ir_pcg<__nv_bfloat16>(bv, vv, w, fb, pw.error, maxiter, use_precond, s)
