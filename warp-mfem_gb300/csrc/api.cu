@@ -1156,7 +1156,7 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
     w.outer_tol = cfg.outer_tolerance;
     alloc(&w.lowp, refined32 ? 16 : nz * 9 * 2);
     alloc(&w.row_scale, (size_t)p->n * sizeof(float));
-    alloc(&w.dx64, 2 * n3 * sizeof(double));
+    alloc(&w.dx_pair, 2 * n3 * sizeof(float2));
     alloc(&w.dx_out, n3 * sizeof(double));
     alloc(&w.e, n3 * sizeof(float));
     alloc(&w.res, n3 * sizeof(float));

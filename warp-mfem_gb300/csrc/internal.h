@@ -255,7 +255,7 @@ struct IrWork {
     double outer_tol;
     void *lowp;                // [nnzb][9] bf16 / fp16, H / row scale
     float *row_scale;          // [n]
-    double *dx64;              // [2][n][3] double-buffered solution
+    float2 *dx_pair;           // [2][n][3] double-buffered solution, each value hi + lo of two floats
     double *dx_out;            // [n][3] the latest iterate
     float *e;                  // [n][3] inner correction
     float *res;                // [n][3] fp32 copy of the fp64 residual (inner rhs)

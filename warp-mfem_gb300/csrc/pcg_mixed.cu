@@ -4,8 +4,9 @@
 //   Hq = BSR blocks of H stored as bf16 or fp16, each block row scaled by its
 //        largest |entry| (one fp32 scale per row), so every stored value is
 //        in [-1, 1]; products accumulate in fp32.
-//   dx (fp64) starts at the reference's warm start x~ - x; each outer
-//   iteration forms r = g - H dx in fp64 from the fp32 H, stops when
+//   dx (hi + lo pairs of floats, about 48 bits) starts at the reference's
+//   warm start x~ - x; each outer iteration forms r = g - H dx from the fp32
+//   H with the products summed in those pairs, stops when
 //   ||r|| <= outer_tol ||g||, else solves Hq e = r to inner_tol with the PCG
 //   (fp32 vectors, the fp32 block-Jacobi inverse) and sets dx += e.
 //   If the refinement diverges (the relative residual rises above 4x its
@@ -20,9 +21,11 @@
 //
 // Kernels:
 //   ir_convert_kernel   Hq and the row scales from H (one warp per row)
-//   ir_begin_kernel     dx = warm start (fp64), state reset
+//   ir_begin_kernel     dx = warm start, state reset
 //   ir_residual_kernel  dx += e (double-buffered, so rows read a consistent dx),
-//                       r = g - H dx (fp64), partial sums; the last block
+//                       r = g - H dx with dx and the sums of products held as
+//                       pairs of floats (about 48 bits; GB300's fp64 pipe is
+//                       narrow), its norm in fp64, partial sums; the last block
 //                       to finish adds the partials in a fixed order and
 //                       decides (converged / outer cap)
 //   ir_pcg_kernel<T>    persistent cooperative PCG on Hq e = r, e0 = 0
@@ -32,8 +35,8 @@
 // for a solution whose fp64 residual reaches the outer tolerance.
 //
 // A plan on the persistent factor PCG (pcg_factor.cu) runs the inner solves
-// there instead: ir_convert_kernel also writes Hq back as fp32 (each 16-bit
-// value times its row scale, the values ir_pcg_kernel multiplies with), and
+// there instead: ir_convert_kernel also writes Hq padded to 20-byte blocks
+// (which that kernel widens and scales by the row scale as it loads them), and
 // the residual kernel hands over r / ||r|| (so the fp32 sums of products
 // cannot underflow) with ||r|| to scale the correction back.
 #include <cuda_bf16.h>
@@ -98,10 +101,52 @@ __global__ void ir_convert_kernel(BsrViews bv, IrWork w) {
     }
 }
 
+// ---- double-float arithmetic ----------------------------------------------
+// A value held as the unevaluated sum hi + lo of two floats (about 48 bits),
+// with the error-free transformations TwoSum (Knuth, TAOCP vol. 2, 4.2.2) and
+// TwoProduct by fused multiply-add (Ogita, Rump & Oishi 2005), all with
+// round-to-nearest intrinsics so that nothing is contracted.  GB300's fp64
+// rate is a small fraction of its fp32 rate; the residual's products run in
+// these pairs instead of in double.
+__device__ __forceinline__ float2 two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+
+// |a| >= |b| (or a == 0)
+__device__ __forceinline__ float2 fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    const float2 s = two_sum(a.x, b.x);
+    return fast_two_sum(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
+}
+
+__device__ __forceinline__ float2 df_add(float2 a, float b) {
+    const float2 s = two_sum(a.x, b);
+    return fast_two_sum(s.x, __fadd_rn(s.y, a.y));
+}
+
+// acc += h (x.hi + x.lo)
+__device__ __forceinline__ void df_fma(float2 &acc, float h, float2 x) {
+    const float p = __fmul_rn(h, x.x);
+    float pe = __fmaf_rn(h, x.x, -p);  // h x.hi = p + pe exactly
+    pe = __fmaf_rn(h, x.y, pe);
+    const float2 s = two_sum(acc.x, p);
+    acc = fast_two_sum(s.x, __fadd_rn(__fadd_rn(s.y, pe), acc.y));
+}
+
+__device__ __forceinline__ float2 df_shfl_xor(unsigned mask, float2 v, int off) {
+    return make_float2(__shfl_xor_sync(mask, v.x, off), __shfl_xor_sync(mask, v.y, off));
+}
+
 __global__ void ir_begin_kernel(VertexViews vv, IrWork w) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < 3 * vv.n) {
-        w.dx64[i] = (double)vv.dx[i];
+        w.dx_pair[i] = make_float2(vv.dx[i], 0.0f);
         w.dx_init[i] = vv.dx[i];
     }
     if (i == 0) {
@@ -126,43 +171,50 @@ __global__ void __launch_bounds__(kResThreads)
     const bool restart = w.state[7] != 0;
     const bool pending = !restart && w.state[3] != 0;
     const size_t vec = (size_t)3 * vv.n;
-    const double *xo = w.dx64 + (size_t)par * vec;
-    double *xn = w.dx64 + (size_t)(par ^ 1) * vec;
+    const float2 *xo = w.dx_pair + (size_t)par * vec;
+    float2 *xn = w.dx_pair + (size_t)(par ^ 1) * vec;
     const int g_lane = threadIdx.x & (kIrGroup - 1);
     const unsigned gmask = ((1u << kIrGroup) - 1u) << (threadIdx.x & (32 - kIrGroup));
     const int row = (blockIdx.x * blockDim.x + threadIdx.x) / kIrGroup;
+    // the iterate of row c: the warm start after a restart, else the last
+    // iterate plus the pending inner correction
+    auto iterate = [&](int c, int q) -> float2 {
+        if (restart) return make_float2(w.dx_init[3 * c + q], 0.0f);
+        const float2 x = xo[3 * c + q];
+        return pending ? df_add(x, w.e[3 * c + q]) : x;
+    };
     double rr = 0.0, gg = 0.0;
     if (row < vv.n) {
-        double acc[3] = {0.0, 0.0, 0.0};
+        float2 acc[3] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
         for (int k = bv.row_ptr[row] + g_lane; k < bv.row_ptr[row + 1]; k += kIrGroup) {
             const int c = bv.col_idx[k];
-            double xc[3];
+            float2 xc[3];
 #pragma unroll
-            for (int q = 0; q < 3; ++q)
-                xc[q] = restart ? (double)w.dx_init[3 * c + q]
-                                : xo[3 * c + q] + (pending ? (double)w.e[3 * c + q] : 0.0);
+            for (int q = 0; q < 3; ++q) xc[q] = iterate(c, q);
             const float *h = bv.values + (size_t)9 * k;
 #pragma unroll
             for (int a = 0; a < 3; ++a)
-                acc[a] += (double)h[3 * a] * xc[0] + (double)h[3 * a + 1] * xc[1] + (double)h[3 * a + 2] * xc[2];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) df_fma(acc[a], h[3 * a + q], xc[q]);
         }
 #pragma unroll
         for (int off = kIrGroup / 2; off > 0; off >>= 1)
 #pragma unroll
-            for (int a = 0; a < 3; ++a) acc[a] += __shfl_xor_sync(gmask, acc[a], off);
+            for (int a = 0; a < 3; ++a) acc[a] = df_add(acc[a], df_shfl_xor(gmask, acc[a], off));
         if (g_lane == 0) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                const double xr = restart ? (double)w.dx_init[3 * row + a]
-                                          : xo[3 * row + a] + (pending ? (double)w.e[3 * row + a] : 0.0);
+                const float2 xr = iterate(row, a);
                 xn[3 * row + a] = xr;
-                w.dx_out[3 * row + a] = xr;
-                vv.dx[3 * row + a] = (float)xr;
-                const double gq = (double)vv.rhs[3 * row + a];
-                const double r = gq - acc[a];
+                w.dx_out[3 * row + a] = (double)xr.x + (double)xr.y;
+                vv.dx[3 * row + a] = __fadd_rn(xr.x, xr.y);
+                // r = g - (acc.hi + acc.lo), as a pair, then its double value
+                const float gq = vv.rhs[3 * row + a];
+                const float2 rp = df_add(two_sum(gq, -acc[a].x), -acc[a].y);
+                const double r = (double)rp.x + (double)rp.y;
                 w.res[3 * row + a] = (float)r;
                 rr += r * r;
-                gg += gq * gq;
+                gg += (double)gq * (double)gq;
             }
         }
     }
