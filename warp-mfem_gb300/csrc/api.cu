@@ -1176,9 +1176,15 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
     alloc(&w.scale, 2 * sizeof(float));
     // a plan on the persistent factor PCG runs its inner solves there, on a
     // copy of the 16-bit blocks padded to 20 bytes (4-byte aligned loads)
-    if (!refined32 && (p->pl.variant == PcgLayout::kFactor || p->ir_pl.variant == PcgLayout::kFactor) &&
-        p->cfg.preconditioner >= 1)
-        alloc(&w.hq_words, nz * 5 * sizeof(uint32_t));
+    const bool persistent = (p->pl.variant == PcgLayout::kFactor || p->ir_pl.variant == PcgLayout::kFactor) &&
+                            p->cfg.preconditioner >= 1;
+    if (!refined32 && persistent) alloc(&w.hq_words, nz * 5 * sizeof(uint32_t));
+    // ... and the whole refinement in one launch there, with the iterate
+    // as hi / lo planes padded like the PCG's exchanged vectors
+    if (persistent) {
+        alloc(&w.xf_hi, (size_t)p->pw.n_pad * 3 * sizeof(float));
+        alloc(&w.xf_lo, (size_t)p->pw.n_pad * 3 * sizeof(float));
+    }
     int max_ctas = 1;
     if (e == cudaSuccess) e = ir_max_ctas(p->device, &max_ctas);
     if (e == cudaSuccess) e = cudaMemset(w.counter, 0, sizeof(unsigned long long));
@@ -1186,6 +1192,8 @@ int mfem_plan_set_solver(mfem_plan *p, const mfem_solver_config *cfg_in) {
     if (e == cudaSuccess) e = cudaMemset(w.state, 0, 8 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(w.stats, 0, (size_t)p->max_stats * sizeof(IrStats));
     if (e == cudaSuccess) e = cudaMemset(w.e, 0, n3 * sizeof(float));
+    if (e == cudaSuccess && w.xf_hi) e = cudaMemset(w.xf_hi, 0, (size_t)p->pw.n_pad * 3 * sizeof(float));
+    if (e == cudaSuccess && w.xf_lo) e = cudaMemset(w.xf_lo, 0, (size_t)p->pw.n_pad * 3 * sizeof(float));
     if (e != cudaSuccess) {
         for (void *a : p->ir_allocs) cudaFree(a);
         p->ir_allocs.clear();

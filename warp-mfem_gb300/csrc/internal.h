@@ -272,6 +272,9 @@ struct IrWork {
     uint32_t *hq_words;        // [nnzb][5] the 16-bit blocks as pairs in words, nine values and a zero
                                // (20 bytes, 4-byte aligned), for the persistent factor PCG (else null)
     float *scale;              // [2] 1 / ||r|| and ||r|| of the latest fp64 residual
+    // the whole refinement in one launch of the persistent factor PCG: the
+    // iterate as hi + lo planes (rows padded to n_pad for bulk copies)
+    float *xf_hi, *xf_lo;      // [n_pad][3]
 };
 
 // Row partition and shared-memory plan of the persistent PCG.
@@ -428,6 +431,12 @@ int ir_residual_blocks(int n);
 cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const IrWork &w, const PcgWork &pw,
                                const BatchViews &fb, const PcgLayout &pl, int pcg_ctas, int slot, int maxiter,
                                int use_precond, cudaStream_t s);
+// The whole mixed refinement in one launch of the persistent factor PCG
+// (needs IrWork's xf_hi / xf_lo): the warm start in vv.dx, the solution
+// written back there.
+cudaError_t launch_pcg_factor_refine(const BsrViews &bv, const VertexViews &vv, const IrWork &ir,
+                                     const PcgWork &pw, const BatchViews &bw, const PcgLayout &L, int ctas, int slot,
+                                     int maxiter, int mode, cudaStream_t s);
 // The inner solve of the mixed refinement, Hq e = r to inner_tol from e = 0,
 // in the persistent factor PCG.
 cudaError_t launch_pcg_factor_inner(const BsrViews &bv, const VertexViews &vv, const IrWork &w, const PcgWork &pw,

@@ -6,6 +6,7 @@
 #pragma once
 
 #include "block_loads.cuh"
+#include "double_float.cuh"
 #include "internal.h"
 
 namespace mfem {
@@ -55,6 +56,12 @@ struct PcgArgs {
     const uint32_t *values_w;
     const float *row_scale;
     int lowp_kind;
+    // the whole refinement in this launch (pcg_factor.cu): every correction's
+    // residual, decision and inner solve
+    int fused;
+    const float *g;      // [n][3] the system's right-hand side
+    float *dx;           // [n][3] the solution as float for the local solve
+    IrWork irw;
 };
 
 // The matrix a product reads: fp32 blocks, or 16-bit blocks (five words of
@@ -182,6 +189,87 @@ __device__ void reduce_totals(const float *partials, unsigned k, float *s_val, f
         for (int b = lane; b < nb; b += 32) {
 #pragma unroll
             for (int i = 0; i < NV; ++i) acc[i] += s_val[b * 4 + i];
+        }
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) acc[i] += __shfl_down_sync(0xffffffffu, acc[i], off);
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int i = 0; i < NV; ++i) tot[i] = acc[i];
+        }
+    }
+    __syncthreads();
+}
+
+// reduce_arrive and reduce_totals in double, on a double partials buffer of
+// the same [2][kMaxCtas][4] shape and the same barrier counter and parity.
+template <int NV>
+__device__ bool reduce_arrive_d(double (&v)[NV], double *partials, unsigned k, unsigned long long *counter,
+                                unsigned long long &target, int *error, double (*s_redd)[32], int *s_ok) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v[i] += __shfl_down_sync(0xffffffffu, v[i], off);
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) s_redd[i][wid] = v[i];
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        double part[NV];
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            part[i] = lane < nw ? s_redd[i][lane] : 0.0;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) part[i] += __shfl_down_sync(0xffffffffu, part[i], off);
+        }
+        if (lane == 0) {
+            double *buf = partials + (size_t)(k & 1u) * kMaxCtas * 4 + (size_t)blockIdx.x * 4;
+#pragma unroll
+            for (int i = 0; i < NV; ++i) buf[i] = part[i];
+            target += gridDim.x;
+            __threadfence();
+            atomicAdd(counter, 1ull);
+            int ok = 1;
+            const long long t0 = clock64();
+            unsigned spins = 0;
+            while (ld_relaxed(counter) < target) {
+                if ((++spins & 1023u) == 0 && (ld_volatile(error) != 0 || clock64() - t0 > kWaitCycles)) {
+                    atomicExch(error, 1);
+                    ok = 0;
+                    break;
+                }
+            }
+            __threadfence();
+            *s_ok = ok;
+        }
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
+template <int NV>
+__device__ void reduce_totals_d(const double *partials, unsigned k, double *s_vald, double *tot) {
+    const int nb = gridDim.x;
+    const double *buf = partials + (size_t)(k & 1u) * kMaxCtas * 4;
+    for (int t = threadIdx.x; t < nb * NV; t += blockDim.x) {
+        const int b = t / NV, i = t - b * NV;
+        s_vald[b * NV + i] = __ldcg(buf + (size_t)b * 4 + i);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        double acc[NV];
+#pragma unroll
+        for (int i = 0; i < NV; ++i) acc[i] = 0.0;
+        for (int b = lane; b < nb; b += 32) {
+#pragma unroll
+            for (int i = 0; i < NV; ++i) acc[i] += s_vald[b * NV + i];
         }
 #pragma unroll
         for (int i = 0; i < NV; ++i) {

@@ -27,7 +27,10 @@
 // again from the same warm start with block-Jacobi inside the launch; every
 // CTA takes that decision from the same totals.  Every wait is bounded.
 //
-// It also serves as the inner solve of the mixed-precision refinement
+// With `fused` it runs the whole mixed-precision refinement in one launch
+// (the residual passes in double-float, the decisions, the inner solves;
+// see the fused block of the kernel).  Without, it also serves as one inner
+// solve of the refinement's launch sequence
 // (pcg_mixed.cu): from e = 0 it solves Hq e = r / ||r||, reading the 16-bit
 // blocks (20 bytes a block, widened and scaled by their row's scale as they
 // are loaded) or H once the refinement has switched to it, reads
@@ -258,6 +261,46 @@ __device__ __forceinline__ void stage_factor_rows(const int *rp, const int *col,
     for (int t = threadIdx.x; t < 5 * nb; t += blockDim.x) s_words[t] = w[t];
 }
 
+// r = g - H x for the CTA's rows, with x over the CTA's column window as hi
+// and lo planes and the fp32 H read through L2, the products summed in
+// double-float; r (as float) to `res`, (r.r, g.g) in double added to acc.
+__device__ __forceinline__ void residual_rows(const PcgArgs &a, const Common &cm, const int *rowoff,
+                                              const float *whi, const float *wlo, float *res, double (&acc)[2]) {
+    const int g_lane = threadIdx.x & (kGroup - 1);
+    const int group = threadIdx.x / kGroup, ngroups = blockDim.x / kGroup;
+    const unsigned gmask = ((1u << kGroup) - 1u) << (threadIdx.x & (32 - kGroup));
+    for (int i = group; i < cm.nrows; i += ngroups) {
+        float2 sum[3] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
+        for (int k = rowoff[i] + g_lane; k < rowoff[i + 1]; k += kGroup) {
+            float h[9];
+            load_block9(a.values, (long long)cm.blk_lo + k, h);
+            const int c = __ldg(a.col_idx + cm.blk_lo + k) - cm.win_lo;
+            float2 x[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) x[q] = make_float2(whi[3 * c + q], wlo[3 * c + q]);
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+                for (int q = 0; q < 3; ++q) df_fma(sum[r], h[3 * r + q], x[q]);
+        }
+#pragma unroll
+        for (int off = kGroup / 2; off > 0; off >>= 1)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) sum[r] = df_add(sum[r], df_shfl_xor(gmask, sum[r], off));
+        if (g_lane == 0) {
+            const int row = cm.row_lo + i;
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                const float gq = a.g[3 * row + r];
+                const double rv = df_residual(gq, sum[r]);
+                res[3 * row + r] = (float)rv;
+                acc[0] += rv * rv;
+                acc[1] += (double)gq * (double)gq;
+            }
+        }
+    }
+}
+
 template <bool CACHE, int FC>
 __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -265,8 +308,9 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
     // when it restarts from the warm start (its state words, as every CTA
     // reads them: the previous launch wrote them)
     const bool inner = a.ir_state != nullptr;
+    const bool fused = inner && a.fused != 0;  // the whole refinement in this launch
     if (inner) {
-        if (ld_volatile(a.ir_state) != 0 || ld_volatile(a.ir_state + 7) != 0) return;
+        if (!fused && (ld_volatile(a.ir_state) != 0 || ld_volatile(a.ir_state + 7) != 0)) return;
         if (ld_volatile(a.error) != 0) {
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 a.ir_state[5] = MFEM_TIMEOUT;
@@ -276,13 +320,18 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
         }
     }
     PCG_PROLOGUE
+    __shared__ double s_redd[2][32];
+    __shared__ double s_vald[2 * kMaxCtas];
+    __shared__ double s_totd[2];
+    __shared__ int s_dec[2];      // the fused refinement's decision: done, restart
+    __shared__ float s_dscale[2];  // 1 / ||r|| and ||r||
     // the inner solve runs on the 16-bit blocks unless the refinement
     // switched to the fp32 H; its right-hand side is scaled to
     // unit norm and its solution scaled back
-    const bool full = !inner || ld_volatile(a.ir_state + 6) != 0;
-    const HBlocks hm = full ? HBlocks{a.values, nullptr, nullptr, 0}
-                            : HBlocks{a.values, a.values_w, a.row_scale, a.lowp_kind};
-    const float bscale = inner ? a.ir_scale[0] : 1.0f;
+    bool full = !inner || ld_volatile(a.ir_state + 6) != 0;
+    HBlocks hm = full ? HBlocks{a.values, nullptr, nullptr, 0}
+                      : HBlocks{a.values, a.values_w, a.row_scale, a.lowp_kind};
+    float bscale = inner && !fused ? a.ir_scale[0] : 1.0f;
     const int rows_max = a.rows_max, win_max = a.win_max;
     float *sX = reinterpret_cast<float *>(smem);
     float *sAp = sX + 3 * rows_max;
@@ -330,6 +379,13 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
     int mode = a.use_precond;  // 2 or 3; 1 after a breakdown
     int it = 0, it_done = 0;
     bool pending = false;  // window copies in flight
+    // One solve from x0 (the warm start, or 0 for an inner solve): sX holds
+    // the solution and sc its outcome on return.
+    auto solve = [&]() {
+    mode = a.use_precond;
+    it = 0;
+    it_done = 0;
+    pending = false;
     for (;;) {  // one attempt
         const bool factor = mode >= 2;
         it = 0;
@@ -559,6 +615,147 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
         break;
     }
     __syncthreads();
+    };
+    if (fused) {
+        // The refinement in one launch (the sequence of ir_residual_kernel
+        // and inner launches, pcg_mixed.cu, without the launches): x starts
+        // at the warm start; each pass publishes x, forms r = g - H x for the
+        // CTA's rows in double-float, reduces ||r||, ||g|| in double, and
+        // every CTA takes the same decision from the same totals: done, a
+        // restart on the fp32 H (divergence on the 16-bit H), or an inner
+        // solve of H e = r / ||r|| from 0 whose e ||r|| the next pass adds.
+        const IrWork &w = a.irw;
+        const int n3own = 3 * cm.nrows;
+        const size_t off = (size_t)3 * cm.row_lo;
+        float *xhi = w.xf_hi, *xlo = w.xf_lo;
+        const uint32_t xbytes = (uint32_t)cm.nwin * 12u;
+        // decision state, kept by thread 0 of every CTA
+        double best = __longlong_as_double(0x7ff0000000000000ll);  // +inf
+        int outer = 0, inner_its = 0, status = MFEM_OK, fp32_inner = full ? 1 : 0;
+        bool restart = true, have_e = false;  // the first pass reads the warm start
+        float es = 1.0f;
+        for (;;) {
+            if (restart || have_e) {
+                for (int i = threadIdx.x; i < n3own; i += blockDim.x) {
+                    if (restart) {
+                        xhi[off + i] = w.dx_init[off + i];
+                        xlo[off + i] = 0.0f;
+                    } else {
+                        const float2 x = df_add(make_float2(xhi[off + i], xlo[off + i]), __fmul_rn(sX[i], es));
+                        xhi[off + i] = x.x;
+                        xlo[off + i] = x.y;
+                    }
+                }
+            }
+            restart = false;
+            have_e = false;
+            // every row's x published: a barrier, then the CTA's window of it
+            float none[1] = {0.0f};
+            bool ok = reduce_arrive<1>(none, a.partials, bar, a.counter, target, a.error, s_redf, &s_ok);
+            ++bar;
+            if (ok && cm.nwin > 0) {
+                if (threadIdx.x == 0) {
+                    tma_expect(&s_mbar, 2u * xbytes);
+                    tma_copy(winA, xhi + (size_t)3 * cm.win_lo, xbytes, &s_mbar);
+                    tma_copy(winB, xlo + (size_t)3 * cm.win_lo, xbytes, &s_mbar);
+                }
+                ok = tma_wait(&s_mbar, parity, a.error);
+            }
+            double acc[2] = {0.0, 0.0};
+            if (ok) residual_rows(a, cm, rowoff, winA, winB, w.res, acc);
+            ok = ok && reduce_arrive_d<2>(acc, w.partials, bar, a.counter, target, a.error, s_redd, &s_ok);
+            if (ok) reduce_totals_d<2>(w.partials, bar, s_vald, s_totd);
+            ++bar;
+            if (threadIdx.x == 0) {
+                int done = 0, rs = 0;
+                double rel = 0.0;
+                if (!ok) {
+                    if (status == MFEM_OK) status = MFEM_TIMEOUT;
+                    done = 1;
+                } else {
+                    const double rr = s_totd[0], gg = s_totd[1];
+                    rel = gg > 0.0 ? sqrt(rr / gg) : sqrt(rr);
+                    // the next inner right-hand side at unit norm: fp32 sums of
+                    // products of a tiny residual's entries would underflow
+                    const double rn = sqrt(rr);
+                    const float inv = (float)(1.0 / rn);
+                    const bool scaled = rn > 0.0 && isfinite(rn) && isfinite(inv);
+                    s_dscale[0] = scaled ? inv : 1.0f;
+                    s_dscale[1] = scaled ? (float)rn : 1.0f;
+                    int st = MFEM_OK;
+                    if (!fp32_inner && isfinite(best) && !(rel <= 4.0 * best) && outer < w.outer_max) {
+                        fp32_inner = 1;  // diverging on the 16-bit H
+                        rs = 1;
+                    } else if (!isfinite(rel)) {
+                        st = MFEM_NONFINITE;
+                        done = 1;
+                    } else if (rel <= w.outer_tol) {
+                        done = 1;
+                    } else if (outer >= w.outer_max) {
+                        st = MFEM_MAXITER;
+                        done = 1;
+                    }
+                    if (isfinite(rel) && rel < best && !rs) best = rel;
+                    if (status == MFEM_OK) status = st;
+                }
+                if (blockIdx.x == 0) {
+                    w.stats[a.slot] = IrStats{outer, inner_its, status, fp32_inner, rel};
+                    a.stats[a.slot] = SolveStats{inner_its, status, (float)rel, 0.0f};
+                }
+                ++outer;
+                s_dec[0] = done;
+                s_dec[1] = rs;
+            }
+            __syncthreads();
+            if (s_dec[0]) break;
+            if (s_dec[1]) {  // restart from the warm start on the fp32 H
+                full = true;
+                hm = HBlocks{a.values, nullptr, nullptr, 0};
+                if (CACHE) {
+                    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE, hm);
+                    __syncthreads();
+                }
+                restart = true;
+                continue;
+            }
+            bscale = s_dscale[0];
+            es = s_dscale[1];
+            solve();
+            if (threadIdx.x == 0) inner_its += it_done + it;
+            if (sc.status == MFEM_NONFINITE && !full) {
+                // the 16-bit H broke the inner solve: restart on the fp32 H
+                if (threadIdx.x == 0) fp32_inner = 1;
+                full = true;
+                hm = HBlocks{a.values, nullptr, nullptr, 0};
+                if (CACHE) {
+                    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE, hm);
+                    __syncthreads();
+                }
+                restart = true;
+                continue;
+            }
+            if (sc.status == MFEM_TIMEOUT || sc.status == MFEM_NONFINITE) {
+                if (threadIdx.x == 0) {
+                    if (status == MFEM_OK) status = sc.status;
+                    if (blockIdx.x == 0) {
+                        w.stats[a.slot] = IrStats{outer, inner_its, status, fp32_inner, 0.0};
+                        a.stats[a.slot] = SolveStats{inner_its, status, 0.0f, 0.0f};
+                    }
+                }
+                break;
+            }
+            have_e = true;  // MAXITER and STAGNATION still hand over their iterate
+        }
+        // the solution: float for the local solve, double for the buffer
+        for (int i = threadIdx.x; i < n3own; i += blockDim.x) {
+            const float hi = xhi[off + i], lo = xlo[off + i];
+            a.dx[off + i] = __fadd_rn(hi, lo);
+            w.dx_out[off + i] = (double)hi + (double)lo;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) w.state[0] = 1;
+        return;
+    }
+    solve();
     if (!inner) {
         finish(a, cm, sX, sc, it_done + it);
         return;
@@ -729,7 +926,7 @@ namespace {
 
 cudaError_t launch_factor_args(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const BatchViews &bw,
                                const PcgLayout &L, int ctas, int slot, float tol, int maxiter, int mode,
-                               const float *b, float *x, const IrWork *ir, cudaStream_t s) {
+                               const float *b, float *x, const IrWork *ir, cudaStream_t s, bool fused = false) {
     // 1 (block-Jacobi) only as an inner solve of a plan without a factor
     if (mode != 2 && mode != 3 && !(ir && mode == 1)) return cudaErrorInvalidValue;
     PcgArgs a = {};
@@ -774,6 +971,12 @@ cudaError_t launch_factor_args(const BsrViews &bv, const VertexViews &vv, const 
         a.values_w = ir->hq_words;
         a.row_scale = ir->row_scale;
         a.lowp_kind = ir->mode == kIrBf16 ? 1 : 2;
+        if (fused) {
+            a.fused = 1;
+            a.g = vv.rhs;
+            a.dx = vv.dx;
+            a.irw = *ir;
+        }
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(ctas);
@@ -802,6 +1005,13 @@ cudaError_t launch_pcg_factor_inner(const BsrViews &bv, const VertexViews &vv, c
                                     const BatchViews &bw, const PcgLayout &L, int ctas, int slot, int maxiter,
                                     int mode, cudaStream_t s) {
     return launch_factor_args(bv, vv, pw, bw, L, ctas, slot, ir.inner_tol, maxiter, mode, ir.res, ir.e, &ir, s);
+}
+
+cudaError_t launch_pcg_factor_refine(const BsrViews &bv, const VertexViews &vv, const IrWork &ir,
+                                     const PcgWork &pw, const BatchViews &bw, const PcgLayout &L, int ctas, int slot,
+                                     int maxiter, int mode, cudaStream_t s) {
+    return launch_factor_args(bv, vv, pw, bw, L, ctas, slot, ir.inner_tol, maxiter, mode, ir.res, ir.e, &ir, s,
+                              true);
 }
 
 }  // namespace mfem

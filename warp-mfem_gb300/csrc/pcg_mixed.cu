@@ -44,6 +44,7 @@
 
 #include <algorithm>
 
+#include "double_float.cuh"
 #include "factor_apply.cuh"
 #include "internal.h"
 
@@ -99,48 +100,6 @@ __global__ void ir_convert_kernel(BsrViews bv, IrWork w) {
             for (int i = 0; i < 5; ++i)
                 w.hq_words[(size_t)5 * k + i] = (uint32_t)bits[2 * i] | ((uint32_t)bits[2 * i + 1] << 16);
     }
-}
-
-// ---- double-float arithmetic ----------------------------------------------
-// A value held as the unevaluated sum hi + lo of two floats (about 48 bits),
-// with the error-free transformations TwoSum (Knuth, TAOCP vol. 2, 4.2.2) and
-// TwoProduct by fused multiply-add (Ogita, Rump & Oishi 2005), all with
-// round-to-nearest intrinsics so that nothing is contracted.  GB300's fp64
-// rate is a small fraction of its fp32 rate; the residual's products run in
-// these pairs instead of in double.
-__device__ __forceinline__ float2 two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
-}
-
-// |a| >= |b| (or a == 0)
-__device__ __forceinline__ float2 fast_two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b);
-    return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
-}
-
-__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
-    const float2 s = two_sum(a.x, b.x);
-    return fast_two_sum(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
-}
-
-__device__ __forceinline__ float2 df_add(float2 a, float b) {
-    const float2 s = two_sum(a.x, b);
-    return fast_two_sum(s.x, __fadd_rn(s.y, a.y));
-}
-
-// acc += h (x.hi + x.lo)
-__device__ __forceinline__ void df_fma(float2 &acc, float h, float2 x) {
-    const float p = __fmul_rn(h, x.x);
-    float pe = __fmaf_rn(h, x.x, -p);  // h x.hi = p + pe exactly
-    pe = __fmaf_rn(h, x.y, pe);
-    const float2 s = two_sum(acc.x, p);
-    acc = fast_two_sum(s.x, __fadd_rn(__fadd_rn(s.y, pe), acc.y));
-}
-
-__device__ __forceinline__ float2 df_shfl_xor(unsigned mask, float2 v, int off) {
-    return make_float2(__shfl_xor_sync(mask, v.x, off), __shfl_xor_sync(mask, v.y, off));
 }
 
 __global__ void ir_begin_kernel(VertexViews vv, IrWork w) {
@@ -210,8 +169,7 @@ __global__ void __launch_bounds__(kResThreads)
                 vv.dx[3 * row + a] = __fadd_rn(xr.x, xr.y);
                 // r = g - (acc.hi + acc.lo), as a pair, then its double value
                 const float gq = vv.rhs[3 * row + a];
-                const float2 rp = df_add(two_sum(gq, -acc[a].x), -acc[a].y);
-                const double r = (double)rp.x + (double)rp.y;
+                const double r = df_residual(gq, acc[a]);
                 w.res[3 * row + a] = (float)r;
                 rr += r * r;
                 gg += (double)gq * (double)gq;
@@ -728,6 +686,9 @@ cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const 
     ir_begin_kernel<<<blocks_for(3 * vv.n, 256), 256, 0, s>>>(vv, w);
     count_launches(fp32 ? 1 : 2);
     e = cudaGetLastError();
+    if (e == cudaSuccess && w.xf_hi && (w.hq_words || fp32) && pl.variant == PcgLayout::kFactor)
+        // every correction inside one launch of the persistent factor PCG
+        return launch_pcg_factor_refine(bv, vv, w, pw, fb, pl, pcg_ctas, slot, maxiter, use_precond, s);
     const int rb = ir_residual_blocks(vv.n);
     for (int k = 0; e == cudaSuccess && k < w.outer_max; ++k) {
         ir_residual_kernel<<<rb, kResThreads, 0, s>>>(bv, vv, w, pw, slot);
