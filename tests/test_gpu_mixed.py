@@ -100,6 +100,29 @@ def test_bf16_stagnation_is_reported():
         assert rel == pytest.approx(st["rel_residual"], rel=1e-3) and rel > 1e-8
 
 
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+def test_one_launch_refinement_takes_the_sequence_decisions(precision):
+    """The refinement inside one launch of the persistent factor PCG
+    (pcg_variant auto) and the launch sequence of residual kernels and inner
+    PCGs (the global-memory inner PCG) decide alike on the ill-conditioned
+    beam: the same corrections, status and fp32 switch, and residuals that
+    agree (FP16 converges, BF16 stagnates at the outer cap)."""
+    stats = {}
+    for variant in ("auto", "global_memory"):
+        mesh, _, solver = make("stiff_beam", (32, 8, 8), precision, outer_max_iterations=12, pcg_variant=variant)
+        H, g, dx64, _ = one_solve(mesh, solver)
+        st = solver.mixed_stats()[0]
+        rel = np.linalg.norm(g - H @ dx64) / np.linalg.norm(g)
+        assert rel == pytest.approx(st["rel_residual"], rel=1e-3, abs=1e-12)
+        stats[variant] = st
+    a, b = stats["auto"], stats["global_memory"]
+    assert (a["outer_iterations"], a["status"], a["fp32_inner"]) == (b["outer_iterations"], b["status"],
+                                                                     b["fp32_inner"]), stats
+    assert a["rel_residual"] == pytest.approx(b["rel_residual"], rel=1e-2)
+    if precision == "fp16":
+        assert a["status"] == _lib.MFEM_OK and a["rel_residual"] <= 1e-8
+
+
 @pytest.mark.parametrize("precision,outer_tolerance", [("fp16", 1e-8), ("bf16", 1e-6)])
 def test_mixed_trajectory_matches_fp64_oracle(precision, outer_tolerance):
     """BF16 targets 1e-6: on later Newton iterations it stagnates near that
