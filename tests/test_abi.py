@@ -78,7 +78,29 @@ def test_host_sparsity_with_isolated_vertex_and_shuffled_tets(built_lib):
     rp_o, ci_o = O.bsr_sparsity(tets, n)
     np.testing.assert_array_equal(rp, rp_o)
     np.testing.assert_array_equal(ci, ci_o)
+    np.testing.assert_array_equal(slots, O.tet_slot_map(tets, rp_o, ci_o))
     assert rp[-1] - rp[-2] == 1 and ci[-1] == n - 1
+
+
+def test_host_sparsity_of_a_refined_mesh(built_lib):
+    """An irregular mesh: the reference test's grid after three refinement
+    passes of the oracle (vertices of valence 4 to 30)."""
+    from oracle import refine_oracle as ro
+    from tests.refine_cases import deformed, grid_mesh
+    mesh = grid_mesh()
+    q = deformed(mesh.rest_q)
+    cfg = ro.RefineConfig(scoring="legacy", threshold=1e-6, tet_score_weight=1.0)
+    rng = np.random.default_rng(8)
+    for _ in range(3):
+        E = rng.uniform(0.0, 1.0, mesh.tets.shape[0]).astype(np.float32)
+        res = ro.refine_pass(mesh, q, q, cfg, tet_scores=E, max_particles=10 ** 6, max_tets=10 ** 6)
+        mesh, q = res.mesh, res.q
+    n = mesh.rest_q.shape[0]
+    rp, ci, slots = _host_sparsity(built_lib, mesh.tets, n)
+    rp_o, ci_o = O.bsr_sparsity(mesh.tets, n)
+    np.testing.assert_array_equal(rp, rp_o)
+    np.testing.assert_array_equal(ci, ci_o)
+    np.testing.assert_array_equal(slots, O.tet_slot_map(mesh.tets, rp_o, ci_o))
 
 
 @pytest.mark.parametrize("bad", ["out_of_range", "negative", "repeated"])

@@ -394,3 +394,49 @@ def test_refined_step_matches_a_plan_of_the_refined_mesh():
     b = plain.state()
     other.step(a, b, None, None, 1.0 / 240.0)
     np.testing.assert_array_equal(b.particle_q.cpu().numpy(), s1.particle_q[:n].cpu().numpy())
+
+
+def test_contact_driven_refinement_through_the_solver():
+    """Geometric scoring driven by contact only (elastic weight 0): the
+    cantilever pressed by a descending capsule tool onto a ground plane, with
+    surface tris in the tri barrier.  Edges split only near the tool, on
+    refining steps; the plan's contact tris stay the boundary of the refined
+    tets; rest volume conserved; the trajectory stays finite."""
+    from tests.test_gpu_contact import PARAMS, PLANE_POSE, tool_pose
+    from mfem_gb300 import beams
+    mesh = beams.build_beam("cantilever")
+    tris = co.boundary_tris(mesh.tet_indices, mesh.rest_q.astype(np.float64))
+    base = Model.from_beam(mesh, device=DEV)
+    base.add_body(tool_pose(0)[0])
+    base.add_shape_plane(PLANE_POSE)
+    base.add_shape_capsule(0.03, 0.15, body=0)
+    base.set_tri_indices(tris)
+    model = base.pad_particles(4 * mesh.n)
+    solver = MixedFEMSolver(model, iterations=8, line_search=False, max_tets=4 * mesh.T, enable_refinement=True,
+                            refine_every_n_steps=2, refine_scoring="geometric", refine_geometric_threshold=0.2,
+                            refine_min_edge_length=0.03, refine_elastic_weight=0.0, refine_density=1000.0,
+                            **PARAMS)
+    vol0 = ro.rest_volume_total(mesh.rest_q, mesh.tet_indices)[0]
+    A, B = model.state(), model.state()
+    grew_on = []
+    for k in range(8):
+        before = solver.active_tet_count
+        B.body_q.copy_(torch.as_tensor(tool_pose(k), device=DEV))
+        A.body_q.copy_(B.body_q)
+        solver.step(A, B, None, None, mesh.spec.dt)
+        A, B = B, A
+        if solver.active_tet_count > before:
+            grew_on.append(k)
+        n = solver.active_particle_count
+        assert np.isfinite(A.particle_q[:n].cpu().numpy()).all()
+    assert grew_on and all(k % 2 == 0 for k in grew_on), grew_on
+    m = solver.refined_mesh()
+    n = solver.active_particle_count
+    assert m["tets"].max() < n
+    vol, vmin = ro.rest_volume_total(m["rest"], m["tets"])
+    assert vmin > 0.0 and vol == pytest.approx(vol0, rel=1e-6)
+    assert ro.is_conforming(m["tets"])
+    new_rest = m["rest"][mesh.n:n]
+    assert new_rest.shape[0] > 0 and np.all(np.abs(new_rest[:, 0] - 0.85) < 0.25), new_rest[:, 0]
+    canon = lambda t: sorted(map(tuple, np.sort(np.asarray(t), axis=1)))
+    assert canon(m["tris"]) == canon(co.boundary_tris(m["tets"], m["rest"].astype(np.float64)))

@@ -49,30 +49,43 @@ static bool check_tets(int n, int T, const int32_t *tets, std::string &err) {
     return true;
 }
 
+// Tets of each vertex, ascending, as codes tet * 4 + corner (a counting sort).
+static void vertex_tets(int n, int T, const int32_t *tets, std::vector<int64_t> &vptr, std::vector<int32_t> &vcode) {
+    vptr.assign((size_t)n + 1, 0);
+    for (int64_t i = 0; i < (int64_t)T * 4; ++i) vptr[tets[i] + 1]++;
+    for (int v = 0; v < n; ++v) vptr[v + 1] += vptr[v];
+    vcode.assign((size_t)T * 4, 0);
+    std::vector<int64_t> fill(vptr.begin(), vptr.end() - 1);
+    for (int64_t i = 0; i < (int64_t)T * 4; ++i) vcode[fill[tets[i]]++] = (int32_t)i;
+}
+
 bool build_sparsity(int n, int T, const int32_t *tets, std::vector<int32_t> &row_ptr, std::vector<int32_t> &col_idx,
                     std::string &err) {
     if (!check_tets(n, T, tets, err)) return false;
-    // candidate columns per row: the diagonal plus 4 per incident tet
-    std::vector<int64_t> cap(n + 1, 0);
-    for (int v = 0; v < n; ++v) cap[v + 1] = 1;
-    for (int64_t i = 0; i < (int64_t)T * 4; ++i) cap[tets[i] + 1] += 4;
-    for (int v = 0; v < n; ++v) cap[v + 1] += cap[v];
-    std::vector<int32_t> cand(cap[n]);
-    std::vector<int64_t> fill(cap.begin(), cap.end() - 1);
-    for (int v = 0; v < n; ++v) cand[fill[v]++] = v;
-    for (int e = 0; e < T; ++e) {
-        const int32_t *t = tets + 4 * (int64_t)e;
-        for (int k = 0; k < 4; ++k)
-            for (int l = 0; l < 4; ++l) cand[fill[t[k]]++] = t[l];
-    }
-    row_ptr.assign(n + 1, 0);
+    // per row: the diagonal and the vertices of the row's tets, made unique
+    // with a stamp array and sorted (a few dozen columns a row)
+    std::vector<int64_t> vptr;
+    std::vector<int32_t> vcode;
+    vertex_tets(n, T, tets, vptr, vcode);
+    std::vector<int32_t> stamp((size_t)n, -1);
+    std::vector<int32_t> row;
+    row_ptr.assign((size_t)n + 1, 0);
     col_idx.clear();
-    col_idx.reserve(cap[n] / 2);
+    col_idx.reserve((size_t)T * 4 + (size_t)n);
     for (int v = 0; v < n; ++v) {
-        auto b = cand.begin() + cap[v], e = cand.begin() + cap[v + 1];
-        std::sort(b, e);
-        auto u = std::unique(b, e);
-        col_idx.insert(col_idx.end(), b, u);
+        row.clear();
+        stamp[v] = v;
+        row.push_back(v);
+        for (int64_t i = vptr[v]; i < vptr[v + 1]; ++i) {
+            const int32_t *t = tets + 4 * (int64_t)(vcode[i] >> 2);
+            for (int l = 0; l < 4; ++l)
+                if (stamp[t[l]] != v) {
+                    stamp[t[l]] = v;
+                    row.push_back(t[l]);
+                }
+        }
+        std::sort(row.begin(), row.end());
+        col_idx.insert(col_idx.end(), row.begin(), row.end());
         if (col_idx.size() > (size_t)INT32_MAX) {
             err = "sparsity exceeds 2^31 blocks";
             return false;
@@ -85,18 +98,31 @@ bool build_sparsity(int n, int T, const int32_t *tets, std::vector<int32_t> &row
 bool build_slot_map(int n, int T, const int32_t *tets, const int32_t *row_ptr, const int32_t *col_idx, int32_t *slots,
                     std::string &err) {
     if (!check_tets(n, T, tets, err)) return false;
-    for (int e = 0; e < T; ++e) {
-        const int32_t *t = tets + 4 * (int64_t)e;
-        for (int k = 0; k < 4; ++k) {
-            const int32_t *b = col_idx + row_ptr[t[k]];
-            const int32_t *en = col_idx + row_ptr[t[k] + 1];
+    // per row: each column's slot through a stamped position array, then
+    // the slots of the row's tet corners
+    std::vector<int64_t> vptr;
+    std::vector<int32_t> vcode;
+    vertex_tets(n, T, tets, vptr, vcode);
+    std::vector<int32_t> stamp((size_t)n, -1), pos((size_t)n, 0);
+    for (int v = 0; v < n; ++v) {
+        for (int32_t j = row_ptr[v]; j < row_ptr[v + 1]; ++j) {
+            const int32_t c = col_idx[j];
+            if (c < 0 || c >= n) {
+                err = "column index out of range in row " + std::to_string(v);
+                return false;
+            }
+            stamp[c] = v;
+            pos[c] = j;
+        }
+        for (int64_t i = vptr[v]; i < vptr[v + 1]; ++i) {
+            const int32_t e = vcode[i] >> 2, k = vcode[i] & 3;
+            const int32_t *t = tets + 4 * (int64_t)e;
             for (int l = 0; l < 4; ++l) {
-                const int32_t *p = std::lower_bound(b, en, t[l]);
-                if (p == en || *p != t[l]) {
-                    err = "sparsity lacks block (" + std::to_string(t[k]) + ", " + std::to_string(t[l]) + ")";
+                if (stamp[t[l]] != v) {
+                    err = "sparsity lacks block (" + std::to_string(v) + ", " + std::to_string(t[l]) + ")";
                     return false;
                 }
-                slots[(int64_t)e * 16 + k * 4 + l] = (int32_t)(p - col_idx);
+                slots[(int64_t)e * 16 + k * 4 + l] = pos[t[l]];
             }
         }
     }
