@@ -36,6 +36,7 @@
 // flag and leaves x and s unchanged, reporting MFEM_TIMEOUT.
 #include <algorithm>
 
+#include "grid_sync.cuh"
 #include "merit.cuh"
 
 namespace mfem {
@@ -138,19 +139,17 @@ __global__ void __launch_bounds__(kLsThreads, 4) line_search_kernel(LsArgs a) {
             }
             // arrive: the partials are released before the counter moves
             target += nb;
-            __threadfence();
-            atomicAdd(w.counter, 1ull);
+            grid_arrive(w.counter);
             int ok = 1;
             const long long t0 = clock64();
             unsigned spins = 0;
-            while (ld_relaxed(w.counter) < target) {
+            while (grid_count(w.counter) < target) {
                 if ((++spins & 1023u) == 0 && (ld_volatile(a.error) != 0 || clock64() - t0 > kWaitCycles)) {
                     atomicExch(a.error, 1);
                     ok = 0;
                     break;
                 }
             }
-            __threadfence();
             s_ok = ok;
         }
         __syncthreads();

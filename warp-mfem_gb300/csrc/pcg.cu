@@ -37,15 +37,20 @@
 // Grid synchronisation is a reduction: each CTA stores its partial sums
 // (double buffered by barrier parity), then arrives on a 64-bit counter that
 // is never reset -- the k-th barrier of a launch releases at base + k * CTAs
-// -- with one thread per CTA polling it.  (Measured on GB300 with 152 CTAs:
-// 1.3 us per barrier, against 4.6 us for per-CTA flag words that every CTA
-// polls.)  After the release every CTA reads all partials in one round trip
-// while its thread 0 issues the next window copies, and sums them in the same
-// fixed order, so all CTAs take the same decisions and the result is
-// deterministic.  Dot products and the scalar recurrence are float32 like
-// the reference's CG (GB300's float64 rate is low); the scalars are computed
-// by one thread per CTA and broadcast.  Stopping test ||r|| <= tol ||g|| on
-// the recurrence residual, before the first iteration and after each one.
+// -- with one thread per CTA polling it (release add, acquire loads:
+// grid_sync.cuh).  Measured on GB300 with 152 CTAs, partials round trip
+// included: 1.94 us per barrier.  Per-CTA flag words that every CTA polls
+// took 4.6 us; per-CTA "published" words polled only by the CTAs whose
+// windows they feed, to start the window copies before the whole grid has
+// arrived, took 3.4 us packed eight to a cache line and 2.3 us one to a line,
+// both slower than this barrier alone.  After the release every CTA reads
+// all partials in one round trip while its thread 0 issues the next window
+// copies, and sums them in the same fixed order, so all CTAs take the same
+// decisions and the result is deterministic.  Dot products and the scalar
+// recurrence are float32 like the reference's CG (GB300's float64 rate is
+// low); the scalars are computed by one thread per CTA and broadcast.
+// Stopping test ||r|| <= tol ||g|| on the recurrence residual, before the
+// first iteration and after each one.
 //
 // Every wait (barrier, mbarrier) is bounded; after a timeout the kernel sets
 // the sticky error flag, waits (bounded) for its own copies in flight and

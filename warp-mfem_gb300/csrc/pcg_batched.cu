@@ -22,6 +22,7 @@
 
 #include "block_loads.cuh"
 #include "factor_apply.cuh"
+#include "grid_sync.cuh"
 #include "internal.h"
 
 namespace mfem {
@@ -74,12 +75,11 @@ __device__ bool bt_reduce(float (&v)[NV], const BatchViews &bw, const Task &tk, 
 #pragma unroll
                 for (int i = 0; i < NV; ++i) buf[(size_t)(tk.first + tk.rank) * 4 + i] = part[i];
                 target += tk.size;
-                __threadfence();
-                atomicAdd(bw.counter + tk.body, 1ull);
+                grid_arrive(bw.counter + tk.body);
                 int ok = 1;
                 const long long t0 = clock64();
                 unsigned spins = 0;
-                while (bt_ld_relaxed(bw.counter + tk.body) < target) {
+                while (grid_count(bw.counter + tk.body) < target) {
                     if ((++spins & 1023u) == 0 &&
                         (*(const volatile int *)error != 0 || clock64() - t0 > kBtWaitCycles)) {
                         atomicExch(error, 1);
@@ -87,7 +87,6 @@ __device__ bool bt_reduce(float (&v)[NV], const BatchViews &bw, const Task &tk, 
                         break;
                     }
                 }
-                __threadfence();
                 *s_ok = ok;
             }
             __syncwarp();

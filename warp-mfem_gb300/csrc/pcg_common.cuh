@@ -7,6 +7,7 @@
 
 #include "block_loads.cuh"
 #include "double_float.cuh"
+#include "grid_sync.cuh"
 #include "internal.h"
 
 namespace mfem {
@@ -149,19 +150,17 @@ __device__ bool reduce_arrive(float (&v)[NV], float *partials, unsigned k, unsig
             // arrive: every earlier store of this CTA (published vectors,
             // partials) is released before the counter moves
             target += gridDim.x;
-            __threadfence();
-            atomicAdd(counter, 1ull);
+            grid_arrive(counter);
             int ok = 1;
             const long long t0 = clock64();
             unsigned spins = 0;
-            while (ld_relaxed(counter) < target) {
+            while (grid_count(counter) < target) {
                 if ((++spins & 1023u) == 0 && (ld_volatile(error) != 0 || clock64() - t0 > kWaitCycles)) {
                     atomicExch(error, 1);
                     ok = 0;
                     break;
                 }
             }
-            __threadfence();
             *s_ok = ok;
         }
     }
@@ -233,19 +232,17 @@ __device__ bool reduce_arrive_d(double (&v)[NV], double *partials, unsigned k, u
 #pragma unroll
             for (int i = 0; i < NV; ++i) buf[i] = part[i];
             target += gridDim.x;
-            __threadfence();
-            atomicAdd(counter, 1ull);
+            grid_arrive(counter);
             int ok = 1;
             const long long t0 = clock64();
             unsigned spins = 0;
-            while (ld_relaxed(counter) < target) {
+            while (grid_count(counter) < target) {
                 if ((++spins & 1023u) == 0 && (ld_volatile(error) != 0 || clock64() - t0 > kWaitCycles)) {
                     atomicExch(error, 1);
                     ok = 0;
                     break;
                 }
             }
-            __threadfence();
             *s_ok = ok;
         }
     }

@@ -46,6 +46,7 @@
 
 #include "double_float.cuh"
 #include "factor_apply.cuh"
+#include "grid_sync.cuh"
 #include "internal.h"
 
 namespace mfem {
@@ -284,19 +285,17 @@ __device__ bool ir_reduce(double (&v)[NV], const IrWork &w, int *error, unsigned
 #pragma unroll
             for (int i = 0; i < NV; ++i) buf[(size_t)blockIdx.x * 4 + i] = part[i];
             target += nb;
-            __threadfence();
-            atomicAdd(w.counter, 1ull);
+            grid_arrive(w.counter);
             int ok = 1;
             const long long t0 = clock64();
             unsigned spins = 0;
-            while (ir_ld_relaxed(w.counter) < target) {
+            while (grid_count(w.counter) < target) {
                 if ((++spins & 1023u) == 0 && (*(const volatile int *)error != 0 || clock64() - t0 > kIrWaitCycles)) {
                     atomicExch(error, 1);
                     ok = 0;
                     break;
                 }
             }
-            __threadfence();
             *s_ok = ok;
         }
     }

@@ -34,6 +34,7 @@
 #include <algorithm>
 #include <string>
 
+#include "grid_sync.cuh"
 #include "internal.h"
 
 namespace mfem {
@@ -111,12 +112,11 @@ __device__ bool na_reduce(float (&v)[NV], const NaArgs &a, unsigned k, unsigned 
 #pragma unroll
             for (int i = 0; i < NV; ++i) buf[(size_t)blockIdx.x * 4 + i] = part[i];
             target += nb;
-            __threadfence();
-            atomicAdd(a.counter, 1ull);
+            grid_arrive(a.counter);
             int ok = 1;
             const long long t0 = clock64();
             unsigned spins = 0;
-            while (na_ld_relaxed(a.counter) < target) {
+            while (grid_count(a.counter) < target) {
                 if ((++spins & 1023u) == 0 &&
                     (*(const volatile int *)a.error != 0 || clock64() - t0 > kNaWaitCycles)) {
                     atomicExch(a.error, 1);
@@ -124,7 +124,6 @@ __device__ bool na_reduce(float (&v)[NV], const NaArgs &a, unsigned k, unsigned 
                     break;
                 }
             }
-            __threadfence();
             *s_ok = ok;
         }
     }
