@@ -63,6 +63,60 @@ namespace {
 // ===========================================================================
 // single-reduction (Chronopoulos-Gear) PCG
 // ===========================================================================
+// The single-reduction kernel keeps its cached slice of H as 48-byte blocks:
+// the nine values, the column relative to the window as int bits, two zeros,
+// read with three 16-byte loads instead of ten 4-byte ones (the sums in the
+// order of window_product, so the iterates are the same bit for bit).
+__device__ __forceinline__ void load_matrix_slice48(const PcgArgs &a, const Common &c, int *rowoff, float *sHB) {
+    for (int i = threadIdx.x; i <= c.nrows; i += blockDim.x) rowoff[i] = a.row_ptr[c.row_lo + i] - c.blk_lo;
+    for (int t = threadIdx.x; t < 12 * c.nblk; t += blockDim.x) {
+        const int k = t / 12, e = t - 12 * k;
+        float v = 0.0f;
+        if (e < 9) v = a.values[(size_t)9 * (c.blk_lo + k) + e];
+        else if (e == 9) v = __int_as_float(a.col_idx[c.blk_lo + k] - c.win_lo);
+        sHB[t] = v;
+    }
+}
+
+template <bool CACHE>
+__device__ __forceinline__ void product48(const PcgArgs &a, const int *rowoff, const float *sH, const int *sCol,
+                                          int blk_lo, int win_lo, int nrows, const float *win, float *out,
+                                          const HBlocks &hm, int row_lo) {
+    if constexpr (!CACHE) {
+        window_product<false>(a, rowoff, sH, sCol, blk_lo, win_lo, nrows, win, out, hm, row_lo);
+    } else {
+        const int g_lane = threadIdx.x & (kGroup - 1);
+        const int group = threadIdx.x / kGroup;
+        const int ngroups = blockDim.x / kGroup;
+        const unsigned gmask = ((1u << kGroup) - 1u) << (threadIdx.x & (32 - kGroup));
+        const float4 *blocks = reinterpret_cast<const float4 *>(sH);
+        for (int i = group; i < nrows; i += ngroups) {
+            const int kb = rowoff[i], ke = rowoff[i + 1];
+            float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+#pragma unroll 4
+            for (int k = kb + g_lane; k < ke; k += kGroup) {
+                const float4 h0 = blocks[3 * k], h1 = blocks[3 * k + 1], h2 = blocks[3 * k + 2];
+                const int c = __float_as_int(h2.y);
+                const float v0 = win[3 * c + 0], v1 = win[3 * c + 1], v2 = win[3 * c + 2];
+                a0 += h0.x * v0 + h0.y * v1 + h0.z * v2;
+                a1 += h0.w * v0 + h1.x * v1 + h1.y * v2;
+                a2 += h1.z * v0 + h1.w * v1 + h2.x * v2;
+            }
+#pragma unroll
+            for (int off = kGroup / 2; off > 0; off >>= 1) {
+                a0 += __shfl_xor_sync(gmask, a0, off);
+                a1 += __shfl_xor_sync(gmask, a1, off);
+                a2 += __shfl_xor_sync(gmask, a2, off);
+            }
+            if (g_lane == 0) {
+                out[3 * i + 0] = a0;
+                out[3 * i + 1] = a1;
+                out[3 * i + 2] = a2;
+            }
+        }
+    }
+}
+
 template <bool CACHE>
 __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -80,8 +134,8 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
     float *wS = wW + 3 * win_max;
     float *wM = wS + 3 * win_max;
     int *rowoff = reinterpret_cast<int *>(wM + 9 * win_max);
-    float *sH = reinterpret_cast<float *>(rowoff + rows_max + 4);
-    int *sCol = reinterpret_cast<int *>(sH + (CACHE ? 9 * a.blk_max : 0));
+    float *sH = reinterpret_cast<float *>(rowoff + rows_max + 4);  // with CACHE: 48-byte blocks
+    int *sCol = nullptr;
 
     const size_t vec = (size_t)3 * a.n_pad;
     float *pubR[2] = {a.pub, a.pub + vec};
@@ -90,7 +144,8 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
     const int own = cm.row_lo - cm.win_lo;  // offset of the own rows inside the window
     const uint32_t wbytes = (uint32_t)cm.nwin * 12u;
 
-    load_matrix_slice(a, cm, rowoff, sH, sCol, CACHE, HBlocks{a.values, nullptr, nullptr, 0});
+    if (CACHE) load_matrix_slice48(a, cm, rowoff, sH);
+    else load_matrix_slice(a, cm, rowoff, sH, sCol, false, hf32);
     // window of M^-1 blocks (kept for the whole solve) and of the warm start
     bool ok = true;
     if (threadIdx.x == 0 && cm.nwin > 0) {
@@ -104,7 +159,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
     // ---- r0 = g - H x0, published
     if (ok) {
         for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = wR[3 * own + i];
-        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wR, sW, hf32, cm.row_lo);
+        product48<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wR, sW, hf32, cm.row_lo);
         __syncthreads();
         float acc[1] = {0.0f};
         for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) {
@@ -139,7 +194,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
             wW[3 * j + 2] = u[2];
         }
         __syncthreads();
-        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wW, sW, hf32, cm.row_lo);
+        product48<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wW, sW, hf32, cm.row_lo);
         __syncthreads();
         float acc[3] = {0.0f, 0.0f, 0.0f};
         for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) {
@@ -223,7 +278,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
             ps[(size_t)3 * cm.row_lo + i] = wS[3 * own + i];
         }
         // w' = H u'
-        window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wW, sW, hf32, cm.row_lo);
+        product48<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wW, sW, hf32, cm.row_lo);
         __syncthreads();
         float *pw = pubW[(it + 1) & 1];
         float acc[3] = {0.0f, 0.0f, 0.0f};
@@ -685,7 +740,7 @@ size_t smem_gather(int rows_max, int blk_max, bool cache) {
 size_t smem_single(int rows_max, int win_max, int blk_max, bool cache) {
     size_t floats = (size_t)rows_max * 12 + (size_t)win_max * 18;
     size_t bytes = floats * 4 + (size_t)(rows_max + 4) * 4;
-    if (cache) bytes += (size_t)blk_max * 40;
+    if (cache) bytes += (size_t)blk_max * 48;  // load_matrix_slice48
     return (bytes + 15) & ~(size_t)15;
 }
 
