@@ -294,15 +294,15 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
             break;
         }
         ++it;
-        // stage the next state while the totals are fetched
-        if (threadIdx.x == 0 && cm.nwin > 0) {
+        // stage the next state from warp 1 while warp 0 fetches the totals
+        if (threadIdx.x == 32 && cm.nwin > 0) {
             tma_expect(&s_mbar, 3u * wbytes);
             tma_copy(wR, pr + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
             tma_copy(wW, pw + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
             tma_copy(wS, ps + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
         }
         pending = cm.nwin > 0;
-        reduce_totals<3>(a.partials, bar, s_val, s_tot);
+        reduce_totals_w0<3>(a.partials, bar, s_tot);
         ++bar;
         if (threadIdx.x == 0) {
             const float gamma_new = s_tot[0], delta = s_tot[1], rr = s_tot[2];
@@ -446,7 +446,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_standard_kernel(PcgArgs a)
             if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
             break;
         }
-        reduce_totals<1>(a.partials, bar, s_val, s_tot);
+        reduce_totals_w0<1>(a.partials, bar, s_tot);
         ++bar;
         if (threadIdx.x == 0) {
             const float pAp = s_tot[0];
@@ -488,13 +488,14 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_standard_kernel(PcgArgs a)
             break;
         }
         ++it;
-        if (threadIdx.x == 0 && cm.nwin > 0) {
+        // the copies from warp 1 while warp 0 fetches the totals
+        if (threadIdx.x == 32 && cm.nwin > 0) {
             tma_expect(&s_mbar, 2u * wbytes);
             tma_copy(winA, pubZ + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
             tma_copy(winB, p_new + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
         }
         pending = cm.nwin > 0;
-        reduce_totals<2>(a.partials, bar, s_val, s_tot);
+        reduce_totals_w0<2>(a.partials, bar, s_tot);
         ++bar;
         if (threadIdx.x == 0) {
             sc.rr = s_tot[1];
@@ -672,7 +673,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_gather_kernel(PcgArgs a) {
             if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
             break;
         }
-        reduce_totals<1>(a.partials, bar, s_val, s_tot);
+        reduce_totals_w0<1>(a.partials, bar, s_tot);
         ++bar;
         if (threadIdx.x == 0) {
             const float pAp = s_tot[0];
@@ -712,7 +713,7 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_gather_kernel(PcgArgs a) {
             break;
         }
         ++it;
-        reduce_totals<2>(a.partials, bar, s_val, s_tot);
+        reduce_totals_w0<2>(a.partials, bar, s_tot);
         ++bar;
         if (threadIdx.x == 0) {
             sc.rr = s_tot[1];

@@ -202,6 +202,45 @@ __device__ void reduce_totals(const float *partials, unsigned k, float *s_val, f
     __syncthreads();
 }
 
+// reduce_totals in warp 0 alone, for callers whose totals only thread 0
+// reads: each lane loads its CTAs' partials into registers first (all in
+// flight at once), then the warp adds them in reduce_totals' order, so the
+// totals are the same bit for bit.  No shared-memory staging and no CTA-wide
+// sync; tot[] is valid in thread 0 on return, and warps 1.. return at once
+// (a window copy issued from warp 1 then leaves while warp 0 loads).
+template <int NV>
+__device__ __forceinline__ void reduce_totals_w0(const float *partials, unsigned k, float *tot) {
+    if (threadIdx.x >= 32) return;
+    const int nb = gridDim.x, lane = threadIdx.x;
+    const float *buf = partials + (size_t)(k & 1u) * kMaxCtas * 4;
+    float v[kMaxCtas / 32][NV];
+#pragma unroll
+    for (int j = 0; j < kMaxCtas / 32; ++j) {
+        const int b = lane + 32 * j;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) v[j][i] = b < nb ? __ldcg(buf + (size_t)b * 4 + i) : 0.0f;
+    }
+    float acc[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) acc[i] = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kMaxCtas / 32; ++j) {
+        if (lane + 32 * j < nb) {
+#pragma unroll
+            for (int i = 0; i < NV; ++i) acc[i] += v[j][i];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc[i] += __shfl_down_sync(0xffffffffu, acc[i], off);
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) tot[i] = acc[i];
+    }
+}
+
 // reduce_arrive and reduce_totals in double, on a double partials buffer of
 // the same [2][kMaxCtas][4] shape and the same barrier counter and parity.
 template <int NV>

@@ -518,12 +518,13 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
                 if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
                 break;
             }
+            // the copy from warp 1 while warp 0 fetches the totals
             const bool ap_pending = factor && nr > 0;
-            if (ap_pending && threadIdx.x == 0) {
+            if (ap_pending && threadIdx.x == 32) {
                 tma_expect(&s_mbar, rbytes);
                 tma_copy(winB, pubAp + (size_t)3 * r_lo, rbytes, &s_mbar);
             }
-            reduce_totals<1>(a.partials, bar, s_val, s_tot);
+            reduce_totals_w0<1>(a.partials, bar, s_tot);
             ++bar;
             if (threadIdx.x == 0) {
                 const float pAp = s_tot[0];
@@ -583,13 +584,13 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
                 break;
             }
             ++it;
-            if (threadIdx.x == 0 && cm.nwin > 0) {
+            if (threadIdx.x == 32 && cm.nwin > 0) {
                 tma_expect(&s_mbar, 2u * wbytes);
                 tma_copy(winA, pubZ + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
                 tma_copy(winB, p_new + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
             }
             pending = cm.nwin > 0;
-            reduce_totals<2>(a.partials, bar, s_val, s_tot);
+            reduce_totals_w0<2>(a.partials, bar, s_tot);
             ++bar;
             if (threadIdx.x == 0) {
                 sc.rr = s_tot[1];
