@@ -251,3 +251,56 @@ def test_mixed_with_line_search_matches_oracle(pc):
         assert all(s["status"] == _lib.MFEM_OK for s in solver.mixed_stats())
         assert all(e["status"] == 0 for e in solver.line_search_stats())
         close(A.particle_q.cpu().numpy(), q, 1e-5)
+
+
+@pytest.mark.parametrize("variant", ["auto", "global_memory"])
+@pytest.mark.parametrize("name,cells", [("nh_beam", (16, 4, 4)), ("stiff_beam", (32, 8, 8))])
+def test_fp32_refined_block_jacobi_reaches_fp64_tolerance(name, cells, variant):
+    """fp32 blocks inside the fp64 refinement with block-Jacobi: the inner
+    solves run in the single-reduction PCG, one launch a correction (auto),
+    or in the global-memory inner PCG.  Either way the fp64 residual of the
+    returned solution, recomputed here, meets the outer tolerance and agrees
+    with the one the solver reports."""
+    mesh, _, solver = make(name, cells, "fp32_refined", pcg_variant=variant)
+    if variant == "auto":
+        assert solver.pcg_layout()["variant"] == "single_reduction"
+    H, g, dx64, dx32 = one_solve(mesh, solver)
+    rel = np.linalg.norm(g - H @ dx64) / np.linalg.norm(g)
+    st = solver.mixed_stats()[0]
+    assert st["status"] == _lib.MFEM_OK and 1 <= st["outer_iterations"] <= 10, st
+    assert st["fp32_inner"] == 1, st
+    assert rel <= 1e-8 and st["rel_residual"] <= 1e-8, (rel, st)
+    # fp32 inner solves end far below the target (near 1e-10), where the
+    # reported residual's double-float pass (about 1e-12 of ||g|| absolute)
+    # and numpy's float64 differ by a few percent
+    assert rel == pytest.approx(st["rel_residual"], rel=1e-3, abs=5e-12)
+    np.testing.assert_array_equal(dx32, dx64.astype(np.float32))
+    s0 = solver.solve_stats()[0]
+    assert s0["iterations"] == st["inner_iterations"] and s0["status"] == st["status"]
+
+
+def test_fp32_refined_trajectory_matches_fp64_oracle():
+    mesh, model, solver = make("nh_beam", (16, 4, 4), "fp32_refined")
+    ref = O.OracleSolver(mesh, dtype=np.float64)
+    A, B = model.state(), model.state()
+    A.particle_q.copy_(torch.as_tensor(mesh.q0, device=DEV))
+    q, qd = mesh.q0, mesh.qd0
+    for _ in range(3):
+        solver.step(A, B, None, None, mesh.spec.dt)
+        A, B = B, A
+        q, qd = ref.step(q, qd, mesh.spec.dt)
+        stats = solver.mixed_stats()
+        assert all(s["status"] == _lib.MFEM_OK and s["rel_residual"] <= 1e-8 for s in stats), stats
+        close(A.particle_q.cpu().numpy(), q, 1e-5)
+
+
+def test_fp32_refined_graph_and_eager_agree_bitwise():
+    outs = []
+    for graph in (True, False):
+        mesh, model, solver = make("nh_beam", (16, 4, 4), "fp32_refined", use_cuda_graph=graph)
+        A, B = model.state(), model.state()
+        for _ in range(2):
+            solver.step(A, B, None, None, mesh.spec.dt)
+            A, B = B, A
+        outs.append(A.particle_q.clone())
+    assert torch.equal(outs[0], outs[1])

@@ -223,7 +223,8 @@ bool net_ready(const mfem_plan *p) { return p->cfg.preconditioner != 3 || p->fv.
 cudaError_t global_solve(mfem_plan *p, int slot, cudaStream_t s) {
     if (p->ir.mode != 0)
         return launch_mixed_solve(p->bv, p->vv, p->ir, p->pw, p->bw,
-                                  p->pl.variant == PcgLayout::kFactor ? p->pl : p->ir_pl, p->pcg_ctas, slot,
+                                  p->pl.variant == PcgLayout::kFactor ? p->pl : p->ir_pl,
+                                  p->pl.variant == PcgLayout::kSingleReduction ? &p->pl : nullptr, p->pcg_ctas, slot,
                                   p->cfg.cg_max_iterations, p->cfg.preconditioner, s);
     if (p->pl.variant == PcgLayout::kFactor)
         return launch_pcg_factor(p->bv, p->vv, p->pw, p->bw, p->pl, p->pcg_ctas, slot, p->cfg.cg_tolerance,

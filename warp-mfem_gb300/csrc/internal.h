@@ -405,6 +405,11 @@ cudaError_t line_search_max_ctas(int device, int *ctas);
 cudaError_t launch_velocity(const float *q_out, float *qd_out, float dt, const VertexViews &vv, cudaStream_t s);
 cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const PcgLayout &L, int ctas,
                        int slot, float tol, int maxiter, int use_precond, cudaStream_t s);
+// The single-reduction PCG (L a kSingleReduction layout) as one inner solve of
+// the refinement's launch sequence: block-Jacobi on the fp32 H, ir.res to
+// inner_tol from 0, the correction in ir.e, ir.state updated.
+cudaError_t launch_pcg_inner(const BsrViews &bv, const VertexViews &vv, const IrWork &ir, const PcgWork &w,
+                             const PcgLayout &L, int ctas, int slot, int maxiter, cudaStream_t s);
 cudaError_t pcg_max_ctas(int device, int *ctas);
 cudaError_t pcg_plan_layout(int device, PcgLayout &L, const int32_t *row_ptr, const int32_t *col_idx, int n,
                             int ctas, int variant, std::vector<int4> &cta_info, std::string &err);
@@ -428,9 +433,11 @@ cudaError_t batch_capacity(int device, int threads, bool factor, int *ctas);
 cudaError_t launch_batched_pcg(const BsrViews &bv, const VertexViews &vv, const BatchViews &bw, int *error, int slot,
                                float tol, int maxiter, int use_precond, cudaStream_t s);
 int ir_residual_blocks(int n);
+// single: the plan's single-reduction layout, or null.  With fp32 blocks and
+// block-Jacobi the inner solves run there, one launch a correction.
 cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const IrWork &w, const PcgWork &pw,
-                               const BatchViews &fb, const PcgLayout &pl, int pcg_ctas, int slot, int maxiter,
-                               int use_precond, cudaStream_t s);
+                               const BatchViews &fb, const PcgLayout &pl, const PcgLayout *single, int pcg_ctas,
+                               int slot, int maxiter, int use_precond, cudaStream_t s);
 // The whole mixed refinement in one launch of the persistent factor PCG
 // (needs IrWork's xf_hi / xf_lo): the warm start in vv.dx, the solution
 // written back there.

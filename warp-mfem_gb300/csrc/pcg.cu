@@ -120,7 +120,24 @@ __device__ __forceinline__ void product48(const PcgArgs &a, const int *rowoff, c
 template <bool CACHE>
 __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
+    // As an inner solve of the mixed-precision refinement's launch sequence
+    // (fp32 blocks, block-Jacobi): nothing to do once the refinement has
+    // finished; otherwise a solve from 0 of the residual scaled to unit norm
+    // (ir_scale[0]), the correction scaled back (ir_scale[1]) and the state
+    // words updated as the factor kernel's inner solve does (pcg_factor.cu).
+    const bool inner = a.ir_state != nullptr;
+    if (inner) {
+        if (ld_volatile(a.ir_state) != 0 || ld_volatile(a.ir_state + 7) != 0) return;
+        if (ld_volatile(a.error) != 0) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                a.ir_state[5] = MFEM_TIMEOUT;
+                a.ir_state[0] = 1;
+            }
+            return;
+        }
+    }
     PCG_PROLOGUE
+    const float bscale = inner ? a.ir_scale[0] : 1.0f;
     const HBlocks hf32{a.values, nullptr, nullptr, 0};
     const int rows_max = a.rows_max, win_max = a.win_max;
     // own rows
@@ -149,21 +166,25 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
     // window of M^-1 blocks (kept for the whole solve) and of the warm start
     bool ok = true;
     if (threadIdx.x == 0 && cm.nwin > 0) {
-        tma_expect(&s_mbar, wbytes * 4u);
+        tma_expect(&s_mbar, wbytes * (inner ? 3u : 4u));
         tma_copy(wM, a.Minv + (size_t)9 * cm.win_lo, wbytes * 3u, &s_mbar);
-        tma_copy(wR, a.x + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
+        if (!inner) tma_copy(wR, a.x + (size_t)3 * cm.win_lo, wbytes, &s_mbar);
     }
     if (cm.nwin > 0) ok = tma_wait(&s_mbar, parity, a.error);
 
     int it = 0;
-    // ---- r0 = g - H x0, published
+    // ---- r0 = g - H x0 (x0 = 0 for an inner solve), published
     if (ok) {
-        for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = wR[3 * own + i];
-        product48<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wR, sW, hf32, cm.row_lo);
+        if (inner) {
+            for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = sW[i] = 0.0f;
+        } else {
+            for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) sX[i] = wR[3 * own + i];
+            product48<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, wR, sW, hf32, cm.row_lo);
+        }
         __syncthreads();
         float acc[1] = {0.0f};
         for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) {
-            const float bg = a.b[(size_t)3 * cm.row_lo + i];
+            const float bg = a.b[(size_t)3 * cm.row_lo + i] * bscale;
             pubR[0][(size_t)3 * cm.row_lo + i] = bg - sW[i];
             acc[0] = __fmaf_rn(bg, bg, acc[0]);
         }
@@ -242,12 +263,10 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
             if (threadIdx.x == 0) sc.status = MFEM_MAXITER;
             break;
         }
-        // state `it` of the window: r, w (and s of the previous iteration)
-        if (pending && !tma_wait(&s_mbar, parity, a.error)) {
-            pending = false;
-            if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
-            break;
-        }
+        // state `it` of the window: r, w (and s of the previous iteration);
+        // each thread waits for the copies itself and the verdicts join the
+        // sync after the window update
+        const bool landed = !pending || tma_wait_local(&s_mbar, parity);
         pending = false;
         const float fa = sc.alpha, fb = sc.beta;
         // s = w + beta s; r' = r - alpha s; u' = M r'   (every window row)
@@ -265,7 +284,13 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
             wW[3 * j + 1] = u[1];
             wW[3 * j + 2] = u[2];
         }
-        __syncthreads();
+        if (!__syncthreads_and(landed)) {
+            if (threadIdx.x == 0) {
+                atomicExch(a.error, 1);
+                sc.status = MFEM_TIMEOUT;
+            }
+            break;
+        }
         // own rows: p = u + beta p, x += alpha p; publish r', s
         float *pr = pubR[(it + 1) & 1];
         float *ps = pubS[(it + 1) & 1];
@@ -329,7 +354,22 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_single_kernel(PcgArgs a) {
     }
     if (pending) tma_wait(&s_mbar, parity, a.error);
     __syncthreads();
-    finish(a, cm, sX, sc, it);
+    if (!inner) {
+        finish(a, cm, sX, sc, it);
+        return;
+    }
+    // the correction for the refinement and its state (a solve that stopped
+    // at the cap or stagnated still hands over its iterate)
+    const float es = a.ir_scale[1];
+    for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x) a.x[(size_t)3 * cm.row_lo + i] = sX[i] * es;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.ir_state[2] += it;
+        a.ir_state[3] = 1;
+        if (sc.status == MFEM_TIMEOUT || sc.status == MFEM_NONFINITE) {
+            a.ir_state[5] = sc.status;
+            a.ir_state[0] = 1;
+        }
+    }
 }
 
 // ===========================================================================
@@ -843,6 +883,52 @@ cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork 
     a.Minv = vv.Minv;
     a.b = vv.rhs;
     a.x = vv.dx;
+    a.pub = w.pub;
+    a.n_pad = w.n_pad;
+    a.cta = L.cta_info;
+    a.rows_max = L.rows_max;
+    a.blk_max = L.blk_max;
+    a.win_max = L.win_max;
+    a.partials = w.partials;
+    a.counter = w.counter;
+    a.error = w.error;
+    a.stats = w.stats;
+    a.slot = slot;
+    a.tol = tol;
+    a.maxiter = maxiter;
+    a.use_precond = use_precond;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(kPcgThreads);
+    cfg.dynamicSmemBytes = L.smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t err = cudaLaunchKernelEx(&cfg, pick_kernel(L), a);
+    count_launches(1);
+    return err;
+}
+
+// The single-reduction PCG as one inner solve of the refinement's launch
+// sequence (block-Jacobi, fp32 blocks): rhs ir.res, correction to ir.e.
+cudaError_t launch_pcg_inner(const BsrViews &bv, const VertexViews &vv, const IrWork &ir, const PcgWork &w,
+                             const PcgLayout &L, int ctas, int slot, int maxiter, cudaStream_t s) {
+    if (L.variant != PcgLayout::kSingleReduction) return cudaErrorInvalidValue;
+    const float tol = ir.inner_tol;
+    const int use_precond = 1;
+    PcgArgs a = {};
+    a.n = bv.n;
+    a.row_ptr = bv.row_ptr;
+    a.col_idx = bv.col_idx;
+    a.values = bv.values;
+    a.Minv = vv.Minv;
+    a.b = ir.res;
+    a.x = ir.e;
+    a.ir_state = ir.state;
+    a.ir_scale = ir.scale;
     a.pub = w.pub;
     a.n_pad = w.n_pad;
     a.cta = L.cta_info;

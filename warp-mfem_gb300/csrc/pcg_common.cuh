@@ -342,6 +342,34 @@ __device__ __forceinline__ void tma_copy(void *dst, const void *src, uint32_t by
                  : "memory");
 }
 
+// tma_wait without the CTA sync: each thread waits for the phase itself
+// (bounded, the same second wait after a timeout), and the caller joins the
+// verdicts at its next __syncthreads_and (setting the error flag if one gave
+// up).  Per thread, not CTA-uniform.
+__device__ __forceinline__ bool tma_wait_local(uint64_t *mbar, uint32_t &parity) {
+    const uint32_t mb = smem_addr(mbar);
+    bool ok = true;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        uint32_t done = 0;
+        const long long t0 = clock64();
+        unsigned spins = 0;
+        while (!done) {
+            asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(done)
+                : "r"(mb), "r"(parity)
+                : "memory");
+            if (!done && (++spins & 255u) == 0 && clock64() - t0 > kWaitCycles / 2) break;
+        }
+        if (done) break;
+        ok = false;
+    }
+    parity ^= 1u;
+    return ok;
+}
+
 // Waits for the mbarrier phase `parity` (bounded; a second bounded wait after
 // a timeout so no copy is still writing when the CTA leaves).  CTA-uniform.
 __device__ bool tma_wait(uint64_t *mbar, uint32_t &parity, int *error) {

@@ -673,8 +673,8 @@ cudaError_t ir_max_ctas(int device, int *ctas) {
 int ir_residual_blocks(int n) { return std::max(1, blocks_for(n * kIrGroup, kResThreads)); }
 
 cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const IrWork &w, const PcgWork &pw,
-                               const BatchViews &fb, const PcgLayout &pl, int pcg_ctas, int slot, int maxiter,
-                               int use_precond, cudaStream_t s) {
+                               const BatchViews &fb, const PcgLayout &pl, const PcgLayout *single, int pcg_ctas,
+                               int slot, int maxiter, int use_precond, cudaStream_t s) {
     if (bv.n == 0) return cudaSuccess;
     const bool bf16 = w.mode == kIrBf16;
     const bool fp32 = w.mode == kIrFp32;  // the inner PCG reads the fp32 H itself
@@ -685,7 +685,11 @@ cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const 
     ir_begin_kernel<<<blocks_for(3 * vv.n, 256), 256, 0, s>>>(vv, w);
     count_launches(fp32 ? 1 : 2);
     e = cudaGetLastError();
-    if (e == cudaSuccess && w.xf_hi && (w.hq_words || fp32) && pl.variant == PcgLayout::kFactor)
+    // block-Jacobi on the fp32 H: the one-barrier single-reduction PCG for
+    // the inner solves (4.8 us an iteration on nh_beam against the factor
+    // kernel's two barriers), a launch per correction
+    const bool single_inner = fp32 && use_precond == 1 && single && single->variant == PcgLayout::kSingleReduction;
+    if (e == cudaSuccess && !single_inner && w.xf_hi && (w.hq_words || fp32) && pl.variant == PcgLayout::kFactor)
         // every correction inside one launch of the persistent factor PCG
         return launch_pcg_factor_refine(bv, vv, w, pw, fb, pl, pcg_ctas, slot, maxiter, use_precond, s);
     const int rb = ir_residual_blocks(vv.n);
@@ -693,7 +697,9 @@ cudaError_t launch_mixed_solve(const BsrViews &bv, const VertexViews &vv, const 
         ir_residual_kernel<<<rb, kResThreads, 0, s>>>(bv, vv, w, pw, slot);
         count_launches(1);
         e = cudaGetLastError();
-        if (e == cudaSuccess && (w.hq_words || fp32) && pl.variant == PcgLayout::kFactor)
+        if (e == cudaSuccess && single_inner)
+            e = launch_pcg_inner(bv, vv, w, pw, *single, pcg_ctas, slot, maxiter, s);
+        else if (e == cudaSuccess && (w.hq_words || fp32) && pl.variant == PcgLayout::kFactor)
             e = launch_pcg_factor_inner(bv, vv, w, pw, fb, pl, pcg_ctas, slot, maxiter, use_precond, s);
         else if (e == cudaSuccess)
             e = bf16 ? launch_ir_pcg<__nv_bfloat16>(bv, vv, w, fb, pw.error, maxiter, use_precond, s)
