@@ -492,18 +492,22 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
             }
             // ---- phase A: p = z + beta p over the window, Ap = H p, p.Ap
             float *p_new = pubP[it & 1];
-            if (pending && !tma_wait(&s_mbar, parity, a.error)) {
-                pending = false;
-                if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
-                break;
-            }
+            // each thread waits for the window copies itself; the verdicts
+            // join the sync after the window update
+            const bool landed = !pending || tma_wait_local(&s_mbar, parity);
             pending = false;
             const float fbeta = sc.beta;
             if (it > 0) {
                 for (int j = threadIdx.x; j < 3 * cm.nwin; j += blockDim.x)
                     winA[j] = __fmaf_rn(fbeta, winB[j], winA[j]);
             }
-            __syncthreads();
+            if (!__syncthreads_and(landed)) {
+                if (threadIdx.x == 0) {
+                    atomicExch(a.error, 1);
+                    sc.status = MFEM_TIMEOUT;
+                }
+                break;
+            }
             for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x)
                 p_new[(size_t)3 * cm.row_lo + i] = winA[3 * own + i];
             window_product<CACHE>(a, rowoff, sH, sCol, cm.blk_lo, cm.win_lo, cm.nrows, winA, sAp, hm, cm.row_lo);
@@ -544,10 +548,8 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
                 break;
             }
             const float alpha = sc.alpha;
-            if (ap_pending && !tma_wait(&s_mbar, parity, a.error)) {
-                if (threadIdx.x == 0) sc.status = MFEM_TIMEOUT;
-                break;
-            }
+            // the copy of Ap over R, waited for by each thread (joined below)
+            const bool ap_landed = !ap_pending || tma_wait_local(&s_mbar, parity);
             // ---- phase B: r -= alpha Ap (over R with a factor), x += alpha p, z = M r
             if (factor) {
                 for (int j = threadIdx.x; j < 3 * nr; j += blockDim.x) sR[j] = __fmaf_rn(-alpha, winB[j], sR[j]);
@@ -557,7 +559,13 @@ __global__ void __launch_bounds__(kPcgThreads, 1) pcg_factor_kernel(PcgArgs a) {
             }
             for (int i = threadIdx.x; i < 3 * cm.nrows; i += blockDim.x)
                 sX[i] = __fmaf_rn(alpha, winA[3 * own + i], sX[i]);
-            __syncthreads();
+            if (!__syncthreads_and(ap_landed)) {
+                if (threadIdx.x == 0) {
+                    atomicExch(a.error, 1);
+                    sc.status = MFEM_TIMEOUT;
+                }
+                break;
+            }
             float acc[2] = {0.0f, 0.0f};
             if (factor) {
                 first_pass<FC>(f0, sR, sY, y_hi - y_lo);
