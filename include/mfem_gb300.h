@@ -493,6 +493,14 @@ int mfem_plan_set_diagnostics(mfem_plan *plan, int32_t on);
  * device and drops captured graphs when the setting changes. */
 int mfem_plan_set_residual_check(mfem_plan *plan, int32_t on);
 
+/* Failure injection on the host, for tests of the timeout path: sets the
+ * plan's sticky device error flag, as a bounded wait that gave up does.  The
+ * step's persistent kernels then leave at their first check (no wait, no
+ * fault), the step's stats calls return MFEM_TIMEOUT and re-arm every grid
+ * barrier of the plan, and the step after that runs normally.  Synchronises
+ * the device; launches nothing. */
+int mfem_plan_inject_timeout(mfem_plan *plan);
+
 /* The check's results for the last step, one per Newton iteration
  * (synchronises the stream; MFEM_BAD_ARG while the check is off). */
 int mfem_step_true_residuals(mfem_plan *plan, double *h_rel_residual, int32_t max_entries, int32_t *count,

@@ -134,6 +134,20 @@ int cuda_fail(mfem_plan *p, cudaError_t err, const char *what) {
     return fail(p, MFEM_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(err));
 }
 
+// After a bounded wait gave up (the sticky error flag is set), with no kernel
+// of the plan in flight: every grid barrier counter of the plan back to 0 (a
+// barrier that timed out leaves partial arrivals, which would release the
+// next launch's barriers early) and the flag cleared.
+cudaError_t rearm_barriers(mfem_plan *p) {
+    cudaError_t e = cudaMemset(p->pw.counter, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(p->ls.counter, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess && p->ir.counter) e = cudaMemset(p->ir.counter, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess && p->bw.n_bodies > 0 && p->bw.counter)
+        e = cudaMemset(p->bw.counter, 0, (size_t)p->bw.n_bodies * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(p->pw.error, 0, sizeof(int));
+    return e;
+}
+
 template <class T>
 cudaError_t dev_alloc(mfem_plan *p, T **ptr, size_t count) {
     void *raw = nullptr;
@@ -889,10 +903,9 @@ int mfem_step_stats(mfem_plan *p, mfem_solve_stats *h_stats, int32_t max_entries
     for (int i = 0; i < k; ++i) std::memcpy(&h_stats[i], &tmp[i], sizeof(mfem_solve_stats));
     if (count) *count = k;
     if (flag) {
-        // a bounded wait gave up: re-arm the grid barrier for the next solve
-        cudaMemset(p->pw.counter, 0, sizeof(unsigned long long));
-        cudaMemset(p->ls.counter, 0, sizeof(unsigned long long));
-        cudaMemset(p->pw.error, 0, sizeof(int));
+        // a bounded wait gave up: re-arm the grid barriers for the next solve
+        e = rearm_barriers(p);
+        if (e != cudaSuccess) return cuda_fail(p, e, "re-arming the grid barriers");
         return fail(p, MFEM_TIMEOUT, "a PCG or line-search grid barrier timed out");
     }
     return MFEM_OK;
@@ -1237,6 +1250,17 @@ int mfem_plan_set_diagnostics(mfem_plan *p, int32_t on) {
         }
     }
     p->diagnostics = on != 0;
+    return MFEM_OK;
+}
+
+int mfem_plan_inject_timeout(mfem_plan *p) {
+    if (!p) return MFEM_BAD_ARG;
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(p, e, "cudaDeviceSynchronize");
+    const int one = 1;
+    e = cudaMemcpy(p->pw.error, &one, sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(p, e, "setting the error flag");
     return MFEM_OK;
 }
 
@@ -1774,7 +1798,7 @@ int mfem_plan_autotune_batch(mfem_plan *p, const float *d_q, float dt, double *h
         if (e == cudaSuccess) e = cudaMemcpy(&flag, p->pw.error, sizeof(int), cudaMemcpyDeviceToHost);
         if (e == cudaSuccess && flag) {
             // a wait gave up: this schedule is not a candidate
-            e = cudaMemset(p->pw.error, 0, sizeof(int));
+            e = rearm_barriers(p);
             continue;
         }
         if (e == cudaSuccess && ms < best) {
@@ -1816,8 +1840,8 @@ int mfem_step_body_stats(mfem_plan *p, mfem_solve_stats *h_stats, int32_t max_en
     e = cudaMemcpy(&flag, p->pw.error, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(p, e, "stats readback");
     if (flag) {
-        for (int b = 0; b < B; ++b) cudaMemsetAsync(p->bw.counter + b, 0, sizeof(unsigned long long));
-        cudaMemset(p->pw.error, 0, sizeof(int));
+        e = rearm_barriers(p);
+        if (e != cudaSuccess) return cuda_fail(p, e, "re-arming the grid barriers");
         return fail(p, MFEM_TIMEOUT, "a batched PCG barrier timed out");
     }
     return MFEM_OK;

@@ -219,6 +219,7 @@ _SIGNATURES = {
     "mfem_local_solve": (ctypes.c_int, [_P, _P, _P]),
     "mfem_true_residual": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _P]),
     "mfem_plan_set_residual_check": (ctypes.c_int, [_P, _I32]),
+    "mfem_plan_inject_timeout": (ctypes.c_int, [_P]),
     "mfem_plan_set_diagnostics": (ctypes.c_int, [_P, _I32]),
     "mfem_step_true_residuals": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _I32, ctypes.POINTER(_I32),
                                                 _P]),

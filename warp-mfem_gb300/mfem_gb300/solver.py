@@ -501,6 +501,13 @@ class MixedFEMSolver:
         _lib.check(self._lib.mfem_plan_set_diagnostics(self._plan, int(bool(on))), self._plan)
         self._diagnostics = bool(on)
 
+    def inject_timeout(self) -> None:
+        """Sets the plan's sticky device error flag, as a bounded wait that
+        gave up does (host-side failure injection for tests): the next step's
+        persistent kernels leave at once, its stats calls raise MFEM_TIMEOUT
+        and re-arm the grid barriers, and the step after runs normally."""
+        _lib.check(self._lib.mfem_plan_inject_timeout(self._plan), self._plan)
+
     def set_residual_check(self, on: bool) -> None:
         """Turns on or off the fp64 check of every global solve inside step()
         (read back with step_true_residuals); the trajectory is unchanged."""
