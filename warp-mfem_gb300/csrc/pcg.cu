@@ -873,8 +873,11 @@ cudaError_t pcg_plan_layout(int device, PcgLayout &L, const int32_t *row_ptr, co
     return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
 }
 
-cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const PcgLayout &L, int ctas,
-                       int slot, float tol, int maxiter, int use_precond, cudaStream_t s) {
+namespace {
+
+// The launch arguments of the plan's PCG from its views and workspace.
+PcgArgs pcg_args(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const PcgLayout &L, int slot, float tol,
+                 int maxiter, int use_precond) {
     PcgArgs a = {};
     a.n = bv.n;
     a.row_ptr = bv.row_ptr;
@@ -897,6 +900,11 @@ cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork 
     a.tol = tol;
     a.maxiter = maxiter;
     a.use_precond = use_precond;
+    return a;
+}
+
+// One cooperative launch of the layout's kernel.
+cudaError_t launch_cooperative(const PcgArgs &a, const PcgLayout &L, int ctas, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(ctas);
     cfg.blockDim = dim3(kPcgThreads);
@@ -912,50 +920,24 @@ cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork 
     return err;
 }
 
+}  // namespace
+
+cudaError_t launch_pcg(const BsrViews &bv, const VertexViews &vv, const PcgWork &w, const PcgLayout &L, int ctas,
+                       int slot, float tol, int maxiter, int use_precond, cudaStream_t s) {
+    return launch_cooperative(pcg_args(bv, vv, w, L, slot, tol, maxiter, use_precond), L, ctas, s);
+}
+
 // The single-reduction PCG as one inner solve of the refinement's launch
 // sequence (block-Jacobi, fp32 blocks): rhs ir.res, correction to ir.e.
 cudaError_t launch_pcg_inner(const BsrViews &bv, const VertexViews &vv, const IrWork &ir, const PcgWork &w,
                              const PcgLayout &L, int ctas, int slot, int maxiter, cudaStream_t s) {
     if (L.variant != PcgLayout::kSingleReduction) return cudaErrorInvalidValue;
-    const float tol = ir.inner_tol;
-    const int use_precond = 1;
-    PcgArgs a = {};
-    a.n = bv.n;
-    a.row_ptr = bv.row_ptr;
-    a.col_idx = bv.col_idx;
-    a.values = bv.values;
-    a.Minv = vv.Minv;
+    PcgArgs a = pcg_args(bv, vv, w, L, slot, ir.inner_tol, maxiter, 1);
     a.b = ir.res;
     a.x = ir.e;
     a.ir_state = ir.state;
     a.ir_scale = ir.scale;
-    a.pub = w.pub;
-    a.n_pad = w.n_pad;
-    a.cta = L.cta_info;
-    a.rows_max = L.rows_max;
-    a.blk_max = L.blk_max;
-    a.win_max = L.win_max;
-    a.partials = w.partials;
-    a.counter = w.counter;
-    a.error = w.error;
-    a.stats = w.stats;
-    a.slot = slot;
-    a.tol = tol;
-    a.maxiter = maxiter;
-    a.use_precond = use_precond;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(ctas);
-    cfg.blockDim = dim3(kPcgThreads);
-    cfg.dynamicSmemBytes = L.smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cudaError_t err = cudaLaunchKernelEx(&cfg, pick_kernel(L), a);
-    count_launches(1);
-    return err;
+    return launch_cooperative(a, L, ctas, s);
 }
 
 }  // namespace mfem
